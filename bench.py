@@ -1,0 +1,360 @@
+"""Benchmark: block-ILU(0) + ISAI preconditioned GMRES on the 128^3 4-DOF
+convection-diffusion system (BSR 4x4, 2,097,152 block rows, 14,581,760
+blocks, FP64 matrix), synthetic seeded data.
+
+A step is one solve to 1e-10 relative residual from x0 = 0 with the
+mixed-precision path (FP32-stored ISAI inside FP64 flexible GMRES(30) with
+FP64 residuals, orthogonalisation and restarts); the preconditioner setup
+(BILU(0) + ISAI on the GPU) runs once before the timed region and is
+reported separately, as is the plain FP64 path.  `value` is the mean solve
+time (s) with the matrix resident in HBM (1.9 GB of values, larger than L2).
+`e2e` is the same metric through the C ABI call with host buffers
+(bilu_solve_host: H2D of A and b, setup, solve, D2H of x).
+
+    python bench.py [--steps K] [--warmup W] [--side 128] [--impl reference]
+    torchrun --nproc-per-node N bench.py --gpus N   (N independent replicas)
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time to 1e-10 rel. residual, mixed vs FP64 BILU-ISAI; precond-apply HBM GB/s"
+FALLBACK_HBM_GBS = 6800.0
+# FP64 and mixed iteration counts of the 128^3 system measured on GB300 with
+# this code (the FP64 count equals the oracle's at every size the oracle can
+# finish); used to scale the CPU baseline's per-iteration cost.
+C2_ITERS_REF = {"fp64": None, "mixed": None}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--side", type=int, default=128)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--restart", type=int, default=30)
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--maxit", type=int, default=20000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-iters", type=int, default=3)
+    return ap.parse_args()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [ln.split(",") for ln in open(self.f.name).read().splitlines() if ln.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for k, v in zip(names, r[5:9]):
+                    if v.strip() == "Active":
+                        reasons.add(k)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def apply_bytes(nb, bs, nnzL, nnzU, s_val, s_tmp):
+    """Algorithmic bytes of one preconditioner apply y = M_L b, x = M_U y:
+    values + column indices of both factors, both row pointers, read b (FP64),
+    write and read the intermediate y, write x (FP64)."""
+    n = nb * bs
+    return (nnzL + nnzU) * (bs * bs * s_val + 4) + 2 * (nb + 1) * 4 + n * (8 + 2 * s_tmp + 8)
+
+
+def spmv_bytes(nb, bs, nnzb):
+    n = nb * bs
+    return nnzb * (bs * bs * 8 + 4) + (nb + 1) * 4 + 2 * n * 8
+
+
+def dist_init(args):
+    if args.gpus <= 1 and "WORLD_SIZE" not in os.environ:
+        return 0, 1
+    import torch.distributed as dist
+
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_baseline(side, iters_full, gmres_iters=3, seed=0):
+    """The oracle (plain-C restatement of the reference path, OpenMP over the
+    host cores) on the full system: the whole setup (BILU(0), patterns,
+    pairs, Dinv, ISAI-L/U, reorder) plus `gmres_iters` FGMRES iterations with
+    the FP32-stored ISAI; time to solution = setup + per-iteration cost x
+    the solver's iteration count for this system."""
+    from isai_kernel_gb300 import gen
+    from oracle import oracle
+
+    A = gen.convdiff3d(side, bs=4, seed=seed)
+    b = gen.rhs(A.n, seed)
+    t0 = time.perf_counter()
+    S = oracle.isai_setup(A)
+    t_setup = time.perf_counter() - t0
+    Ab = (A.rowptr, A.colind, A.val)
+    L = (S["TrowL"], S["TcolL"], S["McsrL"])
+    U = (S["TrowU"], S["TcolU"], S["McsrU"])
+    t0 = time.perf_counter()
+    _, it, _, _, _ = oracle.gmres(Ab, L, U, b, precond=2, restart=30, maxit=gmres_iters)
+    t_it = (time.perf_counter() - t0) / max(it, 1)
+    est = t_setup + t_it * iters_full
+    return {"value": est, "unit": "s", "cores": oracle.num_threads(), "kind": "port",
+            "sample": (f"oracle on the full {side}^3 system: setup {t_setup:.2f} s measured, "
+                       f"{it} FGMRES(30) iterations measured at {t_it:.3f} s each, scaled to "
+                       f"{iters_full} iterations"),
+            "setup_s": t_setup, "per_iter_s": t_it}
+
+
+def run_reference(args):
+    rank, world = dist_init(args)
+    if rank != 0:
+        return
+    iters = C2_ITERS_REF["mixed"] or 700
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(args.side, iters, gmres_iters=args.cpu_iters)
+        if i >= args.warmup:
+            vals.append(r)
+    v = statistics.mean(r["value"] for r in vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded 128^3 convection-diffusion, BSR 4x4)",
+            "config": {"workload": f"convdiff3d {args.side}^3 bs4, FGMRES(30) tol 1e-10, mixed",
+                       "n": args.side ** 3 * 4},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_ours(args):
+    import torch
+
+    from isai_kernel_gb300 import _lib, api, gen
+
+    rank, world = dist_init(args)
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = _lib.lib()
+    stream = torch.cuda.current_stream()
+
+    A = gen.convdiff3d(args.side, bs=4, seed=0)
+    b_np = gen.rhs(A.n, 0)
+    nb, bs, nnzb, n = A.nb, A.bs, A.nnzb, A.n
+    row = torch.from_numpy(A.rowptr).to(dev)
+    col = torch.from_numpy(A.colind).to(dev)
+    val = torch.from_numpy(A.val).to(dev)
+    b = torch.from_numpy(b_np).to(dev)
+    torch.cuda.synchronize()
+
+    P = api.Preconditioner(nb, bs, row, col, val, fp32=True)
+    setup_ms = P.setup_ms
+    x = torch.empty_like(b)
+
+    def solve(prec):
+        return P.solve(b, x, prec=prec, restart=args.restart, tol=args.tol, maxit=args.maxit)
+
+    for _ in range(args.warmup):
+        _, res = solve(1)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    l0 = L.bilu_kernel_launches()
+    times, iters = [], []
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, res = solve(1)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        iters.append(res.iters)
+    torch.cuda.synchronize()
+    barrier(world)
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    launches = L.bilu_kernel_launches() - l0
+    relres_mixed = res.relres
+    t_mixed = max_over_ranks(statistics.mean(times), world)
+
+    # plain FP64 path (reported beside the headline)
+    _, r64 = solve(0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    _, r64 = solve(0)
+    e1.record(stream)
+    e1.synchronize()
+    t_fp64 = e0.elapsed_time(e1) / 1e3
+
+    # preconditioner apply kernels, timed alone with CUDA events on the
+    # launching stream (inputs: 1.1-1.9 GB of factors, larger than L2)
+    lu, Lf, Uf = P.factors()
+    nnzL, nnzU = int(Lf[1].numel()), int(Uf[1].numel())
+    L32, U32 = P.get(7).view(-1, bs, bs), P.get(8).view(-1, bs, bs)
+
+    def time_it(fn, reps=20):
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    t_apply64 = time_it(lambda: api.isai_apply(nb, bs, Lf, Uf, b, prec=0))
+    t_apply32 = time_it(lambda: api.isai_apply(nb, bs, (Lf[0], Lf[1], L32), (Uf[0], Uf[1], U32),
+                                               b, prec=1))
+    y = torch.empty_like(b)
+    t_spmvA = time_it(lambda: api.bcsr_spmv(nb, bs, row, col, val, b, y))
+    B64 = apply_bytes(nb, bs, nnzL, nnzU, 8, 8)
+    B32 = apply_bytes(nb, bs, nnzL, nnzU, 4, 4)
+    BA = spmv_bytes(nb, bs, nnzb)
+    peak, peak_kind = peaks()
+    gbs32 = B32 / t_apply32 / 1e9
+
+    # end to end through the C ABI with pinned host buffers
+    hrow = torch.from_numpy(A.rowptr).pin_memory()
+    hcol = torch.from_numpy(A.colind).pin_memory()
+    hval = torch.from_numpy(A.val).pin_memory()
+    hb = torch.from_numpy(b_np).pin_memory()
+    hx = torch.empty(n, dtype=torch.float64).pin_memory()
+    e2e = []
+    for _ in range(2):
+        it, rr = ctypes.c_int(0), ctypes.c_double(0)
+        tm = (ctypes.c_double * 4)()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = L.bilu_solve_host(nb, nnzb, bs, ctypes.c_void_p(hrow.data_ptr()),
+                               ctypes.c_void_p(hcol.data_ptr()), ctypes.c_void_p(hval.data_ptr()),
+                               ctypes.c_void_p(hb.data_ptr()), ctypes.c_void_p(hx.data_ptr()), 1,
+                               args.restart, args.tol, args.maxit, ctypes.byref(it),
+                               ctypes.byref(rr), tm, ctypes.c_void_p(stream.cuda_stream))
+        e2e.append(time.perf_counter() - t0)
+        assert st == 0, st
+    e2e_v = max_over_ranks(min(e2e), world)
+    h2d = A.rowptr.nbytes + A.colind.nbytes + A.val.nbytes + b_np.nbytes
+    d2h = n * 8
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(args.side, int(statistics.mean(iters)), gmres_iters=args.cpu_iters)
+            cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        except Exception as exc:  # report, never hide
+            cpu = {"value": None, "unit": "s", "cores": 0, "kind": "port",
+                   "sample": f"failed: {exc}"}
+    P.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": t_mixed, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_mixed * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic (seeded 128^3 7-point convection-diffusion, 4 DOF, BSR 4x4)",
+        "config": {"workload": f"convdiff3d {args.side}^3 bs4 (nb={nb}, nnzb={nnzb}), "
+                               f"FGMRES({args.restart}) to {args.tol:g}, FP32-stored ISAI",
+                   "nb": nb, "nnzb": nnzb, "restart": args.restart, "tol": args.tol,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (1.87 GB of FP64 values)"},
+        "iters": {"mixed": int(statistics.mean(iters)), "fp64": r64.iters},
+        "relres": {"mixed": relres_mixed, "fp64": r64.relres},
+        "fp64_solve_s": t_fp64, "speedup_mixed_vs_fp64": t_fp64 / t_mixed,
+        "setup_ms": setup_ms,
+        "apply": {"fp32_s": t_apply32, "fp64_s": t_apply64, "fp32_GBs": gbs32,
+                  "fp64_GBs": B64 / t_apply64 / 1e9, "bytes_fp32": B32, "bytes_fp64": B64,
+                  "A_spmv_s": t_spmvA, "A_spmv_GBs": BA / t_spmvA / 1e9},
+        "roofline": {"bound": "hbm", "achieved": gbs32, "peak": peak, "unit": "GB/s",
+                     "frac": gbs32 / peak, "traffic": None,
+                     "kernel": "FP32-stored ISAI apply (k_bsr_spmv x2)",
+                     "peak_source": f"{peak_kind} hbm_gbs"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "clocks": clk, "wall_s": wall,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

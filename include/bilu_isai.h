@@ -1,0 +1,307 @@
+/*
+ * bilu_isai.h -- C ABI of the GB300 block-ILU(0) + ISAI preconditioner engine
+ * (libbilu_isai.so, sm_103a).
+ *
+ * Drop-in boundary for the host/kernel entry points of gmfff/isai_kernel.
+ * Each declaration names the reference function (file:line) it replaces.
+ * The reference is header-only CUDA C++ with compile-time BS and exit(1) on
+ * error; this ABI takes the block size at run time, returns a status code and
+ * never exits.
+ *
+ * Conventions
+ *   - Pointers are DEVICE pointers unless the name starts with h_.
+ *   - The caller owns every buffer.  Entry points that need scratch take
+ *     (d_ws, ws_bytes); the matching *_ws_bytes() query gives the size.
+ *   - BSR/BCSR: int32 rowPtr[nb+1], colInd[nnzb] strictly ascending per row,
+ *     values nnzb*bs*bs row-major inside a block.  BCSC (ISAI patterns):
+ *     colPtr[nb+1] ("Mbrow"), rowInd ("Mcol") ascending.
+ *   - Packed BILU(0) as cuSPARSE bsrilu02: strictly lower blocks = L,
+ *     diagonal block = unit-lower L_kk (strict lower part) and U_kk,
+ *     strictly upper blocks = U.
+ *   - Supported block sizes: 4, 5, 8.  Precision: BILU_FP64 (plain) or
+ *     BILU_FP32 (FP32-stored ISAI factors, FP32 accumulation).
+ *   - stream may be NULL (legacy default stream).  Calls are asynchronous
+ *     unless documented to return a host value (h_ outputs synchronise).
+ */
+#ifndef BILU_ISAI_H
+#define BILU_ISAI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* bilu_stream_t; /* == cudaStream_t */
+
+enum bilu_status {
+  BILU_OK = 0,
+  BILU_ERR_ARG = -1,           /* bad size, block size, pointer or flag */
+  BILU_ERR_PATTERN = -2,       /* missing diagonal block, unsorted row, ... */
+  BILU_ERR_ZERO_PIVOT = -3,    /* singular pivot; index via h_info */
+  BILU_ERR_TIMEOUT = -4,       /* a sync-free wait gave up (bounded spin) */
+  BILU_ERR_CUDA = -5,          /* CUDA runtime error (launch, copy) */
+  BILU_ERR_NOT_CONVERGED = -6, /* Krylov solver hit maxit */
+  BILU_ERR_WORKSPACE = -7,     /* workspace too small */
+  BILU_ERR_UNSUPPORTED = -8    /* block size / precision not built */
+};
+
+enum bilu_precision { BILU_FP64 = 0, BILU_FP32 = 1 };
+
+const char* bilu_status_string(int status);
+int bilu_version(void);
+/* last CUDA error seen by the library on this thread (cudaError_t value) */
+int bilu_last_cuda_error(void);
+/* number of kernels this library has launched since it was loaded */
+unsigned long long bilu_kernel_launches(void);
+
+/* ------------------------------------------------------------------ */
+/* Format conversions and patterns                                     */
+/* ------------------------------------------------------------------ */
+
+/* Replaces csr_to_bsr5 (csr2bsr.h:14).  Two phases: rowcounts writes
+ * d_bsrRowPtr[nb+1] and *h_nnzb; fill writes colInd/val.  Duplicate scalar
+ * entries are summed, block columns come out ascending. */
+size_t bilu_csr_to_bsr_ws_bytes(int n, int bs);
+int bilu_csr_to_bsr_rowptr(int n, int bs, const int* d_csrRowPtr, const int* d_csrColInd,
+                           int* d_bsrRowPtr, int* h_nnzb, void* d_ws, size_t ws_bytes,
+                           bilu_stream_t stream);
+int bilu_csr_to_bsr_fill(int n, int bs, const int* d_csrRowPtr, const int* d_csrColInd,
+                         const double* d_csrVal, const int* d_bsrRowPtr, int* d_bsrColInd,
+                         double* d_bsrVal, bilu_stream_t stream);
+
+/* Replaces bsr2csr_cusparse (bsr2csr.h:19), row direction, on the device:
+ * csr arrays have mb*bs+1, nnzb*bs*bs, nnzb*bs*bs entries. */
+int bilu_bsr_to_csr(int mb, int bs, const int* d_bsrRowPtr, const int* d_bsrColInd,
+                    const double* d_bsrVal, int* d_csrRowPtr, int* d_csrColInd,
+                    double* d_csrVal, bilu_stream_t stream);
+
+/* Replaces build_bcsc_pattern_from_bsr_scalarILU (isai_bsr.h:246): ISAI
+ * pattern of M_L (lower=1) or M_U (lower=0) in BCSC.  Two phases. */
+size_t bilu_isai_pattern_ws_bytes(int nb, int nnzb); /* nnzb of A */
+int bilu_isai_pattern_colptr(int nb, const int* d_Arow, const int* d_Acol, int lower,
+                             int* d_Mptr, int* h_nnz, void* d_ws, size_t ws_bytes,
+                             bilu_stream_t stream);
+int bilu_isai_pattern_fill(int nb, const int* d_Arow, const int* d_Acol, int lower,
+                           const int* d_Mptr, int* d_Mind, void* d_ws, size_t ws_bytes,
+                           bilu_stream_t stream);
+
+/* Replaces build_triangular_bcsr_pattern_from_A (bcsc2bcsr.h:11). */
+size_t bilu_tri_pattern_ws_bytes(int nb);
+int bilu_tri_pattern_rowptr(int nb, const int* d_Arow, const int* d_Acol, int lower,
+                            int* d_Trow, int* h_nnz, void* d_ws, size_t ws_bytes,
+                            bilu_stream_t stream);
+int bilu_tri_pattern_fill(int nb, const int* d_Arow, const int* d_Acol, int lower,
+                          const int* d_Trow, int* d_Tcol, bilu_stream_t stream);
+
+/* Replaces build_map_bcsc2bcsr_host (bcsc2bcsr.h:32).  Returns
+ * BILU_ERR_PATTERN (and the first missing (row, col) in h_bad[2]) where the
+ * reference exits. */
+int bilu_map_bcsc2bcsr(int nb, const int* d_cscPtr, const int* d_cscInd, const int* d_csrRow,
+                       const int* d_csrCol, int* d_map, int* h_bad, void* d_ws,
+                       size_t ws_bytes, bilu_stream_t stream);
+size_t bilu_map_ws_bytes(void);
+
+/* Replaces reorder_bcsc_val_to_bcsr_bs5 (bcsc2bcsr.h:63). */
+int bilu_reorder_bcsc_to_bcsr(int nnzb, int bs, const int* d_map, const double* d_src,
+                              double* d_dst, bilu_stream_t stream);
+
+/* Replaces bcsc_to_bcsr (bcsc2bcsrAndSpMV.h:76); deterministic: columns
+ * ascending inside each row, row_ptr[mb] written. */
+size_t bilu_bcsc_to_bcsr_ws_bytes(int mb, int nnzb);
+int bilu_bcsc_to_bcsr(int mb, int nbcol, int bs, const int* d_cscPtr, const int* d_cscInd,
+                      const double* d_cscVal, int* d_rowPtr, int* d_colInd, double* d_val,
+                      void* d_ws, size_t ws_bytes, bilu_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Factorisation                                                       */
+/* ------------------------------------------------------------------ */
+
+/* Replaces bsrilu02_inplace (bsrilu.h:20; cuSPARSE bsrilu02, row direction,
+ * no level information): sync-free BILU(0) in place.  h_info[0] receives the
+ * first block row with a zero pivot (or -1); BILU_ERR_ZERO_PIVOT then. */
+size_t bilu_bsrilu0_ws_bytes(int nb);
+int bilu_bsrilu0(int nb, int nnzb, int bs, const int* d_row, const int* d_col, double* d_val,
+                 int* h_info, void* d_ws, size_t ws_bytes, bilu_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* ISAI setup                                                          */
+/* ------------------------------------------------------------------ */
+
+/* Replaces build_DinvL_from_BSR5_kernel_fix (isai_bsr.h:91, lower=1) and
+ * build_DinvU_from_BSR5_kernel_fix (isai_bsr.h:126, lower=0). */
+int bilu_build_dinv(int nb, int bs, const int* d_Arow, const int* d_Acol, const double* d_Aval,
+                    int lower, double* d_Dinv, bilu_stream_t stream);
+
+/* Replaces count_pairs_lower_kernel_v2 (isai_bsr.h:1378) + the exclusive
+ * scan (main.cu:684) + fill_pairs_lower_kernel_v2 (isai_bsr.h:1427).
+ * lower=0 builds the analogous list for M_U (p > idx, descending p), which
+ * the reference resolves by binary search inside its ISAI-U kernel.
+ * pairs_ptr writes d_PairPtr[Mnnz+1] and *h_total; fill writes the lists.
+ * h_nmax (optional) receives the longest ISAI column. */
+size_t bilu_pairs_ws_bytes(int mnnz);
+int bilu_pairs_ptr(int nb, const int* d_Arow, const int* d_Acol, const int* d_Mptr,
+                   const int* d_Mind, int lower, int* d_PairPtr, int* h_total, int* h_nmax,
+                   void* d_ws, size_t ws_bytes, bilu_stream_t stream);
+int bilu_pairs_fill(int nb, const int* d_Arow, const int* d_Acol, const int* d_Mptr,
+                    const int* d_Mind, int lower, const int* d_PairPtr, int* d_PairPLocal,
+                    int* d_PairSrc, bilu_stream_t stream);
+
+/* Replaces the ISAI-L kernels (isai_bsr.h:288,733,869,976,1287,1332,1355,
+ * cacheY_isai.h:159) for lower=1 and isai_upper_bsr5_warpcol_with_Dinv_kernel
+ * (isai_bsr.h:161) for lower=0: M values in BCSC order (nnzbM*bs*bs). */
+int bilu_isai_compute(int nb, int bs, const double* d_Aval, const int* d_Mptr, const int* d_Mind,
+                      int lower, const int* d_PairPtr, const int* d_PairPLocal,
+                      const int* d_PairSrc, const double* d_Dinv, double* d_Mval,
+                      bilu_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Apply: SpMV / SpMM / ISAI apply                                     */
+/* ------------------------------------------------------------------ */
+
+/* Replaces bcsr_spmv (bcsc2bcsrAndSpMV.h:49) and bsr_SpMV_tensorcore
+ * (bsr_tensor_SpMV.h:402): y = M x.  FP64 values and vectors. */
+int bilu_bcsr_spmv(int mb, int bs, const int* d_row, const int* d_col, const double* d_val,
+                   const double* d_x, double* d_y, bilu_stream_t stream);
+/* FP32-stored values, FP32 accumulation; x and y each FP64 or FP32
+ * (x_fp32 / y_fp32 flags). */
+int bilu_bcsr_spmv_f32(int mb, int bs, const int* d_row, const int* d_col, const float* d_val,
+                       const void* d_x, int x_fp32, void* d_y, int y_fp32, bilu_stream_t stream);
+/* Multi-RHS: Y[n, k] = M X[n, k] (row-major, ld = k), k <= 64, FP64. */
+int bilu_bcsr_spmm(int mb, int bs, int k, const int* d_row, const int* d_col,
+                   const double* d_val, const double* d_X, double* d_Y, bilu_stream_t stream);
+/* Multi-RHS with FP32-stored values (FP32 accumulation), FP64 X/Y. */
+int bilu_bcsr_spmm_f32(int mb, int bs, int k, const int* d_row, const int* d_col,
+                       const float* d_val, const double* d_X, double* d_Y,
+                       bilu_stream_t stream);
+/* Convert FP64 values to FP32 storage (round to nearest). */
+int bilu_convert_f64_to_f32(size_t count, const double* d_src, float* d_dst,
+                            bilu_stream_t stream);
+
+/* Preconditioner apply of main.cu:817-846: y = M_L b, x = M_U y.
+ * prec BILU_FP64: d_Lval/d_Uval are double*, d_tmp holds n doubles.
+ * prec BILU_FP32: float* values, d_tmp holds n floats; b and x FP64. */
+int bilu_isai_apply(int nb, int bs, int prec, const int* d_Lrow, const int* d_Lcol,
+                    const void* d_Lval, const int* d_Urow, const int* d_Ucol,
+                    const void* d_Uval, const double* d_b, void* d_tmp, double* d_x,
+                    bilu_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Sync-free block triangular solves                                   */
+/* ------------------------------------------------------------------ */
+
+/* Replaces spTrSolveL / spTrSolveU (cape_sptrsv.h:8,55) and
+ * csr_cape_SpTRSV (cape_sptrsv.h:105), blockwise on the packed BILU(0):
+ * lower: unit-lower L x = b; upper: U x = b.  Block rows are taken in
+ * dynamic ticket order; waits are bounded (BILU_ERR_TIMEOUT). */
+size_t bilu_sptrsv_ws_bytes(int nb);
+int bilu_sptrsv(int nb, int bs, const int* d_row, const int* d_col, const double* d_val,
+                int lower, const double* d_b, double* d_x, void* d_ws, size_t ws_bytes,
+                bilu_stream_t stream);
+/* General form: lower/upper triangle of a packed factor, unit or non-unit
+ * diagonal (bilu_sptrsv uses lower+unit and upper+non-unit). */
+int bilu_sptrsv_ex(int nb, int bs, const int* d_row, const int* d_col, const double* d_val,
+                   int lower, int unit, const double* d_b, double* d_x, void* d_ws,
+                   size_t ws_bytes, bilu_stream_t stream);
+/* Transposed solves over the BCSC view of the same packed factor (adjoint):
+ * lower: L^T x = b (upper-triangular, unit diagonal); upper: U^T x = b.
+ * The workspace holds the transposed factor. */
+size_t bilu_sptrsv_transpose_ws_bytes(int nb, int nnzb, int bs);
+int bilu_sptrsv_transpose(int nb, int bs, const int* d_row, const int* d_col,
+                          const double* d_val, int lower, const double* d_b, double* d_x,
+                          void* d_ws, size_t ws_bytes, bilu_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Adjoint helpers                                                     */
+/* ------------------------------------------------------------------ */
+
+/* BCSC view of a BCSR matrix as a BCSR matrix of the transpose: pattern
+ * transposed (columns ascending) and every block transposed. */
+size_t bilu_bsr_transpose_ws_bytes(int mb, int nnzb);
+int bilu_bsr_transpose(int mb, int bs, const int* d_row, const int* d_col, const double* d_val,
+                       int* d_trow, int* d_tcol, double* d_tval, void* d_ws, size_t ws_bytes,
+                       bilu_stream_t stream);
+/* y = M^T x for a BCSR matrix (transposed SpMV, deterministic). */
+size_t bilu_spmv_transpose_ws_bytes(int mb, int nnzb);
+int bilu_bcsr_spmv_transpose(int mb, int bs, const int* d_row, const int* d_col,
+                             const double* d_val, const double* d_x, double* d_y,
+                             void* d_ws, size_t ws_bytes, bilu_stream_t stream);
+/* Masked outer product: G[p] (+)= scale * u[row(p)] v[col(p)]^T for every
+ * stored block p (gradient of block values).  accumulate: add into G. */
+int bilu_masked_outer(int mb, int bs, const int* d_row, const int* d_col, const double* d_u,
+                      const double* d_v, double scale, int accumulate, double* d_G,
+                      bilu_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Verification                                                        */
+/* ------------------------------------------------------------------ */
+
+/* Replaces compute_rel_errors_csr (residual_check.h:17) on the device for a
+ * BSR matrix: h_out[0] = ||x - x_true|| / ||x_true|| (x_true may be NULL),
+ * h_out[1] = ||b - A x|| / ||b||. */
+size_t bilu_rel_errors_ws_bytes(int nb, int bs);
+int bilu_rel_errors(int nb, int bs, const int* d_row, const int* d_col, const double* d_val,
+                    const double* d_b, const double* d_x_true, const double* d_x,
+                    double* h_out, void* d_ws, size_t ws_bytes, bilu_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Engine handle: setup + preconditioned (F)GMRES                      */
+/* ------------------------------------------------------------------ */
+
+typedef struct bilu_ctx bilu_ctx;
+
+/* Creates a handle bound to the current device and `stream`.  The handle
+ * owns the device memory of everything it builds. */
+int bilu_ctx_create(bilu_ctx** ctx, bilu_stream_t stream);
+int bilu_ctx_destroy(bilu_ctx* ctx);
+
+/* Copies the BSR matrix (device pointers; the values are not modified) and
+ * runs the whole setup on the GPU: BILU(0), ISAI patterns, pair lists, Dinv,
+ * ISAI-L/U, BCSC->BCSR reorder, FP32 copies when prec_mask has BILU_FP32.
+ * h_times (optional, 4 doubles, milliseconds): factor, patterns, isai,
+ * total. */
+int bilu_ctx_setup(bilu_ctx* ctx, int nb, int nnzb, int bs, const int* d_row, const int* d_col,
+                   const double* d_val, int prec_mask, double* h_times);
+
+/* Right-preconditioned restarted (F)GMRES(restart) with CGS2 and Givens
+ * rotations, x0 = 0: prec BILU_FP64 applies the FP64 ISAI, BILU_FP32 the
+ * FP32-stored ISAI (flexible GMRES, FP64 residuals/orthogonalisation,
+ * FP64 true residual at every restart = iterative refinement); prec -1 runs
+ * without preconditioner.  h_iters, h_relres: iteration count and final true
+ * relative residual.  h_hist (optional, maxit+1 doubles) receives the
+ * residual estimate after every iteration. */
+int bilu_ctx_solve(bilu_ctx* ctx, int prec, const double* d_b, double* d_x, int restart,
+                   double tol, int maxit, int* h_iters, double* h_relres, double* h_hist);
+
+/* Host-buffer convenience (the end-to-end call): copies A and b from host
+ * memory, runs setup and solve, copies x back. */
+int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const int* h_col,
+                    const double* h_val, const double* h_b, double* h_x, int prec, int restart,
+                    double tol, int maxit, int* h_iters, double* h_relres, double* h_times,
+                    bilu_stream_t stream);
+
+/* Accessors for the arrays a handle built (device pointers, owned by the
+ * handle): which = 0 A factored values (double), 1 M_L BCSR rowptr,
+ * 2 M_L colind, 3 M_L values (double), 4 M_U rowptr, 5 M_U colind,
+ * 6 M_U values (double), 7 M_L values (float), 8 M_U values (float).
+ * h_count receives the number of elements. */
+int bilu_ctx_get(bilu_ctx* ctx, int which, const void** d_ptr, long long* h_count);
+
+/* ------------------------------------------------------------------ */
+/* Testing hook (no counterpart in the reference)                      */
+/* ------------------------------------------------------------------ */
+
+/* bilu_sptrsv with block row withhold_row never publishing its ready flag and
+ * a spin budget of spin_limit polls (<= the built-in limit): the rows that
+ * depend on it give up and the call returns BILU_ERR_TIMEOUT instead of
+ * hanging.  Exercises the failure path of the sync-free kernels. */
+int bilu_debug_sptrsv_withhold(int nb, int bs, const int* d_row, const int* d_col,
+                               const double* d_val, int lower, const double* d_b, double* d_x,
+                               int withhold_row, long long spin_limit, void* d_ws,
+                               size_t ws_bytes, bilu_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BILU_ISAI_H */

@@ -1,0 +1,32 @@
+// Vector kernels for the Krylov solver: fused multi-dot, multi-axpy with
+// norm, deterministic reductions (fixed CTA count, fixed summation order).
+#pragma once
+#include "common.cuh"
+
+namespace bilu {
+
+constexpr int kRedCTAs = 152 * 4;  // partial-sum slots (fixed => deterministic)
+constexpr int kRedThreads = 256;
+constexpr int kMaxVec = 32;        // vectors per multi-dot / multi-axpy call
+constexpr int kPartStride = kMaxVec + 2;
+
+// partial[cta * kPartStride + i] = sum_e V[i][e] * w[e] (i < nv), and at
+// index nv: sum_e w[e]^2 when with_ww.  Skipped (partials left as they
+// are) when skip_flag is non-null and *skip_flag == 0.
+int multidot(long long n, const double* V, long long ldv, int nv, const double* w, bool with_ww,
+             double* partial, cudaStream_t st, const int* skip_flag = nullptr);
+// w -= sum_i coef[i] V[i]  (or w += when sign > 0); partial[cta*kPartStride]
+// = sum_e w_new[e]^2.  If skip_flag is non-null and *skip_flag == 0 the
+// kernel returns without touching w.
+int multiaxpy_norm(long long n, const double* V, long long ldv, int nv, const double* coef,
+                   double sign, double* w, double* partial, const int* skip_flag,
+                   cudaStream_t st);
+// out[i] = sum_cta partial[cta*kPartStride + i], i < nout (one thread each).
+int reduce_partials(const double* partial, int nout, double* out, cudaStream_t st);
+// y = x * (1/sqrt(*nrm2)) with *nrm2 a device scalar
+int scale_rsqrt(long long n, const double* x, const double* nrm2, double* y, cudaStream_t st);
+// r = b - ax, partial norms of r
+int residual_norm(long long n, const double* b, const double* ax, double* r, double* partial,
+                  cudaStream_t st);
+
+}  // namespace bilu

@@ -1,0 +1,516 @@
+// Engine handle: whole-pipeline setup on the GPU and the preconditioned
+// (F)GMRES solver.  This is the composition main.cu:449-866 performs by hand
+// (patterns, bsrilu02, Dinv, pairs, ISAI-L/U, reorder, one apply), extended
+// with the Krylov solver the reference does not have.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "blas1.cuh"
+#include "common.cuh"
+#include "scan.cuh"
+
+namespace bilu {
+
+thread_local int g_last_cuda_error = 0;
+unsigned long long g_launches = 0;
+
+// implemented in the other translation units
+size_t isai_pattern_ws(int nb, long long nnzb);
+int isai_pattern_colptr_impl(int nb, const int* row, const int* col, int lower, int* Mptr,
+                             int* h_nnz, Carver& ws, cudaStream_t st);
+int isai_pattern_fill_impl(int nb, const int* row, const int* col, int lower, const int* Mptr,
+                           int* Mind, int mnnz, Carver& ws, cudaStream_t st);
+int tri_pattern_rowptr_impl(int nb, const int* row, const int* col, int lower, int* Trow,
+                            int* h_nnz, Carver& ws, cudaStream_t st);
+int tri_pattern_fill_impl(int nb, const int* row, const int* col, int lower, const int* Trow,
+                          int* Tcol, cudaStream_t st);
+int map_impl(int nb, const int* cptr, const int* cind, const int* rrow, const int* rcol, int* map,
+             int* h_bad, Carver& ws, cudaStream_t st);
+int reorder_impl(long long nnzb, int bs, const int* map, const double* src, double* dst,
+                 cudaStream_t st);
+size_t syncfree_ws(int nb);
+int diag_positions(int nb, const int* row, const int* col, int* diag, int* h_bad, Carver& ws,
+                   cudaStream_t st);
+int bilu0_impl(int nb, int bs, const int* row, const int* col, const int* diag, double* val,
+               int* h_zp, Carver& ws, cudaStream_t st);
+int dinv_impl(int nb, int bs, const int* row, const int* col, const double* val, int lower,
+              double* Dinv, int* d_fail, cudaStream_t st);
+size_t pairs_ws(long long mnnz);
+int pairs_ptr_impl(int nb, const int* Arow, const int* Acol, const int* Mptr, const int* Mind,
+                   int lower, int* PairPtr, int mnnz, int* h_total, int* h_nmax, Carver& ws,
+                   cudaStream_t st);
+int pairs_fill_impl(int nb, const int* Arow, const int* Acol, const int* Mptr, const int* Mind,
+                    int lower, const int* PairPtr, int* PL, int* PS, cudaStream_t st);
+int isai_impl(int nb, int bs, const double* Aval, const int* Mptr, const int* Mind, int lower,
+              const int* pp, const int* pl, const int* ps, const double* Dinv, double* Mval,
+              cudaStream_t st);
+int spmv_any(int mb, int bs, int prec, const int* row, const int* col, const void* val,
+             const void* x, int x32, void* y, int y32, cudaStream_t st);
+int isai_apply_impl(int nb, int bs, int prec, const int* Lrow, const int* Lcol, const void* Lval,
+                    const int* Urow, const int* Ucol, const void* Uval, const double* b,
+                    void* tmp, double* x, cudaStream_t st);
+
+namespace {
+
+__global__ void k_dgks_select(double* s, int nv) {
+  // s layout: [0..nv) h1, [nv] ww0 | s+kPartStride: ww1 | s+2*kPartStride:
+  // [0..nv) h2 | s+3*kPartStride: ww2 | flag at s+4*kPartStride (as double)
+  // | selected ww at s+5*kPartStride
+  double ww0 = s[nv], ww1 = s[kPartStride];
+  int flag = ww1 < 0.5 * ww0;
+  ((int*)(s + 4 * kPartStride))[0] = flag;
+}
+
+__global__ void k_pick_norm(double* s) {
+  int flag = ((const int*)(s + 4 * kPartStride))[0];
+  s[5 * kPartStride] = flag ? s[3 * kPartStride] : s[kPartStride];
+}
+
+}  // namespace
+
+}  // namespace bilu
+
+using namespace bilu;
+
+struct bilu_ctx {
+  int dev = 0;
+  cudaStream_t st = nullptr;
+  int nb = 0, nnzb = 0, bs = 0;
+  long long n = 0;
+  int *Arow = nullptr, *Acol = nullptr, *diag = nullptr;
+  double *Aval = nullptr, *LU = nullptr;
+  int *Lrow = nullptr, *Lcol = nullptr, *Urow = nullptr, *Ucol = nullptr;
+  double *Lval = nullptr, *Uval = nullptr;
+  float *Lval32 = nullptr, *Uval32 = nullptr;
+  int nnzL = 0, nnzU = 0;
+  bool ready = false;
+  // solver buffers
+  int m_alloc = 0;
+  double *V = nullptr, *Z = nullptr, *w = nullptr, *r = nullptr, *tmp = nullptr;
+  double *partial = nullptr, *dscal = nullptr, *dcoef = nullptr;
+  double* hpin = nullptr;  // pinned host mirror of dscal
+  std::vector<void*> setup_bufs;
+  void free_setup() {
+    for (void* p : setup_bufs) cudaFree(p);
+    setup_bufs.clear();
+    Arow = Acol = diag = Lrow = Lcol = Urow = Ucol = nullptr;
+    Aval = LU = Lval = Uval = nullptr;
+    Lval32 = Uval32 = nullptr;
+    ready = false;
+  }
+  void free_solver() {
+    cudaFree(V); cudaFree(Z); cudaFree(w); cudaFree(r); cudaFree(tmp);
+    cudaFree(partial); cudaFree(dscal); cudaFree(dcoef);
+    if (hpin) cudaFreeHost(hpin);
+    V = Z = w = r = tmp = partial = dscal = dcoef = hpin = nullptr;
+    m_alloc = 0;
+  }
+  template <class T>
+  int alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+    if (e != cudaSuccess) return cuda_status(e);
+    setup_bufs.push_back(*p);
+    return BILU_OK;
+  }
+};
+
+extern "C" int bilu_ctx_create(bilu_ctx** ctx, bilu_stream_t stream) {
+  if (!ctx) return BILU_ERR_ARG;
+  bilu_ctx* c = new (std::nothrow) bilu_ctx();
+  if (!c) return BILU_ERR_ARG;
+  cudaGetDevice(&c->dev);
+  c->st = S(stream);
+  *ctx = c;
+  return BILU_OK;
+}
+
+extern "C" int bilu_ctx_destroy(bilu_ctx* ctx) {
+  if (!ctx) return BILU_OK;
+  cudaStreamSynchronize(ctx->st);
+  ctx->free_setup();
+  ctx->free_solver();
+  delete ctx;
+  return BILU_OK;
+}
+
+namespace {
+
+struct Timer {
+  cudaEvent_t e[5];
+  cudaStream_t st;
+  explicit Timer(cudaStream_t s) : st(s) {
+    for (auto& x : e) cudaEventCreate(&x);
+  }
+  ~Timer() {
+    for (auto& x : e) cudaEventDestroy(x);
+  }
+  void mark(int i) { cudaEventRecord(e[i], st); }
+  double ms(int a, int b) {
+    float v = 0;
+    cudaEventSynchronize(e[b]);
+    cudaEventElapsedTime(&v, e[a], e[b]);
+    return v;
+  }
+};
+
+// One triangle of the ISAI: pattern (BCSC), BCSR pattern + map, pairs,
+// Dinv, column solves, BCSC->BCSR reorder.  Outputs BCSR rowptr/col/val.
+int build_isai_side(bilu_ctx* c, int lower, Carver& ws, int** orow, int** ocol, double** oval,
+                    int* onnz, double* t_pattern, double* t_isai) {
+  cudaStream_t st = c->st;
+  int nb = c->nb, bs = c->bs, bs2 = bs * bs;
+  Timer tm(st);
+  tm.mark(0);
+  int *Mptr, *Trow;
+  BILU_TRY(c->alloc(&Mptr, nb + 1));
+  BILU_TRY(c->alloc(&Trow, nb + 1));
+  int mnnz = 0, tnnz = 0;
+  {
+    Carver w2 = ws;
+    BILU_TRY(isai_pattern_colptr_impl(nb, c->Arow, c->Acol, lower, Mptr, &mnnz, w2, st));
+  }
+  {
+    Carver w2 = ws;
+    BILU_TRY(tri_pattern_rowptr_impl(nb, c->Arow, c->Acol, lower, Trow, &tnnz, w2, st));
+  }
+  // the reference's guard (main.cu:537-546): both views must hold the same
+  // blocks, i.e. every diagonal block is stored
+  if (mnnz != tnnz) return BILU_ERR_PATTERN;
+  int *Mind, *Tcol, *map;
+  BILU_TRY(c->alloc(&Mind, mnnz));
+  BILU_TRY(c->alloc(&Tcol, tnnz));
+  BILU_TRY(c->alloc(&map, mnnz));
+  {
+    Carver w2 = ws;
+    if (!w2.take<int>(2)) return BILU_ERR_WORKSPACE;
+    BILU_TRY(isai_pattern_fill_impl(nb, c->Arow, c->Acol, lower, Mptr, Mind, mnnz, w2, st));
+  }
+  BILU_TRY(tri_pattern_fill_impl(nb, c->Arow, c->Acol, lower, Trow, Tcol, st));
+  {
+    Carver w2 = ws;
+    BILU_TRY(map_impl(nb, Mptr, Mind, Trow, Tcol, map, nullptr, w2, st));
+  }
+  tm.mark(1);
+  int *pp, *pl, *ps;
+  BILU_TRY(c->alloc(&pp, (size_t)mnnz + 1));
+  int total = 0;
+  {
+    Carver w2 = ws;
+    BILU_TRY(pairs_ptr_impl(nb, c->Arow, c->Acol, Mptr, Mind, lower, pp, mnnz, &total, nullptr,
+                            w2, st));
+  }
+  BILU_TRY(c->alloc(&pl, total));
+  BILU_TRY(c->alloc(&ps, total));
+  BILU_TRY(pairs_fill_impl(nb, c->Arow, c->Acol, Mptr, Mind, lower, pp, pl, ps, st));
+  double *Dinv, *Mcsc, *Mcsr;
+  BILU_TRY(c->alloc(&Dinv, (size_t)nb * bs2));
+  BILU_TRY(c->alloc(&Mcsc, (size_t)mnnz * bs2));
+  BILU_TRY(c->alloc(&Mcsr, (size_t)mnnz * bs2));
+  BILU_TRY(dinv_impl(nb, bs, c->Arow, c->Acol, c->LU, lower, Dinv, nullptr, st));
+  BILU_TRY(isai_impl(nb, bs, c->LU, Mptr, Mind, lower, pp, pl, ps, Dinv, Mcsc, st));
+  BILU_TRY(reorder_impl(mnnz, bs, map, Mcsc, Mcsr, st));
+  tm.mark(2);
+  *t_pattern += tm.ms(0, 1);
+  *t_isai += tm.ms(1, 2);
+  *orow = Trow;
+  *ocol = Tcol;
+  *oval = Mcsr;
+  *onnz = mnnz;
+  return BILU_OK;
+}
+
+}  // namespace
+
+extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* d_row,
+                              const int* d_col, const double* d_val, int prec_mask,
+                              double* h_times) {
+  if (!c || nb < 1 || nnzb < nb || !d_row || !d_col || !d_val) return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  cudaStream_t st = c->st;
+  c->free_setup();
+  c->nb = nb;
+  c->nnzb = nnzb;
+  c->bs = bs;
+  c->n = (long long)nb * bs;
+  size_t bs2 = (size_t)bs * bs;
+  Timer tm(st);
+  tm.mark(0);
+  BILU_TRY(c->alloc(&c->Arow, nb + 1));
+  BILU_TRY(c->alloc(&c->Acol, nnzb));
+  BILU_TRY(c->alloc(&c->Aval, nnzb * bs2));
+  BILU_TRY(c->alloc(&c->LU, nnzb * bs2));
+  BILU_TRY(c->alloc(&c->diag, nb + 1));
+  BILU_TRY_CUDA(cudaMemcpyAsync(c->Arow, d_row, sizeof(int) * (nb + 1), cudaMemcpyDeviceToDevice, st));
+  BILU_TRY_CUDA(cudaMemcpyAsync(c->Acol, d_col, sizeof(int) * nnzb, cudaMemcpyDeviceToDevice, st));
+  BILU_TRY_CUDA(cudaMemcpyAsync(c->Aval, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
+  BILU_TRY_CUDA(cudaMemcpyAsync(c->LU, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
+  // scratch shared by every step
+  size_t wsb = std::max({isai_pattern_ws(nb, nnzb), syncfree_ws(nb), pairs_ws(nnzb + nb),
+                         scan_ws_bytes(nnzb + nb + 1)}) + (1 << 16);
+  void* wsp = nullptr;
+  BILU_TRY(c->alloc((char**)&wsp, wsb));
+  Carver ws(wsp, wsb);
+  {
+    Carver w2 = ws;
+    BILU_TRY(diag_positions(nb, c->Arow, c->Acol, c->diag, nullptr, w2, st));
+  }
+  tm.mark(1);
+  {
+    Carver w2 = ws;
+    int zp = -1;
+    int rc = bilu0_impl(nb, bs, c->Arow, c->Acol, c->diag, c->LU, &zp, w2, st);
+    if (rc != BILU_OK) return rc;
+  }
+  tm.mark(2);
+  double t_pat = 0, t_isai = 0;
+  BILU_TRY(build_isai_side(c, 1, ws, &c->Lrow, &c->Lcol, &c->Lval, &c->nnzL, &t_pat, &t_isai));
+  BILU_TRY(build_isai_side(c, 0, ws, &c->Urow, &c->Ucol, &c->Uval, &c->nnzU, &t_pat, &t_isai));
+  if (prec_mask & (1 << BILU_FP32)) {
+    BILU_TRY(c->alloc(&c->Lval32, (size_t)c->nnzL * bs2));
+    BILU_TRY(c->alloc(&c->Uval32, (size_t)c->nnzU * bs2));
+    BILU_TRY(bilu_convert_f64_to_f32((size_t)c->nnzL * bs2, c->Lval, c->Lval32, st));
+    BILU_TRY(bilu_convert_f64_to_f32((size_t)c->nnzU * bs2, c->Uval, c->Uval32, st));
+  }
+  tm.mark(3);
+  double t_factor = tm.ms(1, 2), t_total = tm.ms(0, 3);
+  BILU_TRY_CUDA(cudaStreamSynchronize(st));
+  if (h_times) {
+    h_times[0] = t_factor;
+    h_times[1] = t_pat;
+    h_times[2] = t_isai;
+    h_times[3] = t_total;
+  }
+  c->ready = true;
+  return BILU_OK;
+}
+
+extern "C" int bilu_ctx_get(bilu_ctx* c, int which, const void** d_ptr, long long* h_count) {
+  if (!c || !d_ptr || !c->ready) return BILU_ERR_ARG;
+  long long bs2 = (long long)c->bs * c->bs;
+  const void* p = nullptr;
+  long long cnt = 0;
+  switch (which) {
+    case 0: p = c->LU; cnt = c->nnzb * bs2; break;
+    case 1: p = c->Lrow; cnt = c->nb + 1; break;
+    case 2: p = c->Lcol; cnt = c->nnzL; break;
+    case 3: p = c->Lval; cnt = c->nnzL * bs2; break;
+    case 4: p = c->Urow; cnt = c->nb + 1; break;
+    case 5: p = c->Ucol; cnt = c->nnzU; break;
+    case 6: p = c->Uval; cnt = c->nnzU * bs2; break;
+    case 7: p = c->Lval32; cnt = c->Lval32 ? c->nnzL * bs2 : 0; break;
+    case 8: p = c->Uval32; cnt = c->Uval32 ? c->nnzU * bs2 : 0; break;
+    default: return BILU_ERR_ARG;
+  }
+  *d_ptr = p;
+  if (h_count) *h_count = cnt;
+  return BILU_OK;
+}
+
+namespace {
+
+int ensure_solver(bilu_ctx* c, int m) {
+  if (c->m_alloc >= m && c->V) return BILU_OK;
+  c->free_solver();
+  size_t n = (size_t)c->n;
+  BILU_TRY_CUDA(cudaMalloc(&c->V, sizeof(double) * n * (m + 1)));
+  BILU_TRY_CUDA(cudaMalloc(&c->Z, sizeof(double) * n * m));
+  BILU_TRY_CUDA(cudaMalloc(&c->w, sizeof(double) * n));
+  BILU_TRY_CUDA(cudaMalloc(&c->r, sizeof(double) * n));
+  BILU_TRY_CUDA(cudaMalloc(&c->tmp, sizeof(double) * n));
+  BILU_TRY_CUDA(cudaMalloc(&c->partial, sizeof(double) * kRedCTAs * kPartStride));
+  BILU_TRY_CUDA(cudaMalloc(&c->dscal, sizeof(double) * 6 * kPartStride));
+  BILU_TRY_CUDA(cudaMalloc(&c->dcoef, sizeof(double) * kPartStride));
+  BILU_TRY_CUDA(cudaMallocHost(&c->hpin, sizeof(double) * 6 * kPartStride));
+  c->m_alloc = m;
+  return BILU_OK;
+}
+
+// ||v||^2 into dscal[slot] (device) and, if host != null, to the host.
+int norm2(bilu_ctx* c, const double* v, double* dslot, double* host) {
+  BILU_TRY(multidot(c->n, nullptr, 0, 0, v, true, c->partial, c->st));
+  BILU_TRY(reduce_partials(c->partial, 1, dslot, c->st));
+  if (host) {
+    BILU_TRY_CUDA(cudaMemcpyAsync(host, dslot, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    BILU_TRY_CUDA(cudaStreamSynchronize(c->st));
+  }
+  return BILU_OK;
+}
+
+int apply_prec(bilu_ctx* c, int prec, const double* v, double* z) {
+  if (prec < 0) {
+    BILU_TRY_CUDA(cudaMemcpyAsync(z, v, sizeof(double) * c->n, cudaMemcpyDeviceToDevice, c->st));
+    return BILU_OK;
+  }
+  const void* L = prec == BILU_FP32 ? (const void*)c->Lval32 : (const void*)c->Lval;
+  const void* U = prec == BILU_FP32 ? (const void*)c->Uval32 : (const void*)c->Uval;
+  if (!L || !U) return BILU_ERR_ARG;
+  return isai_apply_impl(c->nb, c->bs, prec, c->Lrow, c->Lcol, L, c->Urow, c->Ucol, U, v, c->tmp,
+                         z, c->st);
+}
+
+}  // namespace
+
+extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* d_x, int restart,
+                              double tol, int maxit, int* h_iters, double* h_relres,
+                              double* h_hist) {
+  if (!c || !c->ready || !d_b || !d_x || restart < 1 || restart > kMaxVec - 1 || maxit < 0)
+    return BILU_ERR_ARG;
+  if (prec != -1 && prec != BILU_FP64 && prec != BILU_FP32) return BILU_ERR_ARG;
+  BILU_TRY(ensure_solver(c, restart));
+  cudaStream_t st = c->st;
+  const int m = restart;
+  const long long n = c->n;
+  double* s = c->dscal;
+  double* hp = c->hpin;
+  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m);
+  BILU_TRY_CUDA(cudaMemsetAsync(d_x, 0, sizeof(double) * n, st));
+  double bb = 0;
+  BILU_TRY(norm2(c, d_b, s, &bb));
+  double bnorm = std::sqrt(bb);
+  if (bnorm == 0.0) bnorm = 1.0;
+  BILU_TRY_CUDA(cudaMemcpyAsync(c->r, d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  double rr = 0;
+  BILU_TRY(norm2(c, c->r, s + 5 * kPartStride, &rr));
+  double beta = std::sqrt(rr);
+  int total = 0, status = BILU_ERR_NOT_CONVERGED;
+  double res = beta / bnorm;
+  if (h_hist) h_hist[0] = res;
+  if (res <= tol) status = BILU_OK;
+  while (status != BILU_OK && total < maxit) {
+    // V_0 = r / beta (beta^2 sits in s[5*kPartStride])
+    BILU_TRY(scale_rsqrt(n, c->r, s + 5 * kPartStride, c->V, st));
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int jlast = -1;
+    for (int j = 0; j < m && total < maxit; ++j) {
+      double* vj = c->V + (size_t)n * j;
+      double* zj = c->Z + (size_t)n * j;
+      BILU_TRY(apply_prec(c, prec, vj, zj));
+      BILU_TRY(spmv_any(c->nb, c->bs, BILU_FP64, c->Arow, c->Acol, c->Aval, zj, 0, c->w, 0, st));
+      int nv = j + 1;
+      // pass 1: h = V^T w and w.w, then w -= V h with ||w||^2
+      BILU_TRY(multidot(n, c->V, n, nv, c->w, true, c->partial, st));
+      BILU_TRY(reduce_partials(c->partial, nv + 1, s, st));
+      BILU_TRY(multiaxpy_norm(n, c->V, n, nv, s, -1.0, c->w, c->partial, nullptr, st));
+      BILU_TRY(reduce_partials(c->partial, 1, s + kPartStride, st));
+      k_dgks_select<<<1, 1, 0, st>>>(s, nv);
+      BILU_LAUNCH_CHECK();
+      const int* flag = (const int*)(s + 4 * kPartStride);
+      // pass 2 (reorthogonalisation) runs only when the DGKS test fired;
+      // its kernels read the device flag and return early otherwise
+      BILU_TRY(multidot(n, c->V, n, nv, c->w, false, c->partial, st, flag));
+      BILU_TRY(reduce_partials(c->partial, nv, s + 2 * kPartStride, st));
+      BILU_TRY(multiaxpy_norm(n, c->V, n, nv, s + 2 * kPartStride, -1.0, c->w, c->partial, flag,
+                              st));
+      BILU_TRY(reduce_partials(c->partial, 1, s + 3 * kPartStride, st));
+      k_pick_norm<<<1, 1, 0, st>>>(s);
+      BILU_LAUNCH_CHECK();
+      BILU_TRY(scale_rsqrt(n, c->w, s + 5 * kPartStride, c->V + (size_t)n * (j + 1), st));
+      BILU_TRY_CUDA(cudaMemcpyAsync(hp, s, sizeof(double) * 6 * kPartStride,
+                                    cudaMemcpyDeviceToHost, st));
+      BILU_TRY_CUDA(cudaStreamSynchronize(st));
+      int fl = ((const int*)(hp + 4 * kPartStride))[0];
+      for (int i = 0; i <= j; ++i) {
+        double h = 0.0 + hp[i];
+        if (fl) h += hp[2 * kPartStride + i];
+        H[(size_t)i * m + j] = h;
+      }
+      double hn = std::sqrt(hp[5 * kPartStride]);
+      H[(size_t)(j + 1) * m + j] = hn;
+      for (int i = 0; i < j; ++i) {
+        double a = H[(size_t)i * m + j], b = H[(size_t)(i + 1) * m + j];
+        H[(size_t)i * m + j] = cs[i] * a + sn[i] * b;
+        H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * b;
+      }
+      double a = H[(size_t)j * m + j], b = H[(size_t)(j + 1) * m + j];
+      double den = std::sqrt(a * a + b * b);
+      cs[j] = den != 0.0 ? a / den : 1.0;
+      sn[j] = den != 0.0 ? b / den : 0.0;
+      H[(size_t)j * m + j] = cs[j] * a + sn[j] * b;
+      H[(size_t)(j + 1) * m + j] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      ++total;
+      jlast = j;
+      res = std::fabs(g[j + 1]) / bnorm;
+      if (h_hist) h_hist[total] = res;
+      if (res <= tol || hn == 0.0) break;
+    }
+    for (int i = jlast; i >= 0; --i) {
+      double v = g[i];
+      for (int k = i + 1; k <= jlast; ++k) v -= H[(size_t)i * m + k] * y[k];
+      y[i] = v / H[(size_t)i * m + i];
+    }
+    if (jlast >= 0) {
+      BILU_TRY_CUDA(cudaMemcpyAsync(c->dcoef, y.data(), sizeof(double) * (jlast + 1),
+                                    cudaMemcpyHostToDevice, st));
+      BILU_TRY(multiaxpy_norm(n, c->Z, n, jlast + 1, c->dcoef, 1.0, d_x, nullptr, nullptr, st));
+    }
+    BILU_TRY(spmv_any(c->nb, c->bs, BILU_FP64, c->Arow, c->Acol, c->Aval, d_x, 0, c->w, 0, st));
+    BILU_TRY(residual_norm(n, d_b, c->w, c->r, c->partial, st));
+    BILU_TRY(reduce_partials(c->partial, 1, s + 5 * kPartStride, st));
+    BILU_TRY_CUDA(cudaMemcpyAsync(&rr, s + 5 * kPartStride, sizeof(double), cudaMemcpyDeviceToHost, st));
+    BILU_TRY_CUDA(cudaStreamSynchronize(st));
+    beta = std::sqrt(rr);
+    res = beta / bnorm;
+    if (res <= tol) status = BILU_OK;
+    if (beta == 0.0) break;
+  }
+  if (h_iters) *h_iters = total;
+  if (h_relres) *h_relres = res;
+  return status;
+}
+
+extern "C" int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const int* h_col,
+                               const double* h_val, const double* h_b, double* h_x, int prec,
+                               int restart, double tol, int maxit, int* h_iters, double* h_relres,
+                               double* h_times, bilu_stream_t stream) {
+  if (nb < 1 || nnzb < 1 || !h_row || !h_col || !h_val || !h_b || !h_x) return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  cudaStream_t st = S(stream);
+  size_t bs2 = (size_t)bs * bs, n = (size_t)nb * bs;
+  int *row = nullptr, *col = nullptr;
+  double *val = nullptr, *b = nullptr, *x = nullptr;
+  bilu_ctx* c = nullptr;
+  int rc = BILU_OK;
+  auto cu = [&](cudaError_t e) {
+    if (rc == BILU_OK && e != cudaSuccess) rc = cuda_status(e);
+  };
+  cu(cudaMallocAsync(&row, sizeof(int) * (nb + 1), st));
+  cu(cudaMallocAsync(&col, sizeof(int) * nnzb, st));
+  cu(cudaMallocAsync(&val, sizeof(double) * nnzb * bs2, st));
+  cu(cudaMallocAsync(&b, sizeof(double) * n, st));
+  cu(cudaMallocAsync(&x, sizeof(double) * n, st));
+  if (rc == BILU_OK) {
+    cu(cudaMemcpyAsync(row, h_row, sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, st));
+    cu(cudaMemcpyAsync(col, h_col, sizeof(int) * nnzb, cudaMemcpyHostToDevice, st));
+    cu(cudaMemcpyAsync(val, h_val, sizeof(double) * nnzb * bs2, cudaMemcpyHostToDevice, st));
+    cu(cudaMemcpyAsync(b, h_b, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  }
+  if (rc == BILU_OK) rc = bilu_ctx_create(&c, stream);
+  if (rc == BILU_OK)
+    rc = bilu_ctx_setup(c, nb, nnzb, bs, row, col, val,
+                        prec == BILU_FP32 ? (1 << BILU_FP32) : 0, h_times);
+  int src = BILU_OK;
+  if (rc == BILU_OK) {
+    src = bilu_ctx_solve(c, prec, b, x, restart, tol, maxit, h_iters, h_relres, nullptr);
+    if (src != BILU_OK && src != BILU_ERR_NOT_CONVERGED) rc = src;
+  }
+  if (rc == BILU_OK) {
+    cu(cudaMemcpyAsync(h_x, x, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    cu(cudaStreamSynchronize(st));
+  }
+  bilu_ctx_destroy(c);
+  cudaFreeAsync(row, st);
+  cudaFreeAsync(col, st);
+  cudaFreeAsync(val, st);
+  cudaFreeAsync(b, st);
+  cudaFreeAsync(x, st);
+  cudaStreamSynchronize(st);
+  return rc != BILU_OK ? rc : src;
+}

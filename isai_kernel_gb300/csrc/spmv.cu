@@ -1,0 +1,296 @@
+// BSR SpMV / SpMM and the ISAI preconditioner apply (sm_103a).
+//
+// Replaces bcsr_spmv (bcsc2bcsrAndSpMV.h:49, thread per block row, scalar
+// loops) and the DMMA variants of bsr_tensor_SpMV.h:21-400.  On GB300 the FP64
+// pipe (measured 1.2 TFLOP/s DFMA, 1.05 TFLOP/s DMMA m8n8k4) is the binding
+// limit of an FP64 BSR SpMV (1 DFMA per 8 B of values), so the layout spends
+// FP64 instructions only on the block products: one lane per scalar row
+// accumulates across every block of its block row and needs no reduction.
+// The bs lanes of a block row read the bs rows of each block, so every block
+// (bs*bs*8 bytes) is fetched in whole 32-byte sectors by one group, and the x
+// segment is a broadcast within the group.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace bilu {
+
+namespace {
+
+template <class T>
+struct Vec;
+template <>
+struct Vec<double> {
+  static constexpr int W = 2;
+  using V = double2;
+};
+template <>
+struct Vec<float> {
+  static constexpr int W = 4;
+  using V = float4;
+};
+
+__device__ __forceinline__ double to_acc(double v, double) { return v; }
+__device__ __forceinline__ double to_acc(float v, double) { return (double)v; }
+__device__ __forceinline__ float to_acc(double v, float) { return (float)v; }
+__device__ __forceinline__ float to_acc(float v, float) { return v; }
+
+// Load the BS-long x segment of block column bc into registers (AccT).
+template <int BS, class XT, class AccT>
+__device__ __forceinline__ void load_x(const XT* __restrict__ x, long long bc, AccT* xr) {
+  const XT* p = x + bc * BS;
+#pragma unroll
+  for (int c = 0; c < BS; ++c) xr[c] = to_acc(__ldg(p + c), AccT());
+}
+
+// Row r of block p (BS values) into registers, streaming loads.
+template <int BS, class VT, class AccT>
+__device__ __forceinline__ void load_row(const VT* __restrict__ val, long long p, int r, AccT* a) {
+  const VT* q = val + (p * BS + r) * BS;
+  constexpr int W = Vec<VT>::W;
+  if constexpr (BS % W == 0) {
+    using V = typename Vec<VT>::V;
+#pragma unroll
+    for (int c = 0; c < BS / W; ++c) {
+      V v = ld_stream(reinterpret_cast<const V*>(q) + c);
+      if constexpr (W == 2) {
+        a[2 * c] = to_acc(v.x, AccT());
+        a[2 * c + 1] = to_acc(v.y, AccT());
+      } else {
+        a[4 * c] = to_acc(v.x, AccT());
+        a[4 * c + 1] = to_acc(v.y, AccT());
+        a[4 * c + 2] = to_acc(v.z, AccT());
+        a[4 * c + 3] = to_acc(v.w, AccT());
+      }
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < BS; ++c) a[c] = to_acc(ld_stream(q + c), AccT());
+  }
+}
+
+// y = M x: lane group of BS lanes per block row, lane r owns scalar row r.
+// Two blocks per loop trip keep two independent block loads in flight.
+template <int BS, class VT, class XT, class YT, class AccT>
+__global__ void __launch_bounds__(256) k_bsr_spmv(int mb, const int* __restrict__ row,
+                                                  const int* __restrict__ col,
+                                                  const VT* __restrict__ val,
+                                                  const XT* __restrict__ x, YT* __restrict__ y) {
+  constexpr int G = 32 / BS;  // block rows per warp
+  int lane = threadIdx.x & 31;
+  int g = lane / BS, r = lane - g * BS;
+  long long br = ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G + g;
+  if (g >= G || br >= mb) return;
+  int s = __ldg(row + br), e = __ldg(row + br + 1);
+  AccT acc0 = 0, acc1 = 0;
+  int p = s;
+  for (; p + 1 < e; p += 2) {
+    AccT a0[BS], a1[BS], x0[BS], x1[BS];
+    int c0 = __ldg(col + p), c1 = __ldg(col + p + 1);
+    load_row<BS, VT, AccT>(val, p, r, a0);
+    load_row<BS, VT, AccT>(val, p + 1, r, a1);
+    load_x<BS, XT, AccT>(x, c0, x0);
+    load_x<BS, XT, AccT>(x, c1, x1);
+#pragma unroll
+    for (int c = 0; c < BS; ++c) {
+      acc0 = fma(a0[c], x0[c], acc0);
+      acc1 = fma(a1[c], x1[c], acc1);
+    }
+  }
+  if (p < e) {
+    AccT a0[BS], x0[BS];
+    load_row<BS, VT, AccT>(val, p, r, a0);
+    load_x<BS, XT, AccT>(x, __ldg(col + p), x0);
+#pragma unroll
+    for (int c = 0; c < BS; ++c) acc0 = fma(a0[c], x0[c], acc0);
+  }
+  y[br * BS + r] = (YT)(acc0 + acc1);
+}
+
+template <int BS, class VT, class XT, class YT>
+int launch_spmv(int mb, const int* row, const int* col, const VT* val, const XT* x, YT* y,
+                cudaStream_t st) {
+  using AccT = VT;
+  if (mb == 0) return BILU_OK;
+  constexpr int G = 32 / BS;
+  long long warps = (mb + G - 1) / G;
+  unsigned grid = ceil_div(warps, 8);
+  k_bsr_spmv<BS, VT, XT, YT, AccT><<<grid, 256, 0, st>>>(mb, row, col, val, x, y);
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
+}
+
+// Multi-RHS: Y[n,k] = M X[n,k], row-major with ld = k.  One warp per block
+// row; lane c (and c+32) owns right-hand side c; blocks are broadcast reads.
+template <int BS, class VT, int KW>
+__global__ void __launch_bounds__(256) k_bsr_spmm(int mb, int k, const int* __restrict__ row,
+                                                  const int* __restrict__ col,
+                                                  const VT* __restrict__ val,
+                                                  const double* __restrict__ X,
+                                                  double* __restrict__ Y) {
+  using AccT = VT;
+  int lane = threadIdx.x & 31;
+  long long br = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (br >= mb) return;
+  AccT acc[KW][BS];
+#pragma unroll
+  for (int w = 0; w < KW; ++w)
+#pragma unroll
+    for (int r = 0; r < BS; ++r) acc[w][r] = 0;
+  int s = row[br], e = row[br + 1];
+  for (int p = s; p < e; ++p) {
+    long long bc = col[p];
+    const VT* blk = val + (long long)p * BS * BS;
+#pragma unroll
+    for (int kk = 0; kk < BS; ++kk) {
+      AccT xv[KW];
+#pragma unroll
+      for (int w = 0; w < KW; ++w) {
+        int c = lane + 32 * w;
+        xv[w] = c < k ? (AccT)X[(bc * BS + kk) * k + c] : (AccT)0;
+      }
+#pragma unroll
+      for (int r = 0; r < BS; ++r) {
+        AccT a = (AccT)blk[r * BS + kk];
+#pragma unroll
+        for (int w = 0; w < KW; ++w) acc[w][r] = fma(a, xv[w], acc[w][r]);
+      }
+    }
+  }
+#pragma unroll
+  for (int w = 0; w < KW; ++w) {
+    int c = lane + 32 * w;
+    if (c < k)
+#pragma unroll
+      for (int r = 0; r < BS; ++r) Y[(br * BS + r) * k + c] = (double)acc[w][r];
+  }
+}
+
+template <int BS, class VT>
+int launch_spmm(int mb, int k, const int* row, const int* col, const VT* val, const double* X,
+                double* Y, cudaStream_t st) {
+  if (mb == 0) return BILU_OK;
+  unsigned grid = ceil_div(mb, 8);
+  if (k <= 32)
+    k_bsr_spmm<BS, VT, 1><<<grid, 256, 0, st>>>(mb, k, row, col, val, X, Y);
+  else
+    k_bsr_spmm<BS, VT, 2><<<grid, 256, 0, st>>>(mb, k, row, col, val, X, Y);
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
+}
+
+__global__ void k_f64_to_f32(size_t n, const double* __restrict__ s, float* __restrict__ d) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) d[i] = __double2float_rn(s[i]);
+}
+
+template <int BS>
+int spmv_f64(int mb, const int* row, const int* col, const double* val, const double* x,
+             double* y, cudaStream_t st) {
+  return launch_spmv<BS, double, double, double>(mb, row, col, val, x, y, st);
+}
+
+template <int BS>
+int spmv_f32(int mb, const int* row, const int* col, const float* val, const void* x, int x32,
+             void* y, int y32, cudaStream_t st) {
+  if (x32 && y32)
+    return launch_spmv<BS, float, float, float>(mb, row, col, val, (const float*)x, (float*)y, st);
+  if (x32)
+    return launch_spmv<BS, float, float, double>(mb, row, col, val, (const float*)x, (double*)y,
+                                                 st);
+  if (y32)
+    return launch_spmv<BS, float, double, float>(mb, row, col, val, (const double*)x, (float*)y,
+                                                 st);
+  return launch_spmv<BS, float, double, double>(mb, row, col, val, (const double*)x, (double*)y,
+                                                st);
+}
+
+template <int BS>
+int spmm_f64(int mb, int k, const int* row, const int* col, const double* val, const double* X,
+             double* Y, cudaStream_t st) {
+  return launch_spmm<BS, double>(mb, k, row, col, val, X, Y, st);
+}
+template <int BS>
+int spmm_f32(int mb, int k, const int* row, const int* col, const float* val, const double* X,
+             double* Y, cudaStream_t st) {
+  return launch_spmm<BS, float>(mb, k, row, col, val, X, Y, st);
+}
+
+}  // namespace
+
+// internal entry points used by the solver
+int spmv_any(int mb, int bs, int prec, const int* row, const int* col, const void* val,
+             const void* x, int x32, void* y, int y32, cudaStream_t st) {
+  if (prec == BILU_FP64) {
+    if (x32 || y32) return BILU_ERR_ARG;
+    return BILU_DISPATCH_BS(bs, spmv_f64, mb, row, col, (const double*)val, (const double*)x,
+                            (double*)y, st);
+  }
+  return BILU_DISPATCH_BS(bs, spmv_f32, mb, row, col, (const float*)val, x, x32, y, y32, st);
+}
+
+int isai_apply_impl(int nb, int bs, int prec, const int* Lrow, const int* Lcol, const void* Lval,
+                    const int* Urow, const int* Ucol, const void* Uval, const double* b,
+                    void* tmp, double* x, cudaStream_t st) {
+  int tmp32 = prec == BILU_FP32;
+  BILU_TRY(spmv_any(nb, bs, prec, Lrow, Lcol, Lval, b, 0, tmp, tmp32, st));
+  return spmv_any(nb, bs, prec, Urow, Ucol, Uval, tmp, tmp32, x, 0, st);
+}
+
+}  // namespace bilu
+
+using namespace bilu;
+
+extern "C" int bilu_bcsr_spmv(int mb, int bs, const int* d_row, const int* d_col,
+                              const double* d_val, const double* d_x, double* d_y,
+                              bilu_stream_t stream) {
+  if (mb < 0 || (mb > 0 && (!d_row || !d_col || !d_val || !d_x || !d_y))) return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  return spmv_any(mb, bs, BILU_FP64, d_row, d_col, d_val, d_x, 0, d_y, 0, S(stream));
+}
+
+extern "C" int bilu_bcsr_spmv_f32(int mb, int bs, const int* d_row, const int* d_col,
+                                  const float* d_val, const void* d_x, int x_fp32, void* d_y,
+                                  int y_fp32, bilu_stream_t stream) {
+  if (mb < 0 || (mb > 0 && (!d_row || !d_col || !d_val || !d_x || !d_y))) return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  return spmv_any(mb, bs, BILU_FP32, d_row, d_col, d_val, d_x, x_fp32 != 0, d_y, y_fp32 != 0,
+                  S(stream));
+}
+
+extern "C" int bilu_bcsr_spmm(int mb, int bs, int k, const int* d_row, const int* d_col,
+                              const double* d_val, const double* d_X, double* d_Y,
+                              bilu_stream_t stream) {
+  if (mb < 0 || k < 1 || k > 64) return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  return BILU_DISPATCH_BS(bs, spmm_f64, mb, k, d_row, d_col, d_val, d_X, d_Y, S(stream));
+}
+
+extern "C" int bilu_bcsr_spmm_f32(int mb, int bs, int k, const int* d_row, const int* d_col,
+                                  const float* d_val, const double* d_X, double* d_Y,
+                                  bilu_stream_t stream) {
+  if (mb < 0 || k < 1 || k > 64) return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  return BILU_DISPATCH_BS(bs, spmm_f32, mb, k, d_row, d_col, d_val, d_X, d_Y, S(stream));
+}
+
+extern "C" int bilu_convert_f64_to_f32(size_t count, const double* d_src, float* d_dst,
+                                       bilu_stream_t stream) {
+  if (count == 0) return BILU_OK;
+  if (!d_src || !d_dst) return BILU_ERR_ARG;
+  unsigned grid = (unsigned)std::min<size_t>((count + 255) / 256, 152 * 16);
+  k_f64_to_f32<<<grid, 256, 0, S(stream)>>>(count, d_src, d_dst);
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
+}
+
+extern "C" int bilu_isai_apply(int nb, int bs, int prec, const int* d_Lrow, const int* d_Lcol,
+                               const void* d_Lval, const int* d_Urow, const int* d_Ucol,
+                               const void* d_Uval, const double* d_b, void* d_tmp, double* d_x,
+                               bilu_stream_t stream) {
+  if (nb < 0 || (prec != BILU_FP64 && prec != BILU_FP32)) return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  return isai_apply_impl(nb, bs, prec, d_Lrow, d_Lcol, d_Lval, d_Urow, d_Ucol, d_Uval, d_b,
+                         d_tmp, d_x, S(stream));
+}

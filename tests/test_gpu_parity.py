@@ -1,0 +1,392 @@
+"""GPU parity: every CUDA entry point, called through the C ABI
+(libbilu_isai.so via ctypes), against the CPU oracle and the golden vectors
+of the reference's own host code.
+
+Tolerances: integer / index / pattern / copy outputs bit-exact; FP64 factors,
+inverses, ISAI values and triangular solves within 1e-12 relative (max abs
+difference over max abs value); FP64 SpMV within 1e-13 relative; FP32-stored
+SpMV within 2e-6 relative of the FP32 oracle; FP64 GMRES takes exactly the
+oracle's iteration count."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from isai_kernel_gb300 import gen
+
+pytestmark = pytest.mark.gpu
+
+MATS = ["laplace2d_s12", "convdiff3d_s5", "powerlaw_nb120", "laplace2d_s9_bs5"]
+
+
+def T(a, dev):
+    import torch
+
+    a = np.ascontiguousarray(a)
+    return torch.from_numpy(a).to(dev)
+
+
+def N(t):
+    return t.detach().cpu().numpy()
+
+
+def relerr(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)) if b.size else 0.0
+
+
+def mats():
+    return {
+        "c1_s16": gen.laplace2d(16, bs=4, seed=0),
+        "c2_s6": gen.convdiff3d(6, bs=4, seed=0),
+        "c3_nb200": gen.powerlaw(200, bs=8, seed=0, kmax=30),
+        "bs5_s7": gen.laplace2d(7, bs=5, seed=2),
+    }
+
+
+# ------------------------------------------------------------------ formats
+@pytest.mark.parametrize("bs", [4, 5, 8])
+def test_csr_to_bsr_golden(cuda, bs):
+    from isai_kernel_gb300 import api
+
+    g = golden(f"c2b_bs{bs}")
+    nb, r, c, v = api.csr_to_bsr5(int(g["n"]), bs, T(g["csr_row"], cuda), T(g["csr_col"], cuda),
+                                  T(g["csr_val"], cuda))
+    assert np.array_equal(N(r), g["bsr_row"]) and np.array_equal(N(c), g["bsr_col"])
+    assert np.array_equal(N(v), g["bsr_val"])
+
+
+@pytest.mark.parametrize("name", MATS)
+def test_patterns_map_golden(cuda, name):
+    from isai_kernel_gb300 import api
+
+    g = golden(name)
+    nb = int(g["nb"])
+    row, col = T(g["row"], cuda), T(g["col"], cuda)
+    for lower, tag in ((True, "L"), (False, "U")):
+        mp, mi = api.build_bcsc_pattern_from_bsr_scalarILU(nb, row, col, lower)
+        assert np.array_equal(N(mp), g[f"Mptr{tag}"]) and np.array_equal(N(mi), g[f"Mind{tag}"])
+        tr, tc = api.build_triangular_bcsr_pattern_from_A(nb, row, col, lower)
+        assert np.array_equal(N(tr), g[f"Trow{tag}"]) and np.array_equal(N(tc), g[f"Tcol{tag}"])
+        m = api.build_map_bcsc2bcsr_host(nb, mp, mi, tr, tc)
+        assert np.array_equal(N(m), g[f"map{tag}"])
+
+
+@pytest.mark.parametrize("name", MATS)
+def test_spmv_reorder_bcsc_golden(cuda, name):
+    from isai_kernel_gb300 import api
+
+    g = golden(name)
+    nb, bs = int(g["nb"]), int(g["bs"])
+    y = api.bcsr_spmv(nb, bs, T(g["row"], cuda), T(g["col"], cuda), T(g["val"], cuda),
+                      T(g["x"], cuda))
+    assert relerr(N(y), g["spmv_y"]) < 1e-13
+    vals = api.reorder_bcsc_val_to_bcsr(T(g["mapL"], cuda), T(g["bcsc_val"], cuda))
+    yb = api.bcsr_spmv(nb, bs, T(g["TrowL"], cuda), T(g["TcolL"], cuda), vals, T(g["x"], cuda))
+    assert relerr(N(yb), g["bcsc_y"]) < 1e-13
+    rp, ci, v = api.bcsc_to_bcsr(nb, nb, bs, T(g["MptrL"], cuda), T(g["MindL"], cuda),
+                                 T(g["bcsc_val"], cuda))
+    assert np.array_equal(N(rp), g["TrowL"]) and np.array_equal(N(ci), g["TcolL"])
+    assert np.array_equal(N(v), N(vals))
+
+
+@pytest.mark.parametrize("name", list(mats()))
+def test_bsr2csr_and_back(cuda, orc, name):
+    from isai_kernel_gb300 import api
+
+    A = mats()[name]
+    rp, ci, v = api.bsr2csr(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda))
+    orp, oci, ov = orc.bsr_to_csr(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    assert np.array_equal(N(rp), orp) and np.array_equal(N(ci), oci) and np.array_equal(N(v), ov)
+    nb, r2, c2, v2 = api.csr_to_bsr5(A.n, A.bs, rp, ci, v)
+    assert np.array_equal(N(r2), A.rowptr) and np.array_equal(N(c2), A.colind)
+    assert np.array_equal(N(v2), A.val)
+
+
+def test_transpose_view(cuda):
+    from isai_kernel_gb300 import api
+
+    A = gen.powerlaw(150, bs=8, seed=5, kmax=25)
+    tr, tc, tv = api.bsr_transpose(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda))
+    At = gen.BSRMatrix(A.nb, A.bs, N(tr), N(tc), N(tv))
+    assert np.array_equal(At.to_dense(), A.to_dense().T)
+
+
+# ------------------------------------------------------------------ factor + ISAI
+@pytest.mark.parametrize("name", list(mats()))
+def test_bilu0_matches_oracle(cuda, orc, name):
+    from isai_kernel_gb300 import api
+
+    A = mats()[name]
+    ref, zp = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    v = T(A.val, cuda).clone()
+    info = api.bsrilu02_inplace(A.nb, A.nnzb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), v)
+    assert info == zp == -1
+    assert relerr(N(v), ref) < 1e-12
+
+
+@pytest.mark.parametrize("name", list(mats()))
+def test_isai_setup_matches_oracle(cuda, orc, name):
+    """Dinv, pair lists and ISAI-L/U values on the oracle's factor."""
+    from isai_kernel_gb300 import api
+
+    A = mats()[name]
+    S = orc.isai_setup(A)
+    row, col, LU = T(A.rowptr, cuda), T(A.colind, cuda), T(S["LU"], cuda)
+    for lower, tag in ((True, "L"), (False, "U")):
+        D = api.build_Dinv(A.nb, A.bs, row, col, LU, lower)
+        assert relerr(N(D), S[f"Dinv{tag}"]) < 1e-12
+        mp, mi = T(S[f"Mptr{tag}"], cuda), T(S[f"Mind{tag}"], cuda)
+        pp, pl, ps, nmax = api.build_pairs(A.nb, row, col, mp, mi, lower)
+        assert nmax == int(np.diff(S[f"Mptr{tag}"]).max())
+        if lower:
+            assert np.array_equal(N(pp), S["PairPtr"])
+            assert np.array_equal(N(pl), S["PairPLocal"]) and np.array_equal(N(ps), S["PairSrc"])
+        M = api.isai_compute(A.nb, A.bs, LU, mp, mi, pp, pl, ps, D, lower)
+        assert relerr(N(M), S[f"Mcsc{tag}"]) < 1e-12
+
+
+def test_upper_pairs_definition(cuda, orc):
+    """M_U pair list: for entry idx of column j, every p > idx (descending)
+    whose block U(t, S_j[p]) is stored, with its BSR position."""
+    from isai_kernel_gb300 import api
+
+    A = gen.powerlaw(90, bs=8, seed=3, kmax=20)
+    mp, mi = orc.isai_pattern(A.nb, A.rowptr, A.colind, False)
+    pp, pl, ps, _ = api.build_pairs(A.nb, T(A.rowptr, cuda), T(A.colind, cuda), T(mp, cuda),
+                                    T(mi, cuda), False)
+    pp, pl, ps = N(pp), N(pl), N(ps)
+    for j in range(A.nb):
+        s, e = mp[j], mp[j + 1]
+        for idx in range(e - s):
+            t = mi[s + idx]
+            want = []
+            for p in range(e - s - 1, idx, -1):
+                hit = np.nonzero(A.colind[A.rowptr[t]:A.rowptr[t + 1]] == mi[s + p])[0]
+                if hit.size:
+                    want.append((p, A.rowptr[t] + hit[0]))
+            got = list(zip(pl[pp[s + idx]:pp[s + idx + 1]], ps[pp[s + idx]:pp[s + idx + 1]]))
+            assert got == want
+
+
+# ------------------------------------------------------------------ apply
+@pytest.mark.parametrize("name", list(mats()))
+def test_spmv_fp64_fp32(cuda, orc, name):
+    import torch
+    from isai_kernel_gb300 import api
+
+    A = mats()[name]
+    x = gen.rhs(A.n, 11)
+    row, col = T(A.rowptr, cuda), T(A.colind, cuda)
+    y = api.bcsr_spmv(A.nb, A.bs, row, col, T(A.val, cuda), T(x, cuda))
+    assert relerr(N(y), orc.bcsr_spmv(A.nb, A.bs, A.rowptr, A.colind, A.val, x)) < 1e-13
+    v32 = A.val.astype(np.float32)
+    y32 = orc.bcsr_spmv_f32(A.nb, A.bs, A.rowptr, A.colind, v32, x.astype(np.float32))
+    for xt, yt in ((torch.float32, torch.float32), (torch.float64, torch.float64),
+                   (torch.float32, torch.float64), (torch.float64, torch.float32)):
+        xin = T(x, cuda).to(xt)
+        out = torch.empty(A.n, dtype=yt, device=cuda)
+        api.bcsr_spmv(A.nb, A.bs, row, col, T(v32, cuda), xin, out)
+        ref = y32 if xt == torch.float32 else orc.bcsr_spmv_f32(
+            A.nb, A.bs, A.rowptr, A.colind, v32, x.astype(np.float32))
+        assert relerr(N(out), ref) < 2e-6
+
+
+@pytest.mark.parametrize("k", [1, 8, 32, 40])
+def test_spmm_matches_spmv_columns(cuda, orc, k):
+    from isai_kernel_gb300 import api
+
+    A = gen.laplace2d(12, bs=4, seed=1)
+    X = gen.rhs(A.n, 4, k=k) if k > 1 else gen.rhs(A.n, 4).reshape(-1, 1)
+    row, col, val = T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda)
+    Y = N(api.bcsr_spmm(A.nb, A.bs, row, col, val, T(X, cuda)))
+    for c in range(k):
+        ref = orc.bcsr_spmv(A.nb, A.bs, A.rowptr, A.colind, A.val, np.ascontiguousarray(X[:, c]))
+        assert relerr(Y[:, c], ref) < 1e-13
+    Y32 = N(api.bcsr_spmm(A.nb, A.bs, row, col, val.float(), T(X, cuda)))
+    ref32 = orc.bcsr_spmv_f32(A.nb, A.bs, A.rowptr, A.colind, A.val.astype(np.float32),
+                              np.ascontiguousarray(X[:, 0]).astype(np.float32))
+    assert relerr(Y32[:, 0], ref32) < 1e-5
+
+
+def test_spmv_transpose_and_outer(cuda):
+    from isai_kernel_gb300 import api
+
+    A = gen.powerlaw(100, bs=8, seed=9, kmax=20)
+    D = A.to_dense()
+    x, u = gen.rhs(A.n, 1), gen.rhs(A.n, 2)
+    row, col, val = T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda)
+    y = N(api.bcsr_spmv_transpose(A.nb, A.bs, row, col, val, T(x, cuda)))
+    assert relerr(y, D.T @ x) < 1e-13
+    G = N(api.masked_outer(A.nb, A.bs, row, col, T(u, cuda), T(x, cuda), 2.0))
+    bs = A.bs
+    for p in range(0, A.nnzb, 7):
+        i = np.searchsorted(A.rowptr, p, side="right") - 1
+        j = A.colind[p]
+        want = 2.0 * np.outer(u[i * bs:(i + 1) * bs], x[j * bs:(j + 1) * bs])
+        assert np.allclose(G[p], want, rtol=1e-15, atol=0)
+
+
+# ------------------------------------------------------------------ sync-free solves
+@pytest.mark.parametrize("name", list(mats()))
+def test_sptrsv_matches_oracle(cuda, orc, name):
+    from isai_kernel_gb300 import api
+
+    A = mats()[name]
+    LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    b = gen.rhs(A.n, 3)
+    row, col, lu = T(A.rowptr, cuda), T(A.colind, cuda), T(LU, cuda)
+    y = api.sptrsv(A.nb, A.bs, row, col, lu, T(b, cuda), lower=True)
+    yo = orc.sptrsv_lower(A.nb, A.bs, A.rowptr, A.colind, LU, b)
+    assert relerr(N(y), yo) < 1e-12
+    x = api.sptrsv(A.nb, A.bs, row, col, lu, y, lower=False)
+    xo = orc.sptrsv_upper(A.nb, A.bs, A.rowptr, A.colind, LU, yo)
+    assert relerr(N(x), xo) < 1e-12
+
+
+def test_sptrsv_transposed(cuda, orc):
+    from isai_kernel_gb300 import api
+
+    A = gen.powerlaw(120, bs=8, seed=4, kmax=20)
+    LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    M = gen.BSRMatrix(A.nb, A.bs, A.rowptr, A.colind, LU).to_dense()
+    L, U = np.tril(M, -1) + np.eye(A.n), np.triu(M)
+    b = gen.rhs(A.n, 6)
+    row, col, lu = T(A.rowptr, cuda), T(A.colind, cuda), T(LU, cuda)
+    xl = N(api.sptrsv(A.nb, A.bs, row, col, lu, T(b, cuda), lower=True, transpose=True))
+    xu = N(api.sptrsv(A.nb, A.bs, row, col, lu, T(b, cuda), lower=False, transpose=True))
+    assert relerr(xl, np.linalg.solve(L.T, b)) < 1e-10
+    assert relerr(xu, np.linalg.solve(U.T, b)) < 1e-10
+
+
+def test_sptrsv_timeout_path(cuda, orc):
+    """A row that never publishes: dependants give up after a short bounded
+    wait, the call reports BILU_ERR_TIMEOUT, and the context stays usable."""
+    import ctypes
+
+    from isai_kernel_gb300 import _lib, api
+
+    A = gen.laplace2d(10, bs=4, seed=0)
+    LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    row, col, lu = T(A.rowptr, cuda), T(A.colind, cuda), T(LU, cuda)
+    b = T(gen.rhs(A.n, 3), cuda)
+    x = b.clone()
+    ws = api._ws(_lib.lib().bilu_sptrsv_ws_bytes(A.nb), cuda)
+    st = _lib.lib().bilu_debug_sptrsv_withhold(
+        A.nb, A.bs, api._p(row), api._p(col), api._p(lu), 1, api._p(b), api._p(x), 5,
+        ctypes.c_longlong(1 << 14), api._p(ws), ws.numel(), api._s())
+    assert st == -4  # BILU_ERR_TIMEOUT
+    y = api.sptrsv(A.nb, A.bs, row, col, lu, b, lower=True)
+    yo = orc.sptrsv_lower(A.nb, A.bs, A.rowptr, A.colind, LU, N(b))
+    assert relerr(N(y), yo) < 1e-12
+
+
+# ------------------------------------------------------------------ errors
+def test_pattern_errors(cuda):
+    import torch
+    from isai_kernel_gb300 import api
+    from isai_kernel_gb300._lib import BiluError
+
+    row = T(np.array([0, 2, 3], np.int32), cuda)
+    col = T(np.array([1, 0, 0], np.int32), cuda)  # row 0 unsorted
+    with pytest.raises(BiluError) as e:
+        api.build_bcsc_pattern_from_bsr_scalarILU(2, row, col, True)
+    assert e.value.status == -2
+    # missing diagonal block in row 1
+    row = T(np.array([0, 1, 2], np.int32), cuda)
+    col = T(np.array([0, 0], np.int32), cuda)
+    val = torch.ones((2, 4, 4), dtype=torch.float64, device=cuda)
+    with pytest.raises(BiluError) as e:
+        api.bsrilu02_inplace(2, 2, 4, row, col, val)
+    assert e.value.status == -2
+    # map mismatch reports the first missing (row, col) like the reference
+    cp = T(np.array([0, 2, 3], np.int32), cuda)
+    ci = T(np.array([0, 1, 1], np.int32), cuda)
+    rp = T(np.array([0, 1, 2], np.int32), cuda)
+    rc = T(np.array([0, 1], np.int32), cuda)
+    with pytest.raises(BiluError) as e:
+        api.build_map_bcsc2bcsr_host(2, cp, ci, rp, rc)
+    assert e.value.status == -2 and e.value.bad == (1, 0)
+
+
+def test_zero_pivot_reported(cuda, orc):
+    from isai_kernel_gb300 import api
+
+    A = gen.laplace2d(4, bs=4, seed=0)
+    d = [p for p in range(A.rowptr[5], A.rowptr[6]) if A.colind[p] == 5][0]
+    A.val[d][:, :] = 0.0
+    _, zp = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    v = T(A.val, cuda).clone()
+    info = api.bsrilu02_inplace(A.nb, A.nnzb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), v)
+    assert info == zp == 5
+
+
+def test_single_block_and_empty_offdiag(cuda, orc):
+    from isai_kernel_gb300 import api
+
+    rng = np.random.default_rng(0)
+    val = rng.uniform(-1, 1, (1, 8, 8)) + 8 * np.eye(8)
+    row, col = np.array([0, 1], np.int32), np.array([0], np.int32)
+    p = api.Preconditioner(1, 8, T(row, cuda), T(col, cuda), T(val, cuda))
+    b = rng.uniform(-1, 1, 8)
+    x, res = p.solve(T(b, cuda))
+    assert res.converged and res.iters <= 2
+    assert np.allclose(val[0] @ N(x), b, atol=1e-10)
+    p.close()
+
+
+# ------------------------------------------------------------------ engine + GMRES
+@pytest.mark.parametrize("name", ["c1_s16", "c2_s6", "c3_nb200"])
+def test_engine_setup_matches_oracle(cuda, orc, name):
+    from isai_kernel_gb300 import api
+
+    A = mats()[name]
+    S = orc.isai_setup(A)
+    p = api.Preconditioner(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda))
+    lu, L, U = p.factors()
+    assert relerr(N(lu), S["LU"]) < 1e-12
+    assert np.array_equal(N(L[0]), S["TrowL"]) and np.array_equal(N(L[1]), S["TcolL"])
+    assert np.array_equal(N(U[0]), S["TrowU"]) and np.array_equal(N(U[1]), S["TcolU"])
+    assert relerr(N(L[2]), S["McsrL"]) < 1e-12 and relerr(N(U[2]), S["McsrU"]) < 1e-12
+    assert np.array_equal(N(p.get(7)), N(L[2]).astype(np.float32).ravel())
+    p.close()
+
+
+@pytest.mark.parametrize("name", ["c1_s16", "c2_s6"])
+def test_gmres_iterations_match_oracle(cuda, orc, name):
+    from isai_kernel_gb300 import api
+
+    A = mats()[name]
+    S = orc.isai_setup(A)
+    b = gen.rhs(A.n, 0)
+    Ab = (A.rowptr, A.colind, A.val)
+    Lo = (S["TrowL"], S["TcolL"], S["McsrL"])
+    Uo = (S["TrowU"], S["TcolU"], S["McsrU"])
+    xo, ito, rro, ho, st = orc.gmres(Ab, Lo, Uo, b, precond=1, maxit=3000)
+    assert st == 0
+    p = api.Preconditioner(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda))
+    x, res = p.solve(T(b, cuda), prec=0, maxit=3000, history=True)
+    assert res.converged and res.iters == ito
+    assert relerr(N(x), xo) < 1e-8
+    np.testing.assert_allclose(res.history, ho, rtol=1e-6)
+    # mixed precision: FP32-stored ISAI inside FP64 FGMRES
+    xm, resm = p.solve(T(b, cuda), prec=1, maxit=3000)
+    _, itm, _, _, stm = orc.gmres(Ab, Lo, Uo, b, precond=2, maxit=3000)
+    assert resm.converged and resm.relres <= 1e-10 and abs(resm.iters - itm) <= 2
+    # reproducible
+    x2, res2 = p.solve(T(b, cuda), prec=0, maxit=3000)
+    assert res2.iters == res.iters and np.array_equal(N(x2), N(x))
+    e, r = api.compute_rel_errors(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda),
+                                  T(A.val, cuda), T(b, cuda), None, x)
+    assert r <= 1.01e-10
+    p.close()
+
+
+def test_solve_host_end_to_end(cuda, orc):
+    from isai_kernel_gb300 import api
+
+    A = gen.laplace2d(20, bs=4, seed=1)
+    b = gen.rhs(A.n, 5)
+    x, res, times = api.solve_host(A.nb, A.bs, A.rowptr, A.colind, A.val, b, prec=1)
+    assert res.converged
+    r = b - A.to_dense() @ x
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.01e-10

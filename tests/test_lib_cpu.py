@@ -1,0 +1,54 @@
+"""CPU-side checks of the C ABI library: it loads without a GPU, exports
+every function include/bilu_isai.h declares, and answers the host-only
+queries (status strings, version, workspace sizes)."""
+import ctypes
+import os
+import subprocess
+
+import pytest
+
+from isai_kernel_gb300 import _lib
+
+
+def test_header_parses():
+    decl = _lib.declarations()
+    names = [d[0] for d in decl]
+    assert len(names) == len(set(names)) and len(names) >= 45
+    for must in ("bilu_bsrilu0", "bilu_isai_compute", "bilu_bcsr_spmv", "bilu_sptrsv",
+                 "bilu_ctx_solve", "bilu_csr_to_bsr_fill", "bilu_map_bcsc2bcsr"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIBPATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    for name, _, _ in _lib.declarations():
+        assert name in exported, name
+        assert getattr(L, name) is not None
+
+
+def test_host_queries():
+    L = _lib.lib()
+    assert L.bilu_version() >= 10000
+    assert L.bilu_status_string(-4) == b"sync-free wait timed out"
+    assert L.bilu_status_string(0) == b"ok"
+    assert L.bilu_bsrilu0_ws_bytes(1000) > 4000
+    assert L.bilu_isai_pattern_ws_bytes(100, 500) > 0
+    assert L.bilu_sptrsv_transpose_ws_bytes(10, 30, 4) > 30 * 16 * 8
+
+
+def test_argument_errors_without_gpu():
+    """Bad arguments are rejected before any CUDA call."""
+    L = _lib.lib()
+    assert L.bilu_bcsr_spmv(-1, 4, None, None, None, None, None, None) == -1
+    assert L.bilu_bcsr_spmv(10, 6, ctypes.c_void_p(8), ctypes.c_void_p(8), ctypes.c_void_p(8),
+                            ctypes.c_void_p(8), ctypes.c_void_p(8), None) == -8
+    assert L.bilu_bsrilu0(-2, 0, 4, None, None, None, None, None, 0, None) == -1
+    assert L.bilu_isai_apply(10, 4, 7, None, None, None, None, None, None, None, None, None,
+                             None) == -1
+
+
+def test_build_is_in_tree():
+    assert os.path.dirname(_lib.LIBPATH).endswith("isai_kernel_gb300")
