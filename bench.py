@@ -51,7 +51,13 @@ def parse():
     ap.add_argument("--maxit", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-iters", type=int, default=3)
-    return ap.parse_args()
+    ap.add_argument("--profile", action="store_true",
+                    help="short run for ncu launch lists: setup, one warm-up and one timed "
+                         "solve capped at --maxit, the apply loop; no e2e, no CPU baseline")
+    a = ap.parse_args()
+    if a.profile:
+        a.no_cpu_baseline = True
+    return a
 
 
 def peaks():
@@ -246,6 +252,7 @@ def run_ours(args):
     clk = clocks.stop()
     launches = L.bilu_kernel_launches() - l0
     relres_mixed = res.relres
+    reorth_mixed = res.reorth
     t_mixed = max_over_ranks(statistics.mean(times), world)
 
     # plain FP64 path (reported beside the headline)
@@ -274,11 +281,12 @@ def run_ours(args):
         e1.synchronize()
         return e0.elapsed_time(e1) / 1e3 / reps
 
-    t_apply64 = time_it(lambda: api.isai_apply(nb, bs, Lf, Uf, b, prec=0))
+    reps = 3 if args.profile else 20
+    t_apply64 = time_it(lambda: api.isai_apply(nb, bs, Lf, Uf, b, prec=0), reps)
     t_apply32 = time_it(lambda: api.isai_apply(nb, bs, (Lf[0], Lf[1], L32), (Uf[0], Uf[1], U32),
-                                               b, prec=1))
+                                               b, prec=1), reps)
     y = torch.empty_like(b)
-    t_spmvA = time_it(lambda: api.bcsr_spmv(nb, bs, row, col, val, b, y))
+    t_spmvA = time_it(lambda: api.bcsr_spmv(nb, bs, row, col, val, b, y), reps)
     B64 = apply_bytes(nb, bs, nnzL, nnzU, 8, 8)
     B32 = apply_bytes(nb, bs, nnzL, nnzU, 4, 4)
     BA = spmv_bytes(nb, bs, nnzb)
@@ -292,7 +300,7 @@ def run_ours(args):
     hb = torch.from_numpy(b_np).pin_memory()
     hx = torch.empty(n, dtype=torch.float64).pin_memory()
     e2e = []
-    for _ in range(2):
+    for _ in range(0 if args.profile else 2):
         it, rr = ctypes.c_int(0), ctypes.c_double(0)
         tm = (ctypes.c_double * 4)()
         torch.cuda.synchronize()
@@ -304,7 +312,7 @@ def run_ours(args):
                                ctypes.byref(rr), tm, ctypes.c_void_p(stream.cuda_stream))
         e2e.append(time.perf_counter() - t0)
         assert st == 0, st
-    e2e_v = max_over_ranks(min(e2e), world)
+    e2e_v = max_over_ranks(min(e2e), world) if e2e else None
     h2d = A.rowptr.nbytes + A.colind.nbytes + A.val.nbytes + b_np.nbytes
     d2h = n * 8
 
@@ -330,6 +338,7 @@ def run_ours(args):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (1.87 GB of FP64 values)"},
         "iters": {"mixed": int(statistics.mean(iters)), "fp64": r64.iters},
+        "reorth_passes": {"mixed": reorth_mixed, "fp64": r64.reorth},
         "relres": {"mixed": relres_mixed, "fp64": r64.relres},
         "fp64_solve_s": t_fp64, "speedup_mixed_vs_fp64": t_fp64 / t_mixed,
         "setup_ms": setup_ms,

@@ -274,6 +274,9 @@ int bilu_ctx_setup(bilu_ctx* ctx, int nb, int nnzb, int bs, const int* d_row, co
 int bilu_ctx_solve(bilu_ctx* ctx, int prec, const double* d_b, double* d_x, int restart,
                    double tol, int maxit, int* h_iters, double* h_relres, double* h_hist);
 
+/* Counters of the last solve: h_out[0] = reorthogonalisation passes. */
+int bilu_ctx_stats(bilu_ctx* ctx, long long* h_out);
+
 /* Host-buffer convenience (the end-to-end call): copies A and b from host
  * memory, runs setup and solve, copies x back. */
 int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const int* h_col,

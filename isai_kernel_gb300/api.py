@@ -319,6 +319,7 @@ class SolveResult:
     relres: float
     converged: bool
     history: list
+    reorth: int = 0
 
 
 class Preconditioner:
@@ -379,7 +380,9 @@ class Preconditioner:
         if st not in (0, -6):
             raise BiluError("bilu_ctx_solve", st)
         h = list(hist[: it.value + 1]) if history else []
-        return x, SolveResult(it.value, rr.value, st == 0, h)
+        stats = (ctypes.c_longlong * 4)()
+        call("bilu_ctx_stats", self._h, stats)
+        return x, SolveResult(it.value, rr.value, st == 0, h, int(stats[0]))
 
 
 def solve_host(nb: int, bs: int, row, col, val, b, prec: int = BILU_FP64, restart: int = 30,

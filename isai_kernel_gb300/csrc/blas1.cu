@@ -9,21 +9,21 @@ namespace bilu {
 
 namespace {
 
-template <int NV_CAP>
-__device__ __forceinline__ void block_reduce_store(double* acc, int nout, double* out) {
+// Sum NOUT per-thread values over the CTA; thread i < NOUT writes sum i.
+template <int NOUT>
+__device__ __forceinline__ void block_reduce_store(const double (&acc)[NOUT > 0 ? NOUT : 1],
+                                                   double* out) {
   __shared__ double red[kRedThreads / 32][kPartStride];
   int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int i = 0; i < NV_CAP; ++i) {
-    if (i < nout) {
-      double v = acc[i];
+  for (int i = 0; i < NOUT; ++i) {
+    double v = acc[i];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) red[warp][i] = v;
-    }
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][i] = v;
   }
   __syncthreads();
-  if (threadIdx.x < nout) {
+  if (threadIdx.x < NOUT) {
     double s = 0.0;
 #pragma unroll
     for (int w = 0; w < kRedThreads / 32; ++w) s += red[w][threadIdx.x];
@@ -31,58 +31,51 @@ __device__ __forceinline__ void block_reduce_store(double* acc, int nout, double
   }
 }
 
+// h[i] = V_i . w for i < NV (and w.w at index NV when WW): w is read once,
+// each basis vector once; one DFMA per loaded basis element.
+template <int NV, bool WW>
 __global__ void __launch_bounds__(kRedThreads) k_multidot(long long n, const double* __restrict__ V,
-                                                          long long ldv, int nv,
+                                                          long long ldv,
                                                           const double* __restrict__ w,
-                                                          int with_ww,
                                                           double* __restrict__ partial,
                                                           const int* __restrict__ skip_flag) {
   if (skip_flag && *skip_flag == 0) return;
-  double acc[kMaxVec + 1];
+  constexpr int NOUT = NV + (WW ? 1 : 0);
+  double acc[NOUT > 0 ? NOUT : 1];
 #pragma unroll
-  for (int i = 0; i <= kMaxVec; ++i) acc[i] = 0.0;
+  for (int i = 0; i < NOUT; ++i) acc[i] = 0.0;
   long long stride = (long long)gridDim.x * blockDim.x;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
     double we = w[e];
 #pragma unroll
-    for (int i = 0; i < kMaxVec; ++i)
-      if (i < nv) acc[i] = fma(V[i * ldv + e], we, acc[i]);
-    if (with_ww) acc[kMaxVec] = fma(we, we, acc[kMaxVec]);
+    for (int i = 0; i < NV; ++i) acc[i] = fma(__ldcs(V + i * ldv + e), we, acc[i]);
+    if (WW) acc[NOUT - 1] = fma(we, we, acc[NOUT - 1]);
   }
-  if (with_ww) {
-    // move the w.w term next to the nv dots
-#pragma unroll
-    for (int i = 0; i <= kMaxVec; ++i)
-      if (i == nv) acc[i] = acc[kMaxVec];
-  }
-  block_reduce_store<kMaxVec + 1>(acc, nv + (with_ww ? 1 : 0),
-                                  partial + (long long)blockIdx.x * kPartStride);
+  block_reduce_store<NOUT>(acc, partial + (long long)blockIdx.x * kPartStride);
 }
 
+// w += sign * sum_i coef[i] V_i, with ||w_new||^2 partials.
+template <int NV>
 __global__ void __launch_bounds__(kRedThreads) k_multiaxpy_norm(
-    long long n, const double* __restrict__ V, long long ldv, int nv,
-    const double* __restrict__ coef, double sign, double* __restrict__ w,
-    double* __restrict__ partial, const int* __restrict__ skip_flag) {
+    long long n, const double* __restrict__ V, long long ldv, const double* __restrict__ coef,
+    double sign, double* __restrict__ w, double* __restrict__ partial,
+    const int* __restrict__ skip_flag) {
   if (skip_flag && *skip_flag == 0) return;
-  __shared__ double c_s[kMaxVec];
-  if (threadIdx.x < kMaxVec) c_s[threadIdx.x] = threadIdx.x < nv ? sign * coef[threadIdx.x] : 0.0;
-  __syncthreads();
-  double c[kMaxVec];
+  double c[NV > 0 ? NV : 1];
 #pragma unroll
-  for (int i = 0; i < kMaxVec; ++i) c[i] = c_s[i];
+  for (int i = 0; i < NV; ++i) c[i] = sign * __ldg(coef + i);
   double nrm = 0.0;
   long long stride = (long long)gridDim.x * blockDim.x;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
     double s = w[e];
 #pragma unroll
-    for (int i = 0; i < kMaxVec; ++i)
-      if (i < nv) s = fma(c[i], V[i * ldv + e], s);
+    for (int i = 0; i < NV; ++i) s = fma(c[i], __ldcs(V + i * ldv + e), s);
     w[e] = s;
     nrm = fma(s, s, nrm);
   }
   if (partial) {
     double a[1] = {nrm};
-    block_reduce_store<1>(a, 1, partial + (long long)blockIdx.x * kPartStride);
+    block_reduce_store<1>(a, partial + (long long)blockIdx.x * kPartStride);
   }
 }
 
@@ -114,16 +107,51 @@ __global__ void __launch_bounds__(kRedThreads) k_residual(long long n, const dou
     nrm = fma(v, v, nrm);
   }
   double a[1] = {nrm};
-  block_reduce_store<1>(a, 1, partial + (long long)blockIdx.x * kPartStride);
+  block_reduce_store<1>(a, partial + (long long)blockIdx.x * kPartStride);
 }
+
+template <int NV>
+void launch_multidot(long long n, const double* V, long long ldv, const double* w, bool ww,
+                     double* partial, cudaStream_t st, const int* skip) {
+  if (ww)
+    k_multidot<NV, true><<<kRedCTAs, kRedThreads, 0, st>>>(n, V, ldv, w, partial, skip);
+  else
+    k_multidot<NV, false><<<kRedCTAs, kRedThreads, 0, st>>>(n, V, ldv, w, partial, skip);
+}
+
+template <int NV>
+void launch_multiaxpy(long long n, const double* V, long long ldv, const double* coef,
+                      double sign, double* w, double* partial, const int* skip, cudaStream_t st) {
+  k_multiaxpy_norm<NV><<<kRedCTAs, kRedThreads, 0, st>>>(n, V, ldv, coef, sign, w, partial, skip);
+}
+
+#define BILU_NV_CASES(F, ...)                                                        \
+  switch (nv) {                                                                      \
+    case 0: F<0>(__VA_ARGS__); break;   case 1: F<1>(__VA_ARGS__); break;            \
+    case 2: F<2>(__VA_ARGS__); break;   case 3: F<3>(__VA_ARGS__); break;            \
+    case 4: F<4>(__VA_ARGS__); break;   case 5: F<5>(__VA_ARGS__); break;            \
+    case 6: F<6>(__VA_ARGS__); break;   case 7: F<7>(__VA_ARGS__); break;            \
+    case 8: F<8>(__VA_ARGS__); break;   case 9: F<9>(__VA_ARGS__); break;            \
+    case 10: F<10>(__VA_ARGS__); break; case 11: F<11>(__VA_ARGS__); break;          \
+    case 12: F<12>(__VA_ARGS__); break; case 13: F<13>(__VA_ARGS__); break;          \
+    case 14: F<14>(__VA_ARGS__); break; case 15: F<15>(__VA_ARGS__); break;          \
+    case 16: F<16>(__VA_ARGS__); break; case 17: F<17>(__VA_ARGS__); break;          \
+    case 18: F<18>(__VA_ARGS__); break; case 19: F<19>(__VA_ARGS__); break;          \
+    case 20: F<20>(__VA_ARGS__); break; case 21: F<21>(__VA_ARGS__); break;          \
+    case 22: F<22>(__VA_ARGS__); break; case 23: F<23>(__VA_ARGS__); break;          \
+    case 24: F<24>(__VA_ARGS__); break; case 25: F<25>(__VA_ARGS__); break;          \
+    case 26: F<26>(__VA_ARGS__); break; case 27: F<27>(__VA_ARGS__); break;          \
+    case 28: F<28>(__VA_ARGS__); break; case 29: F<29>(__VA_ARGS__); break;          \
+    case 30: F<30>(__VA_ARGS__); break; case 31: F<31>(__VA_ARGS__); break;          \
+    case 32: F<32>(__VA_ARGS__); break;                                              \
+    default: return BILU_ERR_ARG;                                                    \
+  }
 
 }  // namespace
 
 int multidot(long long n, const double* V, long long ldv, int nv, const double* w, bool with_ww,
              double* partial, cudaStream_t st, const int* skip_flag) {
-  if (nv < 0 || nv > kMaxVec) return BILU_ERR_ARG;
-  k_multidot<<<kRedCTAs, kRedThreads, 0, st>>>(n, V, ldv, nv, w, with_ww ? 1 : 0, partial,
-                                               skip_flag);
+  BILU_NV_CASES(launch_multidot, n, V, ldv, w, with_ww, partial, st, skip_flag);
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }
@@ -131,9 +159,7 @@ int multidot(long long n, const double* V, long long ldv, int nv, const double* 
 int multiaxpy_norm(long long n, const double* V, long long ldv, int nv, const double* coef,
                    double sign, double* w, double* partial, const int* skip_flag,
                    cudaStream_t st) {
-  if (nv < 0 || nv > kMaxVec) return BILU_ERR_ARG;
-  k_multiaxpy_norm<<<kRedCTAs, kRedThreads, 0, st>>>(n, V, ldv, nv, coef, sign, w, partial,
-                                                     skip_flag);
+  BILU_NV_CASES(launch_multiaxpy, n, V, ldv, coef, sign, w, partial, skip_flag, st);
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }

@@ -92,6 +92,8 @@ struct bilu_ctx {
   double *V = nullptr, *Z = nullptr, *w = nullptr, *r = nullptr, *tmp = nullptr;
   double *partial = nullptr, *dscal = nullptr, *dcoef = nullptr;
   double* hpin = nullptr;  // pinned host mirror of dscal
+  cudaEvent_t ev = nullptr;
+  long long reorth = 0;    // reorthogonalisation passes of the last solve
   std::vector<void*> setup_bufs;
   void free_setup() {
     for (void* p : setup_bufs) cudaFree(p);
@@ -105,6 +107,8 @@ struct bilu_ctx {
     cudaFree(V); cudaFree(Z); cudaFree(w); cudaFree(r); cudaFree(tmp);
     cudaFree(partial); cudaFree(dscal); cudaFree(dcoef);
     if (hpin) cudaFreeHost(hpin);
+    if (ev) cudaEventDestroy(ev);
+    ev = nullptr;
     V = Z = w = r = tmp = partial = dscal = dcoef = hpin = nullptr;
     m_alloc = 0;
   }
@@ -355,6 +359,46 @@ int apply_prec(bilu_ctx* c, int prec, const double* v, double* z) {
 
 }  // namespace
 
+namespace {
+
+// Launches z_j = M v_j and w = A z_j.
+int arnoldi_front(bilu_ctx* c, int prec, int j) {
+  size_t n = (size_t)c->n;
+  double* zj = c->Z + n * j;
+  BILU_TRY(apply_prec(c, prec, c->V + n * j, zj));
+  return spmv_any(c->nb, c->bs, BILU_FP64, c->Arow, c->Acol, c->Aval, zj, 0, c->w, 0, c->st);
+}
+
+// Orthogonalises w against V_0..V_j (CGS, DGKS reorthogonalisation decided
+// on the device), writes V_{j+1} and queues the Hessenberg column to hpin.
+int arnoldi_back(bilu_ctx* c, int j) {
+  cudaStream_t st = c->st;
+  long long n = c->n;
+  double* s = c->dscal;
+  int nv = j + 1;
+  BILU_TRY(multidot(n, c->V, n, nv, c->w, true, c->partial, st));
+  BILU_TRY(reduce_partials(c->partial, nv + 1, s, st));
+  BILU_TRY(multiaxpy_norm(n, c->V, n, nv, s, -1.0, c->w, c->partial, nullptr, st));
+  BILU_TRY(reduce_partials(c->partial, 1, s + kPartStride, st));
+  k_dgks_select<<<1, 1, 0, st>>>(s, nv);
+  BILU_LAUNCH_CHECK();
+  const int* flag = (const int*)(s + 4 * kPartStride);
+  // pass 2 runs only when the DGKS test fired; its kernels read the device
+  // flag and return at once otherwise
+  BILU_TRY(multidot(n, c->V, n, nv, c->w, false, c->partial, st, flag));
+  BILU_TRY(reduce_partials(c->partial, nv, s + 2 * kPartStride, st));
+  BILU_TRY(multiaxpy_norm(n, c->V, n, nv, s + 2 * kPartStride, -1.0, c->w, c->partial, flag, st));
+  BILU_TRY(reduce_partials(c->partial, 1, s + 3 * kPartStride, st));
+  k_pick_norm<<<1, 1, 0, st>>>(s);
+  BILU_LAUNCH_CHECK();
+  BILU_TRY(scale_rsqrt(n, c->w, s + 5 * kPartStride, c->V + (size_t)n * (j + 1), st));
+  BILU_TRY_CUDA(cudaMemcpyAsync(c->hpin, s, sizeof(double) * 6 * kPartStride,
+                                cudaMemcpyDeviceToHost, st));
+  return BILU_OK;
+}
+
+}  // namespace
+
 extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* d_x, int restart,
                               double tol, int maxit, int* h_iters, double* h_relres,
                               double* h_hist) {
@@ -367,6 +411,7 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
   const long long n = c->n;
   double* s = c->dscal;
   double* hp = c->hpin;
+  if (!c->ev) BILU_TRY_CUDA(cudaEventCreateWithFlags(&c->ev, cudaEventDisableTiming));
   std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m);
   BILU_TRY_CUDA(cudaMemsetAsync(d_x, 0, sizeof(double) * n, st));
   double bb = 0;
@@ -378,6 +423,7 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
   BILU_TRY(norm2(c, c->r, s + 5 * kPartStride, &rr));
   double beta = std::sqrt(rr);
   int total = 0, status = BILU_ERR_NOT_CONVERGED;
+  c->reorth = 0;
   double res = beta / bnorm;
   if (h_hist) h_hist[0] = res;
   if (res <= tol) status = BILU_OK;
@@ -387,34 +433,17 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int jlast = -1;
+    BILU_TRY(arnoldi_front(c, prec, 0));
     for (int j = 0; j < m && total < maxit; ++j) {
-      double* vj = c->V + (size_t)n * j;
-      double* zj = c->Z + (size_t)n * j;
-      BILU_TRY(apply_prec(c, prec, vj, zj));
-      BILU_TRY(spmv_any(c->nb, c->bs, BILU_FP64, c->Arow, c->Acol, c->Aval, zj, 0, c->w, 0, st));
-      int nv = j + 1;
-      // pass 1: h = V^T w and w.w, then w -= V h with ||w||^2
-      BILU_TRY(multidot(n, c->V, n, nv, c->w, true, c->partial, st));
-      BILU_TRY(reduce_partials(c->partial, nv + 1, s, st));
-      BILU_TRY(multiaxpy_norm(n, c->V, n, nv, s, -1.0, c->w, c->partial, nullptr, st));
-      BILU_TRY(reduce_partials(c->partial, 1, s + kPartStride, st));
-      k_dgks_select<<<1, 1, 0, st>>>(s, nv);
-      BILU_LAUNCH_CHECK();
-      const int* flag = (const int*)(s + 4 * kPartStride);
-      // pass 2 (reorthogonalisation) runs only when the DGKS test fired;
-      // its kernels read the device flag and return early otherwise
-      BILU_TRY(multidot(n, c->V, n, nv, c->w, false, c->partial, st, flag));
-      BILU_TRY(reduce_partials(c->partial, nv, s + 2 * kPartStride, st));
-      BILU_TRY(multiaxpy_norm(n, c->V, n, nv, s + 2 * kPartStride, -1.0, c->w, c->partial, flag,
-                              st));
-      BILU_TRY(reduce_partials(c->partial, 1, s + 3 * kPartStride, st));
-      k_pick_norm<<<1, 1, 0, st>>>(s);
-      BILU_LAUNCH_CHECK();
-      BILU_TRY(scale_rsqrt(n, c->w, s + 5 * kPartStride, c->V + (size_t)n * (j + 1), st));
-      BILU_TRY_CUDA(cudaMemcpyAsync(hp, s, sizeof(double) * 6 * kPartStride,
-                                    cudaMemcpyDeviceToHost, st));
-      BILU_TRY_CUDA(cudaStreamSynchronize(st));
+      BILU_TRY(arnoldi_back(c, j));
+      BILU_TRY_CUDA(cudaEventRecord(c->ev, st));
+      // the next basis vector's apply and SpMV do not depend on the host
+      // Givens step: queue them before waiting (discarded if this step
+      // converges)
+      if (j + 1 < m && total + 1 < maxit) BILU_TRY(arnoldi_front(c, prec, j + 1));
+      BILU_TRY_CUDA(cudaEventSynchronize(c->ev));
       int fl = ((const int*)(hp + 4 * kPartStride))[0];
+      c->reorth += fl;
       for (int i = 0; i <= j; ++i) {
         double h = 0.0 + hp[i];
         if (fl) h += hp[2 * kPartStride + i];
@@ -464,6 +493,12 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
   if (h_iters) *h_iters = total;
   if (h_relres) *h_relres = res;
   return status;
+}
+
+extern "C" int bilu_ctx_stats(bilu_ctx* c, long long* h_out) {
+  if (!c || !h_out) return BILU_ERR_ARG;
+  h_out[0] = c->reorth;
+  return BILU_OK;
 }
 
 extern "C" int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const int* h_col,

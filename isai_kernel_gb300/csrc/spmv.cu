@@ -70,41 +70,50 @@ __device__ __forceinline__ void load_row(const VT* __restrict__ val, long long p
 }
 
 // y = M x: lane group of BS lanes per block row, lane r owns scalar row r.
-// Two blocks per loop trip keep two independent block loads in flight.
+// U blocks per loop trip keep U independent block loads in flight per lane
+// (2 for FP64 values, 4 for FP32 values, whose rows are half as wide).
 template <int BS, class VT, class XT, class YT, class AccT>
-__global__ void __launch_bounds__(256) k_bsr_spmv(int mb, const int* __restrict__ row,
-                                                  const int* __restrict__ col,
-                                                  const VT* __restrict__ val,
-                                                  const XT* __restrict__ x, YT* __restrict__ y) {
+__global__ void __launch_bounds__(256, 4) k_bsr_spmv(int mb, const int* __restrict__ row,
+                                                     const int* __restrict__ col,
+                                                     const VT* __restrict__ val,
+                                                     const XT* __restrict__ x,
+                                                     YT* __restrict__ y) {
   constexpr int G = 32 / BS;  // block rows per warp
+  constexpr int U = sizeof(VT) == 4 ? 4 : 2;
   int lane = threadIdx.x & 31;
   int g = lane / BS, r = lane - g * BS;
   long long br = ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G + g;
   if (g >= G || br >= mb) return;
   int s = __ldg(row + br), e = __ldg(row + br + 1);
-  AccT acc0 = 0, acc1 = 0;
-  int p = s;
-  for (; p + 1 < e; p += 2) {
-    AccT a0[BS], a1[BS], x0[BS], x1[BS];
-    int c0 = __ldg(col + p), c1 = __ldg(col + p + 1);
-    load_row<BS, VT, AccT>(val, p, r, a0);
-    load_row<BS, VT, AccT>(val, p + 1, r, a1);
-    load_x<BS, XT, AccT>(x, c0, x0);
-    load_x<BS, XT, AccT>(x, c1, x1);
+  AccT acc[U];
 #pragma unroll
-    for (int c = 0; c < BS; ++c) {
-      acc0 = fma(a0[c], x0[c], acc0);
-      acc1 = fma(a1[c], x1[c], acc1);
-    }
+  for (int u = 0; u < U; ++u) acc[u] = 0;
+  int p = s;
+  for (; p + U <= e; p += U) {
+    AccT a[U][BS], xv[U][BS];
+    int c[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) c[u] = __ldg(col + p + u);
+#pragma unroll
+    for (int u = 0; u < U; ++u) load_row<BS, VT, AccT>(val, p + u, r, a[u]);
+#pragma unroll
+    for (int u = 0; u < U; ++u) load_x<BS, XT, AccT>(x, c[u], xv[u]);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int k = 0; k < BS; ++k) acc[u] = fma(a[u][k], xv[u][k], acc[u]);
   }
-  if (p < e) {
+  for (; p < e; ++p) {
     AccT a0[BS], x0[BS];
     load_row<BS, VT, AccT>(val, p, r, a0);
     load_x<BS, XT, AccT>(x, __ldg(col + p), x0);
 #pragma unroll
-    for (int c = 0; c < BS; ++c) acc0 = fma(a0[c], x0[c], acc0);
+    for (int k = 0; k < BS; ++k) acc[0] = fma(a0[k], x0[k], acc[0]);
   }
-  y[br * BS + r] = (YT)(acc0 + acc1);
+  AccT t = acc[0];
+#pragma unroll
+  for (int u = 1; u < U; ++u) t += acc[u];
+  y[br * BS + r] = (YT)t;
 }
 
 template <int BS, class VT, class XT, class YT>

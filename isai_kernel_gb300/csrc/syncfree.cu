@@ -13,7 +13,10 @@
 // and all other waiters see the error word and leave, so no launch hangs.
 #include <climits>
 
+#include <algorithm>
+
 #include "common.cuh"
+#include "scan.cuh"
 
 namespace bilu {
 
@@ -28,6 +31,7 @@ struct SyncState {
   int* zp;            // first zero pivot row (INT_MAX if none)
   long long spin;     // polls before a wait gives up
   int withhold;       // test hook: this row never publishes (-1: none)
+  const int* order;   // ticket -> block row (dependency-level order), or null
 };
 
 // Warp-wide wait until flags[K] != 0.  Returns false if the launch aborted.
@@ -112,6 +116,7 @@ __global__ void __launch_bounds__(128) k_bilu0(int nb, const int* __restrict__ r
     if (lane == 0) I = atomicAdd(ss.ticket, 1);
     I = __shfl_sync(FULL, I, 0);
     if (I >= nb) return;
+    if (ss.order) I = __ldg(ss.order + I);
     if (__any_sync(FULL, ld_relaxed(ss.err) != 0)) return;
     int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
     for (int pk = rs; pk < dI; ++pk) {
@@ -229,7 +234,7 @@ __global__ void __launch_bounds__(128) k_sptrsv(int nb, const int* __restrict__ 
     if (lane == 0) t = atomicAdd(ss.ticket, 1);
     t = __shfl_sync(FULL, t, 0);
     if (t >= nb) return;
-    int I = LOWER ? t : nb - 1 - t;
+    int I = ss.order ? __ldg(ss.order + t) : (LOWER ? t : nb - 1 - t);
     int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
     int ps = LOWER ? rs : dI + 1, pe = LOWER ? dI : re;
     double s = 0.0;
@@ -284,6 +289,52 @@ __global__ void __launch_bounds__(128) k_sptrsv(int nb, const int* __restrict__ 
   }
 }
 
+// ------------------------------------------------------------------ levels
+// Dependency level of every block row (1 + the deepest row it waits on),
+// thread per row, sync-free like the solves: rows are taken in ticket order,
+// a row waits (bounded) for the levels of its dependencies and publishes its
+// own.  The lower DAG follows the strictly lower blocks, the upper DAG the
+// strictly upper ones in reverse order.
+template <bool LOWER>
+__global__ void __launch_bounds__(256) k_levels(int nb, const int* __restrict__ row,
+                                                const int* __restrict__ col,
+                                                const int* __restrict__ diag, int* level,
+                                                int* ticket, int* err, long long spin) {
+  while (true) {
+    int t = atomicAdd(ticket, 1);
+    if (t >= nb) return;
+    int I = LOWER ? t : nb - 1 - t;
+    int ps = LOWER ? __ldg(row + I) : __ldg(diag + I) + 1;
+    int pe = LOWER ? __ldg(diag + I) : __ldg(row + I + 1);
+    int lv = 0;
+    for (int p = ps; p < pe; ++p) {
+      const int* f = level + __ldg(col + p);
+      long long n = 0;
+      int v;
+      while ((v = ld_acquire(f)) == 0) {
+        if (ld_relaxed(err) != 0) return;
+        if (++n > spin) {
+          atomicCAS(err, 0, (int)BILU_ERR_TIMEOUT);
+          return;
+        }
+        __nanosleep(32);
+      }
+      lv = max(lv, v);
+    }
+    st_release(level + I, lv + 1);
+  }
+}
+
+__global__ void k_level_count(int nb, const int* __restrict__ level, int* cnt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nb) atomicAdd(cnt + level[i] - 1, 1);
+}
+
+__global__ void k_level_scatter(int nb, const int* __restrict__ level, int* cursor, int* order) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nb) order[atomicAdd(cursor + level[i] - 1, 1)] = i;
+}
+
 int occupancy_grid(const void* fn, int threads) {
   static int sms = 0;
   if (!sms) {
@@ -302,6 +353,7 @@ int sync_init(SyncState& ss, int nb, Carver& ws, cudaStream_t st, long long spin
               int withhold = -1) {
   ss.spin = spin;
   ss.withhold = withhold;
+  ss.order = nullptr;
   ss.flags = ws.take<int>((size_t)nb + 1);
   int* misc = ws.take<int>(4);
   if (!ss.flags || !misc) return BILU_ERR_WORKSPACE;
@@ -321,6 +373,38 @@ int sync_finish(const SyncState& ss, int* h_zp, cudaStream_t st) {
   if (h_zp) *h_zp = h[1] == INT_MAX ? -1 : h[1];
   if (h[0] != 0) return h[0];
   if (h[1] != INT_MAX) return BILU_ERR_ZERO_PIVOT;
+  return BILU_OK;
+}
+
+// Ticket order by dependency level (ascending).  Rows of one level are
+// independent, so consecutive tickets can run concurrently; every row's
+// dependencies sit at lower levels, i.e. at earlier tickets.
+int build_order(int nb, const int* row, const int* col, const int* diag, int lower, int* order,
+                Carver& ws, cudaStream_t st) {
+  int* level = ws.take<int>((size_t)nb + 1);
+  int* cnt = ws.take<int>((size_t)nb + 1);
+  int* misc = ws.take<int>(4);
+  if (!level || !cnt || !misc) return BILU_ERR_WORKSPACE;
+  BILU_TRY_CUDA(cudaMemsetAsync(level, 0, sizeof(int) * ((size_t)nb + 1), st));
+  BILU_TRY_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * ((size_t)nb + 1), st));
+  BILU_TRY_CUDA(cudaMemsetAsync(misc, 0, sizeof(int) * 4, st));
+  if (nb == 0) return BILU_OK;
+  const void* fn = lower ? (const void*)k_levels<true> : (const void*)k_levels<false>;
+  int grid = std::min<long long>(occupancy_grid(fn, 256), (nb + 255) / 256);
+  if (lower)
+    k_levels<true><<<grid, 256, 0, st>>>(nb, row, col, diag, level, misc, misc + 1, kSpinLimit);
+  else
+    k_levels<false><<<grid, 256, 0, st>>>(nb, row, col, diag, level, misc, misc + 1, kSpinLimit);
+  BILU_LAUNCH_CHECK();
+  int herr = 0;
+  BILU_TRY_CUDA(cudaMemcpyAsync(&herr, misc + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BILU_TRY_CUDA(cudaStreamSynchronize(st));
+  if (herr != 0) return herr;
+  k_level_count<<<ceil_div(nb, 256), 256, 0, st>>>(nb, level, cnt);
+  BILU_LAUNCH_CHECK();
+  BILU_TRY(scan_exclusive(cnt, cnt, nb, nullptr, ws, st));
+  k_level_scatter<<<ceil_div(nb, 256), 256, 0, st>>>(nb, level, cnt, order);
+  BILU_LAUNCH_CHECK();
   return BILU_OK;
 }
 
@@ -355,8 +439,9 @@ int launch_sptrsv(int nb, const int* row, const int* col, const int* diag, const
 }  // namespace
 
 size_t syncfree_ws(int nb) {
-  return carve_size(sizeof(int) * ((size_t)nb + 1)) * 2 + carve_size(sizeof(int) * 4) +
-         carve_size(sizeof(int) * 2);
+  // flags + order + (levels, counts, misc, scan) + sync misc + error words
+  return carve_size(sizeof(int) * ((size_t)nb + 1)) * 4 + carve_size(sizeof(int) * 4) * 2 +
+         carve_size(sizeof(int) * 2) + scan_ws_bytes(nb + 1);
 }
 
 // diagonal positions (validates the pattern); returns BILU_ERR_PATTERN with
@@ -379,8 +464,15 @@ int diag_positions(int nb, const int* row, const int* col, int* diag, int* h_bad
 
 int bilu0_impl(int nb, int bs, const int* row, const int* col, const int* diag, double* val,
                int* h_zp, Carver& ws, cudaStream_t st) {
+  int* order = ws.take<int>((size_t)nb + 1);
+  if (!order) return BILU_ERR_WORKSPACE;
+  {
+    Carver w2 = ws;
+    BILU_TRY(build_order(nb, row, col, diag, 1, order, w2, st));
+  }
   SyncState ss;
   BILU_TRY(sync_init(ss, nb, ws, st));
+  ss.order = order;
   if (nb > 0) BILU_TRY(BILU_DISPATCH_BS(bs, launch_bilu0, nb, row, col, diag, val, ss, st));
   return sync_finish(ss, h_zp, st);
 }
@@ -388,8 +480,15 @@ int bilu0_impl(int nb, int bs, const int* row, const int* col, const int* diag, 
 int sptrsv_impl(int nb, int bs, const int* row, const int* col, const int* diag,
                 const double* val, int lower, int unit, const double* b, double* x, Carver& ws,
                 cudaStream_t st, long long spin = kSpinLimit, int withhold = -1) {
+  int* order = ws.take<int>((size_t)nb + 1);
+  if (!order) return BILU_ERR_WORKSPACE;
+  {
+    Carver w2 = ws;
+    BILU_TRY(build_order(nb, row, col, diag, lower, order, w2, st));
+  }
   SyncState ss;
   BILU_TRY(sync_init(ss, nb, ws, st, spin, withhold));
+  ss.order = order;
   if (nb > 0)
     BILU_TRY(BILU_DISPATCH_BS(bs, launch_sptrsv, nb, row, col, diag, val, lower, unit, b, x, ss,
                               st));
