@@ -292,6 +292,31 @@ int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const int* h_col
 int bilu_ctx_get(bilu_ctx* ctx, int which, const void** d_ptr, long long* h_count);
 
 /* ------------------------------------------------------------------ */
+/* Allocation-free solve                                               */
+/* ------------------------------------------------------------------ */
+
+/* No counterpart in the reference.  The sync-free block triangular solve of
+ * bilu_sptrsv for callers that cannot allocate device memory (code running
+ * while a CUDA graph is being captured, hosts whose device memory belongs to
+ * a fixed arena or budget, plugins limited to the buffers they are handed):
+ * it takes only inputs and the output and keeps its scratch in one fixed,
+ * file-scope device array of about 6 MiB that every device holds from the
+ * moment the library is loaded until the process exits.  It never calls
+ * cudaMalloc, cudaFree or any allocating routine.
+ *   - nb may not exceed bilu_sptrsv_noalloc_max_rows() (262144 block rows);
+ *     larger systems return BILU_ERR_WORKSPACE without touching the GPU.
+ *   - The first call on a device looks up the array's device address with
+ *     cudaGetSymbolAddress (no allocation) and caches it; make that first call
+ *     before any stream capture on that device.
+ *   - All calls share the one array and every call re-initialises the parts
+ *     that must start at zero.  Calls whose executions overlap on the GPU
+ *     (different streams, or different host threads) race on it: serialise
+ *     them. */
+int bilu_sptrsv_noalloc_max_rows(void);
+int bilu_sptrsv_noalloc(int nb, int bs, const int* d_row, const int* d_col, const double* d_val,
+                        int lower, const double* d_b, double* d_x, bilu_stream_t stream);
+
+/* ------------------------------------------------------------------ */
 /* Testing hook (no counterpart in the reference)                      */
 /* ------------------------------------------------------------------ */
 
