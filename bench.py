@@ -252,7 +252,7 @@ def run_ours(args):
     clk = clocks.stop()
     launches = L.bilu_kernel_launches() - l0
     relres_mixed = res.relres
-    reorth_mixed = res.reorth
+    restarts_mixed = res.restarts
     t_mixed = max_over_ranks(statistics.mean(times), world)
 
     # plain FP64 path (reported beside the headline)
@@ -292,6 +292,13 @@ def run_ours(args):
     BA = spmv_bytes(nb, bs, nnzb)
     peak, peak_kind = peaks()
     gbs32 = B32 / t_apply32 / 1e9
+    rates = (ctypes.c_double * 3)()
+    _lib.check("bilu_probe_rates", L.bilu_probe_rates(rates))
+    dfma_tf = rates[0]
+    # FP64 kernels: one DFMA per stored FP64 value, so their compute roofline
+    # is 2 * (#values) / DFMA rate
+    flops64 = 2.0 * (nnzL + nnzU) * bs * bs
+    flopsA = 2.0 * nnzb * bs * bs
 
     # end to end through the C ABI with pinned host buffers
     hrow = torch.from_numpy(A.rowptr).pin_memory()
@@ -338,7 +345,7 @@ def run_ours(args):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (1.87 GB of FP64 values)"},
         "iters": {"mixed": int(statistics.mean(iters)), "fp64": r64.iters},
-        "reorth_passes": {"mixed": reorth_mixed, "fp64": r64.reorth},
+        "restart_cycles": {"mixed": restarts_mixed, "fp64": r64.restarts},
         "relres": {"mixed": relres_mixed, "fp64": r64.relres},
         "fp64_solve_s": t_fp64, "speedup_mixed_vs_fp64": t_fp64 / t_mixed,
         "setup_ms": setup_ms,
@@ -349,6 +356,12 @@ def run_ours(args):
                      "frac": gbs32 / peak, "traffic": None,
                      "kernel": "FP32-stored ISAI apply (k_bsr_spmv x2)",
                      "peak_source": f"{peak_kind} hbm_gbs"},
+        "fp64_compute_roofline": {
+            "dfma_tflops": dfma_tf, "dmma_tflops": rates[1], "ffma_tflops": rates[2],
+            "apply_fp64_frac_of_dfma": flops64 / t_apply64 / 1e12 / dfma_tf,
+            "A_spmv_frac_of_dfma": flopsA / t_spmvA / 1e12 / dfma_tf,
+            "apply_fp64_bound_s": max(flops64 / (dfma_tf * 1e12), B64 / (peak * 1e9)),
+            "A_spmv_bound_s": max(flopsA / (dfma_tf * 1e12), BA / (peak * 1e9))},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),

@@ -55,6 +55,10 @@ int bilu_version(void);
 int bilu_last_cuda_error(void);
 /* number of kernels this library has launched since it was loaded */
 unsigned long long bilu_kernel_launches(void);
+/* Measured pipe throughput of the current GPU in TFLOP/s: h_out[0] DFMA,
+ * h_out[1] DMMA (mma.sync m8n8k4 f64), h_out[2] FFMA.  Sets the compute
+ * roofline of the FP64 kernels (allocates and frees a scratch buffer). */
+int bilu_probe_rates(double* h_out);
 
 /* ------------------------------------------------------------------ */
 /* Format conversions and patterns                                     */
@@ -199,6 +203,18 @@ size_t bilu_sptrsv_ws_bytes(int nb);
 int bilu_sptrsv(int nb, int bs, const int* d_row, const int* d_col, const double* d_val,
                 int lower, const double* d_b, double* d_x, void* d_ws, size_t ws_bytes,
                 bilu_stream_t stream);
+/* Analysis / solve split (as cuSPARSE bsrsv2 analysis + solve,
+ * BILU_cusparse.h:203-220): the analysis (diagonal positions and dependency
+ * level order, bilu_sptrsv_analysis_bytes(nb) bytes in d_info) is computed
+ * once per pattern and triangle; each solve then only runs the sync-free
+ * kernel. */
+size_t bilu_sptrsv_analysis_bytes(int nb);
+size_t bilu_sptrsv_solve_ws_bytes(int nb);
+int bilu_sptrsv_analysis(int nb, int bs, const int* d_row, const int* d_col, int lower,
+                         void* d_info, void* d_ws, size_t ws_bytes, bilu_stream_t stream);
+int bilu_sptrsv_solve(int nb, int bs, const int* d_row, const int* d_col, const double* d_val,
+                      int lower, int unit, const void* d_info, const double* d_b, double* d_x,
+                      void* d_ws, size_t ws_bytes, bilu_stream_t stream);
 /* General form: lower/upper triangle of a packed factor, unit or non-unit
  * diagonal (bilu_sptrsv uses lower+unit and upper+non-unit). */
 int bilu_sptrsv_ex(int nb, int bs, const int* d_row, const int* d_col, const double* d_val,
@@ -264,8 +280,8 @@ int bilu_ctx_destroy(bilu_ctx* ctx);
 int bilu_ctx_setup(bilu_ctx* ctx, int nb, int nnzb, int bs, const int* d_row, const int* d_col,
                    const double* d_val, int prec_mask, double* h_times);
 
-/* Right-preconditioned restarted (F)GMRES(restart) with CGS2 and Givens
- * rotations, x0 = 0: prec BILU_FP64 applies the FP64 ISAI, BILU_FP32 the
+/* Right-preconditioned restarted (F)GMRES(restart) with modified
+ * Gram-Schmidt and Givens rotations, x0 = 0: prec BILU_FP64 applies the FP64 ISAI, BILU_FP32 the
  * FP32-stored ISAI (flexible GMRES, FP64 residuals/orthogonalisation,
  * FP64 true residual at every restart = iterative refinement); prec -1 runs
  * without preconditioner.  h_iters, h_relres: iteration count and final true
@@ -274,7 +290,8 @@ int bilu_ctx_setup(bilu_ctx* ctx, int nb, int nnzb, int bs, const int* d_row, co
 int bilu_ctx_solve(bilu_ctx* ctx, int prec, const double* d_b, double* d_x, int restart,
                    double tol, int maxit, int* h_iters, double* h_relres, double* h_hist);
 
-/* Counters of the last solve: h_out[0] = reorthogonalisation passes. */
+/* Counters of the last solve: h_out[0] = Arnoldi steps, h_out[1] = restart
+ * cycles. */
 int bilu_ctx_stats(bilu_ctx* ctx, long long* h_out);
 
 /* Host-buffer convenience (the end-to-end call): copies A and b from host

@@ -319,7 +319,7 @@ class SolveResult:
     relres: float
     converged: bool
     history: list
-    reorth: int = 0
+    restarts: int = 0
 
 
 class Preconditioner:
@@ -382,7 +382,7 @@ class Preconditioner:
         h = list(hist[: it.value + 1]) if history else []
         stats = (ctypes.c_longlong * 4)()
         call("bilu_ctx_stats", self._h, stats)
-        return x, SolveResult(it.value, rr.value, st == 0, h, int(stats[0]))
+        return x, SolveResult(it.value, rr.value, st == 0, h, int(stats[1]))
 
 
 def solve_host(nb: int, bs: int, row, col, val, b, prec: int = BILU_FP64, restart: int = 30,

@@ -88,11 +88,15 @@ __global__ void k_reduce(const double* __restrict__ partial, int nout, double* _
 }
 
 __global__ void k_scale_rsqrt(long long n, const double* __restrict__ x,
-                              const double* __restrict__ nrm2, double* __restrict__ y) {
+                              const double* __restrict__ nrm2, double* __restrict__ y,
+                              float* __restrict__ y32) {
   double a = 1.0 / sqrt(*nrm2);
   long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride)
-    y[e] = x[e] * a;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+    double v = x[e] * a;
+    y[e] = v;
+    if (y32) y32[e] = __double2float_rn(v);
+  }
 }
 
 __global__ void __launch_bounds__(kRedThreads) k_residual(long long n, const double* __restrict__ b,
@@ -147,6 +151,61 @@ void launch_multiaxpy(long long n, const double* V, long long ldv, const double*
     default: return BILU_ERR_ARG;                                                    \
   }
 
+// One modified Gram-Schmidt step fused with the next one's dot product:
+// w -= h_prev * v_prev (h_prev read from device memory), then the partial of
+// v_next . w (or w . w).  The basis vectors stream through with evict-first
+// loads; w (one vector, 67 MB at 128^3) is left to the L2.  The CTA that
+// finishes last sums the CTA partials in index order, so the result does not
+// depend on which CTA that is.
+__global__ void __launch_bounds__(kRedThreads) k_mgs_sweep(
+    long long n, const double* __restrict__ vp, const double* __restrict__ hp,
+    const double* __restrict__ vn, double* __restrict__ w, double* __restrict__ partial,
+    unsigned* counter, double* out) {
+  double h = vp ? -__ldg(hp) : 0.0;
+  double acc = 0.0;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+    double we = w[e];
+    if (vp) {
+      we = fma(h, __ldcs(vp + e), we);
+      w[e] = we;
+    }
+    double o = vn ? __ldcs(vn + e) : we;
+    acc = fma(o, we, acc);
+  }
+  __shared__ double red[kRedThreads / 32];
+  __shared__ bool last;
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) red[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < kRedThreads / 32; ++i) s += red[i];
+    partial[blockIdx.x] = s;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double s = 0.0;
+  for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) s += __ldcg(partial + c);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) red[warp] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+#pragma unroll
+    for (int i = 0; i < kRedThreads / 32; ++i) t += red[i];
+    *out = t;
+    *counter = 0u;
+  }
+}
+
 }  // namespace
 
 int multidot(long long n, const double* V, long long ldv, int nv, const double* w, bool with_ww,
@@ -171,8 +230,16 @@ int reduce_partials(const double* partial, int nout, double* out, cudaStream_t s
   return BILU_OK;
 }
 
-int scale_rsqrt(long long n, const double* x, const double* nrm2, double* y, cudaStream_t st) {
-  k_scale_rsqrt<<<kRedCTAs, kRedThreads, 0, st>>>(n, x, nrm2, y);
+int scale_rsqrt(long long n, const double* x, const double* nrm2, double* y, cudaStream_t st,
+                float* y32) {
+  k_scale_rsqrt<<<kRedCTAs, kRedThreads, 0, st>>>(n, x, nrm2, y, y32);
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
+}
+
+int mgs_sweep(long long n, const double* vp, const double* hp, const double* vn, double* w,
+              double* partial, unsigned* counter, double* out, cudaStream_t st) {
+  k_mgs_sweep<<<kSweepCTAs, kRedThreads, 0, st>>>(n, vp, hp, vn, w, partial, counter, out);
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }

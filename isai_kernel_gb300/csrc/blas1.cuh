@@ -9,6 +9,7 @@ constexpr int kRedCTAs = 152 * 4;  // partial-sum slots (fixed => deterministic)
 constexpr int kRedThreads = 256;
 constexpr int kMaxVec = 32;        // vectors per multi-dot / multi-axpy call
 constexpr int kPartStride = kMaxVec + 2;
+constexpr int kSweepCTAs = 152 * 8;  // CTAs of one MGS sweep (one partial each)
 
 // partial[cta * kPartStride + i] = sum_e V[i][e] * w[e] (i < nv), and at
 // index nv: sum_e w[e]^2 when with_ww.  Skipped (partials left as they
@@ -23,10 +24,18 @@ int multiaxpy_norm(long long n, const double* V, long long ldv, int nv, const do
                    cudaStream_t st);
 // out[i] = sum_cta partial[cta*kPartStride + i], i < nout (one thread each).
 int reduce_partials(const double* partial, int nout, double* out, cudaStream_t st);
-// y = x * (1/sqrt(*nrm2)) with *nrm2 a device scalar
-int scale_rsqrt(long long n, const double* x, const double* nrm2, double* y, cudaStream_t st);
+// y = x * (1/sqrt(*nrm2)) with *nrm2 a device scalar; y32 (optional)
+// receives the same vector rounded to FP32 (input of the FP32 apply).
+int scale_rsqrt(long long n, const double* x, const double* nrm2, double* y, cudaStream_t st,
+                float* y32 = nullptr);
 // r = b - ax, partial norms of r
 int residual_norm(long long n, const double* b, const double* ax, double* r, double* partial,
                   cudaStream_t st);
+
+// One modified Gram-Schmidt sweep over w: if vp != null, w -= (*hp) * vp;
+// then *out = vn . w (or w . w when vn == null), the CTA partials summed in a
+// fixed order by the last CTA to finish (counter returns to 0 afterwards).
+int mgs_sweep(long long n, const double* vp, const double* hp, const double* vn, double* w,
+              double* partial, unsigned* counter, double* out, cudaStream_t st);
 
 }  // namespace bilu

@@ -52,22 +52,11 @@ int spmv_any(int mb, int bs, int prec, const int* row, const int* col, const voi
 int isai_apply_impl(int nb, int bs, int prec, const int* Lrow, const int* Lcol, const void* Lval,
                     const int* Urow, const int* Ucol, const void* Uval, const double* b,
                     void* tmp, double* x, cudaStream_t st);
+int isai_apply_f32_staged(int nb, int bs, const int* Lrow, const int* Lcol, const float* Lval,
+                          const int* Urow, const int* Ucol, const float* Uval, const float* b32,
+                          float* tmp, double* x, cudaStream_t st);
 
 namespace {
-
-__global__ void k_dgks_select(double* s, int nv) {
-  // s layout: [0..nv) h1, [nv] ww0 | s+kPartStride: ww1 | s+2*kPartStride:
-  // [0..nv) h2 | s+3*kPartStride: ww2 | flag at s+4*kPartStride (as double)
-  // | selected ww at s+5*kPartStride
-  double ww0 = s[nv], ww1 = s[kPartStride];
-  int flag = ww1 < 0.5 * ww0;
-  ((int*)(s + 4 * kPartStride))[0] = flag;
-}
-
-__global__ void k_pick_norm(double* s) {
-  int flag = ((const int*)(s + 4 * kPartStride))[0];
-  s[5 * kPartStride] = flag ? s[3 * kPartStride] : s[kPartStride];
-}
 
 }  // namespace
 
@@ -90,10 +79,12 @@ struct bilu_ctx {
   // solver buffers
   int m_alloc = 0;
   double *V = nullptr, *Z = nullptr, *w = nullptr, *r = nullptr, *tmp = nullptr;
+  float* v32 = nullptr;  // FP32 copy of the newest basis vector (mixed apply input)
   double *partial = nullptr, *dscal = nullptr, *dcoef = nullptr;
   double* hpin = nullptr;  // pinned host mirror of dscal
   cudaEvent_t ev = nullptr;
-  long long reorth = 0;    // reorthogonalisation passes of the last solve
+  unsigned* counter = nullptr;  // arrival counter of the MGS sweep reductions
+  long long steps = 0, restarts = 0;  // Arnoldi steps and cycles of the last solve
   std::vector<void*> setup_bufs;
   void free_setup() {
     for (void* p : setup_bufs) cudaFree(p);
@@ -104,8 +95,10 @@ struct bilu_ctx {
     ready = false;
   }
   void free_solver() {
-    cudaFree(V); cudaFree(Z); cudaFree(w); cudaFree(r); cudaFree(tmp);
-    cudaFree(partial); cudaFree(dscal); cudaFree(dcoef);
+    cudaFree(V); cudaFree(Z); cudaFree(w); cudaFree(r); cudaFree(tmp); cudaFree(v32);
+    v32 = nullptr;
+    cudaFree(partial); cudaFree(dscal); cudaFree(dcoef); cudaFree(counter);
+    counter = nullptr;
     if (hpin) cudaFreeHost(hpin);
     if (ev) cudaEventDestroy(ev);
     ev = nullptr;
@@ -326,10 +319,13 @@ int ensure_solver(bilu_ctx* c, int m) {
   BILU_TRY_CUDA(cudaMalloc(&c->w, sizeof(double) * n));
   BILU_TRY_CUDA(cudaMalloc(&c->r, sizeof(double) * n));
   BILU_TRY_CUDA(cudaMalloc(&c->tmp, sizeof(double) * n));
+  BILU_TRY_CUDA(cudaMalloc(&c->v32, sizeof(float) * n));
   BILU_TRY_CUDA(cudaMalloc(&c->partial, sizeof(double) * kRedCTAs * kPartStride));
   BILU_TRY_CUDA(cudaMalloc(&c->dscal, sizeof(double) * 6 * kPartStride));
   BILU_TRY_CUDA(cudaMalloc(&c->dcoef, sizeof(double) * kPartStride));
   BILU_TRY_CUDA(cudaMallocHost(&c->hpin, sizeof(double) * 6 * kPartStride));
+  BILU_TRY_CUDA(cudaMalloc(&c->counter, sizeof(unsigned)));
+  BILU_TRY_CUDA(cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->st));
   c->m_alloc = m;
   return BILU_OK;
 }
@@ -350,11 +346,14 @@ int apply_prec(bilu_ctx* c, int prec, const double* v, double* z) {
     BILU_TRY_CUDA(cudaMemcpyAsync(z, v, sizeof(double) * c->n, cudaMemcpyDeviceToDevice, c->st));
     return BILU_OK;
   }
-  const void* L = prec == BILU_FP32 ? (const void*)c->Lval32 : (const void*)c->Lval;
-  const void* U = prec == BILU_FP32 ? (const void*)c->Uval32 : (const void*)c->Uval;
-  if (!L || !U) return BILU_ERR_ARG;
-  return isai_apply_impl(c->nb, c->bs, prec, c->Lrow, c->Lcol, L, c->Urow, c->Ucol, U, v, c->tmp,
-                         z, c->st);
+  if (prec == BILU_FP32) {
+    // v32 (written with v by the normalisation kernel) is the FP32 copy of v
+    if (!c->Lval32 || !c->Uval32) return BILU_ERR_ARG;
+    return isai_apply_f32_staged(c->nb, c->bs, c->Lrow, c->Lcol, c->Lval32, c->Urow, c->Ucol,
+                                 c->Uval32, c->v32, (float*)c->tmp, z, c->st);
+  }
+  return isai_apply_impl(c->nb, c->bs, prec, c->Lrow, c->Lcol, c->Lval, c->Urow, c->Ucol,
+                         c->Uval, v, c->tmp, z, c->st);
 }
 
 }  // namespace
@@ -369,30 +368,25 @@ int arnoldi_front(bilu_ctx* c, int prec, int j) {
   return spmv_any(c->nb, c->bs, BILU_FP64, c->Arow, c->Acol, c->Aval, zj, 0, c->w, 0, c->st);
 }
 
-// Orthogonalises w against V_0..V_j (CGS, DGKS reorthogonalisation decided
-// on the device), writes V_{j+1} and queues the Hessenberg column to hpin.
-int arnoldi_back(bilu_ctx* c, int j) {
+// Orthogonalises w against V_0..V_j by modified Gram-Schmidt: j+2 fused
+// sweeps (w -= h_{i-1} v_{i-1} together with h_i = v_i . w; the last one
+// gives ||w||^2), each reduced in a fixed order on the device, then
+// V_{j+1} = w / ||w|| and the Hessenberg column is queued to hpin.
+// s[0..j] = h, s[kPartStride] = ||w||^2.
+int arnoldi_back(bilu_ctx* c, int j, int prec) {
   cudaStream_t st = c->st;
   long long n = c->n;
   double* s = c->dscal;
-  int nv = j + 1;
-  BILU_TRY(multidot(n, c->V, n, nv, c->w, true, c->partial, st));
-  BILU_TRY(reduce_partials(c->partial, nv + 1, s, st));
-  BILU_TRY(multiaxpy_norm(n, c->V, n, nv, s, -1.0, c->w, c->partial, nullptr, st));
-  BILU_TRY(reduce_partials(c->partial, 1, s + kPartStride, st));
-  k_dgks_select<<<1, 1, 0, st>>>(s, nv);
-  BILU_LAUNCH_CHECK();
-  const int* flag = (const int*)(s + 4 * kPartStride);
-  // pass 2 runs only when the DGKS test fired; its kernels read the device
-  // flag and return at once otherwise
-  BILU_TRY(multidot(n, c->V, n, nv, c->w, false, c->partial, st, flag));
-  BILU_TRY(reduce_partials(c->partial, nv, s + 2 * kPartStride, st));
-  BILU_TRY(multiaxpy_norm(n, c->V, n, nv, s + 2 * kPartStride, -1.0, c->w, c->partial, flag, st));
-  BILU_TRY(reduce_partials(c->partial, 1, s + 3 * kPartStride, st));
-  k_pick_norm<<<1, 1, 0, st>>>(s);
-  BILU_LAUNCH_CHECK();
-  BILU_TRY(scale_rsqrt(n, c->w, s + 5 * kPartStride, c->V + (size_t)n * (j + 1), st));
-  BILU_TRY_CUDA(cudaMemcpyAsync(c->hpin, s, sizeof(double) * 6 * kPartStride,
+  const double* V = c->V;
+  BILU_TRY(mgs_sweep(n, nullptr, nullptr, V, c->w, c->partial, c->counter, s, st));
+  for (int i = 1; i <= j; ++i)
+    BILU_TRY(mgs_sweep(n, V + (size_t)n * (i - 1), s + i - 1, V + (size_t)n * i, c->w, c->partial,
+                       c->counter, s + i, st));
+  BILU_TRY(mgs_sweep(n, V + (size_t)n * j, s + j, nullptr, c->w, c->partial, c->counter,
+                     s + kPartStride, st));
+  BILU_TRY(scale_rsqrt(n, c->w, s + kPartStride, c->V + (size_t)n * (j + 1), st,
+                       prec == BILU_FP32 ? c->v32 : nullptr));
+  BILU_TRY_CUDA(cudaMemcpyAsync(c->hpin, s, sizeof(double) * (kPartStride + 1),
                                 cudaMemcpyDeviceToHost, st));
   return BILU_OK;
 }
@@ -423,33 +417,29 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
   BILU_TRY(norm2(c, c->r, s + 5 * kPartStride, &rr));
   double beta = std::sqrt(rr);
   int total = 0, status = BILU_ERR_NOT_CONVERGED;
-  c->reorth = 0;
+  c->steps = 0;
+  c->restarts = 0;
   double res = beta / bnorm;
   if (h_hist) h_hist[0] = res;
   if (res <= tol) status = BILU_OK;
   while (status != BILU_OK && total < maxit) {
     // V_0 = r / beta (beta^2 sits in s[5*kPartStride])
-    BILU_TRY(scale_rsqrt(n, c->r, s + 5 * kPartStride, c->V, st));
+    BILU_TRY(scale_rsqrt(n, c->r, s + 5 * kPartStride, c->V, st,
+                         prec == BILU_FP32 ? c->v32 : nullptr));
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int jlast = -1;
     BILU_TRY(arnoldi_front(c, prec, 0));
     for (int j = 0; j < m && total < maxit; ++j) {
-      BILU_TRY(arnoldi_back(c, j));
+      BILU_TRY(arnoldi_back(c, j, prec));
       BILU_TRY_CUDA(cudaEventRecord(c->ev, st));
       // the next basis vector's apply and SpMV do not depend on the host
       // Givens step: queue them before waiting (discarded if this step
       // converges)
       if (j + 1 < m && total + 1 < maxit) BILU_TRY(arnoldi_front(c, prec, j + 1));
       BILU_TRY_CUDA(cudaEventSynchronize(c->ev));
-      int fl = ((const int*)(hp + 4 * kPartStride))[0];
-      c->reorth += fl;
-      for (int i = 0; i <= j; ++i) {
-        double h = 0.0 + hp[i];
-        if (fl) h += hp[2 * kPartStride + i];
-        H[(size_t)i * m + j] = h;
-      }
-      double hn = std::sqrt(hp[5 * kPartStride]);
+      for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hp[i];
+      double hn = std::sqrt(hp[kPartStride]);
       H[(size_t)(j + 1) * m + j] = hn;
       for (int i = 0; i < j; ++i) {
         double a = H[(size_t)i * m + j], b = H[(size_t)(i + 1) * m + j];
@@ -470,6 +460,8 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
       if (h_hist) h_hist[total] = res;
       if (res <= tol || hn == 0.0) break;
     }
+    c->steps += jlast + 1;
+    c->restarts += 1;
     for (int i = jlast; i >= 0; --i) {
       double v = g[i];
       for (int k = i + 1; k <= jlast; ++k) v -= H[(size_t)i * m + k] * y[k];
@@ -497,7 +489,8 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
 
 extern "C" int bilu_ctx_stats(bilu_ctx* c, long long* h_out) {
   if (!c || !h_out) return BILU_ERR_ARG;
-  h_out[0] = c->reorth;
+  h_out[0] = c->steps;
+  h_out[1] = c->restarts;
   return BILU_OK;
 }
 

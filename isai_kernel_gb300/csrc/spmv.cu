@@ -39,8 +39,28 @@ __device__ __forceinline__ float to_acc(float v, float) { return v; }
 template <int BS, class XT, class AccT>
 __device__ __forceinline__ void load_x(const XT* __restrict__ x, long long bc, AccT* xr) {
   const XT* p = x + bc * BS;
+  constexpr int W = Vec<XT>::W;
+  if constexpr (BS % W == 0) {
+    // the segment starts at bc*BS elements: 16-byte aligned when BS is a
+    // multiple of the vector width
+    using V = typename Vec<XT>::V;
 #pragma unroll
-  for (int c = 0; c < BS; ++c) xr[c] = to_acc(__ldg(p + c), AccT());
+    for (int c = 0; c < BS / W; ++c) {
+      V v = __ldg(reinterpret_cast<const V*>(p) + c);
+      if constexpr (W == 2) {
+        xr[2 * c] = to_acc(v.x, AccT());
+        xr[2 * c + 1] = to_acc(v.y, AccT());
+      } else {
+        xr[4 * c] = to_acc(v.x, AccT());
+        xr[4 * c + 1] = to_acc(v.y, AccT());
+        xr[4 * c + 2] = to_acc(v.z, AccT());
+        xr[4 * c + 3] = to_acc(v.w, AccT());
+      }
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < BS; ++c) xr[c] = to_acc(__ldg(p + c), AccT());
+  }
 }
 
 // Row r of block p (BS values) into registers, streaming loads.
@@ -70,50 +90,82 @@ __device__ __forceinline__ void load_row(const VT* __restrict__ val, long long p
 }
 
 // y = M x: lane group of BS lanes per block row, lane r owns scalar row r.
-// U blocks per loop trip keep U independent block loads in flight per lane
-// (2 for FP64 values, 4 for FP32 values, whose rows are half as wide).
-template <int BS, class VT, class XT, class YT, class AccT>
-__global__ void __launch_bounds__(256, 4) k_bsr_spmv(int mb, const int* __restrict__ row,
+// A group handles RPG consecutive block rows and issues the loads of the
+// first U blocks of all of them before any arithmetic, so a warp keeps
+// RPG*U independent block loads per lane in flight (the rows of the ISAI
+// factors hold about 4 blocks, so one batch usually covers them).  FP64
+// values: U = 2, RPG = 1 (the DFMA pipe, not memory, is the limit); FP32
+// values: U = 4, RPG = 2 (memory latency is the limit).
+template <int BS, class VT, class XT, class YT, class AccT, int RPG>
+__global__ void __launch_bounds__(256, 2) k_bsr_spmv(int mb, const int* __restrict__ row,
                                                      const int* __restrict__ col,
                                                      const VT* __restrict__ val,
                                                      const XT* __restrict__ x,
                                                      YT* __restrict__ y) {
-  constexpr int G = 32 / BS;  // block rows per warp
+  constexpr int G = 32 / BS;  // lane groups per warp
   constexpr int U = sizeof(VT) == 4 ? 4 : 2;
   int lane = threadIdx.x & 31;
   int g = lane / BS, r = lane - g * BS;
-  long long br = ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G + g;
-  if (g >= G || br >= mb) return;
-  int s = __ldg(row + br), e = __ldg(row + br + 1);
-  AccT acc[U];
+  long long base = (((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G + g) * RPG;
+  if (g >= G || base >= mb) return;
+  int s[RPG], e[RPG];
 #pragma unroll
-  for (int u = 0; u < U; ++u) acc[u] = 0;
-  int p = s;
-  for (; p + U <= e; p += U) {
-    AccT a[U][BS], xv[U][BS];
-    int c[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) c[u] = __ldg(col + p + u);
-#pragma unroll
-    for (int u = 0; u < U; ++u) load_row<BS, VT, AccT>(val, p + u, r, a[u]);
-#pragma unroll
-    for (int u = 0; u < U; ++u) load_x<BS, XT, AccT>(x, c[u], xv[u]);
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-#pragma unroll
-      for (int k = 0; k < BS; ++k) acc[u] = fma(a[u][k], xv[u][k], acc[u]);
+  for (int q = 0; q < RPG; ++q) {
+    bool ok = base + q < mb;
+    s[q] = ok ? __ldg(row + base + q) : 0;
+    e[q] = ok ? __ldg(row + base + q + 1) : 0;
   }
-  for (; p < e; ++p) {
-    AccT a0[BS], x0[BS];
-    load_row<BS, VT, AccT>(val, p, r, a0);
-    load_x<BS, XT, AccT>(x, __ldg(col + p), x0);
+  AccT acc[RPG];
 #pragma unroll
-    for (int k = 0; k < BS; ++k) acc[0] = fma(a0[k], x0[k], acc[0]);
+  for (int q = 0; q < RPG; ++q) acc[q] = 0;
+  // batches of U blocks per row; every load of a batch (column indices,
+  // block rows, x segments) is issued before its FMAs
+  for (int off = 0;; off += U) {
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < RPG; ++q) any |= s[q] + off < e[q];
+    if (!any) break;
+    int c[RPG][U];
+#pragma unroll
+    for (int q = 0; q < RPG; ++q)
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        int p = s[q] + off + u;
+        c[q][u] = p < e[q] ? __ldg(col + p) : -1;
+      }
+    AccT a[RPG][U][BS], xv[RPG][U][BS];
+#pragma unroll
+    for (int q = 0; q < RPG; ++q)
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (c[q][u] >= 0) {
+          load_row<BS, VT, AccT>(val, s[q] + off + u, r, a[q][u]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < BS; ++k) a[q][u][k] = 0;
+        }
+      }
+#pragma unroll
+    for (int q = 0; q < RPG; ++q)
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (c[q][u] >= 0) {
+          load_x<BS, XT, AccT>(x, c[q][u], xv[q][u]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < BS; ++k) xv[q][u][k] = 0;
+        }
+      }
+#pragma unroll
+    for (int q = 0; q < RPG; ++q)
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int k = 0; k < BS; ++k) acc[q] = fma(a[q][u][k], xv[q][u][k], acc[q]);
   }
-  AccT t = acc[0];
 #pragma unroll
-  for (int u = 1; u < U; ++u) t += acc[u];
-  y[br * BS + r] = (YT)t;
+  for (int q = 0; q < RPG; ++q)
+    if (base + q < mb) y[(base + q) * BS + r] = (YT)acc[q];
 }
 
 template <int BS, class VT, class XT, class YT>
@@ -122,9 +174,11 @@ int launch_spmv(int mb, const int* row, const int* col, const VT* val, const XT*
   using AccT = VT;
   if (mb == 0) return BILU_OK;
   constexpr int G = 32 / BS;
-  long long warps = (mb + G - 1) / G;
+  constexpr int RPG = sizeof(VT) == 4 ? 2 : 1;
+  long long groups = (mb + RPG - 1) / RPG;
+  long long warps = (groups + G - 1) / G;
   unsigned grid = ceil_div(warps, 8);
-  k_bsr_spmv<BS, VT, XT, YT, AccT><<<grid, 256, 0, st>>>(mb, row, col, val, x, y);
+  k_bsr_spmv<BS, VT, XT, YT, AccT, RPG><<<grid, 256, 0, st>>>(mb, row, col, val, x, y);
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }
@@ -239,12 +293,38 @@ int spmv_any(int mb, int bs, int prec, const int* row, const int* col, const voi
   return BILU_DISPATCH_BS(bs, spmv_f32, mb, row, col, (const float*)val, x, x32, y, y32, st);
 }
 
+int convert_f64_f32(size_t count, const double* src, float* dst, cudaStream_t st) {
+  if (count == 0) return BILU_OK;
+  unsigned grid = (unsigned)std::min<size_t>((count + 255) / 256, 152 * 16);
+  k_f64_to_f32<<<grid, 256, 0, st>>>(count, src, dst);
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
+}
+
+// FP32 path: b is rounded to FP32 once (n conversions; converting inside the
+// SpMV would cost one FP64-pipe conversion per block element, the slowest
+// operation on GB300), staged in the output buffer (n doubles hold n floats),
+// then y32 = M_L b32 and x = M_U y32 with FP32 accumulation.
 int isai_apply_impl(int nb, int bs, int prec, const int* Lrow, const int* Lcol, const void* Lval,
                     const int* Urow, const int* Ucol, const void* Uval, const double* b,
                     void* tmp, double* x, cudaStream_t st) {
-  int tmp32 = prec == BILU_FP32;
-  BILU_TRY(spmv_any(nb, bs, prec, Lrow, Lcol, Lval, b, 0, tmp, tmp32, st));
-  return spmv_any(nb, bs, prec, Urow, Ucol, Uval, tmp, tmp32, x, 0, st);
+  if (prec == BILU_FP32) {
+    float* b32 = reinterpret_cast<float*>(x);
+    BILU_TRY(convert_f64_f32((size_t)nb * bs, b, b32, st));
+    BILU_TRY(spmv_any(nb, bs, prec, Lrow, Lcol, Lval, b32, 1, tmp, 1, st));
+    return spmv_any(nb, bs, prec, Urow, Ucol, Uval, tmp, 1, x, 0, st);
+  }
+  BILU_TRY(spmv_any(nb, bs, prec, Lrow, Lcol, Lval, b, 0, tmp, 0, st));
+  return spmv_any(nb, bs, prec, Urow, Ucol, Uval, tmp, 0, x, 0, st);
+}
+
+// Solver form: the FP32 copy of the input is already there (written by the
+// kernel that produced the FP64 basis vector).
+int isai_apply_f32_staged(int nb, int bs, const int* Lrow, const int* Lcol, const float* Lval,
+                          const int* Urow, const int* Ucol, const float* Uval, const float* b32,
+                          float* tmp, double* x, cudaStream_t st) {
+  BILU_TRY(spmv_any(nb, bs, BILU_FP32, Lrow, Lcol, Lval, b32, 1, tmp, 1, st));
+  return spmv_any(nb, bs, BILU_FP32, Urow, Ucol, Uval, tmp, 1, x, 0, st);
 }
 
 }  // namespace bilu

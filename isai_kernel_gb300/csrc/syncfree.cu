@@ -495,9 +495,58 @@ int sptrsv_impl(int nb, int bs, const int* row, const int* col, const int* diag,
   return sync_finish(ss, nullptr, st);
 }
 
+// Solve with a precomputed analysis (diagonal positions + level order).
+// With sync=false the call returns without waiting for the GPU; the error
+// word is then not read back (use for repeated solves inside a solver).
+int sptrsv_ordered(int nb, int bs, const int* row, const int* col, const int* diag,
+                   const int* order, const double* val, int lower, int unit, const double* b,
+                   double* x, Carver& ws, cudaStream_t st, bool sync) {
+  SyncState ss;
+  BILU_TRY(sync_init(ss, nb, ws, st));
+  ss.order = order;
+  if (nb > 0)
+    BILU_TRY(BILU_DISPATCH_BS(bs, launch_sptrsv, nb, row, col, diag, val, lower, unit, b, x, ss,
+                              st));
+  return sync ? sync_finish(ss, nullptr, st) : BILU_OK;
+}
+
 }  // namespace bilu
 
 using namespace bilu;
+
+extern "C" size_t bilu_sptrsv_analysis_bytes(int nb) {
+  return 2 * carve_size(sizeof(int) * ((size_t)nb + 1));
+}
+
+extern "C" size_t bilu_sptrsv_solve_ws_bytes(int nb) { return syncfree_ws(nb); }
+
+extern "C" int bilu_sptrsv_analysis(int nb, int bs, const int* d_row, const int* d_col, int lower,
+                                    void* d_info, void* d_ws, size_t ws_bytes,
+                                    bilu_stream_t stream) {
+  if (nb < 0 || !d_info || (nb > 0 && (!d_row || !d_col))) return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  Carver info(d_info, bilu_sptrsv_analysis_bytes(nb));
+  int* diag = info.take<int>((size_t)nb + 1);
+  int* order = info.take<int>((size_t)nb + 1);
+  Carver ws(d_ws, ws_bytes);
+  BILU_TRY(diag_positions(nb, d_row, d_col, diag, nullptr, ws, S(stream)));
+  return build_order(nb, d_row, d_col, diag, lower != 0, order, ws, S(stream));
+}
+
+extern "C" int bilu_sptrsv_solve(int nb, int bs, const int* d_row, const int* d_col,
+                                 const double* d_val, int lower, int unit, const void* d_info,
+                                 const double* d_b, double* d_x, void* d_ws, size_t ws_bytes,
+                                 bilu_stream_t stream) {
+  if (nb < 0 || !d_info || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)))
+    return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  Carver info(const_cast<void*>(d_info), bilu_sptrsv_analysis_bytes(nb));
+  const int* diag = info.take<int>((size_t)nb + 1);
+  const int* order = info.take<int>((size_t)nb + 1);
+  Carver ws(d_ws, ws_bytes);
+  return sptrsv_ordered(nb, bs, d_row, d_col, diag, order, d_val, lower != 0, unit != 0, d_b, d_x,
+                        ws, S(stream), true);
+}
 
 extern "C" size_t bilu_bsrilu0_ws_bytes(int nb) {
   return syncfree_ws(nb) + carve_size(sizeof(int) * ((size_t)nb + 1));

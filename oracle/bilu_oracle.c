@@ -681,9 +681,7 @@ static void isai_apply(const isai_apply_t* P, int precond, const double* v,
 /* Restarted right-preconditioned (F)GMRES(m):
  *   r0 = b - A x0 (x0 = 0), beta = ||r0||; V_0 = r0 * (1/beta); g = beta e_1
  *   for j: z_j = M v_j; w = A z_j;
- *          classical Gram-Schmidt h = V^T w, w -= V h, with one
- *          reorthogonalisation pass when ||w_new||^2 < ||w_old||^2 / 2
- *          (DGKS criterion, eta = 1/sqrt 2);
+ *          modified Gram-Schmidt: for i = 0..j: h_i = v_i . w, w -= h_i v_i;
  *          h(j+1,j) = ||w||; v_{j+1} = w * (1/h(j+1,j)); Givens rotations;
  *          stop the cycle when |g_{j+1}| <= tol*||b|| or the budget is used
  *   x += Z y (upper-triangular solve of H y = g); true residual at restart.
@@ -738,21 +736,15 @@ int orc_gmres(int nb, int bs, const int* Arow, const int* Acol,
       double* zj = Z + n * (size_t)j;
       isai_apply(&P, precond, vj, zj, n);
       orc_bcsr_spmv(nb, bs, Arow, Acol, Aval, zj, w);
-      double ww0 = dot_chunked(n, w, w), hn = 0.0;
-      for (int i = 0; i <= j; ++i) H[i * m + j] = 0.0;
-      for (int pass = 0; pass < 2; ++pass) {
-        for (int i = 0; i <= j; ++i) hcol[i] = dot_chunked(n, V + n * (size_t)i, w);
+      /* modified Gram-Schmidt */
+      for (int i = 0; i <= j; ++i) {
+        const double* vi = V + n * (size_t)i;
+        double h = dot_chunked(n, vi, w);
+        H[i * m + j] = h;
 #pragma omp parallel for schedule(static)
-        for (long e = 0; e < (long)n; ++e) {
-          double s = w[e];
-          for (int i = 0; i <= j; ++i) s -= hcol[i] * V[n * (size_t)i + e];
-          w[e] = s;
-        }
-        for (int i = 0; i <= j; ++i) H[i * m + j] += hcol[i];
-        double ww1 = dot_chunked(n, w, w);
-        hn = sqrt(ww1);
-        if (!(ww1 < 0.5 * ww0)) break;
+        for (long e = 0; e < (long)n; ++e) w[e] -= h * vi[e];
       }
+      double hn = sqrt(dot_chunked(n, w, w));
       H[(j + 1) * m + j] = hn;
       double* vn = V + n * (size_t)(j + 1);
       if (hn != 0.0) {

@@ -110,7 +110,7 @@ int orc_rel_errors_csr(int n, const int* row, const int* col, const double* val,
                        const double* b, const double* x_true, const double* x,
                        double* rel_err, double* rel_res);
 
-/* Right-preconditioned restarted (F)GMRES(m), CGS2 orthogonalisation,
+/* Right-preconditioned restarted (F)GMRES(m), modified Gram-Schmidt,
  * Givens rotations, x0 = 0.  The reference has no Krylov solver; this is the
  * oracle that defines iteration counts.  precond: 0 none, 1 ISAI FP64
  * (z = M_U (M_L v)), 2 ISAI with FP32-stored factors and FP32 accumulation.

@@ -252,7 +252,7 @@ def rel_errors(n, row, col, val, b, x_true, x):
 
 
 def gmres(A, L, U, b, precond=1, restart=30, tol=1e-10, maxit=3000):
-    """Restarted right-preconditioned (F)GMRES(m) with CGS2 (no counterpart
+    """Restarted right-preconditioned (F)GMRES(m) with modified Gram-Schmidt (no counterpart
     in the reference).  A, L, U: (rowptr, colind, val) triples in BCSR.
     Returns (x, iters, relres, history, status)."""
     nb = A[0].shape[0] - 1
