@@ -36,7 +36,7 @@ FALLBACK_HBM_GBS = 6800.0
 # FP64 and mixed iteration counts of the 128^3 system measured on GB300 with
 # this code (the FP64 count equals the oracle's at every size the oracle can
 # finish); used to scale the CPU baseline's per-iteration cost.
-C2_ITERS_REF = {"fp64": None, "mixed": None}
+C2_ITERS_REF = {"fp64": 328, "mixed": 328}
 
 
 def parse():
@@ -51,6 +51,16 @@ def parse():
     ap.add_argument("--maxit", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-iters", type=int, default=3)
+    ap.add_argument("--workload", default="convdiff",
+                    choices=["convdiff", "batch", "powerlaw", "sptrsv"],
+                    help="convdiff: the headline line; batch / powerlaw / sptrsv: secondary lines")
+    ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--batch-lo", type=int, default=32)
+    ap.add_argument("--batch-hi", type=int, default=512)
+    ap.add_argument("--batch-rhs", type=int, default=32)
+    ap.add_argument("--batch-seed", type=int, default=0)
+    ap.add_argument("--batch-mem-gb", type=float, default=160.0)
+    ap.add_argument("--pl-nb", type=int, default=500000)
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu launch lists: setup, one warm-up and one timed "
                          "solve capped at --maxit, the apply loop; no e2e, no CPU baseline")
@@ -370,10 +380,145 @@ def run_ours(args):
     print(json.dumps(line))
 
 
+def run_batch(args):
+    """Secondary line: 256 seeded 2D 5-point 4-DOF systems, grid sides
+    U{32..512} (seed s for system s), 32 uniform right-hand sides each, FP32
+    ISAI apply inside FP64 FGMRES(30), all systems in one block-diagonal setup
+    and per-step single launches; --maxit caps the Arnoldi steps per wave."""
+    import torch
+
+    from isai_kernel_gb300 import api, gen
+
+    rng = np.random.default_rng(args.batch_seed)
+    sides = rng.integers(args.batch_lo, args.batch_hi + 1, size=args.batch_count)
+    mats = [gen.laplace2d(int(s), bs=4, seed=args.batch_seed + i) for i, s in enumerate(sides)]
+    k = args.batch_rhs
+    B = np.concatenate([gen.rhs(A.n, args.batch_seed + i, k=k) for i, A in enumerate(mats)])
+    t0 = time.perf_counter()
+    bt = api.Batch(mats)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    Bd = torch.from_numpy(B).cuda()
+    X, iters, relres, stats = bt.solve(Bd, restart=args.restart, tol=args.tol, maxit=args.maxit,
+                                       mem_budget=int(args.batch_mem_gb * (1 << 30)))
+    cfg, tune_ms = bt.tuning()
+    conv = float(np.mean(relres <= args.tol))
+    line = {"workload": f"batch {args.batch_count} x laplace2d U{{{args.batch_lo}..{args.batch_hi}}}"
+                        f" bs4, {k} rhs, FGMRES({args.restart}) FP32 ISAI, maxit {args.maxit}",
+            "systems": args.batch_count, "rhs": k, "block_rows": bt.nb,
+            "setup_s": t_setup, "solve_s": stats[3] / 1e3, "waves": int(stats[0]),
+            "graph_launches": int(stats[1]), "pair_steps": int(stats[2]),
+            "pair_steps_per_s": stats[2] / (stats[3] / 1e3),
+            "converged_fraction": conv, "median_iters": float(np.median(iters)),
+            "autotune": {"rows_per_warp_A": cfg[0], "rows_per_warp_apply": cfg[1],
+                         "candidates_ms_A": tune_ms[:3], "candidates_ms_apply": tune_ms[3:]}}
+    bt.close()
+    print(json.dumps(line))
+
+
+def run_powerlaw(args):
+    """Secondary line: random power-law block matrix (500k block rows, 8x8
+    blocks), BILU(0)+ISAI setup and FP64 / mixed FGMRES(30) to 1e-10."""
+    import torch
+
+    from isai_kernel_gb300 import api, gen
+
+    A = gen.powerlaw(args.pl_nb, bs=8, seed=0)
+    b = torch.from_numpy(gen.rhs(A.n, 0)).cuda()
+    row, col, val = (torch.from_numpy(a).cuda() for a in (A.rowptr, A.colind, A.val))
+    P = api.Preconditioner(A.nb, 8, row, col, val)
+    out = {"workload": f"powerlaw nb={A.nb} bs8 nnzb={A.nnzb}", "setup_ms": P.setup_ms}
+    for prec, tag in ((0, "fp64"), (1, "mixed")):
+        P.solve(b, prec=prec, maxit=args.maxit)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _, res = P.solve(b, prec=prec, maxit=args.maxit)
+        e1.record()
+        e1.synchronize()
+        out[tag] = {"s": e0.elapsed_time(e1) / 1e3, "iters": res.iters, "relres": res.relres}
+    lu, Lf, Uf = P.factors()
+    x = torch.empty_like(b)
+    t = []
+    for lower in (True, False):
+        api.sptrsv(A.nb, 8, row, col, lu.view(-1, 8, 8), b, lower=lower)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        api.sptrsv(A.nb, 8, row, col, lu.view(-1, 8, 8), b, lower=lower)
+        e1.record()
+        e1.synchronize()
+        t.append(e0.elapsed_time(e1))
+    out["sptrsv_ms_incl_analysis"] = {"L": t[0], "U": t[1]}
+    P.close()
+    print(json.dumps(out))
+
+
+def run_sptrsv(args):
+    """Secondary line: block triangular solves with the packed BILU(0) of the
+    --side^3 convection-diffusion system.  One level analysis per triangle,
+    then the level-scheduled and the sync-free solve on it (CUDA events over
+    --steps solves each, after --warmup).  Bytes per solve: the triangle's
+    blocks with their column indices, the diagonal blocks, row pointers,
+    the order, b and x."""
+    import torch
+
+    from isai_kernel_gb300 import _lib, api, gen
+
+    L = _lib.lib()
+    A = gen.convdiff3d(args.side, bs=4, seed=0)
+    nb, bs, nnzb = A.nb, A.bs, A.nnzb
+    dev = torch.device("cuda", 0)
+    row, col, val = (torch.from_numpy(a).to(dev) for a in (A.rowptr, A.colind, A.val))
+    lu = val.clone()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    zp = api.bsrilu02_inplace(nb, nnzb, bs, row, col, lu)
+    e1.record()
+    e1.synchronize()
+    out = {"workload": f"sptrsv convdiff3d {args.side}^3 bs4 (nb={nb}, nnzb={nnzb})",
+           "bilu0_ms_incl_analysis": e0.elapsed_time(e1), "zero_pivot": zp}
+    b = torch.from_numpy(gen.rhs(A.n, 1)).to(dev)
+    x = torch.empty_like(b)
+    P = api._p
+    info = api._ws(L.bilu_sptrsv_analysis_bytes(nb), dev)
+    ws = api._ws(max(L.bilu_sptrsv_analysis_ws_bytes(nb, nnzb), L.bilu_sptrsv_solve_ws_bytes(nb)),
+                 dev)
+    strict = (nnzb - nb) // 2
+    for lower in (1, 0):
+        tag = "L" if lower else "U"
+        e0.record()
+        api.call("bilu_sptrsv_analysis", nb, nnzb, bs, P(row), P(col), lower, P(info), P(ws),
+                 ws.numel(), api._s())
+        e1.record()
+        e1.synchronize()
+        out[f"{tag}_analysis_ms"] = e0.elapsed_time(e1)
+        for fn, name in (("bilu_sptrsv_solve", "level"), ("bilu_sptrsv_solve_syncfree", "syncfree")):
+            def solve():
+                api.call(fn, nb, bs, P(row), P(col), P(lu), lower, lower, P(info), P(b), P(x),
+                         P(ws), ws.numel(), api._s())
+            for _ in range(args.warmup):
+                solve()
+            e0.record()
+            for _ in range(args.steps):
+                solve()
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            nbytes = (strict + nb) * (bs * bs * 8 + 4) + (nb + 1) * 4 * 3 + 2 * A.n * 8
+            out[f"{tag}_{name}_ms"] = ms
+            out[f"{tag}_{name}_GBs"] = nbytes / ms / 1e6
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
+    elif args.workload == "powerlaw":
+        run_powerlaw(args)
+    elif args.workload == "sptrsv":
+        run_sptrsv(args)
     else:
         run_ours(args)
 

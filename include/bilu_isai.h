@@ -123,9 +123,11 @@ int bilu_bcsc_to_bcsr(int mb, int nbcol, int bs, const int* d_cscPtr, const int*
 /* ------------------------------------------------------------------ */
 
 /* Replaces bsrilu02_inplace (bsrilu.h:20; cuSPARSE bsrilu02, row direction,
- * no level information): sync-free BILU(0) in place.  h_info[0] receives the
- * first block row with a zero pivot (or -1); BILU_ERR_ZERO_PIVOT then. */
-size_t bilu_bsrilu0_ws_bytes(int nb);
+ * no level information): BILU(0) in place, scheduled by dependency level
+ * (level analysis of the lower DAG, then one cooperative launch with a
+ * bounded grid barrier per level).  h_info[0] receives the first block row
+ * with a zero pivot (or -1); BILU_ERR_ZERO_PIVOT then. */
+size_t bilu_bsrilu0_ws_bytes(int nb, int nnzb);
 int bilu_bsrilu0(int nb, int nnzb, int bs, const int* d_row, const int* d_col, double* d_val,
                  int* h_info, void* d_ws, size_t ws_bytes, bilu_stream_t stream);
 
@@ -197,29 +199,39 @@ int bilu_isai_apply(int nb, int bs, int prec, const int* d_Lrow, const int* d_Lc
 
 /* Replaces spTrSolveL / spTrSolveU (cape_sptrsv.h:8,55) and
  * csr_cape_SpTRSV (cape_sptrsv.h:105), blockwise on the packed BILU(0):
- * lower: unit-lower L x = b; upper: U x = b.  Block rows are taken in
- * dynamic ticket order; waits are bounded (BILU_ERR_TIMEOUT). */
-size_t bilu_sptrsv_ws_bytes(int nb);
-int bilu_sptrsv(int nb, int bs, const int* d_row, const int* d_col, const double* d_val,
+ * lower: unit-lower L x = b; upper: U x = b.  One-shot form: level analysis
+ * then the level-scheduled solve (warp per block row, one bounded grid
+ * barrier per dependency level). */
+size_t bilu_sptrsv_ws_bytes(int nb, int nnzb);
+int bilu_sptrsv(int nb, int nnzb, int bs, const int* d_row, const int* d_col, const double* d_val,
                 int lower, const double* d_b, double* d_x, void* d_ws, size_t ws_bytes,
                 bilu_stream_t stream);
 /* Analysis / solve split (as cuSPARSE bsrsv2 analysis + solve,
- * BILU_cusparse.h:203-220): the analysis (diagonal positions and dependency
- * level order, bilu_sptrsv_analysis_bytes(nb) bytes in d_info) is computed
- * once per pattern and triangle; each solve then only runs the sync-free
- * kernel. */
+ * BILU_cusparse.h:203-220): the analysis (diagonal positions, dependency
+ * levels and the rows in level order; bilu_sptrsv_analysis_bytes(nb) bytes
+ * in d_info, scratch bilu_sptrsv_analysis_ws_bytes) is computed once per
+ * pattern and triangle.  bilu_sptrsv_solve then runs the level-scheduled
+ * kernel; bilu_sptrsv_solve_syncfree runs the sync-free kernel of the
+ * reference's design on the same analysis (block rows taken by atomic
+ * tickets in level order, per-row ready flags polled by the dependent rows,
+ * every wait bounded: BILU_ERR_TIMEOUT).  Both give identical x. */
 size_t bilu_sptrsv_analysis_bytes(int nb);
+size_t bilu_sptrsv_analysis_ws_bytes(int nb, int nnzb);
 size_t bilu_sptrsv_solve_ws_bytes(int nb);
-int bilu_sptrsv_analysis(int nb, int bs, const int* d_row, const int* d_col, int lower,
+int bilu_sptrsv_analysis(int nb, int nnzb, int bs, const int* d_row, const int* d_col, int lower,
                          void* d_info, void* d_ws, size_t ws_bytes, bilu_stream_t stream);
 int bilu_sptrsv_solve(int nb, int bs, const int* d_row, const int* d_col, const double* d_val,
                       int lower, int unit, const void* d_info, const double* d_b, double* d_x,
                       void* d_ws, size_t ws_bytes, bilu_stream_t stream);
+int bilu_sptrsv_solve_syncfree(int nb, int bs, const int* d_row, const int* d_col,
+                               const double* d_val, int lower, int unit, const void* d_info,
+                               const double* d_b, double* d_x, void* d_ws, size_t ws_bytes,
+                               bilu_stream_t stream);
 /* General form: lower/upper triangle of a packed factor, unit or non-unit
  * diagonal (bilu_sptrsv uses lower+unit and upper+non-unit). */
-int bilu_sptrsv_ex(int nb, int bs, const int* d_row, const int* d_col, const double* d_val,
-                   int lower, int unit, const double* d_b, double* d_x, void* d_ws,
-                   size_t ws_bytes, bilu_stream_t stream);
+int bilu_sptrsv_ex(int nb, int nnzb, int bs, const int* d_row, const int* d_col,
+                   const double* d_val, int lower, int unit, const double* d_b, double* d_x,
+                   void* d_ws, size_t ws_bytes, bilu_stream_t stream);
 /* Transposed solves over the BCSC view of the same packed factor (adjoint):
  * lower: L^T x = b (upper-triangular, unit diagonal); upper: U^T x = b.
  * The workspace holds the transposed factor. */
@@ -307,6 +319,38 @@ int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const int* h_col
  * 6 M_U values (double), 7 M_L values (float), 8 M_U values (float).
  * h_count receives the number of elements. */
 int bilu_ctx_get(bilu_ctx* ctx, int which, const void** d_ptr, long long* h_count);
+
+/* ------------------------------------------------------------------ */
+/* Batched multi-RHS solves (no counterpart in the reference)          */
+/* ------------------------------------------------------------------ */
+
+typedef struct bilu_batch bilu_batch;
+
+int bilu_batch_create(bilu_batch** batch, bilu_stream_t stream);
+int bilu_batch_destroy(bilu_batch* batch);
+/* S systems given as one block-diagonal BSR matrix with global column
+ * indices: system s owns block rows [h_sys_ptr[s], h_sys_ptr[s+1]) and every
+ * block of those rows must lie in the same range (BILU_ERR_PATTERN
+ * otherwise).  Runs the whole setup once on the union (FP32 ISAI included);
+ * the device arrays must stay valid until the batch is destroyed. */
+int bilu_batch_setup(bilu_batch* batch, int S, const int* h_sys_ptr, int nnzb, int bs,
+                     const int* d_row, const int* d_col, const double* d_val, double* h_times);
+/* k (<= 32) right-hand sides per system, B and X row-major [nb*bs, k]:
+ * every (system, right-hand side) pair runs FGMRES(restart) with the FP32
+ * ISAI apply (BSR x dense SpMM, one launch over the batch), FP64 operator,
+ * modified Gram-Schmidt segmented by system and device-side Givens
+ * rotations; each Arnoldi step is a replayed CUDA graph.  Systems are
+ * processed in contiguous waves whose Krylov storage fits mem_budget bytes
+ * (<= 0: 64 GiB).  h_iters / h_relres [S*k] (system-major) receive the
+ * per-pair iteration counts and final true relative residuals; h_stats (4):
+ * waves, graph launches, pair-steps, solve milliseconds. */
+int bilu_batch_solve(bilu_batch* batch, int k, const double* d_B, double* d_X, int restart,
+                     double tol, int maxit, long long mem_budget, int* h_iters,
+                     double* h_relres, double* h_stats);
+/* Autotuner result: h_cfg = {rows per warp of the operator SpMM, of the
+ * apply SpMM, tile rows}; h_ms[6] = timed candidates (1, 2, 4 rows per warp)
+ * for the operator and the apply. */
+int bilu_batch_tuning(bilu_batch* batch, int* h_cfg, double* h_ms);
 
 /* ------------------------------------------------------------------ */
 /* Allocation-free solve                                               */

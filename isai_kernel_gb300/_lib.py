@@ -77,6 +77,9 @@ class BiluError(RuntimeError):
         self.status = status
         self.func = func
         msg = _LIB.bilu_status_string(status).decode() if _LIB is not None else ""
+        self.cuda_error = _LIB.bilu_last_cuda_error() if _LIB is not None else 0
+        if status == -5:  # BILU_ERR_CUDA
+            msg += f" (cudaError_t {self.cuda_error})"
         super().__init__(f"{func} returned {STATUS.get(status, status)}: {msg}")
 
 

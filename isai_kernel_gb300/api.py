@@ -170,7 +170,7 @@ def bsrilu02_inplace(nb: int, nnzb: int, bs: int, bsrRow, bsrCol, bsrVal) -> int
     zero-pivot block row or -1 (the reference prints it)."""
     dev = _dev(bsrVal)
     info = ctypes.c_int(-1)
-    ws = _ws(lib().bilu_bsrilu0_ws_bytes(nb), dev)
+    ws = _ws(lib().bilu_bsrilu0_ws_bytes(nb, nnzb), dev)
     call("bilu_bsrilu0", nb, nnzb, bs, _p(_ci(bsrRow)), _p(_ci(bsrCol)), _p(bsrVal),
          ctypes.byref(info), _p(ws), ws.numel(), _s(), ok=(0, -3))
     return info.value
@@ -283,12 +283,12 @@ def sptrsv(nb: int, bs: int, row, col, val, b, lower: bool, unit=None, transpose
         call("bilu_sptrsv_transpose", nb, bs, _p(_ci(row)), _p(_ci(col)), _p(_cf(val)),
              int(lower), _p(_cf(b)), _p(x), _p(ws), ws.numel(), _s())
         return x
-    ws = _ws(lib().bilu_sptrsv_ws_bytes(nb), dev)
+    ws = _ws(lib().bilu_sptrsv_ws_bytes(nb, nnzb), dev)
     if unit is None:
-        call("bilu_sptrsv", nb, bs, _p(_ci(row)), _p(_ci(col)), _p(_cf(val)), int(lower),
+        call("bilu_sptrsv", nb, nnzb, bs, _p(_ci(row)), _p(_ci(col)), _p(_cf(val)), int(lower),
              _p(_cf(b)), _p(x), _p(ws), ws.numel(), _s())
     else:
-        call("bilu_sptrsv_ex", nb, bs, _p(_ci(row)), _p(_ci(col)), _p(_cf(val)), int(lower),
+        call("bilu_sptrsv_ex", nb, nnzb, bs, _p(_ci(row)), _p(_ci(col)), _p(_cf(val)), int(lower),
              int(unit), _p(_cf(b)), _p(x), _p(ws), ws.numel(), _s())
     return x
 
@@ -383,6 +383,84 @@ class Preconditioner:
         stats = (ctypes.c_longlong * 4)()
         call("bilu_ctx_stats", self._h, stats)
         return x, SolveResult(it.value, rr.value, st == 0, h, int(stats[1]))
+
+
+def block_diagonal_union(mats):
+    """Concatenate BSR systems into one block-diagonal BSR matrix with global
+    column indices -> (sys_ptr[S+1], rowptr, colind, val[nnzb, bs, bs])."""
+    import numpy as np
+
+    sys_ptr = np.zeros(len(mats) + 1, np.int32)
+    rows, cols, vals = [np.zeros(1, np.int64)], [], []
+    off_r, off_nz = 0, 0
+    for i, A in enumerate(mats):
+        rows.append(A.rowptr[1:].astype(np.int64) + off_nz)
+        cols.append(A.colind.astype(np.int64) + off_r)
+        vals.append(A.val)
+        off_r += A.nb
+        off_nz += A.nnzb
+        sys_ptr[i + 1] = off_r
+    return (sys_ptr, np.concatenate(rows).astype(np.int32), np.concatenate(cols).astype(np.int32),
+            np.concatenate(vals))
+
+
+class Batch:
+    """Many uneven systems with k right-hand sides each (bilu_batch): one
+    setup on the block-diagonal union, then per-(system, rhs) FGMRES with the
+    FP32 ISAI apply as BSR x dense SpMM, graph-replayed Arnoldi steps and an
+    autotuned SpMM tile."""
+
+    def __init__(self, mats, stream=None):
+        import numpy as np
+
+        self._h = ctypes.c_void_p()
+        self.bs = mats[0].bs
+        sys_ptr, rowptr, colind, val = block_diagonal_union(mats)
+        self.sys_ptr = sys_ptr
+        self.S = len(mats)
+        self.nb = int(sys_ptr[-1])
+        self.row = torch.from_numpy(rowptr).cuda()
+        self.col = torch.from_numpy(colind).cuda()
+        self.val = torch.from_numpy(val).cuda()
+        call("bilu_batch_create", ctypes.byref(self._h), _s(stream))
+        times = (ctypes.c_double * 4)()
+        call("bilu_batch_setup", self._h, self.S, sys_ptr.ctypes.data_as(ctypes.c_void_p),
+             int(colind.shape[0]), self.bs, _p(self.row), _p(self.col), _p(self.val), times)
+        self.setup_ms = list(times)
+        self._np = np
+
+    def close(self):
+        if self._h:
+            lib().bilu_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, B, restart: int = 30, tol: float = 1e-10, maxit: int = 10000,
+              mem_budget: int = 0):
+        """B: [n, k] FP64 CUDA tensor.  Returns X, iters[S, k], relres[S, k],
+        stats (waves, graph launches, pair-steps, solve ms)."""
+        np = self._np
+        B = _cf(B)
+        k = B.shape[1]
+        X = torch.empty_like(B)
+        iters = np.zeros(self.S * k, np.int32)
+        relres = np.zeros(self.S * k)
+        stats = (ctypes.c_double * 4)()
+        call("bilu_batch_solve", self._h, k, _p(B), _p(X), restart, tol, maxit,
+             ctypes.c_longlong(mem_budget), iters.ctypes.data_as(ctypes.c_void_p),
+             relres.ctypes.data_as(ctypes.c_void_p), stats)
+        return X, iters.reshape(self.S, k), relres.reshape(self.S, k), list(stats)
+
+    def tuning(self):
+        cfg = (ctypes.c_int * 3)()
+        ms = (ctypes.c_double * 6)()
+        call("bilu_batch_tuning", self._h, cfg, ms)
+        return list(cfg), list(ms)
 
 
 def solve_host(nb: int, bs: int, row, col, val, b, prec: int = BILU_FP64, restart: int = 30,

@@ -15,9 +15,10 @@ int transpose_pattern(int mb, int nbcol, const int* cptr, const int* cind, long 
 size_t syncfree_ws(int nb);
 int diag_positions(int nb, const int* row, const int* col, int* diag, int* h_bad, Carver& ws,
                    cudaStream_t st);
-int sptrsv_impl(int nb, int bs, const int* row, const int* col, const int* diag,
-                const double* val, int lower, int unit, const double* b, double* x, Carver& ws,
-                cudaStream_t st, long long spin = kSpinLimit, int withhold = -1);
+size_t level_sched_ws(int nb, long long nnzb);
+int sptrsv_level_impl(int nb, long long nnzb, int bs, const int* row, const int* col,
+                      const int* diag, const double* val, int lower, int unit, const double* b,
+                      double* x, Carver& ws, cudaStream_t st);
 int spmv_any(int mb, int bs, int prec, const int* row, const int* col, const void* val,
              const void* x, int x32, void* y, int y32, cudaStream_t st);
 
@@ -154,7 +155,9 @@ extern "C" int bilu_bsr_transpose(int mb, int bs, const int* d_row, const int* d
 static size_t sptrsv_t_ws(int nb, long long nnzb, int bs) {
   return carve_size(sizeof(int) * (size_t)(nb + 1)) + carve_size(sizeof(int) * (size_t)nnzb) +
          carve_size(sizeof(double) * (size_t)nnzb * bs * bs) +
-         std::max(bsr_transpose_ws(nb, nnzb), syncfree_ws(nb) + carve_size(sizeof(int) * (nb + 1)));
+         std::max(bsr_transpose_ws(nb, nnzb),
+                  level_sched_ws(nb, nnzb) + carve_size(sizeof(int) * ((size_t)nb + 1)) +
+                      carve_size(sizeof(int) * 2));
 }
 
 extern "C" size_t bilu_sptrsv_transpose_ws_bytes(int nb, int nnzb, int bs) {
@@ -187,8 +190,8 @@ extern "C" int bilu_sptrsv_transpose(int nb, int bs, const int* d_row, const int
   BILU_TRY(diag_positions(nb, trow, tcol, diag, nullptr, ws, st));
   // L^T: upper, unit (strict upper of the transposed diagonal block);
   // U^T: lower, non-unit (lower part incl. diagonal)
-  return sptrsv_impl(nb, bs, trow, tcol, diag, tval, lower ? 0 : 1, lower ? 1 : 0, d_b, d_x, ws,
-                     st);
+  return sptrsv_level_impl(nb, nnzb, bs, trow, tcol, diag, tval, lower ? 0 : 1, lower ? 1 : 0, d_b,
+                           d_x, ws, st);
 }
 
 extern "C" size_t bilu_spmv_transpose_ws_bytes(int mb, int nnzb) {

@@ -114,6 +114,7 @@ __device__ __forceinline__ float ld_stream(const float* p) {
 
 // Bounded spin budget for sync-free kernels: after this many polls of a
 // dependency flag the waiter records BILU_ERR_TIMEOUT and returns.
-constexpr long long kSpinLimit = 1ll << 24;
+// Polls back off up to 256 ns, so the budget bounds a wait at a few seconds.
+constexpr long long kSpinLimit = 1ll << 22;
 
 }  // namespace bilu

@@ -34,8 +34,9 @@ int reorder_impl(long long nnzb, int bs, const int* map, const double* src, doub
 size_t syncfree_ws(int nb);
 int diag_positions(int nb, const int* row, const int* col, int* diag, int* h_bad, Carver& ws,
                    cudaStream_t st);
-int bilu0_impl(int nb, int bs, const int* row, const int* col, const int* diag, double* val,
-               int* h_zp, Carver& ws, cudaStream_t st);
+size_t level_sched_ws(int nb, long long nnzb);
+int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, const int* diag,
+               double* val, int* h_zp, Carver& ws, cudaStream_t st);
 int dinv_impl(int nb, int bs, const int* row, const int* col, const double* val, int lower,
               double* Dinv, int* d_fail, cudaStream_t st);
 size_t pairs_ws(long long mnnz);
@@ -78,6 +79,7 @@ struct bilu_ctx {
   bool ready = false;
   // solver buffers
   int m_alloc = 0;
+  long long ldv = 0;  // stride of the basis vectors in V and Z (n rounded up to 32)
   double *V = nullptr, *Z = nullptr, *w = nullptr, *r = nullptr, *tmp = nullptr;
   float* v32 = nullptr;  // FP32 copy of the newest basis vector (mixed apply input)
   double *partial = nullptr, *dscal = nullptr, *dcoef = nullptr;
@@ -230,6 +232,8 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   cudaStream_t st = c->st;
   c->free_setup();
+  // solver buffers are sized for n: a new system size reallocates them
+  if (c->n != (long long)nb * bs) c->free_solver();
   c->nb = nb;
   c->nnzb = nnzb;
   c->bs = bs;
@@ -247,7 +251,7 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   BILU_TRY_CUDA(cudaMemcpyAsync(c->Aval, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->LU, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
   // scratch shared by every step
-  size_t wsb = std::max({isai_pattern_ws(nb, nnzb), syncfree_ws(nb), pairs_ws(nnzb + nb),
+  size_t wsb = std::max({isai_pattern_ws(nb, nnzb), level_sched_ws(nb, nnzb), pairs_ws(nnzb + nb),
                          scan_ws_bytes(nnzb + nb + 1)}) + (1 << 16);
   void* wsp = nullptr;
   BILU_TRY(c->alloc((char**)&wsp, wsb));
@@ -260,7 +264,7 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   {
     Carver w2 = ws;
     int zp = -1;
-    int rc = bilu0_impl(nb, bs, c->Arow, c->Acol, c->diag, c->LU, &zp, w2, st);
+    int rc = bilu0_impl(nb, nnzb, bs, c->Arow, c->Acol, c->diag, c->LU, &zp, w2, st);
     if (rc != BILU_OK) return rc;
   }
   tm.mark(2);
@@ -314,8 +318,10 @@ int ensure_solver(bilu_ctx* c, int m) {
   if (c->m_alloc >= m && c->V) return BILU_OK;
   c->free_solver();
   size_t n = (size_t)c->n;
-  BILU_TRY_CUDA(cudaMalloc(&c->V, sizeof(double) * n * (m + 1)));
-  BILU_TRY_CUDA(cudaMalloc(&c->Z, sizeof(double) * n * m));
+  // basis vectors start on 256-byte boundaries (16-byte vector loads)
+  c->ldv = (long long)((n + 31) & ~(size_t)31);
+  BILU_TRY_CUDA(cudaMalloc(&c->V, sizeof(double) * c->ldv * (m + 1)));
+  BILU_TRY_CUDA(cudaMalloc(&c->Z, sizeof(double) * c->ldv * m));
   BILU_TRY_CUDA(cudaMalloc(&c->w, sizeof(double) * n));
   BILU_TRY_CUDA(cudaMalloc(&c->r, sizeof(double) * n));
   BILU_TRY_CUDA(cudaMalloc(&c->tmp, sizeof(double) * n));
@@ -362,9 +368,9 @@ namespace {
 
 // Launches z_j = M v_j and w = A z_j.
 int arnoldi_front(bilu_ctx* c, int prec, int j) {
-  size_t n = (size_t)c->n;
-  double* zj = c->Z + n * j;
-  BILU_TRY(apply_prec(c, prec, c->V + n * j, zj));
+  size_t ld = (size_t)c->ldv;
+  double* zj = c->Z + ld * j;
+  BILU_TRY(apply_prec(c, prec, c->V + ld * j, zj));
   return spmv_any(c->nb, c->bs, BILU_FP64, c->Arow, c->Acol, c->Aval, zj, 0, c->w, 0, c->st);
 }
 
@@ -376,15 +382,16 @@ int arnoldi_front(bilu_ctx* c, int prec, int j) {
 int arnoldi_back(bilu_ctx* c, int j, int prec) {
   cudaStream_t st = c->st;
   long long n = c->n;
+  size_t ld = (size_t)c->ldv;
   double* s = c->dscal;
   const double* V = c->V;
   BILU_TRY(mgs_sweep(n, nullptr, nullptr, V, c->w, c->partial, c->counter, s, st));
   for (int i = 1; i <= j; ++i)
-    BILU_TRY(mgs_sweep(n, V + (size_t)n * (i - 1), s + i - 1, V + (size_t)n * i, c->w, c->partial,
+    BILU_TRY(mgs_sweep(n, V + ld * (i - 1), s + i - 1, V + ld * i, c->w, c->partial,
                        c->counter, s + i, st));
-  BILU_TRY(mgs_sweep(n, V + (size_t)n * j, s + j, nullptr, c->w, c->partial, c->counter,
+  BILU_TRY(mgs_sweep(n, V + ld * j, s + j, nullptr, c->w, c->partial, c->counter,
                      s + kPartStride, st));
-  BILU_TRY(scale_rsqrt(n, c->w, s + kPartStride, c->V + (size_t)n * (j + 1), st,
+  BILU_TRY(scale_rsqrt(n, c->w, s + kPartStride, c->V + ld * (j + 1), st,
                        prec == BILU_FP32 ? c->v32 : nullptr));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->hpin, s, sizeof(double) * (kPartStride + 1),
                                 cudaMemcpyDeviceToHost, st));
@@ -470,7 +477,7 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
     if (jlast >= 0) {
       BILU_TRY_CUDA(cudaMemcpyAsync(c->dcoef, y.data(), sizeof(double) * (jlast + 1),
                                     cudaMemcpyHostToDevice, st));
-      BILU_TRY(multiaxpy_norm(n, c->Z, n, jlast + 1, c->dcoef, 1.0, d_x, nullptr, nullptr, st));
+      BILU_TRY(multiaxpy_norm(n, c->Z, c->ldv, jlast + 1, c->dcoef, 1.0, d_x, nullptr, nullptr, st));
     }
     BILU_TRY(spmv_any(c->nb, c->bs, BILU_FP64, c->Arow, c->Acol, c->Aval, d_x, 0, c->w, 0, st));
     BILU_TRY(residual_norm(n, d_b, c->w, c->r, c->partial, st));

@@ -97,7 +97,7 @@ __device__ __forceinline__ void load_row(const VT* __restrict__ val, long long p
 // values: U = 2, RPG = 1 (the DFMA pipe, not memory, is the limit); FP32
 // values: U = 4, RPG = 2 (memory latency is the limit).
 template <int BS, class VT, class XT, class YT, class AccT, int RPG>
-__global__ void __launch_bounds__(256, 2) k_bsr_spmv(int mb, const int* __restrict__ row,
+__global__ void __launch_bounds__(256, sizeof(VT) == 4 ? 4 : 2) k_bsr_spmv(int mb, const int* __restrict__ row,
                                                      const int* __restrict__ col,
                                                      const VT* __restrict__ val,
                                                      const XT* __restrict__ x,
@@ -145,23 +145,18 @@ __global__ void __launch_bounds__(256, 2) k_bsr_spmv(int mb, const int* __restri
           for (int k = 0; k < BS; ++k) a[q][u][k] = 0;
         }
       }
+    // x segments (mostly L2 hits) are consumed as they arrive, which keeps
+    // the register footprint low enough for 4 CTAs per SM with FP32 values
 #pragma unroll
     for (int q = 0; q < RPG; ++q)
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         if (c[q][u] >= 0) {
           load_x<BS, XT, AccT>(x, c[q][u], xv[q][u]);
-        } else {
 #pragma unroll
-          for (int k = 0; k < BS; ++k) xv[q][u][k] = 0;
+          for (int k = 0; k < BS; ++k) acc[q] = fma(a[q][u][k], xv[q][u][k], acc[q]);
         }
       }
-#pragma unroll
-    for (int q = 0; q < RPG; ++q)
-#pragma unroll
-      for (int u = 0; u < U; ++u)
-#pragma unroll
-        for (int k = 0; k < BS; ++k) acc[q] = fma(a[q][u][k], xv[q][u][k], acc[q]);
   }
 #pragma unroll
   for (int q = 0; q < RPG; ++q)

@@ -7,8 +7,9 @@
 // ticket counter, so every row a warp waits on was taken by a warp that is
 // already running (the reference maps rows to threads statically and relies
 // on scheduling order).  A finished row publishes its flag with st.release
-// after a __threadfence by every writer lane; waiters poll with ld.acquire
-// and read the producer's data through L2 (ld.cg).  Every wait is bounded:
+// after a __threadfence by every writer lane; waiters poll with relaxed loads,
+// take one acquire fence when the flag is set, and read the producer's data
+// through L2 (ld.cg).  Every wait is bounded:
 // after kSpinLimit polls the waiter sets the error word to BILU_ERR_TIMEOUT,
 // and all other waiters see the error word and leave, so no launch hangs.
 #include <climits>
@@ -34,32 +35,54 @@ struct SyncState {
   const int* order;   // ticket -> block row (dependency-level order), or null
 };
 
+// Exponential back-off between polls (32 ns doubling to 256 ns): waiters that
+// spin at full rate flood the L2 with flag reads and slow the rows they wait
+// for.
+__device__ __forceinline__ void backoff(unsigned& ns) {
+  __nanosleep(ns);
+  ns = ns < 256u ? ns * 2u : 256u;
+}
+
+// Acquire side of the flag handshake.  Flags are polled with relaxed loads
+// (an acquire load per poll would invalidate L1 on every iteration of every
+// spinning warp); once the release store is observed, one acquire fence
+// orders the reads of the producer's data after it.
+__device__ __forceinline__ void fence_acquire() {
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
+
 // Warp-wide wait until flags[K] != 0.  Returns false if the launch aborted.
 __device__ __forceinline__ bool warp_wait(const int* flag, int* err, long long spin) {
   long long n = 0;
+  unsigned ns = 32;
   while (true) {
-    int v = ld_acquire(flag);
-    if (__all_sync(FULL, v != 0)) return true;
+    int v = ld_relaxed(flag);
+    if (__all_sync(FULL, v != 0)) {
+      fence_acquire();
+      return true;
+    }
     if (__any_sync(FULL, ld_relaxed(err) != 0)) return false;
     if (++n > spin) {
       if ((threadIdx.x & 31) == 0) atomicCAS(err, 0, (int)BILU_ERR_TIMEOUT);
       return false;
     }
-    __nanosleep(32);
+    backoff(ns);
   }
 }
 
 // Single-lane wait (lanes of a warp may wait on different rows).
 __device__ __forceinline__ bool lane_wait(const int* flag, int* err, long long spin) {
   long long n = 0;
-  while (ld_acquire(flag) == 0) {
+  unsigned ns = 32;
+  while (ld_relaxed(flag) == 0) {
     if (ld_relaxed(err) != 0) return false;
     if (++n > spin) {
       atomicCAS(err, 0, (int)BILU_ERR_TIMEOUT);
       return false;
     }
-    __nanosleep(32);
+    backoff(ns);
   }
+  fence_acquire();
   return true;
 }
 
@@ -97,11 +120,15 @@ __global__ void k_diag_pos(int nb, const int* __restrict__ row, const int* __res
 //   then LU of the diagonal block (no pivoting) and U_IJ = L_II^-1 A_IJ.
 // Each element sees the same sequence of a -= l*u updates as the scalar IKJ
 // loop, with ascending k.
-template <int BS>
-__global__ void __launch_bounds__(128) k_bilu0(int nb, const int* __restrict__ row,
-                                               const int* __restrict__ col,
-                                               const int* __restrict__ diag, double* val,
-                                               SyncState ss) {
+// One block row of the factorisation, executed by one warp.  WAIT: the
+// rows K it reads may still be in progress (sync-free schedule) and are
+// waited for through their flags; otherwise every K is already final
+// (level schedule).  Returns false if the launch aborted.
+template <int BS, bool WAIT>
+__device__ __forceinline__ bool bilu0_row(int I, const int* __restrict__ row,
+                                          const int* __restrict__ col,
+                                          const int* __restrict__ diag, double* val,
+                                          const SyncState& ss) {
   constexpr int BS2 = BS * BS;
   constexpr int EPL = BS2 > 32 ? 2 : 1;
   constexpr int TL = BS2 / EPL + (BS2 % EPL ? 1 : 0);
@@ -111,6 +138,126 @@ __global__ void __launch_bounds__(128) k_bilu0(int nb, const int* __restrict__ r
   int lane = threadIdx.x & 31;
   int team = lane / SPAN, tl = lane - team * SPAN;
   bool team_on = team < TPW && tl < TL;
+  int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
+  for (int pk = rs; pk < dI; ++pk) {
+    int K = __ldg(col + pk);
+    if (WAIT && !warp_wait(ss.flags + K, ss.err, ss.spin)) return false;
+    int dK = __ldg(diag + K), ke = __ldg(row + K + 1);
+    double* L = val + (long long)pk * BS2;
+    const double* Ukk = val + (long long)dK * BS2;
+    // phase 1: lane r owns row r of A_IK
+    if (lane < BS) {
+      double a[BS];
+#pragma unroll
+      for (int c = 0; c < BS; ++c) a[c] = L[lane * BS + c];
+#pragma unroll
+      for (int k = 0; k < BS; ++k) {
+        a[k] = a[k] / __ldcg(Ukk + k * BS + k);
+#pragma unroll
+        for (int c = k + 1; c < BS; ++c) a[c] -= a[k] * __ldcg(Ukk + k * BS + c);
+      }
+#pragma unroll
+      for (int c = 0; c < BS; ++c) L[lane * BS + c] = a[c];
+    }
+    __syncwarp();
+    // phase 2: A_IJ -= L_IK U_KJ for J > K in rows I and K.  The shorter
+    // of the two column lists supplies the candidates, 32 at a time, each
+    // lane binary-searching one of them in the other list (hub rows of
+    // power-law matrices hold thousands of blocks); then the teams update
+    // the matched blocks.  Every block is updated once per K, so the
+    // update order of each element is the same either way.
+    {
+      const bool from_i = (re - pk - 1) <= (ke - dK - 1);
+      const int cs = from_i ? pk + 1 : dK + 1, ce = from_i ? re : ke;
+      const int ss_ = from_i ? dK + 1 : pk + 1, se = from_i ? ke : re;
+      for (int c0 = cs; c0 < ce; c0 += 32) {
+        int pc = c0 + lane, other = -1;
+        if (pc < ce) other = find_in_row(col, ss_, se, __ldg(col + pc));
+        unsigned found = __ballot_sync(FULL, other >= 0);
+        while (found) {
+          // the next TPW matches go to the TPW teams
+          int src = -1;
+#pragma unroll
+          for (int t = 0; t < TPW; ++t) {
+            int bit = found ? __ffs(found) - 1 : -1;
+            if (bit >= 0) found &= found - 1;
+            if (t == team) src = bit;
+          }
+          int o = __shfl_sync(FULL, other, src < 0 ? 0 : src);
+          if (team_on && src >= 0) {
+            int pj = from_i ? c0 + src : o;
+            int pos = from_i ? o : c0 + src;
+            double* Aij = val + (long long)pj * BS2;
+            const double* Ukj = val + (long long)pos * BS2;
+#pragma unroll
+            for (int q = 0; q < EPL; ++q) {
+              int e = tl * EPL + q;
+              if (e < BS2) {
+                int r = e / BS, c = e - r * BS;
+                double v = Aij[e];
+#pragma unroll
+                for (int k = 0; k < BS; ++k) v -= L[r * BS + k] * __ldcg(Ukj + k * BS + c);
+                Aij[e] = v;
+              }
+            }
+          }
+        }
+      }
+    }
+    __syncwarp();
+  }
+  // diagonal block: lane c owns column c
+  double* D = val + (long long)dI * BS2;
+  double dc[BS];
+  if (lane < BS) {
+#pragma unroll
+    for (int r = 0; r < BS; ++r) dc[r] = D[r * BS + lane];
+  } else {
+#pragma unroll
+    for (int r = 0; r < BS; ++r) dc[r] = 1.0;
+  }
+#pragma unroll
+  for (int r = 1; r < BS; ++r) {
+#pragma unroll
+    for (int k = 0; k < r; ++k) {
+      double lk = dc[r] / dc[k];  // meaningful on lane k
+      double l = __shfl_sync(FULL, lk, k);
+      if (lane == k) dc[r] = l;
+      else if (lane > k && lane < BS) dc[r] -= l * dc[k];
+    }
+  }
+  if (lane < BS) {
+    if (dc[lane] == 0.0) atomicMin(ss.zp, I);
+#pragma unroll
+    for (int r = 0; r < BS; ++r) D[r * BS + lane] = dc[r];
+  }
+  __syncwarp();
+  // U blocks right of the diagonal: U_IJ = L_II^-1 A_IJ, lane per column
+  for (int pj0 = dI + 1; pj0 < re; pj0 += GU) {
+    int slot = lane / BS, c = lane - slot * BS;
+    int pj = pj0 + slot;
+    if (slot < GU && pj < re) {
+      double* U = val + (long long)pj * BS2;
+      double u[BS];
+#pragma unroll
+      for (int r = 0; r < BS; ++r) u[r] = U[r * BS + c];
+#pragma unroll
+      for (int r = 1; r < BS; ++r)
+#pragma unroll
+        for (int k = 0; k < r; ++k) u[r] -= D[r * BS + k] * u[k];
+#pragma unroll
+      for (int r = 1; r < BS; ++r) U[r * BS + c] = u[r];
+    }
+  }
+  return true;
+}
+
+template <int BS>
+__global__ void __launch_bounds__(128) k_bilu0(int nb, const int* __restrict__ row,
+                                               const int* __restrict__ col,
+                                               const int* __restrict__ diag, double* val,
+                                               SyncState ss) {
+  int lane = threadIdx.x & 31;
   while (true) {
     int I = 0;
     if (lane == 0) I = atomicAdd(ss.ticket, 1);
@@ -118,94 +265,7 @@ __global__ void __launch_bounds__(128) k_bilu0(int nb, const int* __restrict__ r
     if (I >= nb) return;
     if (ss.order) I = __ldg(ss.order + I);
     if (__any_sync(FULL, ld_relaxed(ss.err) != 0)) return;
-    int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
-    for (int pk = rs; pk < dI; ++pk) {
-      int K = __ldg(col + pk);
-      if (!warp_wait(ss.flags + K, ss.err, ss.spin)) return;
-      int dK = __ldg(diag + K), ke = __ldg(row + K + 1);
-      double* L = val + (long long)pk * BS2;
-      const double* Ukk = val + (long long)dK * BS2;
-      // phase 1: lane r owns row r of A_IK
-      if (lane < BS) {
-        double a[BS];
-#pragma unroll
-        for (int c = 0; c < BS; ++c) a[c] = L[lane * BS + c];
-#pragma unroll
-        for (int k = 0; k < BS; ++k) {
-          a[k] = a[k] / __ldcg(Ukk + k * BS + k);
-#pragma unroll
-          for (int c = k + 1; c < BS; ++c) a[c] -= a[k] * __ldcg(Ukk + k * BS + c);
-        }
-#pragma unroll
-        for (int c = 0; c < BS; ++c) L[lane * BS + c] = a[c];
-      }
-      __syncwarp();
-      // phase 2: A_IJ -= L_IK U_KJ, team per candidate block J of row I
-      for (int pj0 = pk + 1; pj0 < re; pj0 += TPW) {
-        int pj = pj0 + team;
-        int pos = -1;
-        if (team < TPW && pj < re) pos = find_in_row(col, dK + 1, ke, __ldg(col + pj));
-        if (team_on && pos >= 0) {
-          double* Aij = val + (long long)pj * BS2;
-          const double* Ukj = val + (long long)pos * BS2;
-#pragma unroll
-          for (int q = 0; q < EPL; ++q) {
-            int e = tl * EPL + q;
-            if (e < BS2) {
-              int r = e / BS, c = e - r * BS;
-              double v = Aij[e];
-#pragma unroll
-              for (int k = 0; k < BS; ++k) v -= L[r * BS + k] * __ldcg(Ukj + k * BS + c);
-              Aij[e] = v;
-            }
-          }
-        }
-      }
-      __syncwarp();
-    }
-    // diagonal block: lane c owns column c
-    double* D = val + (long long)dI * BS2;
-    double dc[BS];
-    if (lane < BS) {
-#pragma unroll
-      for (int r = 0; r < BS; ++r) dc[r] = D[r * BS + lane];
-    } else {
-#pragma unroll
-      for (int r = 0; r < BS; ++r) dc[r] = 1.0;
-    }
-#pragma unroll
-    for (int r = 1; r < BS; ++r) {
-#pragma unroll
-      for (int k = 0; k < r; ++k) {
-        double lk = dc[r] / dc[k];  // meaningful on lane k
-        double l = __shfl_sync(FULL, lk, k);
-        if (lane == k) dc[r] = l;
-        else if (lane > k && lane < BS) dc[r] -= l * dc[k];
-      }
-    }
-    if (lane < BS) {
-      if (dc[lane] == 0.0) atomicMin(ss.zp, I);
-#pragma unroll
-      for (int r = 0; r < BS; ++r) D[r * BS + lane] = dc[r];
-    }
-    __syncwarp();
-    // U blocks right of the diagonal: U_IJ = L_II^-1 A_IJ, lane per column
-    for (int pj0 = dI + 1; pj0 < re; pj0 += GU) {
-      int slot = lane / BS, c = lane - slot * BS;
-      int pj = pj0 + slot;
-      if (slot < GU && pj < re) {
-        double* U = val + (long long)pj * BS2;
-        double u[BS];
-#pragma unroll
-        for (int r = 0; r < BS; ++r) u[r] = U[r * BS + c];
-#pragma unroll
-        for (int r = 1; r < BS; ++r)
-#pragma unroll
-          for (int k = 0; k < r; ++k) u[r] -= D[r * BS + k] * u[k];
-#pragma unroll
-        for (int r = 1; r < BS; ++r) U[r * BS + c] = u[r];
-      }
-    }
+    if (!bilu0_row<BS, true>(I, row, col, diag, val, ss)) return;
     __threadfence();
     __syncwarp();
     if (lane == 0 && I != ss.withhold) st_release(ss.flags + I, 1);
@@ -218,6 +278,77 @@ __global__ void __launch_bounds__(128) k_bilu0(int nb, const int* __restrict__ r
 // in reverse ticket order.  UNIT: the diagonal block contributes its strict
 // triangle and no division (unit diagonal).  Lane (slot, r) accumulates row
 // r of blocks slot, slot+G, ...; slots are summed by shuffles.
+// One block row of the solve, executed by one warp.  WAIT: the rows it
+// reads may still be in progress and are waited for through their flags;
+// otherwise they are final (level schedule).  x_I is stored by lane 0.
+// Returns false if the launch aborted.
+template <int BS, bool LOWER, bool UNIT, bool WAIT>
+__device__ __forceinline__ bool sptrsv_row(int I, const int* __restrict__ row,
+                                           const int* __restrict__ col,
+                                           const int* __restrict__ diag,
+                                           const double* __restrict__ val,
+                                           const double* __restrict__ b, double* x,
+                                           const SyncState& ss) {
+  constexpr int BS2 = BS * BS;
+  constexpr int G = 32 / BS;
+  int lane = threadIdx.x & 31;
+  int slot = lane / BS, r = lane - slot * BS;
+  int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
+  int ps = LOWER ? rs : dI + 1, pe = LOWER ? dI : re;
+  double s = 0.0;
+  bool ok = true;
+  for (int p0 = ps; p0 < pe; p0 += G) {
+    int p = p0 + slot;
+    if (slot < G && p < pe && ok) {
+      int K = __ldg(col + p);
+      if (WAIT) ok = lane_wait(ss.flags + K, ss.err, ss.spin);
+      if (ok) {
+        const double* blk = val + (long long)p * BS2 + r * BS;
+        const double* xk = x + (long long)K * BS;
+#pragma unroll
+        for (int c = 0; c < BS; ++c) s = fma(__ldg(blk + c), __ldcg(xk + c), s);
+      }
+    }
+  }
+  if (WAIT && __any_sync(FULL, !ok)) return false;
+  double tot = 0.0;
+#pragma unroll
+  for (int g = 0; g < G; ++g) tot += __shfl_sync(FULL, s, g * BS + r);
+  // diagonal block on lane 0
+  double xr[BS];
+#pragma unroll
+  for (int q = 0; q < BS; ++q) xr[q] = __shfl_sync(FULL, tot, q);
+  if (lane == 0) {
+    const double* D = val + (long long)dI * BS2;
+    const double* bi = b + (long long)I * BS;
+    if (LOWER) {
+#pragma unroll
+      for (int q = 0; q < BS; ++q) {
+        double v = bi[q] - xr[q];
+#pragma unroll
+        for (int c = 0; c < q; ++c) v -= __ldg(D + q * BS + c) * xr[c];
+        xr[q] = UNIT ? v : v / __ldg(D + q * BS + q);
+      }
+    } else {
+#pragma unroll
+      for (int q = BS - 1; q >= 0; --q) {
+        double v = bi[q] - xr[q];
+#pragma unroll
+        for (int c = q + 1; c < BS; ++c) v -= __ldg(D + q * BS + c) * xr[c];
+        xr[q] = UNIT ? v : v / __ldg(D + q * BS + q);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < BS; ++q) x[(long long)I * BS + q] = xr[q];
+  }
+  return true;
+}
+
+// Block-row solve on a packed factor.  LOWER: x_I = b_I - sum_{K<I} B_IK x_K
+// then the diagonal block's lower part; otherwise the upper part and J > I
+// in reverse ticket order.  UNIT: the diagonal block contributes its strict
+// triangle and no division (unit diagonal).  Lane (slot, r) accumulates row
+// r of blocks slot, slot+G, ...; slots are summed by shuffles.
 template <int BS, bool LOWER, bool UNIT>
 __global__ void __launch_bounds__(128) k_sptrsv(int nb, const int* __restrict__ row,
                                                 const int* __restrict__ col,
@@ -225,64 +356,16 @@ __global__ void __launch_bounds__(128) k_sptrsv(int nb, const int* __restrict__ 
                                                 const double* __restrict__ val,
                                                 const double* __restrict__ b, double* x,
                                                 SyncState ss) {
-  constexpr int BS2 = BS * BS;
-  constexpr int G = 32 / BS;
   int lane = threadIdx.x & 31;
-  int slot = lane / BS, r = lane - slot * BS;
   while (true) {
     int t = 0;
     if (lane == 0) t = atomicAdd(ss.ticket, 1);
     t = __shfl_sync(FULL, t, 0);
     if (t >= nb) return;
     int I = ss.order ? __ldg(ss.order + t) : (LOWER ? t : nb - 1 - t);
-    int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
-    int ps = LOWER ? rs : dI + 1, pe = LOWER ? dI : re;
-    double s = 0.0;
-    bool ok = true;
-    for (int p0 = ps; p0 < pe; p0 += G) {
-      int p = p0 + slot;
-      if (slot < G && p < pe && ok) {
-        int K = __ldg(col + p);
-        ok = lane_wait(ss.flags + K, ss.err, ss.spin);
-        if (ok) {
-          const double* blk = val + (long long)p * BS2 + r * BS;
-          const double* xk = x + (long long)K * BS;
-#pragma unroll
-          for (int c = 0; c < BS; ++c) s = fma(__ldg(blk + c), __ldcg(xk + c), s);
-        }
-      }
-    }
-    if (__any_sync(FULL, !ok)) return;
-    double tot = 0.0;
-#pragma unroll
-    for (int g = 0; g < G; ++g) tot += __shfl_sync(FULL, s, g * BS + r);
-    // diagonal block on lane 0
-    double xr[BS];
-#pragma unroll
-    for (int q = 0; q < BS; ++q) xr[q] = __shfl_sync(FULL, tot, q);
+    if (!sptrsv_row<BS, LOWER, UNIT, true>(I, row, col, diag, val, b, x, ss)) return;
     if (lane == 0) {
-      const double* D = val + (long long)dI * BS2;
-      const double* bi = b + (long long)I * BS;
-      if (LOWER) {
-#pragma unroll
-        for (int q = 0; q < BS; ++q) {
-          double v = bi[q] - xr[q];
-#pragma unroll
-          for (int c = 0; c < q; ++c) v -= __ldg(D + q * BS + c) * xr[c];
-          xr[q] = UNIT ? v : v / __ldg(D + q * BS + q);
-        }
-      } else {
-#pragma unroll
-        for (int q = BS - 1; q >= 0; --q) {
-          double v = bi[q] - xr[q];
-#pragma unroll
-          for (int c = q + 1; c < BS; ++c) v -= __ldg(D + q * BS + c) * xr[c];
-          xr[q] = UNIT ? v : v / __ldg(D + q * BS + q);
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < BS; ++q) x[(long long)I * BS + q] = xr[q];
-      __threadfence();
+      // st.release orders lane 0's stores of x_I before the flag
       if (I != ss.withhold) st_release(ss.flags + I, 1);
     }
     __syncwarp();
@@ -310,16 +393,17 @@ __global__ void __launch_bounds__(256) k_levels(int nb, const int* __restrict__ 
     for (int p = ps; p < pe; ++p) {
       const int* f = level + __ldg(col + p);
       long long n = 0;
+      unsigned ns = 32;
       int v;
-      while ((v = ld_acquire(f)) == 0) {
+      while ((v = ld_relaxed(f)) == 0) {
         if (ld_relaxed(err) != 0) return;
         if (++n > spin) {
           atomicCAS(err, 0, (int)BILU_ERR_TIMEOUT);
           return;
         }
-        __nanosleep(32);
+        backoff(ns);
       }
-      lv = max(lv, v);
+      lv = max(lv, v);  // the level value itself is the only datum read
     }
     st_release(level + I, lv + 1);
   }
@@ -333,6 +417,168 @@ __global__ void k_level_count(int nb, const int* __restrict__ level, int* cnt) {
 __global__ void k_level_scatter(int nb, const int* __restrict__ level, int* cursor, int* order) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < nb) order[atomicAdd(cursor + level[i] - 1, 1)] = i;
+}
+
+// ------------------------------------------------------------------ level schedule
+// The dependency DAG is cut into levels (level 0: rows without dependencies;
+// level l+1: rows whose dependencies all sit in levels <= l).  A level
+// scheduled kernel is one cooperative launch (all CTAs co-resident) that
+// processes the rows of a level with one warp each and then meets at a
+// grid-wide barrier; no per-row flags are polled.
+
+struct GridSync {
+  unsigned* count;  // arrivals at the current barrier
+  unsigned* gen;    // barriers completed
+  int* err;         // 0 or a bilu_status; set on a barrier timeout
+  long long spin;   // polls before a waiting CTA gives up
+};
+
+__device__ __forceinline__ unsigned ld_relaxed_u(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier.  Thread 0 of each CTA fences the CTA's writes and
+// arrives; the last CTA to arrive resets the count, runs last() and releases
+// the others, which poll the generation (bounded).  Returns false in every
+// thread of the CTA if the launch aborted.
+template <class F>
+__device__ __forceinline__ bool grid_sync(const GridSync& g, unsigned& gen_seen, F last) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned target = gen_seen + 1u;
+    __threadfence();
+    if (atomicAdd(g.count, 1u) == gridDim.x - 1u) {
+      atomicExch(g.count, 0u);
+      last();
+      __threadfence();
+      st_release_u(g.gen, target);
+    } else {
+      long long n = 0;
+      unsigned ns = 32;
+      while (ld_relaxed_u(g.gen) != target) {
+        if (ld_relaxed(g.err) != 0) { ok = 0; break; }
+        if (++n > g.spin) {
+          atomicCAS(g.err, 0, (int)BILU_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        backoff(ns);
+      }
+      fence_acquire();
+    }
+    gen_seen = target;
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+struct NoOp {
+  __device__ void operator()() const {}
+};
+
+// Dependencies of row I: lower -> columns in [row[I], diag[I]); upper ->
+// columns in (diag[I], row[I+1]).  cnt[K] += 1 per dependent of K.
+__global__ void k_dep_count(int nb, const int* __restrict__ row, const int* __restrict__ col,
+                            const int* __restrict__ diag, int lower, int* __restrict__ cnt,
+                            int* __restrict__ indeg) {
+  int I = blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= nb) return;
+  int ps = lower ? row[I] : diag[I] + 1, pe = lower ? diag[I] : row[I + 1];
+  indeg[I] = pe - ps;
+  for (int p = ps; p < pe; ++p) atomicAdd(cnt + col[p], 1);
+}
+
+// Successor lists: sidx[sptr[K] ...] = rows that depend on K (any order).
+__global__ void k_dep_fill(int nb, const int* __restrict__ row, const int* __restrict__ col,
+                           const int* __restrict__ diag, int lower, const int* __restrict__ sptr,
+                           int* __restrict__ cursor, int* __restrict__ sidx) {
+  int I = blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= nb) return;
+  int ps = lower ? row[I] : diag[I] + 1, pe = lower ? diag[I] : row[I + 1];
+  for (int p = ps; p < pe; ++p) {
+    int K = col[p];
+    sidx[sptr[K] + atomicAdd(cursor + K, 1)] = I;
+  }
+}
+
+// Breadth-first level sweep (Kahn's algorithm, one level per barrier):
+// order[] receives the rows level by level, lvl_ptr[l] the start of level l
+// (lvl_ptr[nlev] = nb), *nlev the number of levels.  The rows inside a level
+// come in atomic-append order; the level sizes do not depend on it.
+__global__ void __launch_bounds__(256) k_bfs_levels(int nb, const int* __restrict__ sptr,
+                                                    const int* __restrict__ sidx, int* indeg,
+                                                    int* order, int* lvl_ptr, int* tail,
+                                                    int* nlev, GridSync gs) {
+  unsigned gen = 0;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nthr = (long long)gridDim.x * blockDim.x;
+  for (long long I = tid; I < nb; I += nthr)
+    if (indeg[I] == 0) order[atomicAdd(tail, 1)] = (int)I;
+  if (!grid_sync(gs, gen, [&] {
+        lvl_ptr[0] = 0;
+        lvl_ptr[1] = atomicAdd(tail, 0);
+      }))
+    return;
+  for (int l = 0;; ++l) {
+    int s = __ldcg(lvl_ptr + l), e = __ldcg(lvl_ptr + l + 1);
+    if (s == e) {
+      if (tid == 0) *nlev = l;
+      return;
+    }
+    for (long long q = s + tid; q < e; q += nthr) {
+      int I = __ldcg(order + q);
+      for (int p = __ldg(sptr + I), pe = __ldg(sptr + I + 1); p < pe; ++p) {
+        int J = __ldg(sidx + p);
+        if (atomicSub(indeg + J, 1) == 1) order[atomicAdd(tail, 1)] = J;
+      }
+    }
+    if (!grid_sync(gs, gen, [&] { lvl_ptr[l + 2] = atomicAdd(tail, 0); })) return;
+  }
+}
+
+constexpr int kLvlThreads = 256;
+
+template <int BS, bool LOWER, bool UNIT>
+__global__ void __launch_bounds__(kLvlThreads) k_sptrsv_levels(
+    const int* __restrict__ row, const int* __restrict__ col, const int* __restrict__ diag,
+    const double* __restrict__ val, const double* __restrict__ b, double* x,
+    const int* __restrict__ order, const int* __restrict__ lvl_ptr, const int* __restrict__ nlev_p,
+    SyncState ss, GridSync gs) {
+  unsigned gen = 0;
+  const int warp = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nw = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+  const int nlev = __ldg(nlev_p);
+  for (int l = 0; l < nlev; ++l) {
+    int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
+    for (int t = s + warp; t < e; t += nw)
+      sptrsv_row<BS, LOWER, UNIT, false>(__ldg(order + t), row, col, diag, val, b, x, ss);
+    if (l + 1 < nlev && !grid_sync(gs, gen, NoOp{})) return;
+  }
+}
+
+template <int BS>
+__global__ void __launch_bounds__(kLvlThreads) k_bilu0_levels(
+    const int* __restrict__ row, const int* __restrict__ col, const int* __restrict__ diag,
+    double* val, const int* __restrict__ order, const int* __restrict__ lvl_ptr,
+    const int* __restrict__ nlev_p, SyncState ss, GridSync gs) {
+  unsigned gen = 0;
+  const int warp = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nw = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+  const int nlev = __ldg(nlev_p);
+  for (int l = 0; l < nlev; ++l) {
+    int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
+    for (int t = s + warp; t < e; t += nw)
+      bilu0_row<BS, false>(__ldg(order + t), row, col, diag, val, ss);
+    if (l + 1 < nlev && !grid_sync(gs, gen, NoOp{})) return;
+  }
 }
 
 int occupancy_grid(const void* fn, int threads) {
@@ -436,12 +682,128 @@ int launch_sptrsv(int nb, const int* row, const int* col, const int* diag, const
   return BILU_OK;
 }
 
+// ---------------------------------------------------------------- level schedule (host)
+int coop_grid(const void* fn, int threads) { return occupancy_grid(fn, threads); }
+
+// misc words of a level-scheduled launch: count, gen, err, spare
+int grid_sync_init(GridSync& gs, Carver& ws, cudaStream_t st) {
+  unsigned* misc = ws.take<unsigned>(4);
+  if (!misc) return BILU_ERR_WORKSPACE;
+  BILU_TRY_CUDA(cudaMemsetAsync(misc, 0, sizeof(unsigned) * 4, st));
+  gs.count = misc;
+  gs.gen = misc + 1;
+  gs.err = (int*)(misc + 2);
+  gs.spin = kSpinLimit;
+  return BILU_OK;
+}
+
+int grid_sync_finish(const GridSync& gs, cudaStream_t st) {
+  int herr = 0;
+  BILU_TRY_CUDA(cudaMemcpyAsync(&herr, gs.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BILU_TRY_CUDA(cudaStreamSynchronize(st));
+  return herr;
+}
+
+int launch_coop(const void* fn, int grid, int threads, void** args, cudaStream_t st) {
+  BILU_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3((unsigned)grid), dim3((unsigned)threads),
+                                            args, 0, st));
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
+}
+
+// Level analysis of the lower (or upper) dependency DAG: successor lists by
+// counting sort, then the breadth-first level sweep.  order[nb],
+// lvl_ptr[nb+2] and *nlev_d on the device; *h_nlev on the host.
+int build_levels(int nb, const int* row, const int* col, const int* diag, int lower,
+                 long long ndeps_max, int* order, int* lvl_ptr, int* nlev_d, int* h_nlev,
+                 Carver& ws, cudaStream_t st) {
+  int* sptr = ws.take<int>((size_t)nb + 1);
+  int* cursor = ws.take<int>((size_t)nb + 1);
+  int* indeg = ws.take<int>((size_t)nb + 1);
+  int* sidx = ws.take<int>((size_t)std::max(ndeps_max, 1ll));
+  int* tail = ws.take<int>(2);
+  if (!sptr || !cursor || !indeg || !sidx || !tail) return BILU_ERR_WORKSPACE;
+  GridSync gs;
+  BILU_TRY(grid_sync_init(gs, ws, st));
+  BILU_TRY_CUDA(cudaMemsetAsync(sptr, 0, sizeof(int) * ((size_t)nb + 1), st));
+  BILU_TRY_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * ((size_t)nb + 1), st));
+  BILU_TRY_CUDA(cudaMemsetAsync(tail, 0, sizeof(int) * 2, st));
+  BILU_TRY_CUDA(cudaMemsetAsync(nlev_d, 0, sizeof(int), st));
+  BILU_TRY_CUDA(cudaMemsetAsync(lvl_ptr, 0, sizeof(int) * ((size_t)nb + 2), st));
+  if (nb == 0) {
+    if (h_nlev) *h_nlev = 0;
+    return BILU_OK;
+  }
+  k_dep_count<<<ceil_div(nb, 256), 256, 0, st>>>(nb, row, col, diag, lower, sptr, indeg);
+  BILU_LAUNCH_CHECK();
+  int total = 0;
+  BILU_TRY(scan_exclusive(sptr, sptr, nb, &total, ws, st));
+  if (total > ndeps_max) return BILU_ERR_WORKSPACE;
+  k_dep_fill<<<ceil_div(nb, 256), 256, 0, st>>>(nb, row, col, diag, lower, sptr, cursor, sidx);
+  BILU_LAUNCH_CHECK();
+  int grid = std::min<long long>(coop_grid((const void*)k_bfs_levels, 256), ceil_div(nb, 256));
+  void* args[] = {&nb, &sptr, &sidx, &indeg, &order, &lvl_ptr, &tail, &nlev_d, &gs};
+  BILU_TRY(launch_coop((const void*)k_bfs_levels, grid, 256, args, st));
+  int herr = grid_sync_finish(gs, st);
+  if (herr != 0) return herr;
+  int h[2] = {0, 0};
+  BILU_TRY_CUDA(cudaMemcpyAsync(&h[0], nlev_d, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BILU_TRY_CUDA(cudaStreamSynchronize(st));
+  BILU_TRY_CUDA(cudaMemcpyAsync(&h[1], lvl_ptr + h[0], sizeof(int), cudaMemcpyDeviceToHost, st));
+  BILU_TRY_CUDA(cudaStreamSynchronize(st));
+  if (h[1] != nb) return BILU_ERR_PATTERN;  // a row was never reached
+  if (h_nlev) *h_nlev = h[0];
+  return BILU_OK;
+}
+
+template <int BS>
+int launch_sptrsv_levels(int nb, const int* row, const int* col, const int* diag,
+                         const double* val, int lower, int unit, const double* b, double* x,
+                         const int* order, const int* lvl_ptr, const int* nlev_d, int nlev,
+                         SyncState ss, GridSync gs, cudaStream_t st) {
+  const void* fn = lower ? (unit ? (const void*)k_sptrsv_levels<BS, true, true>
+                                 : (const void*)k_sptrsv_levels<BS, true, false>)
+                         : (unit ? (const void*)k_sptrsv_levels<BS, false, true>
+                                 : (const void*)k_sptrsv_levels<BS, false, false>);
+  // no more warps than rows; fewer CTAs make the barrier cheaper
+  int grid = std::min<long long>(coop_grid(fn, kLvlThreads),
+                                 ceil_div(nb, kLvlThreads / 32));
+  (void)nlev;
+  void* args[] = {&row, &col, &diag, &val, &b, &x, &order, &lvl_ptr, &nlev_d, &ss, &gs};
+  return launch_coop(fn, grid, kLvlThreads, args, st);
+}
+
+template <int BS>
+int launch_bilu0_levels(int nb, const int* row, const int* col, const int* diag, double* val,
+                        const int* order, const int* lvl_ptr, const int* nlev_d, SyncState ss,
+                        GridSync gs, cudaStream_t st) {
+  const void* fn = (const void*)k_bilu0_levels<BS>;
+  int grid = std::min<long long>(coop_grid(fn, kLvlThreads), ceil_div(nb, kLvlThreads / 32));
+  void* args[] = {&row, &col, &diag, &val, &order, &lvl_ptr, &nlev_d, &ss, &gs};
+  return launch_coop(fn, grid, kLvlThreads, args, st);
+}
+
 }  // namespace
 
 size_t syncfree_ws(int nb) {
   // flags + order + (levels, counts, misc, scan) + sync misc + error words
   return carve_size(sizeof(int) * ((size_t)nb + 1)) * 4 + carve_size(sizeof(int) * 4) * 2 +
          carve_size(sizeof(int) * 2) + scan_ws_bytes(nb + 1);
+}
+
+// Level analysis scratch (successor lists of up to ndeps dependencies).
+size_t levels_ws(int nb, long long ndeps) {
+  return carve_size(sizeof(int) * ((size_t)nb + 1)) * 3 +
+         carve_size(sizeof(int) * (size_t)std::max(ndeps, 1ll)) + carve_size(sizeof(int) * 2) +
+         carve_size(sizeof(unsigned) * 4) + scan_ws_bytes(nb + 1);
+}
+
+// Level-scheduled factor / solve scratch: the analysis output (order,
+// lvl_ptr, nlev), the analysis scratch, and the error / barrier words.
+size_t level_sched_ws(int nb, long long nnzb) {
+  return carve_size(sizeof(int) * ((size_t)nb + 1)) + carve_size(sizeof(int) * ((size_t)nb + 2)) +
+         carve_size(sizeof(int) * 2) + levels_ws(nb, std::max(nnzb - nb, 0ll)) +
+         carve_size(sizeof(int) * 4) + carve_size(sizeof(unsigned) * 4);
 }
 
 // diagonal positions (validates the pattern); returns BILU_ERR_PATTERN with
@@ -462,21 +824,49 @@ int diag_positions(int nb, const int* row, const int* col, int* diag, int* h_bad
   return hb == INT_MAX ? BILU_OK : BILU_ERR_PATTERN;
 }
 
-int bilu0_impl(int nb, int bs, const int* row, const int* col, const int* diag, double* val,
-               int* h_zp, Carver& ws, cudaStream_t st) {
+namespace {
+
+// error and zero-pivot words without per-row flags (level schedule)
+int sync_init_words(SyncState& ss, Carver& ws, cudaStream_t st) {
+  int* misc = ws.take<int>(4);
+  if (!misc) return BILU_ERR_WORKSPACE;
+  ss = SyncState{nullptr, misc, misc + 1, misc + 2, kSpinLimit, -1, nullptr};
+  int init[4] = {0, 0, INT_MAX, 0};
+  BILU_TRY_CUDA(cudaMemcpyAsync(misc, init, sizeof(init), cudaMemcpyHostToDevice, st));
+  return BILU_OK;
+}
+
+}  // namespace
+
+// BILU(0) in place, level scheduled (one cooperative launch, one grid
+// barrier per dependency level of the lower DAG).
+int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, const int* diag,
+               double* val, int* h_zp, Carver& ws, cudaStream_t st) {
   int* order = ws.take<int>((size_t)nb + 1);
-  if (!order) return BILU_ERR_WORKSPACE;
+  int* lvl = ws.take<int>((size_t)nb + 2);
+  int* nlev_d = ws.take<int>(2);
+  if (!order || !lvl || !nlev_d) return BILU_ERR_WORKSPACE;
+  int nlev = 0;
   {
     Carver w2 = ws;
-    BILU_TRY(build_order(nb, row, col, diag, 1, order, w2, st));
+    BILU_TRY(build_levels(nb, row, col, diag, 1, std::max(nnzb - nb, 0ll), order, lvl, nlev_d,
+                          &nlev, w2, st));
   }
   SyncState ss;
-  BILU_TRY(sync_init(ss, nb, ws, st));
-  ss.order = order;
-  if (nb > 0) BILU_TRY(BILU_DISPATCH_BS(bs, launch_bilu0, nb, row, col, diag, val, ss, st));
+  BILU_TRY(sync_init_words(ss, ws, st));
+  GridSync gs;
+  BILU_TRY(grid_sync_init(gs, ws, st));
+  if (nb > 0)
+    BILU_TRY(BILU_DISPATCH_BS(bs, launch_bilu0_levels, nb, row, col, diag, val, order, lvl,
+                              nlev_d, ss, gs, st));
+  int herr = grid_sync_finish(gs, st);
+  if (herr != 0) return herr;
   return sync_finish(ss, h_zp, st);
 }
 
+// Sync-free solve (dynamic tickets over the level order, per-row flags).
+// Needs only nb-sized scratch (no successor lists): used by the
+// allocation-free entry point and the timeout test hook.
 int sptrsv_impl(int nb, int bs, const int* row, const int* col, const int* diag,
                 const double* val, int lower, int unit, const double* b, double* x, Carver& ws,
                 cudaStream_t st, long long spin = kSpinLimit, int withhold = -1) {
@@ -495,42 +885,83 @@ int sptrsv_impl(int nb, int bs, const int* row, const int* col, const int* diag,
   return sync_finish(ss, nullptr, st);
 }
 
-// Solve with a precomputed analysis (diagonal positions + level order).
-// With sync=false the call returns without waiting for the GPU; the error
-// word is then not read back (use for repeated solves inside a solver).
-int sptrsv_ordered(int nb, int bs, const int* row, const int* col, const int* diag,
-                   const int* order, const double* val, int lower, int unit, const double* b,
-                   double* x, Carver& ws, cudaStream_t st, bool sync) {
+// Level-scheduled solve with a level analysis (order, lvl_ptr, nlev_d).
+int sptrsv_levels(int nb, int bs, const int* row, const int* col, const int* diag,
+                  const int* order, const int* lvl, const int* nlev_d, const double* val,
+                  int lower, int unit, const double* b, double* x, Carver& ws, cudaStream_t st) {
   SyncState ss;
-  BILU_TRY(sync_init(ss, nb, ws, st));
-  ss.order = order;
+  BILU_TRY(sync_init_words(ss, ws, st));
+  GridSync gs;
+  BILU_TRY(grid_sync_init(gs, ws, st));
   if (nb > 0)
-    BILU_TRY(BILU_DISPATCH_BS(bs, launch_sptrsv, nb, row, col, diag, val, lower, unit, b, x, ss,
-                              st));
-  return sync ? sync_finish(ss, nullptr, st) : BILU_OK;
+    BILU_TRY(BILU_DISPATCH_BS(bs, launch_sptrsv_levels, nb, row, col, diag, val, lower, unit, b,
+                              x, order, lvl, nlev_d, 0, ss, gs, st));
+  return grid_sync_finish(gs, st);
+}
+
+// One-shot level-scheduled solve: analysis then solve.
+int sptrsv_level_impl(int nb, long long nnzb, int bs, const int* row, const int* col,
+                      const int* diag, const double* val, int lower, int unit, const double* b,
+                      double* x, Carver& ws, cudaStream_t st) {
+  int* order = ws.take<int>((size_t)nb + 1);
+  int* lvl = ws.take<int>((size_t)nb + 2);
+  int* nlev_d = ws.take<int>(2);
+  if (!order || !lvl || !nlev_d) return BILU_ERR_WORKSPACE;
+  {
+    Carver w2 = ws;
+    BILU_TRY(build_levels(nb, row, col, diag, lower, std::max(nnzb - nb, 0ll), order, lvl,
+                          nlev_d, nullptr, w2, st));
+  }
+  return sptrsv_levels(nb, bs, row, col, diag, order, lvl, nlev_d, val, lower, unit, b, x, ws,
+                       st);
 }
 
 }  // namespace bilu
 
 using namespace bilu;
 
+namespace {
+
+// analysis record: diag[nb+1] | order[nb+1] | lvl_ptr[nb+2] | nlev[2]
+struct AnalysisView {
+  int *diag, *order, *lvl, *nlev;
+  AnalysisView(void* p, int nb) {
+    Carver c(p, (size_t)-1 / 2);
+    diag = c.take<int>((size_t)nb + 1);
+    order = c.take<int>((size_t)nb + 1);
+    lvl = c.take<int>((size_t)nb + 2);
+    nlev = c.take<int>(2);
+  }
+};
+
+}  // namespace
+
 extern "C" size_t bilu_sptrsv_analysis_bytes(int nb) {
-  return 2 * carve_size(sizeof(int) * ((size_t)nb + 1));
+  if (nb < 0) return 0;
+  return 2 * carve_size(sizeof(int) * ((size_t)nb + 1)) +
+         carve_size(sizeof(int) * ((size_t)nb + 2)) + carve_size(sizeof(int) * 2);
 }
 
-extern "C" size_t bilu_sptrsv_solve_ws_bytes(int nb) { return syncfree_ws(nb); }
+extern "C" size_t bilu_sptrsv_analysis_ws_bytes(int nb, int nnzb) {
+  if (nb < 0 || nnzb < 0) return 0;
+  return levels_ws(nb, std::max((long long)nnzb - nb, 0ll)) + carve_size(sizeof(int) * 2);
+}
 
-extern "C" int bilu_sptrsv_analysis(int nb, int bs, const int* d_row, const int* d_col, int lower,
-                                    void* d_info, void* d_ws, size_t ws_bytes,
+extern "C" size_t bilu_sptrsv_solve_ws_bytes(int nb) {
+  if (nb < 0) return 0;
+  return syncfree_ws(nb);
+}
+
+extern "C" int bilu_sptrsv_analysis(int nb, int nnzb, int bs, const int* d_row, const int* d_col,
+                                    int lower, void* d_info, void* d_ws, size_t ws_bytes,
                                     bilu_stream_t stream) {
-  if (nb < 0 || !d_info || (nb > 0 && (!d_row || !d_col))) return BILU_ERR_ARG;
+  if (nb < 0 || nnzb < nb || !d_info || (nb > 0 && (!d_row || !d_col))) return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
-  Carver info(d_info, bilu_sptrsv_analysis_bytes(nb));
-  int* diag = info.take<int>((size_t)nb + 1);
-  int* order = info.take<int>((size_t)nb + 1);
+  AnalysisView a(d_info, nb);
   Carver ws(d_ws, ws_bytes);
-  BILU_TRY(diag_positions(nb, d_row, d_col, diag, nullptr, ws, S(stream)));
-  return build_order(nb, d_row, d_col, diag, lower != 0, order, ws, S(stream));
+  BILU_TRY(diag_positions(nb, d_row, d_col, a.diag, nullptr, ws, S(stream)));
+  return build_levels(nb, d_row, d_col, a.diag, lower != 0, (long long)nnzb - nb, a.order, a.lvl,
+                      a.nlev, nullptr, ws, S(stream));
 }
 
 extern "C" int bilu_sptrsv_solve(int nb, int bs, const int* d_row, const int* d_col,
@@ -540,16 +971,34 @@ extern "C" int bilu_sptrsv_solve(int nb, int bs, const int* d_row, const int* d_
   if (nb < 0 || !d_info || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)))
     return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
-  Carver info(const_cast<void*>(d_info), bilu_sptrsv_analysis_bytes(nb));
-  const int* diag = info.take<int>((size_t)nb + 1);
-  const int* order = info.take<int>((size_t)nb + 1);
+  AnalysisView a(const_cast<void*>(d_info), nb);
   Carver ws(d_ws, ws_bytes);
-  return sptrsv_ordered(nb, bs, d_row, d_col, diag, order, d_val, lower != 0, unit != 0, d_b, d_x,
-                        ws, S(stream), true);
+  return sptrsv_levels(nb, bs, d_row, d_col, a.diag, a.order, a.lvl, a.nlev, d_val, lower != 0,
+                       unit != 0, d_b, d_x, ws, S(stream));
 }
 
-extern "C" size_t bilu_bsrilu0_ws_bytes(int nb) {
-  return syncfree_ws(nb) + carve_size(sizeof(int) * ((size_t)nb + 1));
+extern "C" int bilu_sptrsv_solve_syncfree(int nb, int bs, const int* d_row, const int* d_col,
+                                          const double* d_val, int lower, int unit,
+                                          const void* d_info, const double* d_b, double* d_x,
+                                          void* d_ws, size_t ws_bytes, bilu_stream_t stream) {
+  if (nb < 0 || !d_info || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)))
+    return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  AnalysisView a(const_cast<void*>(d_info), nb);
+  Carver ws(d_ws, ws_bytes);
+  SyncState ss;
+  BILU_TRY(sync_init(ss, nb, ws, S(stream)));
+  ss.order = a.order;
+  if (nb > 0)
+    BILU_TRY(BILU_DISPATCH_BS(bs, launch_sptrsv, nb, d_row, d_col, a.diag, d_val, lower != 0,
+                              unit != 0, d_b, d_x, ss, S(stream)));
+  return sync_finish(ss, nullptr, S(stream));
+}
+
+extern "C" size_t bilu_bsrilu0_ws_bytes(int nb, int nnzb) {
+  if (nb < 0 || nnzb < 0) return 0;
+  return carve_size(sizeof(int) * ((size_t)nb + 1)) + carve_size(sizeof(int) * 2) +
+         level_sched_ws(nb, nnzb);
 }
 
 extern "C" int bilu_bsrilu0(int nb, int nnzb, int bs, const int* d_row, const int* d_col,
@@ -567,37 +1016,34 @@ extern "C" int bilu_bsrilu0(int nb, int nnzb, int bs, const int* d_row, const in
     if (h_info) *h_info = bad;
     return rc;
   }
-  return bilu0_impl(nb, bs, d_row, d_col, diag, d_val, h_info, ws, S(stream));
+  return bilu0_impl(nb, nnzb, bs, d_row, d_col, diag, d_val, h_info, ws, S(stream));
 }
 
-extern "C" size_t bilu_sptrsv_ws_bytes(int nb) {
-  return syncfree_ws(nb) + carve_size(sizeof(int) * ((size_t)nb + 1));
+extern "C" size_t bilu_sptrsv_ws_bytes(int nb, int nnzb) {
+  if (nb < 0 || nnzb < 0) return 0;
+  return carve_size(sizeof(int) * ((size_t)nb + 1)) + carve_size(sizeof(int) * 2) +
+         level_sched_ws(nb, nnzb);
 }
 
-extern "C" int bilu_sptrsv(int nb, int bs, const int* d_row, const int* d_col, const double* d_val,
-                           int lower, const double* d_b, double* d_x, void* d_ws,
-                           size_t ws_bytes, bilu_stream_t stream) {
-  if (nb < 0 || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x))) return BILU_ERR_ARG;
-  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
-  Carver ws(d_ws, ws_bytes);
-  int* diag = ws.take<int>((size_t)nb + 1);
-  if (!diag) return BILU_ERR_WORKSPACE;
-  BILU_TRY(diag_positions(nb, d_row, d_col, diag, nullptr, ws, S(stream)));
-  return sptrsv_impl(nb, bs, d_row, d_col, diag, d_val, lower != 0, lower != 0, d_b, d_x, ws,
-                     S(stream));
+extern "C" int bilu_sptrsv(int nb, int nnzb, int bs, const int* d_row, const int* d_col,
+                           const double* d_val, int lower, const double* d_b, double* d_x,
+                           void* d_ws, size_t ws_bytes, bilu_stream_t stream) {
+  return bilu_sptrsv_ex(nb, nnzb, bs, d_row, d_col, d_val, lower, lower, d_b, d_x, d_ws, ws_bytes,
+                        stream);
 }
 
-extern "C" int bilu_sptrsv_ex(int nb, int bs, const int* d_row, const int* d_col,
+extern "C" int bilu_sptrsv_ex(int nb, int nnzb, int bs, const int* d_row, const int* d_col,
                               const double* d_val, int lower, int unit, const double* d_b,
                               double* d_x, void* d_ws, size_t ws_bytes, bilu_stream_t stream) {
-  if (nb < 0 || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x))) return BILU_ERR_ARG;
+  if (nb < 0 || nnzb < nb || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)))
+    return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   Carver ws(d_ws, ws_bytes);
   int* diag = ws.take<int>((size_t)nb + 1);
   if (!diag) return BILU_ERR_WORKSPACE;
   BILU_TRY(diag_positions(nb, d_row, d_col, diag, nullptr, ws, S(stream)));
-  return sptrsv_impl(nb, bs, d_row, d_col, diag, d_val, lower != 0, unit != 0, d_b, d_x, ws,
-                     S(stream));
+  return sptrsv_level_impl(nb, nnzb, bs, d_row, d_col, diag, d_val, lower != 0, unit != 0, d_b,
+                           d_x, ws, S(stream));
 }
 
 // Test hook: the sync-free solve with block row `withhold_row` never

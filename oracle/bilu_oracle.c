@@ -667,6 +667,11 @@ static void isai_apply(const isai_apply_t* P, int precond, const double* v,
                        double* z, size_t n) {
   if (precond == 0) {
     memcpy(z, v, sizeof(double) * n);
+  } else if (precond == 3) {
+    /* exact BILU(0): L (Lrow/Lcol/Lval = packed factor) unit-lower solve,
+     * then the upper solve on the same packed factor */
+    orc_sptrsv_lower(P->nb, P->bs, P->Lrow, P->Lcol, P->Lval, v, P->y);
+    orc_sptrsv_upper(P->nb, P->bs, P->Lrow, P->Lcol, P->Lval, P->y, z);
   } else if (precond == 1) {
     orc_bcsr_spmv(P->nb, P->bs, P->Lrow, P->Lcol, P->Lval, v, P->y);
     orc_bcsr_spmv(P->nb, P->bs, P->Urow, P->Ucol, P->Uval, P->y, z);

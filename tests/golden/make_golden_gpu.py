@@ -212,7 +212,7 @@ def time_factor_and_solves(A, reps=5):
         best = (ms[0], ms[1]) if best is None or ms[1] < best[1] else best
     out["cusparse_bsrilu02_analysis_ms"], out["cusparse_bsrilu02_factor_ms"] = best
     lu_ref = v
-    ws = api._ws(L.bilu_bsrilu0_ws_bytes(A.nb), dev)
+    ws = api._ws(L.bilu_bsrilu0_ws_bytes(A.nb, A.nnzb), dev)
     ts = []
     for _ in range(3):
         v = A0.clone()
@@ -234,11 +234,12 @@ def time_factor_and_solves(A, reps=5):
         C.cusp_bsrsv2(A.nb, A.nnzb, A.bs, P(row), P(col), P(lu_ref), lower, P(b), P(x), reps, ms)
         out[f"cusparse_bsrsv2_{tag}_analysis_ms"], out[f"cusparse_bsrsv2_{tag}_solve_ms"] = ms[0], ms[1]
         info = torch.empty(L.bilu_sptrsv_analysis_bytes(A.nb), dtype=torch.uint8, device=dev)
-        ws = api._ws(max(L.bilu_sptrsv_ws_bytes(A.nb), L.bilu_sptrsv_solve_ws_bytes(A.nb)), dev)
+        ws = api._ws(max(L.bilu_sptrsv_analysis_ws_bytes(A.nb, A.nnzb),
+                         L.bilu_sptrsv_solve_ws_bytes(A.nb)), dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        L.bilu_sptrsv_analysis(A.nb, A.bs, P(row), P(col), lower, P(info), P(ws), ws.numel(),
-                               api._s())
+        L.bilu_sptrsv_analysis(A.nb, A.nnzb, A.bs, P(row), P(col), lower, P(info), P(ws),
+                               ws.numel(), api._s())
         e1.record()
         e1.synchronize()
         out[f"ours_sptrsv_{tag}_analysis_ms"] = e0.elapsed_time(e1)
@@ -252,6 +253,17 @@ def time_factor_and_solves(A, reps=5):
         e1.record()
         e1.synchronize()
         out[f"ours_sptrsv_{tag}_solve_ms"] = e0.elapsed_time(e1) / reps
+        y2 = torch.empty_like(b)
+        L.bilu_sptrsv_solve_syncfree(A.nb, A.bs, P(row), P(col), P(lu_ref), lower, lower, P(info),
+                                     P(b), P(y2), P(ws), ws.numel(), api._s())
+        e0.record()
+        for _ in range(reps):
+            L.bilu_sptrsv_solve_syncfree(A.nb, A.bs, P(row), P(col), P(lu_ref), lower, lower,
+                                         P(info), P(b), P(y2), P(ws), ws.numel(), api._s())
+        e1.record()
+        e1.synchronize()
+        out[f"ours_sptrsv_{tag}_syncfree_solve_ms"] = e0.elapsed_time(e1) / reps
+        out[f"sptrsv_{tag}_level_vs_syncfree_identical"] = bool(torch.equal(y, y2))
         out[f"sptrsv_{tag}_max_rel_diff_vs_cusparse"] = float((y - x).abs().max() / x.abs().max())
     return out
 

@@ -258,6 +258,58 @@ def test_sptrsv_transposed(cuda, orc):
     assert relerr(xu, np.linalg.solve(U.T, b)) < 1e-10
 
 
+@pytest.mark.parametrize("name", ["laplace2d_s12", "convdiff3d_s5", "powerlaw_nb120"])
+def test_sptrsv_level_and_syncfree_schedules(cuda, orc, name):
+    """Analysis once, then the level-scheduled and the sync-free solve on
+    it: identical x (each row's arithmetic does not depend on the schedule),
+    equal to the oracle within 1e-12; level counts match the oracle's
+    longest-path levels."""
+    import torch
+
+    from isai_kernel_gb300 import _lib, api
+
+    d = golden(name)
+    nb, bs = int(d["nb"]), int(d["bs"])
+    LU, _ = orc.bsrilu0(nb, bs, d["row"], d["col"], d["val"])
+    row, col, lu = T(d["row"], cuda), T(d["col"], cuda), T(LU, cuda)
+    nnzb = int(d["col"].shape[0])
+    b = gen.rhs(nb * bs, 5)
+    L = _lib.lib()
+    for lower in (1, 0):
+        info = api._ws(L.bilu_sptrsv_analysis_bytes(nb), cuda)
+        ws = api._ws(max(L.bilu_sptrsv_analysis_ws_bytes(nb, nnzb), L.bilu_sptrsv_solve_ws_bytes(nb)),
+                     cuda)
+        api.call("bilu_sptrsv_analysis", nb, nnzb, bs, api._p(row), api._p(col), lower,
+                 api._p(info), api._p(ws), ws.numel(), api._s())
+        bd = T(b, cuda)
+        x1, x2 = torch.empty_like(bd), torch.empty_like(bd)
+        for fn, x in (("bilu_sptrsv_solve", x1), ("bilu_sptrsv_solve_syncfree", x2)):
+            api.call(fn, nb, bs, api._p(row), api._p(col), api._p(lu), lower, lower, api._p(info),
+                     api._p(bd), api._p(x), api._p(ws), ws.numel(), api._s())
+        assert torch.equal(x1, x2)
+        ref = (orc.sptrsv_lower if lower else orc.sptrsv_upper)(nb, bs, d["row"], d["col"],
+                                                                LU, b)
+        assert relerr(N(x1), ref) < 1e-12
+        # level sizes: oracle longest-path levels over the same DAG
+        lv = np.zeros(nb, np.int64)
+        rp, ci = d["row"], d["col"]
+        rows = range(nb) if lower else range(nb - 1, -1, -1)
+        for i in rows:
+            deps = ci[rp[i]:rp[i + 1]]
+            deps = deps[deps < i] if lower else deps[deps > i]
+            lv[i] = 1 + (lv[deps].max() if deps.size else 0)
+        words = N(info).view(np.int32)
+        # record layout: diag | order | lvl_ptr | nlev, each carved on 256 B
+        def carve(n):
+            return ((n * 4 + 255) // 256) * 64
+        o_lvl = 2 * carve(nb + 1)
+        o_nlev = o_lvl + carve(nb + 2)
+        nlev = int(words[o_nlev])
+        ptr = words[o_lvl:o_lvl + nlev + 1]
+        assert nlev == lv.max() and ptr[-1] == nb
+        assert np.array_equal(np.diff(ptr), np.bincount(lv - 1, minlength=nlev))
+
+
 def test_sptrsv_timeout_path(cuda, orc):
     """A row that never publishes: dependants give up after a short bounded
     wait, the call reports BILU_ERR_TIMEOUT, and the context stays usable."""
@@ -270,7 +322,7 @@ def test_sptrsv_timeout_path(cuda, orc):
     row, col, lu = T(A.rowptr, cuda), T(A.colind, cuda), T(LU, cuda)
     b = T(gen.rhs(A.n, 3), cuda)
     x = b.clone()
-    ws = api._ws(_lib.lib().bilu_sptrsv_ws_bytes(A.nb), cuda)
+    ws = api._ws(_lib.lib().bilu_sptrsv_ws_bytes(A.nb, A.nnzb), cuda)
     st = _lib.lib().bilu_debug_sptrsv_withhold(
         A.nb, A.bs, api._p(row), api._p(col), api._p(lu), 1, api._p(b), api._p(x), 5,
         ctypes.c_longlong(1 << 14), api._p(ws), ws.numel(), api._s())

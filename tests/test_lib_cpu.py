@@ -34,7 +34,10 @@ def test_host_queries():
     assert L.bilu_version() >= 10000
     assert L.bilu_status_string(-4) == b"sync-free wait timed out"
     assert L.bilu_status_string(0) == b"ok"
-    assert L.bilu_bsrilu0_ws_bytes(1000) > 4000
+    assert L.bilu_bsrilu0_ws_bytes(1000, 5000) > 4000
+    # level analysis scratch grows with the dependency count
+    assert L.bilu_sptrsv_analysis_ws_bytes(1000, 9000) > L.bilu_sptrsv_analysis_ws_bytes(1000, 5000)
+    assert L.bilu_sptrsv_ws_bytes(1000, 5000) >= L.bilu_sptrsv_solve_ws_bytes(1000)
     assert L.bilu_isai_pattern_ws_bytes(100, 500) > 0
     assert L.bilu_sptrsv_transpose_ws_bytes(10, 30, 4) > 30 * 16 * 8
 
