@@ -233,7 +233,7 @@ def run_ours(args):
     b = torch.from_numpy(b_np).to(dev)
     torch.cuda.synchronize()
 
-    P = api.Preconditioner(nb, bs, row, col, val, fp32=True)
+    P = api.Preconditioner(nb, bs, row, col, val, fp32=True, fp32_inner=True)
     setup_ms = P.setup_ms
     x = torch.empty_like(b)
 
@@ -273,6 +273,15 @@ def run_ours(args):
     e1.record(stream)
     e1.synchronize()
     t_fp64 = e0.elapsed_time(e1) / 1e3
+
+    # FP32 ISAI plus FP32-stored A in the Arnoldi products (FP64
+    # orthogonalisation, true residuals and restarts), reported beside
+    _, r32i = solve(3)
+    e0.record(stream)
+    _, r32i = solve(3)
+    e1.record(stream)
+    e1.synchronize()
+    t_f32i = e0.elapsed_time(e1) / 1e3
 
     # preconditioner apply kernels, timed alone with CUDA events on the
     # launching stream (inputs: 1.1-1.9 GB of factors, larger than L2)
@@ -358,6 +367,10 @@ def run_ours(args):
         "restart_cycles": {"mixed": restarts_mixed, "fp64": r64.restarts},
         "relres": {"mixed": relres_mixed, "fp64": r64.relres},
         "fp64_solve_s": t_fp64, "speedup_mixed_vs_fp64": t_fp64 / t_mixed,
+        "fp32_inner": {"s": t_f32i, "iters": r32i.iters, "relres": r32i.relres,
+                       "restart_cycles": r32i.restarts, "speedup_vs_fp64": t_fp64 / t_f32i,
+                       "what": "FP32 ISAI + FP32-stored A in the Arnoldi products; FP64 "
+                               "orthogonalisation, true residual and restarts"},
         "setup_ms": setup_ms,
         "apply": {"fp32_s": t_apply32, "fp64_s": t_apply64, "fp32_GBs": gbs32,
                   "fp64_GBs": B64 / t_apply64 / 1e9, "bytes_fp32": B32, "bytes_fp64": B64,
@@ -506,6 +519,20 @@ def run_sptrsv(args):
             nbytes = (strict + nb) * (bs * bs * 8 + 4) + (nb + 1) * 4 * 3 + 2 * A.n * 8
             out[f"{tag}_{name}_ms"] = ms
             out[f"{tag}_{name}_GBs"] = nbytes / ms / 1e6
+    # GMRES(30) with the exact BILU(0) (two level-scheduled solves per apply)
+    # against the FP32 ISAI apply, and the measured switch between them
+    Pc = api.Preconditioner(nb, bs, row, col, val, fp32=True, ilu=True)
+    for prec, tag in ((api.BILU_ILU, "ilu"), (api.BILU_FP32, "isai_fp32")):
+        e0.record()
+        _, res = Pc.solve(b, x, prec=prec, maxit=args.maxit)
+        e1.record()
+        e1.synchronize()
+        out[f"gmres_{tag}"] = {"s": e0.elapsed_time(e1) / 1e3, "iters": res.iters,
+                               "relres": res.relres}
+    choice, rate = Pc.select(b, cycles=1)
+    out["switch"] = {"choice": {0: "isai_fp64", 1: "isai_fp32", 2: "ilu", 3: "fp32_inner"}[choice],
+                     "digits_per_s": rate}
+    Pc.close()
     print(json.dumps(out))
 
 

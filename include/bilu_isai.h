@@ -18,8 +18,12 @@
  *   - Packed BILU(0) as cuSPARSE bsrilu02: strictly lower blocks = L,
  *     diagonal block = unit-lower L_kk (strict lower part) and U_kk,
  *     strictly upper blocks = U.
- *   - Supported block sizes: 4, 5, 8.  Precision: BILU_FP64 (plain) or
- *     BILU_FP32 (FP32-stored ISAI factors, FP32 accumulation).
+ *   - Supported block sizes: 4, 5, 8.  Preconditioner choice: BILU_FP64
+ *     (plain ISAI), BILU_FP32 (FP32-stored ISAI factors, FP32
+ *     accumulation), BILU_ILU (exact BILU(0): two block triangular solves
+ *     per apply, FP64) or BILU_FP32_INNER (FP32 ISAI and an FP32-stored A in
+ *     the Arnoldi products; orthogonalisation, true residuals and restarts
+ *     stay FP64).
  *   - stream may be NULL (legacy default stream).  Calls are asynchronous
  *     unless documented to return a host value (h_ outputs synchronise).
  */
@@ -44,10 +48,11 @@ enum bilu_status {
   BILU_ERR_CUDA = -5,          /* CUDA runtime error (launch, copy) */
   BILU_ERR_NOT_CONVERGED = -6, /* Krylov solver hit maxit */
   BILU_ERR_WORKSPACE = -7,     /* workspace too small */
-  BILU_ERR_UNSUPPORTED = -8    /* block size / precision not built */
+  BILU_ERR_UNSUPPORTED = -8,   /* block size / precision / file kind not built */
+  BILU_ERR_IO = -9             /* file missing, unreadable, malformed or corrupt */
 };
 
-enum bilu_precision { BILU_FP64 = 0, BILU_FP32 = 1 };
+enum bilu_precision { BILU_FP64 = 0, BILU_FP32 = 1, BILU_ILU = 2, BILU_FP32_INNER = 3 };
 
 const char* bilu_status_string(int status);
 int bilu_version(void);
@@ -286,7 +291,10 @@ int bilu_ctx_destroy(bilu_ctx* ctx);
 
 /* Copies the BSR matrix (device pointers; the values are not modified) and
  * runs the whole setup on the GPU: BILU(0), ISAI patterns, pair lists, Dinv,
- * ISAI-L/U, BCSC->BCSR reorder, FP32 copies when prec_mask has BILU_FP32.
+ * ISAI-L/U, BCSC->BCSR reorder, FP32 copies when prec_mask has
+ * 1 << BILU_FP32, level analyses of both triangles when it has
+ * 1 << BILU_ILU, FP32 copies of the ISAI factors and of A when it has
+ * 1 << BILU_FP32_INNER.
  * h_times (optional, 4 doubles, milliseconds): factor, patterns, isai,
  * total. */
 int bilu_ctx_setup(bilu_ctx* ctx, int nb, int nnzb, int bs, const int* d_row, const int* d_col,
@@ -295,8 +303,11 @@ int bilu_ctx_setup(bilu_ctx* ctx, int nb, int nnzb, int bs, const int* d_row, co
 /* Right-preconditioned restarted (F)GMRES(restart) with modified
  * Gram-Schmidt and Givens rotations, x0 = 0: prec BILU_FP64 applies the FP64 ISAI, BILU_FP32 the
  * FP32-stored ISAI (flexible GMRES, FP64 residuals/orthogonalisation,
- * FP64 true residual at every restart = iterative refinement); prec -1 runs
- * without preconditioner.  h_iters, h_relres: iteration count and final true
+ * FP64 true residual at every restart = iterative refinement), BILU_ILU the
+ * exact BILU(0) by level-scheduled triangular solves, BILU_FP32_INNER the
+ * FP32 ISAI with the FP32-stored A in the Arnoldi products (the true FP64
+ * residual at every restart corrects the inner precision, as in GMRES with
+ * iterative refinement); prec -1 runs without preconditioner.  A choice the setup did not build returns BILU_ERR_ARG.  h_iters, h_relres: iteration count and final true
  * relative residual.  h_hist (optional, maxit+1 doubles) receives the
  * residual estimate after every iteration. */
 int bilu_ctx_solve(bilu_ctx* ctx, int prec, const double* d_b, double* d_x, int restart,
@@ -305,6 +316,15 @@ int bilu_ctx_solve(bilu_ctx* ctx, int prec, const double* d_b, double* d_x, int 
 /* Counters of the last solve: h_out[0] = Arnoldi steps, h_out[1] = restart
  * cycles. */
 int bilu_ctx_stats(bilu_ctx* ctx, long long* h_out);
+
+/* Preconditioner switch by measurement (SpTRSV apply vs SpMV apply):
+ * runs `cycles` restart cycles from x0 = 0 with each choice whose bit
+ * (1 << BILU_FP64 / BILU_FP32 / BILU_ILU / BILU_FP32_INNER) is in `mask`
+ * and that the setup built, and returns in *h_choice the one with the
+ * largest residual reduction per second; h_rate (optional, 4 doubles)
+ * receives the scores in decimal digits per second, indexed by choice. */
+int bilu_ctx_select(bilu_ctx* ctx, const double* d_b, int restart, int cycles, int mask,
+                    int* h_choice, double* h_rate);
 
 /* Host-buffer convenience (the end-to-end call): copies A and b from host
  * memory, runs setup and solve, copies x back. */
@@ -319,6 +339,35 @@ int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const int* h_col
  * 6 M_U values (double), 7 M_L values (float), 8 M_U values (float).
  * h_count receives the number of elements. */
 int bilu_ctx_get(bilu_ctx* ctx, int which, const void** d_ptr, long long* h_count);
+
+/* ------------------------------------------------------------------ */
+/* Host-side ingest                                                    */
+/* ------------------------------------------------------------------ */
+
+/* Replaces read_matrix_market_to_csr (read_matrix.h:12): a Matrix Market
+ * coordinate file to 0-based CSR with rows sorted by column (ties keep file
+ * order, duplicates are kept, as the reference keeps them).  Real and
+ * integer values; "pattern" entries read as 1.0; "symmetric" / "hermitian"
+ * files are expanded to both triangles and "skew-symmetric" ones with the
+ * mirrored value negated (the reference ignores the symmetry qualifier).
+ * Two calls: with h_row/h_col/h_val NULL it returns the sizes (h_nnz = the
+ * expanded entry count); then with arrays of nrows+1 / h_nnz / h_nnz
+ * elements (*h_nnz = their capacity) it fills them.  BILU_ERR_IO for a
+ * missing file, a missing banner or size line, or a bad entry (its 0-based
+ * index in *h_bad_entry); BILU_ERR_UNSUPPORTED for array or complex files. */
+int bilu_mtx_read(const char* path, int* h_nrows, int* h_ncols, long long* h_nnz, int* h_row,
+                  int* h_col, double* h_val, long long* h_bad_entry);
+/* Binary BSR file (no counterpart in the reference): a 40-byte header
+ * (magic "BILUBSR1", block size, nb, nnzb, a 64-bit FNV-1a checksum of the
+ * payload), then rowptr[nb+1], colind[nnzb] (int32) and the values
+ * (nnzb*bs*bs doubles, row-major blocks), little-endian.  bilu_bsr_load
+ * with NULL arrays reads the header only; with arrays it checks the sizes
+ * against *h_nb/*h_nnzb/*h_bs, the checksum (BILU_ERR_IO on mismatch) and
+ * the structure (BILU_ERR_PATTERN). */
+int bilu_bsr_save(const char* path, int nb, int nnzb, int bs, const int* h_row, const int* h_col,
+                  const double* h_val);
+int bilu_bsr_load(const char* path, int* h_nb, int* h_nnzb, int* h_bs, int* h_row, int* h_col,
+                  double* h_val);
 
 /* ------------------------------------------------------------------ */
 /* Batched multi-RHS solves (no counterpart in the reference)          */

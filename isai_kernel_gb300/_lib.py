@@ -35,8 +35,9 @@ STATUS = {
     -6: "BILU_ERR_NOT_CONVERGED",
     -7: "BILU_ERR_WORKSPACE",
     -8: "BILU_ERR_UNSUPPORTED",
+    -9: "BILU_ERR_IO",
 }
-BILU_FP64, BILU_FP32 = 0, 1
+BILU_FP64, BILU_FP32, BILU_ILU, BILU_FP32_INNER = 0, 1, 2, 3
 
 
 def _ctype(t: str):

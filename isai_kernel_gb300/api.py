@@ -9,11 +9,12 @@ where the reference calls exit(1).
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass
 
 import torch
 
-from ._lib import BILU_FP32, BILU_FP64, BiluError, call, lib
+from ._lib import BILU_FP32, BILU_FP32_INNER, BILU_FP64, BILU_ILU, BiluError, call, lib
 
 _I32, _F64, _F32 = torch.int32, torch.float64, torch.float32
 
@@ -326,7 +327,8 @@ class Preconditioner:
     """BILU(0)+ISAI engine handle (bilu_ctx): GPU setup of the whole
     preconditioner from a BSR matrix, then preconditioned (F)GMRES solves."""
 
-    def __init__(self, nb: int, bs: int, row, col, val, fp32: bool = True, stream=None):
+    def __init__(self, nb: int, bs: int, row, col, val, fp32: bool = True, ilu: bool = False,
+                 fp32_inner: bool = False, stream=None):
         self._h = ctypes.c_void_p()
         self.nb, self.bs = nb, bs
         self.stream = stream
@@ -334,7 +336,8 @@ class Preconditioner:
         self._keep = (row, col, val)
         times = (ctypes.c_double * 4)()
         call("bilu_ctx_setup", self._h, nb, int(col.numel()), bs, _p(_ci(row)), _p(_ci(col)),
-             _p(_cf(val)), (1 << BILU_FP32) if fp32 else 0, times)
+             _p(_cf(val)), ((1 << BILU_FP32) if fp32 else 0) | ((1 << BILU_ILU) if ilu else 0)
+             | ((1 << BILU_FP32_INNER) if fp32_inner else 0), times)
         self.setup_ms = {"factor": times[0], "patterns": times[1], "isai": times[2],
                          "total": times[3]}
 
@@ -368,9 +371,22 @@ class Preconditioner:
         U = (self.get(4), self.get(5), self.get(6).view(-1, bs, bs))
         return lu, L, U
 
-    def solve(self, b, x=None, prec: int = BILU_FP64, restart: int = 30, tol: float = 1e-10,
+    def select(self, b, restart: int = 30, cycles: int = 1, mask: int = 15):
+        """bilu_ctx_select: the preconditioner (BILU_FP64 / BILU_FP32 /
+        BILU_ILU / BILU_FP32_INNER) with the best measured residual reduction
+        per second over `cycles` restart cycles -> (choice, [digits/s])."""
+        choice, rate = ctypes.c_int(-1), (ctypes.c_double * 4)()
+        call("bilu_ctx_select", self._h, _p(_cf(b)), restart, cycles, mask,
+             ctypes.byref(choice), rate)
+        return choice.value, list(rate)
+
+    def solve(self, b, x=None, prec=BILU_FP64, restart: int = 30, tol: float = 1e-10,
               maxit: int = 10000, history: bool = False) -> tuple:
+        """prec: BILU_FP64, BILU_FP32, BILU_ILU, BILU_FP32_INNER, -1 (none) or
+        "auto" (measured choice by select())."""
         b = _cf(b)
+        if prec == "auto":
+            prec, _ = self.select(b, restart)
         if x is None:
             x = torch.empty_like(b)
         it, rr = ctypes.c_int(0), ctypes.c_double(0)
@@ -383,6 +399,56 @@ class Preconditioner:
         stats = (ctypes.c_longlong * 4)()
         call("bilu_ctx_stats", self._h, stats)
         return x, SolveResult(it.value, rr.value, st == 0, h, int(stats[1]))
+
+
+# ------------------------------------------------------------ host ingest
+def read_matrix_market_to_csr(path: str):
+    """read_matrix.h:12 read_matrix_market_to_csr (bilu_mtx_read; also
+    expands symmetric / skew-symmetric files and reads pattern files)
+    -> (nrows, ncols, rowPtr, colInd, vals) as numpy arrays."""
+    import numpy as np
+
+    m, n, nnz, bad = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_longlong(0), ctypes.c_longlong(-1)
+    p = os.fsencode(path)
+    call("bilu_mtx_read", p, ctypes.byref(m), ctypes.byref(n), ctypes.byref(nnz), None, None,
+         None, ctypes.byref(bad))
+    row = np.zeros(m.value + 1, np.int32)
+    col = np.zeros(max(nnz.value, 1), np.int32)
+    val = np.zeros(max(nnz.value, 1), np.float64)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    call("bilu_mtx_read", p, ctypes.byref(m), ctypes.byref(n), ctypes.byref(nnz), P(row), P(col),
+         P(val), ctypes.byref(bad))
+    return m.value, n.value, row, col[: nnz.value], val[: nnz.value]
+
+
+def bsr_save(path: str, nb: int, bs: int, rowptr, colind, val):
+    """Write a BSR matrix (numpy arrays) to the binary format of bilu_bsr_save."""
+    import numpy as np
+
+    row = np.ascontiguousarray(rowptr, np.int32)
+    col = np.ascontiguousarray(colind, np.int32)
+    v = np.ascontiguousarray(val, np.float64)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    call("bilu_bsr_save", os.fsencode(path), nb, int(col.shape[0]), bs, P(row), P(col), P(v))
+
+
+def bsr_load(path: str):
+    """Read a file written by bsr_save -> (nb, bs, rowptr, colind, val[nnzb, bs, bs])."""
+    import numpy as np
+
+    nb, nnzb, bs = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+    p = os.fsencode(path)
+    call("bilu_bsr_load", p, ctypes.byref(nb), ctypes.byref(nnzb), ctypes.byref(bs), None, None,
+         None)
+    row = np.zeros(nb.value + 1, np.int32)
+    col = np.zeros(max(nnzb.value, 1), np.int32)
+    val = np.zeros(max(nnzb.value * bs.value * bs.value, 1), np.float64)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    call("bilu_bsr_load", p, ctypes.byref(nb), ctypes.byref(nnzb), ctypes.byref(bs), P(row),
+         P(col), P(val))
+    k = nnzb.value
+    return nb.value, bs.value, row, col[:k], val[: k * bs.value * bs.value].reshape(k, bs.value,
+                                                                                  bs.value)
 
 
 def block_diagonal_union(mats):

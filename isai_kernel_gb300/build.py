@@ -26,7 +26,13 @@ def nvcc() -> str:
 
 
 def sources():
-    return sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
+    """CUDA translation units (.cu) and host-only C++ (.cpp, compiled by nvcc's
+    host compiler)."""
+    return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
+
+
+def _obj(f: str) -> str:
+    return os.path.join(OBJ, os.path.splitext(f)[0] + ".o")
 
 
 def _stale(obj: str, src: str) -> bool:
@@ -44,7 +50,7 @@ def build(verbose: bool = False, extra=()) -> str:
     jobs = []
     for f in sources():
         src = os.path.join(CSRC, f)
-        obj = os.path.join(OBJ, f[:-3] + ".o")
+        obj = _obj(f)
         if _stale(obj, src):
             jobs.append([nv, *ARCH, *FLAGS, *extra, "-c", src, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
@@ -53,7 +59,7 @@ def build(verbose: bool = False, extra=()) -> str:
                 sys.stderr.write(res.stdout + res.stderr)
             if res.returncode:
                 raise RuntimeError("nvcc failed: " + " ".join(cmd))
-    objs = [os.path.join(OBJ, f[:-3] + ".o") for f in sources()]
+    objs = [_obj(f) for f in sources()]
     if jobs or not os.path.exists(LIB):
         cmd = [nv, *ARCH, "-shared", "-o", LIB, *objs]
         res = subprocess.run(cmd, capture_output=True, text=True)

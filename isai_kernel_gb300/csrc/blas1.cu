@@ -87,29 +87,15 @@ __global__ void k_reduce(const double* __restrict__ partial, int nout, double* _
   out[i] = s;
 }
 
-// Elements in 16-byte pairs (x and y start on 16-byte boundaries); an odd
-// last element is taken by thread 0 of CTA 0.
 __global__ void k_scale_rsqrt(long long n, const double* __restrict__ x,
                               const double* __restrict__ nrm2, double* __restrict__ y,
                               float* __restrict__ y32) {
   double a = 1.0 / sqrt(*nrm2);
-  const long long n2 = n >> 1;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const double2* x2 = reinterpret_cast<const double2*>(x);
-  double2* yv = reinterpret_cast<double2*>(y);
-  float2* y32v = reinterpret_cast<float2*>(y32);
-  for (long long e = tid; e < n2; e += stride) {
-    double2 v = x2[e];
-    v.x *= a;
-    v.y *= a;
-    yv[e] = v;
-    if (y32) y32v[e] = make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
-  }
-  if ((n & 1) && tid == 0) {
-    double v = x[n - 1] * a;
-    y[n - 1] = v;
-    if (y32) y32[n - 1] = __double2float_rn(v);
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+    double v = x[e] * a;
+    y[e] = v;
+    if (y32) y32[e] = __double2float_rn(v);
   }
 }
 
@@ -167,45 +153,25 @@ void launch_multiaxpy(long long n, const double* V, long long ldv, const double*
 
 // One modified Gram-Schmidt step fused with the next one's dot product:
 // w -= h_prev * v_prev (h_prev read from device memory), then the partial of
-// v_next . w (or w . w).  Elements move in 16-byte pairs (the basis vectors
-// start on 256-byte boundaries; an odd last element is taken by thread 0 of
-// CTA 0).  The basis vectors stream through with evict-first loads; w (one
-// vector, 67 MB at 128^3) is left to the L2.  The CTA that finishes last sums
-// the CTA partials in index order, so the result does not depend on which CTA
-// that is.
+// v_next . w (or w . w).  The basis vectors stream through with evict-first
+// loads; w (one vector, 67 MB at 128^3) is left to the L2.  The CTA that
+// finishes last sums the CTA partials in index order, so the result does not
+// depend on which CTA that is.
 __global__ void __launch_bounds__(kRedThreads) k_mgs_sweep(
     long long n, const double* __restrict__ vp, const double* __restrict__ hp,
     const double* __restrict__ vn, double* __restrict__ w, double* __restrict__ partial,
     unsigned* counter, double* out) {
   double h = vp ? -__ldg(hp) : 0.0;
   double acc = 0.0;
-  const long long n2 = n >> 1;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double2* w2 = reinterpret_cast<double2*>(w);
-  const double2* vp2 = reinterpret_cast<const double2*>(vp);
-  const double2* vn2 = reinterpret_cast<const double2*>(vn);
-#pragma unroll 2
-  for (long long e = tid; e < n2; e += stride) {
-    double2 we = w2[e];
-    if (vp) {
-      double2 a = ld_stream(vp2 + e);
-      we.x = fma(h, a.x, we.x);
-      we.y = fma(h, a.y, we.y);
-      w2[e] = we;
-    }
-    double2 o = vn ? ld_stream(vn2 + e) : we;
-    acc = fma(o.x, we.x, acc);
-    acc = fma(o.y, we.y, acc);
-  }
-  if ((n & 1) && tid == 0) {
-    long long e = n - 1;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
     double we = w[e];
     if (vp) {
-      we = fma(h, vp[e], we);
+      we = fma(h, __ldcs(vp + e), we);
       w[e] = we;
     }
-    acc = fma(vn ? vn[e] : we, we, acc);
+    double o = vn ? __ldcs(vn + e) : we;
+    acc = fma(o, we, acc);
   }
   __shared__ double red[kRedThreads / 32];
   __shared__ bool last;

@@ -26,7 +26,6 @@ int multiaxpy_norm(long long n, const double* V, long long ldv, int nv, const do
 int reduce_partials(const double* partial, int nout, double* out, cudaStream_t st);
 // y = x * (1/sqrt(*nrm2)) with *nrm2 a device scalar; y32 (optional)
 // receives the same vector rounded to FP32 (input of the FP32 apply).
-// x, y and y32 start on 16-byte boundaries.
 int scale_rsqrt(long long n, const double* x, const double* nrm2, double* y, cudaStream_t st,
                 float* y32 = nullptr);
 // r = b - ax, partial norms of r
@@ -34,7 +33,6 @@ int residual_norm(long long n, const double* b, const double* ax, double* r, dou
                   cudaStream_t st);
 
 // One modified Gram-Schmidt sweep over w: if vp != null, w -= (*hp) * vp;
-// (vp, vn and w start on 16-byte boundaries)
 // then *out = vn . w (or w . w when vn == null), the CTA partials summed in a
 // fixed order by the last CTA to finish (counter returns to 0 afterwards).
 int mgs_sweep(long long n, const double* vp, const double* hp, const double* vn, double* w,

@@ -122,7 +122,8 @@ extern "C" const char* bilu_status_string(int s) {
     case BILU_ERR_CUDA: return "CUDA error";
     case BILU_ERR_NOT_CONVERGED: return "not converged";
     case BILU_ERR_WORKSPACE: return "workspace too small";
-    case BILU_ERR_UNSUPPORTED: return "unsupported block size or precision";
+    case BILU_ERR_UNSUPPORTED: return "unsupported block size, precision or file kind";
+    case BILU_ERR_IO: return "file missing, unreadable, malformed or corrupt";
     default: return "unknown status";
   }
 }

@@ -35,6 +35,14 @@ size_t syncfree_ws(int nb);
 int diag_positions(int nb, const int* row, const int* col, int* diag, int* h_bad, Carver& ws,
                    cudaStream_t st);
 size_t level_sched_ws(int nb, long long nnzb);
+size_t levels_ws(int nb, long long ndeps);
+int level_analysis(int nb, long long nnzb, const int* row, const int* col, const int* diag,
+                   int lower, int* order, int* lvl, int* nlev_d, int* h_nlev, Carver& ws,
+                   cudaStream_t st);
+int sptrsv_levels_async(int nb, int bs, const int* row, const int* col, const int* diag,
+                        const int* order, const int* lvl, const int* nlev_d, const double* val,
+                        int lower, int unit, const double* b, double* x, unsigned* words,
+                        cudaStream_t st);
 int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, const int* diag,
                double* val, int* h_zp, Carver& ws, cudaStream_t st);
 int dinv_impl(int nb, int bs, const int* row, const int* col, const double* val, int lower,
@@ -55,7 +63,7 @@ int isai_apply_impl(int nb, int bs, int prec, const int* Lrow, const int* Lcol, 
                     void* tmp, double* x, cudaStream_t st);
 int isai_apply_f32_staged(int nb, int bs, const int* Lrow, const int* Lcol, const float* Lval,
                           const int* Urow, const int* Ucol, const float* Uval, const float* b32,
-                          float* tmp, double* x, cudaStream_t st);
+                          float* tmp, double* x, cudaStream_t st, float* x32 = nullptr);
 
 namespace {
 
@@ -75,13 +83,21 @@ struct bilu_ctx {
   int *Lrow = nullptr, *Lcol = nullptr, *Urow = nullptr, *Ucol = nullptr;
   double *Lval = nullptr, *Uval = nullptr;
   float *Lval32 = nullptr, *Uval32 = nullptr;
+  float* Aval32 = nullptr;  // FP32 copy of A for the Arnoldi products (BILU_FP32_INNER)
   int nnzL = 0, nnzU = 0;
   bool ready = false;
+  // exact BILU(0) apply (BILU_ILU): level analyses of the lower and upper
+  // DAGs, and the barrier / error words of the launch-only solves
+  int *ordL = nullptr, *lvlL = nullptr, *nlevL = nullptr;
+  int *ordU = nullptr, *lvlU = nullptr, *nlevU = nullptr;
+  unsigned* ilu_words = nullptr;
+  int nlev_host[2] = {0, 0};
   // solver buffers
   int m_alloc = 0;
   long long ldv = 0;  // stride of the basis vectors in V and Z (n rounded up to 32)
   double *V = nullptr, *Z = nullptr, *w = nullptr, *r = nullptr, *tmp = nullptr;
   float* v32 = nullptr;  // FP32 copy of the newest basis vector (mixed apply input)
+  float* z32 = nullptr;  // FP32 copy of z_j (input of the FP32 operator product)
   double *partial = nullptr, *dscal = nullptr, *dcoef = nullptr;
   double* hpin = nullptr;  // pinned host mirror of dscal
   cudaEvent_t ev = nullptr;
@@ -94,11 +110,16 @@ struct bilu_ctx {
     Arow = Acol = diag = Lrow = Lcol = Urow = Ucol = nullptr;
     Aval = LU = Lval = Uval = nullptr;
     Lval32 = Uval32 = nullptr;
+    Aval32 = nullptr;
+    ordL = lvlL = nlevL = ordU = lvlU = nlevU = nullptr;
+    ilu_words = nullptr;
     ready = false;
   }
   void free_solver() {
     cudaFree(V); cudaFree(Z); cudaFree(w); cudaFree(r); cudaFree(tmp); cudaFree(v32);
+    cudaFree(z32);
     v32 = nullptr;
+    z32 = nullptr;
     cudaFree(partial); cudaFree(dscal); cudaFree(dcoef); cudaFree(counter);
     counter = nullptr;
     if (hpin) cudaFreeHost(hpin);
@@ -252,6 +273,7 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   BILU_TRY_CUDA(cudaMemcpyAsync(c->LU, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
   // scratch shared by every step
   size_t wsb = std::max({isai_pattern_ws(nb, nnzb), level_sched_ws(nb, nnzb), pairs_ws(nnzb + nb),
+                         levels_ws(nb, nnzb),
                          scan_ws_bytes(nnzb + nb + 1)}) + (1 << 16);
   void* wsp = nullptr;
   BILU_TRY(c->alloc((char**)&wsp, wsb));
@@ -271,12 +293,33 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   double t_pat = 0, t_isai = 0;
   BILU_TRY(build_isai_side(c, 1, ws, &c->Lrow, &c->Lcol, &c->Lval, &c->nnzL, &t_pat, &t_isai));
   BILU_TRY(build_isai_side(c, 0, ws, &c->Urow, &c->Ucol, &c->Uval, &c->nnzU, &t_pat, &t_isai));
-  if (prec_mask & (1 << BILU_FP32)) {
+  if (prec_mask & (1 << BILU_FP32_INNER)) {
+    BILU_TRY(c->alloc(&c->Aval32, (size_t)nnzb * bs2));
+    BILU_TRY(bilu_convert_f64_to_f32((size_t)nnzb * bs2, c->Aval, c->Aval32, st));
+  }
+  if (prec_mask & ((1 << BILU_FP32) | (1 << BILU_FP32_INNER))) {
     BILU_TRY(c->alloc(&c->Lval32, (size_t)c->nnzL * bs2));
     BILU_TRY(c->alloc(&c->Uval32, (size_t)c->nnzU * bs2));
     BILU_TRY(bilu_convert_f64_to_f32((size_t)c->nnzL * bs2, c->Lval, c->Lval32, st));
     BILU_TRY(bilu_convert_f64_to_f32((size_t)c->nnzU * bs2, c->Uval, c->Uval32, st));
   }
+  if (prec_mask & (1 << BILU_ILU)) {
+    // level analyses of both triangles of the packed factor for the exact
+    // BILU(0) apply (two level-scheduled triangular solves per apply)
+    for (int lower = 1; lower >= 0; --lower) {
+      int **ord = lower ? &c->ordL : &c->ordU, **lvl = lower ? &c->lvlL : &c->lvlU,
+          **nl = lower ? &c->nlevL : &c->nlevU;
+      BILU_TRY(c->alloc(ord, (size_t)nb + 1));
+      BILU_TRY(c->alloc(lvl, (size_t)nb + 2));
+      BILU_TRY(c->alloc(nl, 2));
+      Carver w2 = ws;
+      BILU_TRY(level_analysis(nb, nnzb, c->Arow, c->Acol, c->diag, lower, *ord, *lvl, *nl,
+                              &c->nlev_host[lower ? 0 : 1], w2, st));
+    }
+    BILU_TRY(c->alloc(&c->ilu_words, 4));
+    BILU_TRY_CUDA(cudaMemsetAsync(c->ilu_words, 0, sizeof(unsigned) * 4, st));
+  }
+
   tm.mark(3);
   double t_factor = tm.ms(1, 2), t_total = tm.ms(0, 3);
   BILU_TRY_CUDA(cudaStreamSynchronize(st));
@@ -326,6 +369,7 @@ int ensure_solver(bilu_ctx* c, int m) {
   BILU_TRY_CUDA(cudaMalloc(&c->r, sizeof(double) * n));
   BILU_TRY_CUDA(cudaMalloc(&c->tmp, sizeof(double) * n));
   BILU_TRY_CUDA(cudaMalloc(&c->v32, sizeof(float) * n));
+  BILU_TRY_CUDA(cudaMalloc(&c->z32, sizeof(float) * n));
   BILU_TRY_CUDA(cudaMalloc(&c->partial, sizeof(double) * kRedCTAs * kPartStride));
   BILU_TRY_CUDA(cudaMalloc(&c->dscal, sizeof(double) * 6 * kPartStride));
   BILU_TRY_CUDA(cudaMalloc(&c->dcoef, sizeof(double) * kPartStride));
@@ -348,15 +392,23 @@ int norm2(bilu_ctx* c, const double* v, double* dslot, double* host) {
 }
 
 int apply_prec(bilu_ctx* c, int prec, const double* v, double* z) {
+  if (prec == BILU_ILU) {
+    // z = U^-1 (L^-1 v): unit-lower then upper solve on the packed factor
+    BILU_TRY(sptrsv_levels_async(c->nb, c->bs, c->Arow, c->Acol, c->diag, c->ordL, c->lvlL,
+                                 c->nlevL, c->LU, 1, 1, v, c->tmp, c->ilu_words, c->st));
+    return sptrsv_levels_async(c->nb, c->bs, c->Arow, c->Acol, c->diag, c->ordU, c->lvlU,
+                               c->nlevU, c->LU, 0, 0, c->tmp, z, c->ilu_words, c->st);
+  }
   if (prec < 0) {
     BILU_TRY_CUDA(cudaMemcpyAsync(z, v, sizeof(double) * c->n, cudaMemcpyDeviceToDevice, c->st));
     return BILU_OK;
   }
-  if (prec == BILU_FP32) {
+  if (prec == BILU_FP32 || prec == BILU_FP32_INNER) {
     // v32 (written with v by the normalisation kernel) is the FP32 copy of v
     if (!c->Lval32 || !c->Uval32) return BILU_ERR_ARG;
     return isai_apply_f32_staged(c->nb, c->bs, c->Lrow, c->Lcol, c->Lval32, c->Urow, c->Ucol,
-                                 c->Uval32, c->v32, (float*)c->tmp, z, c->st);
+                                 c->Uval32, c->v32, (float*)c->tmp, z, c->st,
+                                 prec == BILU_FP32_INNER ? c->z32 : nullptr);
   }
   return isai_apply_impl(c->nb, c->bs, prec, c->Lrow, c->Lcol, c->Lval, c->Urow, c->Ucol,
                          c->Uval, v, c->tmp, z, c->st);
@@ -371,6 +423,9 @@ int arnoldi_front(bilu_ctx* c, int prec, int j) {
   size_t ld = (size_t)c->ldv;
   double* zj = c->Z + ld * j;
   BILU_TRY(apply_prec(c, prec, c->V + ld * j, zj));
+  if (prec == BILU_FP32_INNER)  // FP32-stored A and z (written by the apply), FP64 w
+    return spmv_any(c->nb, c->bs, BILU_FP32, c->Arow, c->Acol, c->Aval32, c->z32, 1, c->w, 0,
+                    c->st);
   return spmv_any(c->nb, c->bs, BILU_FP64, c->Arow, c->Acol, c->Aval, zj, 0, c->w, 0, c->st);
 }
 
@@ -392,7 +447,7 @@ int arnoldi_back(bilu_ctx* c, int j, int prec) {
   BILU_TRY(mgs_sweep(n, V + ld * j, s + j, nullptr, c->w, c->partial, c->counter,
                      s + kPartStride, st));
   BILU_TRY(scale_rsqrt(n, c->w, s + kPartStride, c->V + ld * (j + 1), st,
-                       prec == BILU_FP32 ? c->v32 : nullptr));
+                       (prec == BILU_FP32 || prec == BILU_FP32_INNER) ? c->v32 : nullptr));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->hpin, s, sizeof(double) * (kPartStride + 1),
                                 cudaMemcpyDeviceToHost, st));
   return BILU_OK;
@@ -405,9 +460,15 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
                               double* h_hist) {
   if (!c || !c->ready || !d_b || !d_x || restart < 1 || restart > kMaxVec - 1 || maxit < 0)
     return BILU_ERR_ARG;
-  if (prec != -1 && prec != BILU_FP64 && prec != BILU_FP32) return BILU_ERR_ARG;
+  if (prec != -1 && prec != BILU_FP64 && prec != BILU_FP32 && prec != BILU_ILU &&
+      prec != BILU_FP32_INNER)
+    return BILU_ERR_ARG;
+  if ((prec == BILU_FP32 && !c->Lval32) || (prec == BILU_ILU && !c->ilu_words) ||
+      (prec == BILU_FP32_INNER && !c->Aval32))
+    return BILU_ERR_ARG;  // the setup did not build this preconditioner
   BILU_TRY(ensure_solver(c, restart));
   cudaStream_t st = c->st;
+  if (prec == BILU_ILU) BILU_TRY_CUDA(cudaMemsetAsync(c->ilu_words, 0, sizeof(unsigned) * 4, st));
   const int m = restart;
   const long long n = c->n;
   double* s = c->dscal;
@@ -432,7 +493,7 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
   while (status != BILU_OK && total < maxit) {
     // V_0 = r / beta (beta^2 sits in s[5*kPartStride])
     BILU_TRY(scale_rsqrt(n, c->r, s + 5 * kPartStride, c->V, st,
-                         prec == BILU_FP32 ? c->v32 : nullptr));
+                         (prec == BILU_FP32 || prec == BILU_FP32_INNER) ? c->v32 : nullptr));
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int jlast = -1;
@@ -483,7 +544,12 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
     BILU_TRY(residual_norm(n, d_b, c->w, c->r, c->partial, st));
     BILU_TRY(reduce_partials(c->partial, 1, s + 5 * kPartStride, st));
     BILU_TRY_CUDA(cudaMemcpyAsync(&rr, s + 5 * kPartStride, sizeof(double), cudaMemcpyDeviceToHost, st));
+    int ilu_err = 0;
+    if (prec == BILU_ILU)
+      BILU_TRY_CUDA(cudaMemcpyAsync(&ilu_err, c->ilu_words + 2, sizeof(int),
+                                    cudaMemcpyDeviceToHost, st));
     BILU_TRY_CUDA(cudaStreamSynchronize(st));
+    if (ilu_err != 0) return ilu_err;  // a triangular-solve barrier timed out
     beta = std::sqrt(rr);
     res = beta / bnorm;
     if (res <= tol) status = BILU_OK;
@@ -498,6 +564,57 @@ extern "C" int bilu_ctx_stats(bilu_ctx* c, long long* h_out) {
   if (!c || !h_out) return BILU_ERR_ARG;
   h_out[0] = c->steps;
   h_out[1] = c->restarts;
+  return BILU_OK;
+}
+
+// Preconditioner switch by measurement: `cycles` restart cycles of the solve
+// from x0 = 0 with every choice in `mask` (bits 1 << BILU_FP64 / BILU_FP32 /
+// BILU_ILU / BILU_FP32_INNER that the setup built), timed with events on the
+// handle's stream; the score is the residual reduction per second (decimal
+// digits / s).  Returns the best choice in *h_choice and the scores in
+// h_rate[4] (0 for choices not tried).
+extern "C" int bilu_ctx_select(bilu_ctx* c, const double* d_b, int restart, int cycles, int mask,
+                               int* h_choice, double* h_rate) {
+  if (!c || !c->ready || !d_b || !h_choice || cycles < 1 || restart < 1) return BILU_ERR_ARG;
+  double* x = nullptr;
+  BILU_TRY_CUDA(cudaMalloc(&x, sizeof(double) * c->n));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = -1, rc = BILU_OK;
+  double best_rate = -1.0;
+  for (int p = 0; p < 4 && rc == BILU_OK; ++p) {
+    if (h_rate) h_rate[p] = 0.0;
+    if (!(mask & (1 << p))) continue;
+    if ((p == BILU_FP32 && !c->Lval32) || (p == BILU_ILU && !c->ilu_words) ||
+        (p == BILU_FP32_INNER && !c->Aval32))
+      continue;
+    int it = 0;
+    double rr = 1.0;
+    cudaEventRecord(e0, c->st);
+    int st = bilu_ctx_solve(c, p, d_b, x, restart, 0.0, restart * cycles, &it, &rr, nullptr);
+    cudaEventRecord(e1, c->st);
+    cudaEventSynchronize(e1);
+    if (st != BILU_OK && st != BILU_ERR_NOT_CONVERGED) {
+      rc = st;
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    double digits = rr > 0.0 ? -std::log10(rr) : 16.0;
+    double rate = ms > 0.f ? digits / (ms * 1e-3) : 0.0;
+    if (h_rate) h_rate[p] = rate;
+    if (rate > best_rate) {
+      best_rate = rate;
+      best = p;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(x);
+  if (rc != BILU_OK) return rc;
+  if (best < 0) return BILU_ERR_ARG;
+  *h_choice = best;
   return BILU_OK;
 }
 

@@ -117,6 +117,73 @@ __global__ void __launch_bounds__(256) k_dinv(int nb, const int* __restrict__ ro
   for (int j = 0; j < BS; ++j) Dinv[((long long)k * BS + i) * BS + j] = Iv[j];
 }
 
+// Thread per block row (bs 4 and 5: the 2*bs*bs work values fit in
+// registers): the same Gauss-Jordan steps as the team version above, in the
+// same order, without the redundant per-lane divisions and shuffles.
+template <int BS>
+__device__ __forceinline__ bool gauss_jordan_t(double (&M)[BS][BS], double (&Iv)[BS][BS]) {
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < BS; ++k) {
+    double piv = M[k][k];
+    ok = ok && fabs(piv) >= 1e-14;
+    double invp = 1.0 / piv;
+#pragma unroll
+    for (int j = 0; j < BS; ++j) {
+      M[k][j] *= invp;
+      Iv[k][j] *= invp;
+    }
+#pragma unroll
+    for (int i = 0; i < BS; ++i) {
+      if (i == k) continue;
+      double f = M[i][k];
+#pragma unroll
+      for (int j = 0; j < BS; ++j) {
+        M[i][j] -= f * M[k][j];
+        Iv[i][j] -= f * Iv[k][j];
+      }
+    }
+  }
+  return ok;
+}
+
+template <int BS>
+__global__ void __launch_bounds__(128) k_dinv_t(int nb, const int* __restrict__ row,
+                                                const int* __restrict__ col,
+                                                const double* __restrict__ val, int lower,
+                                                double* __restrict__ Dinv, int* fail) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nb) return;
+  int pos = find_in_row(col, __ldg(row + k), __ldg(row + k + 1), k);
+  double B[BS][BS], M[BS][BS], Iv[BS][BS];
+#pragma unroll
+  for (int i = 0; i < BS; ++i)
+#pragma unroll
+    for (int j = 0; j < BS; ++j) {
+      double v = pos >= 0 ? __ldg(val + ((long long)pos * BS + i) * BS + j) : 0.0;
+      if (lower ? (j > i) : (j < i)) v = 0.0;
+      if (lower && j == i) v = 1.0;
+      B[i][j] = v;
+      M[i][j] = v;
+      Iv[i][j] = (j == i) ? 1.0 : 0.0;
+    }
+  if (!gauss_jordan_t<BS>(M, Iv)) {
+#pragma unroll
+    for (int i = 0; i < BS; ++i)
+#pragma unroll
+      for (int j = 0; j < BS; ++j) {
+        M[i][j] = B[i][j] + ((j == i) ? 1e-12 : 0.0);
+        Iv[i][j] = (j == i) ? 1.0 : 0.0;
+      }
+    if (!gauss_jordan_t<BS>(M, Iv)) atomicMin(fail, k);
+  }
+  double* out = Dinv + (long long)k * BS * BS;
+#pragma unroll
+  for (int i = 0; i < BS; ++i)
+#pragma unroll
+    for (int j = 0; j < BS; ++j) out[i * BS + j] = Iv[i][j];
+}
+
 // ---------------------------------------------------------------- pairs
 // Warp per ISAI column j; lane per entry idx.  lower: pairs p < idx with
 // A(t, S_j[p]) stored, ascending p (the reference's merge order); upper:
@@ -269,9 +336,13 @@ template <int BS>
 int launch_dinv(int nb, const int* row, const int* col, const double* val, int lower,
                 double* Dinv, int* d_fail, cudaStream_t st) {
   if (nb == 0) return BILU_OK;
-  constexpr int G = 32 / BS;
-  long long warps = (nb + G - 1) / G;
-  k_dinv<BS><<<ceil_div(warps, 8), 256, 0, st>>>(nb, row, col, val, lower, Dinv, d_fail);
+  if constexpr (BS <= 5) {
+    k_dinv_t<BS><<<ceil_div(nb, 128), 128, 0, st>>>(nb, row, col, val, lower, Dinv, d_fail);
+  } else {
+    constexpr int G = 32 / BS;
+    long long warps = (nb + G - 1) / G;
+    k_dinv<BS><<<ceil_div(warps, 8), 256, 0, st>>>(nb, row, col, val, lower, Dinv, d_fail);
+  }
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }

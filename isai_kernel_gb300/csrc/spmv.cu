@@ -101,7 +101,8 @@ __global__ void __launch_bounds__(256, sizeof(VT) == 4 ? 4 : 2) k_bsr_spmv(int m
                                                      const int* __restrict__ col,
                                                      const VT* __restrict__ val,
                                                      const XT* __restrict__ x,
-                                                     YT* __restrict__ y) {
+                                                     YT* __restrict__ y,
+                                                     float* __restrict__ y32) {
   constexpr int G = 32 / BS;  // lane groups per warp
   constexpr int U = sizeof(VT) == 4 ? 4 : 2;
   int lane = threadIdx.x & 31;
@@ -160,12 +161,15 @@ __global__ void __launch_bounds__(256, sizeof(VT) == 4 ? 4 : 2) k_bsr_spmv(int m
   }
 #pragma unroll
   for (int q = 0; q < RPG; ++q)
-    if (base + q < mb) y[(base + q) * BS + r] = (YT)acc[q];
+    if (base + q < mb) {
+      y[(base + q) * BS + r] = (YT)acc[q];
+      if (y32) y32[(base + q) * BS + r] = (float)acc[q];  // optional FP32 copy
+    }
 }
 
 template <int BS, class VT, class XT, class YT>
 int launch_spmv(int mb, const int* row, const int* col, const VT* val, const XT* x, YT* y,
-                cudaStream_t st) {
+                cudaStream_t st, float* y32 = nullptr) {
   using AccT = VT;
   if (mb == 0) return BILU_OK;
   constexpr int G = 32 / BS;
@@ -173,7 +177,7 @@ int launch_spmv(int mb, const int* row, const int* col, const VT* val, const XT*
   long long groups = (mb + RPG - 1) / RPG;
   long long warps = (groups + G - 1) / G;
   unsigned grid = ceil_div(warps, 8);
-  k_bsr_spmv<BS, VT, XT, YT, AccT, RPG><<<grid, 256, 0, st>>>(mb, row, col, val, x, y);
+  k_bsr_spmv<BS, VT, XT, YT, AccT, RPG><<<grid, 256, 0, st>>>(mb, row, col, val, x, y, y32);
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }
@@ -264,6 +268,13 @@ int spmv_f32(int mb, const int* row, const int* col, const float* val, const voi
                                                 st);
 }
 
+// FP32 values and x, FP64 y plus its FP32 copy y32
+template <int BS>
+int spmv_f32_dual(int mb, const int* row, const int* col, const float* val, const float* x,
+                  double* y, float* y32, cudaStream_t st) {
+  return launch_spmv<BS, float, float, double>(mb, row, col, val, x, y, st, y32);
+}
+
 template <int BS>
 int spmm_f64(int mb, int k, const int* row, const int* col, const double* val, const double* X,
              double* Y, cudaStream_t st) {
@@ -317,8 +328,10 @@ int isai_apply_impl(int nb, int bs, int prec, const int* Lrow, const int* Lcol, 
 // kernel that produced the FP64 basis vector).
 int isai_apply_f32_staged(int nb, int bs, const int* Lrow, const int* Lcol, const float* Lval,
                           const int* Urow, const int* Ucol, const float* Uval, const float* b32,
-                          float* tmp, double* x, cudaStream_t st) {
+                          float* tmp, double* x, cudaStream_t st, float* x32) {
   BILU_TRY(spmv_any(nb, bs, BILU_FP32, Lrow, Lcol, Lval, b32, 1, tmp, 1, st));
+  if (x32)  // x also in FP32 (input of an FP32 operator product)
+    return BILU_DISPATCH_BS(bs, spmv_f32_dual, nb, Urow, Ucol, Uval, tmp, x, x32, st);
   return spmv_any(nb, bs, BILU_FP32, Urow, Ucol, Uval, tmp, 1, x, 0, st);
 }
 

@@ -278,6 +278,133 @@ __global__ void __launch_bounds__(128) k_bilu0(int nb, const int* __restrict__ r
 // in reverse ticket order.  UNIT: the diagonal block contributes its strict
 // triangle and no division (unit diagonal).  Lane (slot, r) accumulates row
 // r of blocks slot, slot+G, ...; slots are summed by shuffles.
+// Structural part of one block row of a triangular solve: everything that
+// does not depend on x (the row, its diagonal position, the first pass of
+// blocks with their column indices).  The level schedule loads it for the
+// next level before the barrier, so only the x reads follow the barrier.
+template <int BS>
+struct RowPre {
+  int I, dI, ps, pe;  // warp-uniform; I < 0: no row
+  int K;              // this lane's block column in the first pass, or -1
+  double a[BS];       // row r of that block
+  double dq[BS];      // lanes q < BS: row q of the diagonal block
+  double bq, rq;      // lanes q < BS: b_q and 1 / D_qq (1 when UNIT)
+};
+
+template <int BS, bool LOWER, bool UNIT>
+__device__ __forceinline__ void sptrsv_prefetch(int I, const int* __restrict__ row,
+                                                const int* __restrict__ col,
+                                                const int* __restrict__ diag,
+                                                const double* __restrict__ val,
+                                                const double* __restrict__ b, RowPre<BS>& p) {
+  constexpr int G = 32 / BS;
+  const int lane = threadIdx.x & 31, slot = lane / BS, r = lane - slot * BS;
+  p.I = I;
+  p.K = -1;
+  if (I < 0) return;
+  int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
+  p.dI = dI;
+  p.ps = LOWER ? rs : dI + 1;
+  p.pe = LOWER ? dI : re;
+  int q = p.ps + slot;
+  if (slot < G && q < p.pe) {
+    p.K = __ldg(col + q);
+    const double* blk = val + (long long)q * BS * BS + r * BS;
+#pragma unroll
+    for (int c = 0; c < BS; ++c) p.a[c] = __ldg(blk + c);
+  }
+  // the diagonal block row, b and the pivot reciprocal do not depend on x:
+  // the division (a long FP64 sequence on this GPU) leaves the critical path
+  p.bq = 0.0;
+  p.rq = 1.0;
+  if (lane < BS) {
+    const double* D = val + (long long)dI * BS * BS + lane * BS;
+#pragma unroll
+    for (int c = 0; c < BS; ++c) p.dq[c] = __ldg(D + c);
+    p.bq = __ldg(b + (long long)I * BS + lane);
+#pragma unroll
+    for (int c = 0; c < BS; ++c)
+      if (c == lane && !UNIT) p.rq = 1.0 / p.dq[c];
+  } else {
+#pragma unroll
+    for (int c = 0; c < BS; ++c) p.dq[c] = 1.0;
+  }
+}
+
+// The x-dependent part of the row, one warp.  Lane (slot, r) accumulates
+// row r of blocks slot, slot+G, ...; slots are summed by shuffles.  The
+// diagonal block is solved by substitution spread over lanes 0..BS-1 (lane
+// q holds row q of the block): step c finalises x_c on lane c (times the
+// pivot reciprocal unless UNIT) and broadcasts it; LOWER runs c ascending,
+// otherwise descending, so every x_q subtracts its terms in the oracle's
+// order.  WAIT: the rows read may still be in progress (sync-free
+// schedule); PUBLISH: lane 0 stores x_I and releases the row's flag.
+// Returns false if the launch aborted.
+template <int BS, bool LOWER, bool UNIT, bool WAIT, bool PUBLISH>
+__device__ __forceinline__ bool sptrsv_finish(const RowPre<BS>& p, const int* __restrict__ col,
+                                              const double* __restrict__ val, double* x,
+                                              const SyncState& ss) {
+  constexpr int BS2 = BS * BS;
+  constexpr int G = 32 / BS;
+  const int lane = threadIdx.x & 31, slot = lane / BS, r = lane - slot * BS;
+  double s = 0.0;
+  bool ok = true;
+  if (p.K >= 0) {
+    if (WAIT) ok = lane_wait(ss.flags + p.K, ss.err, ss.spin);
+    if (ok) {
+      const double* xk = x + (long long)p.K * BS;
+#pragma unroll
+      for (int c = 0; c < BS; ++c) s = fma(p.a[c], __ldcg(xk + c), s);
+    }
+  }
+  for (int p0 = p.ps + G; p0 < p.pe; p0 += G) {  // rows with more than G blocks
+    int q = p0 + slot;
+    if (slot < G && q < p.pe && ok) {
+      int K = __ldg(col + q);
+      if (WAIT) ok = lane_wait(ss.flags + K, ss.err, ss.spin);
+      if (ok) {
+        const double* blk = val + (long long)q * BS2 + r * BS;
+        const double* xk = x + (long long)K * BS;
+#pragma unroll
+        for (int c = 0; c < BS; ++c) s = fma(__ldg(blk + c), __ldcg(xk + c), s);
+      }
+    }
+  }
+  if (WAIT && __any_sync(FULL, !ok)) return false;
+  double tot = 0.0;
+#pragma unroll
+  for (int g = 0; g < G; ++g) tot += __shfl_sync(FULL, s, g * BS + r);
+  double v = p.bq - tot, xv = 0.0;
+#pragma unroll
+  for (int k = 0; k < BS; ++k) {
+    const int c = LOWER ? k : BS - 1 - k;
+    double mine = (UNIT || lane != c) ? v : v * p.rq;
+    double xc = __shfl_sync(FULL, mine, c);
+    if (lane == c) xv = xc;
+    if (LOWER ? (lane > c && lane < BS) : (lane < c)) v -= p.dq[c] * xc;
+  }
+  if (PUBLISH) {
+    // lane 0 stores the row and releases its flag (st.release orders its own
+    // stores before the flag)
+    double xs[BS];
+#pragma unroll
+    for (int c = 0; c < BS; ++c) xs[c] = __shfl_sync(FULL, xv, c);
+    if (lane == 0) {
+#pragma unroll
+      for (int c = 0; c < BS; ++c) x[(long long)p.I * BS + c] = xs[c];
+      if (p.I != ss.withhold) st_release(ss.flags + p.I, 1);
+    }
+  } else if (lane < BS) {
+    x[(long long)p.I * BS + lane] = xv;
+  }
+  return true;
+}
+
+// Block-row solve on a packed factor.  LOWER: x_I = b_I - sum_{K<I} B_IK x_K
+// then the diagonal block's lower part; otherwise the upper part and J > I
+// in reverse ticket order.  UNIT: the diagonal block contributes its strict
+// triangle and no division (unit diagonal).  Lane (slot, r) accumulates row
+// r of blocks slot, slot+G, ...; slots are summed by shuffles.
 // One block row of the solve, executed by one warp.  WAIT: the rows it
 // reads may still be in progress and are waited for through their flags;
 // otherwise they are final (level schedule).  x_I is stored by lane 0.
@@ -363,11 +490,9 @@ __global__ void __launch_bounds__(128) k_sptrsv(int nb, const int* __restrict__ 
     t = __shfl_sync(FULL, t, 0);
     if (t >= nb) return;
     int I = ss.order ? __ldg(ss.order + t) : (LOWER ? t : nb - 1 - t);
-    if (!sptrsv_row<BS, LOWER, UNIT, true>(I, row, col, diag, val, b, x, ss)) return;
-    if (lane == 0) {
-      // st.release orders lane 0's stores of x_I before the flag
-      if (I != ss.withhold) st_release(ss.flags + I, 1);
-    }
+    RowPre<BS> p;
+    sptrsv_prefetch<BS, LOWER, UNIT>(I, row, col, diag, val, b, p);
+    if (!sptrsv_finish<BS, LOWER, UNIT, true, true>(p, col, val, x, ss)) return;
     __syncwarp();
   }
 }
@@ -546,21 +671,42 @@ __global__ void __launch_bounds__(256) k_bfs_levels(int nb, const int* __restric
 
 constexpr int kLvlThreads = 256;
 
+// Level-scheduled solve.  Each warp keeps the structural part of its first
+// row of the next level in registers, loaded before the barrier; after the
+// barrier only the x reads of that row remain.
 template <int BS, bool LOWER, bool UNIT>
-__global__ void __launch_bounds__(kLvlThreads) k_sptrsv_levels(
+__global__ void __launch_bounds__(kLvlThreads, BS == 8 ? 2 : (BS == 5 ? 3 : 4)) k_sptrsv_levels(
     const int* __restrict__ row, const int* __restrict__ col, const int* __restrict__ diag,
     const double* __restrict__ val, const double* __restrict__ b, double* x,
     const int* __restrict__ order, const int* __restrict__ lvl_ptr, const int* __restrict__ nlev_p,
     SyncState ss, GridSync gs) {
-  unsigned gen = 0;
+  // generation at launch: no barrier completes before every CTA has read it,
+  // so consecutive launches need no reset of the barrier words
+  unsigned gen = threadIdx.x == 0 ? ld_relaxed_u(gs.gen) : 0u;
   const int warp = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int nw = (int)(((long long)gridDim.x * blockDim.x) >> 5);
   const int nlev = __ldg(nlev_p);
+  if (nlev <= 0) return;
+  RowPre<BS> pre;
+  {
+    int t = __ldg(lvl_ptr) + warp;
+    sptrsv_prefetch<BS, LOWER, UNIT>(t < __ldg(lvl_ptr + 1) ? __ldg(order + t) : -1, row, col,
+                                     diag, val, b, pre);
+  }
   for (int l = 0; l < nlev; ++l) {
     int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
-    for (int t = s + warp; t < e; t += nw)
-      sptrsv_row<BS, LOWER, UNIT, false>(__ldg(order + t), row, col, diag, val, b, x, ss);
-    if (l + 1 < nlev && !grid_sync(gs, gen, NoOp{})) return;
+    if (pre.I >= 0) sptrsv_finish<BS, LOWER, UNIT, false, false>(pre, col, val, x, ss);
+    for (int t = s + warp + nw; t < e; t += nw) {
+      RowPre<BS> q;
+      sptrsv_prefetch<BS, LOWER, UNIT>(__ldg(order + t), row, col, diag, val, b, q);
+      sptrsv_finish<BS, LOWER, UNIT, false, false>(q, col, val, x, ss);
+    }
+    if (l + 1 < nlev) {
+      int t = e + warp;
+      sptrsv_prefetch<BS, LOWER, UNIT>(t < __ldg(lvl_ptr + l + 2) ? __ldg(order + t) : -1, row,
+                                       col, diag, val, b, pre);
+      if (!grid_sync(gs, gen, NoOp{})) return;
+    }
   }
 }
 
@@ -569,7 +715,7 @@ __global__ void __launch_bounds__(kLvlThreads) k_bilu0_levels(
     const int* __restrict__ row, const int* __restrict__ col, const int* __restrict__ diag,
     double* val, const int* __restrict__ order, const int* __restrict__ lvl_ptr,
     const int* __restrict__ nlev_p, SyncState ss, GridSync gs) {
-  unsigned gen = 0;
+  unsigned gen = threadIdx.x == 0 ? ld_relaxed_u(gs.gen) : 0u;
   const int warp = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int nw = (int)(((long long)gridDim.x * blockDim.x) >> 5);
   const int nlev = __ldg(nlev_p);
@@ -914,6 +1060,30 @@ int sptrsv_level_impl(int nb, long long nnzb, int bs, const int* row, const int*
   }
   return sptrsv_levels(nb, bs, row, col, diag, order, lvl, nlev_d, val, lower, unit, b, x, ws,
                        st);
+}
+
+// Level analysis into caller-owned arrays (order[nb+1], lvl[nb+2], nlev[2]).
+int level_analysis(int nb, long long nnzb, const int* row, const int* col, const int* diag,
+                   int lower, int* order, int* lvl, int* nlev_d, int* h_nlev, Carver& ws,
+                   cudaStream_t st) {
+  return build_levels(nb, row, col, diag, lower, std::max(nnzb - nb, 0ll), order, lvl, nlev_d,
+                      h_nlev, ws, st);
+}
+
+// Launch-only level-scheduled solve for use inside a solver: no host
+// synchronisation.  words: [0] barrier count (0 between launches), [1]
+// barrier generation, [2] error word (0 or a bilu_status, read by the caller
+// later), [3] zero-pivot word.
+int sptrsv_levels_async(int nb, int bs, const int* row, const int* col, const int* diag,
+                        const int* order, const int* lvl, const int* nlev_d, const double* val,
+                        int lower, int unit, const double* b, double* x, unsigned* words,
+                        cudaStream_t st) {
+  if (nb == 0) return BILU_OK;
+  int* w = (int*)words;
+  SyncState ss{nullptr, nullptr, w + 2, w + 3, kSpinLimit, -1, nullptr};
+  GridSync gs{words, words + 1, w + 2, kSpinLimit};
+  return BILU_DISPATCH_BS(bs, launch_sptrsv_levels, nb, row, col, diag, val, lower, unit, b, x,
+                          order, lvl, nlev_d, 0, ss, gs, st);
 }
 
 }  // namespace bilu

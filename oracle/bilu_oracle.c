@@ -709,8 +709,14 @@ int orc_gmres(int nb, int bs, const int* Arow, const int* Acol,
   double *g = (double*)calloc((size_t)m + 1, sizeof(double)), *yv = (double*)calloc((size_t)m, sizeof(double));
   double* hcol = (double*)calloc((size_t)m + 1, sizeof(double));
   isai_apply_t P = {nb, bs, Lrow, Lcol, Urow, Ucol, Lval, Uval, NULL, NULL, NULL, NULL, NULL, NULL};
+  float* A32 = NULL;
   if (precond >= 1) P.y = (double*)malloc(sizeof(double) * n);
-  if (precond == 2) {
+  if (precond == 4) {
+    size_t na = (size_t)Arow[nb] * bs * bs;
+    A32 = (float*)malloc(sizeof(float) * na);
+    for (size_t i = 0; i < na; ++i) A32[i] = (float)Aval[i];
+  }
+  if (precond == 2 || precond == 4) {
     int nL = Lrow[nb], nU = Urow[nb];
     size_t bs2 = (size_t)bs * bs;
     P.Lval32 = (float*)malloc(sizeof(float) * nL * bs2);
@@ -739,8 +745,16 @@ int orc_gmres(int nb, int bs, const int* Arow, const int* Acol,
     for (int j = 0; j < m && total < maxit; ++j) {
       double* vj = V + n * (size_t)j;
       double* zj = Z + n * (size_t)j;
-      isai_apply(&P, precond, vj, zj, n);
-      orc_bcsr_spmv(nb, bs, Arow, Acol, Aval, zj, w);
+      isai_apply(&P, precond == 4 ? 2 : precond, vj, zj, n);
+      if (precond == 4) {
+        /* FP32-stored A in the Arnoldi product: z rounded to FP32, FP32
+         * accumulation, result widened to FP64 */
+        for (size_t i = 0; i < n; ++i) P.v32[i] = (float)zj[i];
+        orc_bcsr_spmv_f32(nb, bs, Arow, Acol, A32, P.v32, P.y32);
+        for (size_t i = 0; i < n; ++i) w[i] = (double)P.y32[i];
+      } else {
+        orc_bcsr_spmv(nb, bs, Arow, Acol, Aval, zj, w);
+      }
       /* modified Gram-Schmidt */
       for (int i = 0; i <= j; ++i) {
         const double* vi = V + n * (size_t)i;
@@ -797,5 +811,6 @@ int orc_gmres(int nb, int bs, const int* Arow, const int* Acol,
   if (relres) *relres = res;
   free(V); free(Z); free(w); free(r); free(H); free(cs); free(sn); free(g); free(yv); free(hcol);
   free(P.y); free(P.Lval32); free(P.Uval32); free(P.v32); free(P.y32); free(P.z32);
+  free(A32);
   return status;
 }

@@ -115,7 +115,9 @@ int orc_rel_errors_csr(int n, const int* row, const int* col, const double* val,
  * oracle that defines iteration counts.  precond: 0 none, 1 ISAI FP64
  * (z = M_U (M_L v)), 2 ISAI with FP32-stored factors and FP32 accumulation,
  * 3 exact BILU(0) (z = U^-1 L^-1 v by the two block triangular solves; the
- * packed factor is passed as Lrow/Lcol/Lval, U is unused).
+ * packed factor is passed as Lrow/Lcol/Lval, U is unused), 4 as 2 plus an
+ * FP32-stored A in the Arnoldi product (z rounded to FP32, FP32
+ * accumulation); the true residual at every restart uses the FP64 A.
  * hist (optional, length maxit+1) receives the residual estimate per
  * iteration. */
 int orc_gmres(int nb, int bs, const int* Arow, const int* Acol,

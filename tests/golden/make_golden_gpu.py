@@ -184,7 +184,82 @@ def main():
         _, times = run_reference(kernels[4], A, LU, 4, timing_reps=5)
         print(json.dumps({"workload": f"convdiff3d {side}^3 bs4", "reference_kernels_ms": times}))
         print(json.dumps({"workload": f"convdiff3d {side}^3 bs4",
+                          "ours_isai_steps_ms": time_our_isai_steps(A, LU, reps=5)}))
+        print(json.dumps({"workload": f"convdiff3d {side}^3 bs4",
                           "factor_and_solve_ms": time_factor_and_solves(A)}))
+
+
+def time_our_isai_steps(A, LU, reps=5):
+    """This library's ISAI setup steps on the same factor as the reference
+    kernels above, through the C ABI with preallocated outputs (CUDA events,
+    mean of `reps` after one warm-up): Dinv, pair lists (count + fill, which
+    includes a scan and the host read of the total), ISAI column solves,
+    BCSC->BCSR reorder of both factors, and the FP64 / FP32 apply."""
+    import torch
+
+    from isai_kernel_gb300 import _lib, api
+
+    L = _lib.lib()
+    P = api._p
+    dev = "cuda"
+    nb, bs, bs2 = A.nb, A.bs, A.bs * A.bs
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    Ar, Ac, Av = T(A.rowptr), T(A.colind), T(LU)
+    times = {}
+
+    def timed(key, fn):
+        fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        e1.synchronize()
+        times[key] = e0.elapsed_time(e1) / reps
+
+    side = {}
+    for lower, tag in ((1, "L"), (0, "U")):
+        mp, mi = oracle.isai_pattern(nb, A.rowptr, A.colind, bool(lower))
+        tr, tc = oracle.tri_pattern(nb, A.rowptr, A.colind, bool(lower))
+        mp_, mi_ = T(mp), T(mi)
+        mnnz = int(mp[-1])
+        D = torch.empty(nb * bs2, dtype=torch.float64, device=dev)
+        timed(f"Dinv{tag}", lambda: api.call("bilu_build_dinv", nb, bs, P(Ar), P(Ac), P(Av),
+                                             lower, P(D), api._s()))
+        pp = torch.empty(mnnz + 1, dtype=torch.int32, device=dev)
+        ws = api._ws(L.bilu_pairs_ws_bytes(mnnz), dev)
+        tot, nmx = ctypes.c_int(0), ctypes.c_int(0)
+
+        def count():
+            api.call("bilu_pairs_ptr", nb, P(Ar), P(Ac), P(mp_), P(mi_), lower, P(pp),
+                     ctypes.byref(tot), ctypes.byref(nmx), P(ws), ws.numel(), api._s())
+        timed(f"count_pairs_{tag}", count)
+        pl = torch.empty(max(tot.value, 1), dtype=torch.int32, device=dev)
+        ps = torch.empty(max(tot.value, 1), dtype=torch.int32, device=dev)
+        timed(f"fill_pairs_{tag}", lambda: api.call("bilu_pairs_fill", nb, P(Ar), P(Ac), P(mp_),
+                                                    P(mi_), lower, P(pp), P(pl), P(ps),
+                                                    api._s()))
+        M = torch.empty(mnnz * bs2, dtype=torch.float64, device=dev)
+        timed(f"isai_{tag}", lambda: api.call("bilu_isai_compute", nb, bs, P(Av), P(mp_), P(mi_),
+                                              lower, P(pp), P(pl), P(ps), P(D), P(M), api._s()))
+        mp_map = T(oracle.map_bcsc2bcsr(nb, mp, mi, tr, tc))
+        side[tag] = (mnnz, mp_map, M, torch.empty_like(M), T(tr), T(tc))
+
+    def reorder():
+        for tag in ("L", "U"):
+            mnnz, mp_map, M, R, _, _ = side[tag]
+            api.call("bilu_reorder_bcsc_to_bcsr", mnnz, bs, P(mp_map), P(M), P(R), api._s())
+    timed("reorder_L_and_U", reorder)
+    b = T(gen.rhs(A.n, 3))
+    x = torch.empty_like(b)
+    tmp = torch.empty_like(b)
+    (_, _, _, RL, trL, tcL), (_, _, _, RU, trU, tcU) = side["L"], side["U"]
+    RL32, RU32 = RL.float(), RU.float()
+    timed("apply_fp64", lambda: api.call("bilu_isai_apply", nb, bs, 0, P(trL), P(tcL), P(RL),
+                                         P(trU), P(tcU), P(RU), P(b), P(tmp), P(x), api._s()))
+    timed("apply_fp32", lambda: api.call("bilu_isai_apply", nb, bs, 1, P(trL), P(tcL), P(RL32),
+                                         P(trU), P(tcU), P(RU32), P(b), P(tmp), P(x), api._s()))
+    return times
 
 
 def time_factor_and_solves(A, reps=5):

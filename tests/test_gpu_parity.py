@@ -435,6 +435,48 @@ def test_gmres_iterations_match_oracle(cuda, orc, name):
     p.close()
 
 
+@pytest.mark.parametrize("name", ["c1_s16", "c2_s6", "c3_nb200", "bs5_s7"])
+def test_gmres_exact_ilu_and_switch(cuda, orc, name):
+    """BILU_ILU: z = U^-1 L^-1 v by the level-scheduled triangular solves;
+    the iteration count equals the oracle's exact-ILU GMRES, x within 1e-8.
+    bilu_ctx_select then returns one of the built choices with positive
+    scores, and solve(prec="auto") converges."""
+    from isai_kernel_gb300 import api
+
+    A = mats()[name]
+    LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    b = gen.rhs(A.n, 0)
+    Ab = (A.rowptr, A.colind, A.val)
+    xo, ito, rro, ho, st = orc.gmres(Ab, (A.rowptr, A.colind, LU), None, b, precond=3,
+                                     maxit=3000)
+    assert st == 0
+    p = api.Preconditioner(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda),
+                           ilu=True, fp32_inner=True)
+    x, res = p.solve(T(b, cuda), prec=api.BILU_ILU, maxit=3000, history=True)
+    assert res.converged and res.iters == ito
+    assert relerr(N(x), xo) < 1e-8
+    np.testing.assert_allclose(res.history, ho, rtol=1e-6)
+    # FP32 ISAI + FP32-stored A in the Arnoldi products, FP64 restarts: the
+    # oracle's mode 4 within 3 iterations, true residual 1e-10
+    S = orc.isai_setup(A)
+    Lo = (S["TrowL"], S["TcolL"], S["McsrL"])
+    Uo = (S["TrowU"], S["TcolU"], S["McsrU"])
+    _, it4, _, _, st4 = orc.gmres(Ab, Lo, Uo, b, precond=4, maxit=3000)
+    assert st4 == 0
+    x4, res4 = p.solve(T(b, cuda), prec=api.BILU_FP32_INNER, maxit=3000)
+    assert res4.converged and res4.relres <= 1e-10 and abs(res4.iters - it4) <= 3
+    choice, rate = p.select(T(b, cuda), cycles=1)
+    assert choice in (0, 1, 2, 3) and all(r > 0 for r in rate)
+    xa, resa = p.solve(T(b, cuda), prec="auto", maxit=3000)
+    assert resa.converged
+    p.close()
+    # a handle built without the ILU analyses refuses BILU_ILU
+    q = api.Preconditioner(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda))
+    with pytest.raises(api.BiluError):
+        q.solve(T(b, cuda), prec=api.BILU_ILU)
+    q.close()
+
+
 def test_solve_host_end_to_end(cuda, orc):
     from isai_kernel_gb300 import api
 
