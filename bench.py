@@ -529,7 +529,18 @@ def run_sptrsv(args):
         e1.synchronize()
         out[f"gmres_{tag}"] = {"s": e0.elapsed_time(e1) / 1e3, "iters": res.iters,
                                "relres": res.relres}
-    choice, rate = Pc.select(b, cycles=1)
+    # ISAI(2): M patterns from pattern(A^2)
+    P2 = api.Preconditioner(nb, bs, row, col, val, fp32=True, isai_level=2)
+    e0.record()
+    _, res = P2.solve(b, x, prec=api.BILU_FP32, maxit=args.maxit)
+    e1.record()
+    e1.synchronize()
+    nnz2 = int(P2.get(2).numel())
+    out["gmres_isai2_fp32"] = {"s": e0.elapsed_time(e1) / 1e3, "iters": res.iters,
+                               "relres": res.relres, "nnzb_ML": nnz2,
+                               "setup_ms": P2.setup_ms["total"]}
+    P2.close()
+    choice, rate = Pc.select(b, cycles=3)
     out["switch"] = {"choice": {0: "isai_fp64", 1: "isai_fp32", 2: "ilu", 3: "fp32_inner"}[choice],
                      "digits_per_s": rate}
     Pc.close()

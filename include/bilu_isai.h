@@ -96,6 +96,21 @@ int bilu_isai_pattern_fill(int nb, const int* d_Arow, const int* d_Acol, int low
                            const int* d_Mptr, int* d_Mind, void* d_ws, size_t ws_bytes,
                            bilu_stream_t stream);
 
+/* Symbolic block-pattern product C = pattern(X A) (no counterpart in the
+ * reference; ISAI(k) uses the lower / upper triangle of pattern(A^k) as the
+ * M_L / M_U pattern, and the pattern functions of this section accept it in
+ * place of A's).  Two phases like the others: row pointer (h_nnz = nnz(C)),
+ * then columns (sorted, distinct).  A row that gathers more than 1024
+ * candidate columns returns BILU_ERR_UNSUPPORTED with its index in
+ * *h_bad_row. */
+size_t bilu_pattern_product_ws_bytes(int nb);
+int bilu_pattern_product_rowptr(int nb, const int* d_Xrow, const int* d_Xcol, const int* d_Arow,
+                                const int* d_Acol, int* d_Crow, int* h_nnz, int* h_bad_row,
+                                void* d_ws, size_t ws_bytes, bilu_stream_t stream);
+int bilu_pattern_product_fill(int nb, const int* d_Xrow, const int* d_Xcol, const int* d_Arow,
+                              const int* d_Acol, const int* d_Crow, int* d_Ccol, void* d_ws,
+                              size_t ws_bytes, bilu_stream_t stream);
+
 /* Replaces build_triangular_bcsr_pattern_from_A (bcsc2bcsr.h:11). */
 size_t bilu_tri_pattern_ws_bytes(int nb);
 int bilu_tri_pattern_rowptr(int nb, const int* d_Arow, const int* d_Acol, int lower,
@@ -300,6 +315,12 @@ int bilu_ctx_destroy(bilu_ctx* ctx);
 int bilu_ctx_setup(bilu_ctx* ctx, int nb, int nnzb, int bs, const int* d_row, const int* d_col,
                    const double* d_val, int prec_mask, double* h_times);
 
+/* ISAI level for the next bilu_ctx_setup: k = 1 (default) uses the
+ * pattern of A as the reference does; k = 2, 3 use the pattern of A^k
+ * (ISAI(k): denser approximate inverses, fewer iterations, a costlier
+ * apply). */
+int bilu_ctx_set_isai_level(bilu_ctx* ctx, int k);
+
 /* Right-preconditioned restarted (F)GMRES(restart) with modified
  * Gram-Schmidt and Givens rotations, x0 = 0: prec BILU_FP64 applies the FP64 ISAI, BILU_FP32 the
  * FP32-stored ISAI (flexible GMRES, FP64 residuals/orthogonalisation,
@@ -318,13 +339,15 @@ int bilu_ctx_solve(bilu_ctx* ctx, int prec, const double* d_b, double* d_x, int 
 int bilu_ctx_stats(bilu_ctx* ctx, long long* h_out);
 
 /* Preconditioner switch by measurement (SpTRSV apply vs SpMV apply):
- * runs `cycles` restart cycles from x0 = 0 with each choice whose bit
+ * runs up to `cycles` restart cycles (fewer when it reaches tol) from x0 = 0
+ * with each choice whose bit
  * (1 << BILU_FP64 / BILU_FP32 / BILU_ILU / BILU_FP32_INNER) is in `mask`
  * and that the setup built, and returns in *h_choice the one with the
- * largest residual reduction per second; h_rate (optional, 4 doubles)
+ * largest residual reduction per second over its last cycle (restarted
+ * GMRES gains most in its first cycle); h_rate (optional, 4 doubles)
  * receives the scores in decimal digits per second, indexed by choice. */
-int bilu_ctx_select(bilu_ctx* ctx, const double* d_b, int restart, int cycles, int mask,
-                    int* h_choice, double* h_rate);
+int bilu_ctx_select(bilu_ctx* ctx, const double* d_b, int restart, int cycles, double tol,
+                    int mask, int* h_choice, double* h_rate);
 
 /* Host-buffer convenience (the end-to-end call): copies A and b from host
  * memory, runs setup and solve, copies x back. */

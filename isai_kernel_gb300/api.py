@@ -98,6 +98,22 @@ def build_bcsc_pattern_from_bsr_scalarILU(nb: int, Abrow, Abcol, for_lower: bool
     return mp, mi
 
 
+def pattern_product(nb: int, Xrow, Xcol, Arow, Acol):
+    """Symbolic block-pattern product pattern(X A) -> (rowptr, colind)
+    (bilu_pattern_product_*; ISAI(k) patterns are pattern(A^k))."""
+    dev = _dev(Xrow)
+    cr = torch.empty(nb + 1, dtype=_I32, device=dev)
+    nnz, bad = ctypes.c_int(0), ctypes.c_int(-1)
+    ws = _ws(lib().bilu_pattern_product_ws_bytes(nb), dev)
+    xr, xc, ar, ac = _ci(Xrow), _ci(Xcol), _ci(Arow), _ci(Acol)
+    call("bilu_pattern_product_rowptr", nb, _p(xr), _p(xc), _p(ar), _p(ac), _p(cr),
+         ctypes.byref(nnz), ctypes.byref(bad), _p(ws), ws.numel(), _s())
+    cc = torch.empty(max(nnz.value, 1), dtype=_I32, device=dev)
+    call("bilu_pattern_product_fill", nb, _p(xr), _p(xc), _p(ar), _p(ac), _p(cr), _p(cc), _p(ws),
+         ws.numel(), _s())
+    return cr, cc[: nnz.value]
+
+
 def build_triangular_bcsr_pattern_from_A(nb: int, A_bsrRow, A_bsrCol, lower: bool):
     """bcsc2bcsr.h:11 -> (T_bsrRow, T_bsrCol)."""
     dev = _dev(A_bsrRow)
@@ -328,11 +344,12 @@ class Preconditioner:
     preconditioner from a BSR matrix, then preconditioned (F)GMRES solves."""
 
     def __init__(self, nb: int, bs: int, row, col, val, fp32: bool = True, ilu: bool = False,
-                 fp32_inner: bool = False, stream=None):
+                 fp32_inner: bool = False, isai_level: int = 1, stream=None):
         self._h = ctypes.c_void_p()
         self.nb, self.bs = nb, bs
         self.stream = stream
         call("bilu_ctx_create", ctypes.byref(self._h), _s(stream))
+        call("bilu_ctx_set_isai_level", self._h, isai_level)
         self._keep = (row, col, val)
         times = (ctypes.c_double * 4)()
         call("bilu_ctx_setup", self._h, nb, int(col.numel()), bs, _p(_ci(row)), _p(_ci(col)),
@@ -371,12 +388,13 @@ class Preconditioner:
         U = (self.get(4), self.get(5), self.get(6).view(-1, bs, bs))
         return lu, L, U
 
-    def select(self, b, restart: int = 30, cycles: int = 1, mask: int = 15):
+    def select(self, b, restart: int = 30, cycles: int = 3, tol: float = 1e-10, mask: int = 15):
         """bilu_ctx_select: the preconditioner (BILU_FP64 / BILU_FP32 /
         BILU_ILU / BILU_FP32_INNER) with the best measured residual reduction
-        per second over `cycles` restart cycles -> (choice, [digits/s])."""
+        per second over the last of up to `cycles` restart cycles
+        -> (choice, [digits/s])."""
         choice, rate = ctypes.c_int(-1), (ctypes.c_double * 4)()
-        call("bilu_ctx_select", self._h, _p(_cf(b)), restart, cycles, mask,
+        call("bilu_ctx_select", self._h, _p(_cf(b)), restart, cycles, tol, mask,
              ctypes.byref(choice), rate)
         return choice.value, list(rate)
 
@@ -386,7 +404,7 @@ class Preconditioner:
         "auto" (measured choice by select())."""
         b = _cf(b)
         if prec == "auto":
-            prec, _ = self.select(b, restart)
+            prec, _ = self.select(b, restart, tol=tol)
         if x is None:
             x = torch.empty_like(b)
         it, rr = ctypes.c_int(0), ctypes.c_double(0)

@@ -36,6 +36,13 @@ int diag_positions(int nb, const int* row, const int* col, int* diag, int* h_bad
                    cudaStream_t st);
 size_t level_sched_ws(int nb, long long nnzb);
 size_t levels_ws(int nb, long long ndeps);
+size_t pattern_product_ws(int n);
+int pattern_product_rowptr(int n, const int* Xrow, const int* Xcol, const int* Arow,
+                           const int* Acol, int* Crow, int* h_nnz, int* h_bad, Carver& ws,
+                           cudaStream_t st);
+int pattern_product_fill(int n, const int* Xrow, const int* Xcol, const int* Arow,
+                         const int* Acol, const int* Crow, int* Ccol, Carver& ws,
+                         cudaStream_t st);
 int level_analysis(int nb, long long nnzb, const int* row, const int* col, const int* diag,
                    int lower, int* order, int* lvl, int* nlev_d, int* h_nlev, Carver& ws,
                    cudaStream_t st);
@@ -85,6 +92,9 @@ struct bilu_ctx {
   float *Lval32 = nullptr, *Uval32 = nullptr;
   float* Aval32 = nullptr;  // FP32 copy of A for the Arnoldi products (BILU_FP32_INNER)
   int nnzL = 0, nnzU = 0;
+  int isai_level = 1;                     // ISAI(k): M patterns from pattern(A^k)
+  int *Prow = nullptr, *Pcol = nullptr;   // pattern(A^k) when isai_level > 1
+  int nnzP = 0;
   bool ready = false;
   // exact BILU(0) apply (BILU_ILU): level analyses of the lower and upper
   // DAGs, and the barrier / error words of the launch-only solves
@@ -112,6 +122,7 @@ struct bilu_ctx {
     Lval32 = Uval32 = nullptr;
     Aval32 = nullptr;
     ordL = lvlL = nlevL = ordU = lvlU = nlevU = nullptr;
+    Prow = Pcol = nullptr;
     ilu_words = nullptr;
     ready = false;
   }
@@ -184,6 +195,10 @@ int build_isai_side(bilu_ctx* c, int lower, Carver& ws, int** orow, int** ocol, 
                     int* onnz, double* t_pattern, double* t_isai) {
   cudaStream_t st = c->st;
   int nb = c->nb, bs = c->bs, bs2 = bs * bs;
+  // the M patterns come from pattern(A^k) for ISAI(k); the pair lists, Dinv
+  // and the column solves still read the factor on A's pattern
+  const int* pr = c->Prow ? c->Prow : c->Arow;
+  const int* pc = c->Pcol ? c->Pcol : c->Acol;
   Timer tm(st);
   tm.mark(0);
   int *Mptr, *Trow;
@@ -192,11 +207,11 @@ int build_isai_side(bilu_ctx* c, int lower, Carver& ws, int** orow, int** ocol, 
   int mnnz = 0, tnnz = 0;
   {
     Carver w2 = ws;
-    BILU_TRY(isai_pattern_colptr_impl(nb, c->Arow, c->Acol, lower, Mptr, &mnnz, w2, st));
+    BILU_TRY(isai_pattern_colptr_impl(nb, pr, pc, lower, Mptr, &mnnz, w2, st));
   }
   {
     Carver w2 = ws;
-    BILU_TRY(tri_pattern_rowptr_impl(nb, c->Arow, c->Acol, lower, Trow, &tnnz, w2, st));
+    BILU_TRY(tri_pattern_rowptr_impl(nb, pr, pc, lower, Trow, &tnnz, w2, st));
   }
   // the reference's guard (main.cu:537-546): both views must hold the same
   // blocks, i.e. every diagonal block is stored
@@ -208,9 +223,9 @@ int build_isai_side(bilu_ctx* c, int lower, Carver& ws, int** orow, int** ocol, 
   {
     Carver w2 = ws;
     if (!w2.take<int>(2)) return BILU_ERR_WORKSPACE;
-    BILU_TRY(isai_pattern_fill_impl(nb, c->Arow, c->Acol, lower, Mptr, Mind, mnnz, w2, st));
+    BILU_TRY(isai_pattern_fill_impl(nb, pr, pc, lower, Mptr, Mind, mnnz, w2, st));
   }
-  BILU_TRY(tri_pattern_fill_impl(nb, c->Arow, c->Acol, lower, Trow, Tcol, st));
+  BILU_TRY(tri_pattern_fill_impl(nb, pr, pc, lower, Trow, Tcol, st));
   {
     Carver w2 = ws;
     BILU_TRY(map_impl(nb, Mptr, Mind, Trow, Tcol, map, nullptr, w2, st));
@@ -273,7 +288,7 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   BILU_TRY_CUDA(cudaMemcpyAsync(c->LU, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
   // scratch shared by every step
   size_t wsb = std::max({isai_pattern_ws(nb, nnzb), level_sched_ws(nb, nnzb), pairs_ws(nnzb + nb),
-                         levels_ws(nb, nnzb),
+                         levels_ws(nb, nnzb), pattern_product_ws(nb),
                          scan_ws_bytes(nnzb + nb + 1)}) + (1 << 16);
   void* wsp = nullptr;
   BILU_TRY(c->alloc((char**)&wsp, wsb));
@@ -291,6 +306,37 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   }
   tm.mark(2);
   double t_pat = 0, t_isai = 0;
+  if (c->isai_level > 1) {
+    // pattern(A^k) by repeated symbolic products with A
+    const int *xr = c->Arow, *xc = c->Acol;
+    for (int k = 2; k <= c->isai_level; ++k) {
+      int *cr = nullptr, *cc = nullptr, nnz = 0;
+      BILU_TRY(c->alloc(&cr, (size_t)nb + 1));
+      {
+        Carver w2 = ws;
+        BILU_TRY(pattern_product_rowptr(nb, xr, xc, c->Arow, c->Acol, cr, &nnz, nullptr, w2, st));
+      }
+      BILU_TRY(c->alloc(&cc, (size_t)nnz));
+      {
+        Carver w2 = ws;
+        BILU_TRY(pattern_product_fill(nb, xr, xc, c->Arow, c->Acol, cr, cc, w2, st));
+      }
+      xr = cr;
+      xc = cc;
+      c->Prow = cr;
+      c->Pcol = cc;
+      c->nnzP = nnz;
+    }
+    // the pattern steps below scale with nnz(pattern(A^k))
+    long long np = c->nnzP;
+    size_t need = std::max({isai_pattern_ws(nb, np), pairs_ws(np + nb),
+                            scan_ws_bytes(np + nb + 1)}) + (1 << 16);
+    if (need > wsb) {
+      void* wsq = nullptr;
+      BILU_TRY(c->alloc((char**)&wsq, need));
+      ws = Carver(wsq, need);
+    }
+  }
   BILU_TRY(build_isai_side(c, 1, ws, &c->Lrow, &c->Lcol, &c->Lval, &c->nnzL, &t_pat, &t_isai));
   BILU_TRY(build_isai_side(c, 0, ws, &c->Urow, &c->Ucol, &c->Uval, &c->nnzU, &t_pat, &t_isai));
   if (prec_mask & (1 << BILU_FP32_INNER)) {
@@ -330,6 +376,12 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
     h_times[3] = t_total;
   }
   c->ready = true;
+  return BILU_OK;
+}
+
+extern "C" int bilu_ctx_set_isai_level(bilu_ctx* c, int k) {
+  if (!c || k < 1 || k > 3) return BILU_ERR_ARG;
+  c->isai_level = k;
   return BILU_OK;
 }
 
@@ -567,20 +619,23 @@ extern "C" int bilu_ctx_stats(bilu_ctx* c, long long* h_out) {
   return BILU_OK;
 }
 
-// Preconditioner switch by measurement: `cycles` restart cycles of the solve
-// from x0 = 0 with every choice in `mask` (bits 1 << BILU_FP64 / BILU_FP32 /
-// BILU_ILU / BILU_FP32_INNER that the setup built), timed with events on the
-// handle's stream; the score is the residual reduction per second (decimal
-// digits / s).  Returns the best choice in *h_choice and the scores in
+// Preconditioner switch by measurement: up to `cycles` restart cycles (fewer
+// if it reaches tol) of the solve from x0 = 0 with every choice in `mask` (bits 1 << BILU_FP64 /
+// BILU_FP32 / BILU_ILU / BILU_FP32_INNER that the setup built), timed with
+// events on the handle's stream.  The score is the residual reduction per
+// second over the last cycle run (decimal digits / s): restarted GMRES gains
+// most in its first cycle, so a one-cycle rate flatters the weaker
+// preconditioner.  Returns the best choice in *h_choice and the scores in
 // h_rate[4] (0 for choices not tried).
-extern "C" int bilu_ctx_select(bilu_ctx* c, const double* d_b, int restart, int cycles, int mask,
-                               int* h_choice, double* h_rate) {
+extern "C" int bilu_ctx_select(bilu_ctx* c, const double* d_b, int restart, int cycles,
+                               double tol, int mask, int* h_choice, double* h_rate) {
   if (!c || !c->ready || !d_b || !h_choice || cycles < 1 || restart < 1) return BILU_ERR_ARG;
   double* x = nullptr;
   BILU_TRY_CUDA(cudaMalloc(&x, sizeof(double) * c->n));
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  std::vector<double> hist((size_t)restart * cycles + 1);
   int best = -1, rc = BILU_OK;
   double best_rate = -1.0;
   for (int p = 0; p < 4 && rc == BILU_OK; ++p) {
@@ -592,7 +647,7 @@ extern "C" int bilu_ctx_select(bilu_ctx* c, const double* d_b, int restart, int 
     int it = 0;
     double rr = 1.0;
     cudaEventRecord(e0, c->st);
-    int st = bilu_ctx_solve(c, p, d_b, x, restart, 0.0, restart * cycles, &it, &rr, nullptr);
+    int st = bilu_ctx_solve(c, p, d_b, x, restart, tol, restart * cycles, &it, &rr, hist.data());
     cudaEventRecord(e1, c->st);
     cudaEventSynchronize(e1);
     if (st != BILU_OK && st != BILU_ERR_NOT_CONVERGED) {
@@ -601,8 +656,14 @@ extern "C" int bilu_ctx_select(bilu_ctx* c, const double* d_b, int restart, int 
     }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    double digits = rr > 0.0 ? -std::log10(rr) : 16.0;
-    double rate = ms > 0.f ? digits / (ms * 1e-3) : 0.0;
+    if (it < 1) continue;
+    // last cycle: iterations (it - 1) / restart * restart .. it
+    int first = ((it - 1) / restart) * restart;
+    double r0 = hist[first] > 0.0 ? hist[first] : 1.0;
+    double r1 = rr > 0.0 ? rr : 1e-300;
+    double digits = std::max(0.0, std::log10(r0) - std::log10(r1));
+    double sec = ms * 1e-3 * (double)(it - first) / (double)it;
+    double rate = sec > 0.0 ? digits / sec : 0.0;
     if (h_rate) h_rate[p] = rate;
     if (rate > best_rate) {
       best_rate = rate;

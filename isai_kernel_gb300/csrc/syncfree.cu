@@ -1,17 +1,24 @@
-// Sync-free kernels with per-block-row ready flags (sm_103a):
+// BILU(0) and block triangular solves on the dependency DAG (sm_103a):
 //
-//   bsrilu02_inplace (bsrilu.h:20, cuSPARSE bsrilu02)   -> k_bilu0
-//   spTrSolveL / spTrSolveU (cape_sptrsv.h:8,55)         -> k_sptrsv
+//   bsrilu02_inplace (bsrilu.h:20, cuSPARSE bsrilu02)   -> k_bilu0_levels
+//   spTrSolveL / spTrSolveU (cape_sptrsv.h:8,55)         -> k_sptrsv_levels,
+//                                                            k_sptrsv (sync-free)
 //
-// A warp owns one block row at a time.  Rows are handed out by an atomic
-// ticket counter, so every row a warp waits on was taken by a warp that is
-// already running (the reference maps rows to threads statically and relies
-// on scheduling order).  A finished row publishes its flag with st.release
-// after a __threadfence by every writer lane; waiters poll with relaxed loads,
-// take one acquire fence when the flag is set, and read the producer's data
-// through L2 (ld.cg).  Every wait is bounded:
-// after kSpinLimit polls the waiter sets the error word to BILU_ERR_TIMEOUT,
-// and all other waiters see the error word and leave, so no launch hangs.
+// Level schedule (default): a breadth-first sweep (k_bfs_levels) groups the
+// block rows by dependency level; one cooperative launch then processes a
+// level with a group of bs lanes per row and meets at a bounded grid barrier.
+//
+// Sync-free schedule (the reference's design, kept for the solve): a warp
+// owns one block row at a time.  Rows are handed out by an atomic ticket
+// counter in level order, so every row a warp waits on was taken by a warp
+// that is already running (the reference maps rows to threads statically and
+// relies on scheduling order).  A finished row publishes its flag with
+// st.release; waiters poll with relaxed loads, take one acquire fence when
+// the flag is set, and read the producer's data through L2 (ld.cg).
+//
+// Every wait is bounded: after kSpinLimit polls the waiter sets the error
+// word to BILU_ERR_TIMEOUT, and all other waiters see the error word and
+// leave, so no launch hangs.
 #include <climits>
 
 #include <algorithm>
@@ -49,25 +56,6 @@ __device__ __forceinline__ void backoff(unsigned& ns) {
 // orders the reads of the producer's data after it.
 __device__ __forceinline__ void fence_acquire() {
   asm volatile("fence.acq_rel.gpu;" ::: "memory");
-}
-
-// Warp-wide wait until flags[K] != 0.  Returns false if the launch aborted.
-__device__ __forceinline__ bool warp_wait(const int* flag, int* err, long long spin) {
-  long long n = 0;
-  unsigned ns = 32;
-  while (true) {
-    int v = ld_relaxed(flag);
-    if (__all_sync(FULL, v != 0)) {
-      fence_acquire();
-      return true;
-    }
-    if (__any_sync(FULL, ld_relaxed(err) != 0)) return false;
-    if (++n > spin) {
-      if ((threadIdx.x & 31) == 0) atomicCAS(err, 0, (int)BILU_ERR_TIMEOUT);
-      return false;
-    }
-    backoff(ns);
-  }
 }
 
 // Single-lane wait (lanes of a warp may wait on different rows).
@@ -113,165 +101,6 @@ __global__ void k_diag_pos(int nb, const int* __restrict__ row, const int* __res
   if (d < 0) atomicMin(bad, i);
 }
 
-// ------------------------------------------------------------------ BILU(0)
-// Scalar ILU(0) on the block pattern in IKJ order, blockwise:
-//   for K < I in row I:  L_IK = A_IK U_KK^-1 (row-wise forward elimination),
-//                        A_IJ -= L_IK U_KJ for J > K present in rows I and K;
-//   then LU of the diagonal block (no pivoting) and U_IJ = L_II^-1 A_IJ.
-// Each element sees the same sequence of a -= l*u updates as the scalar IKJ
-// loop, with ascending k.
-// One block row of the factorisation, executed by one warp.  WAIT: the
-// rows K it reads may still be in progress (sync-free schedule) and are
-// waited for through their flags; otherwise every K is already final
-// (level schedule).  Returns false if the launch aborted.
-template <int BS, bool WAIT>
-__device__ __forceinline__ bool bilu0_row(int I, const int* __restrict__ row,
-                                          const int* __restrict__ col,
-                                          const int* __restrict__ diag, double* val,
-                                          const SyncState& ss) {
-  constexpr int BS2 = BS * BS;
-  constexpr int EPL = BS2 > 32 ? 2 : 1;
-  constexpr int TL = BS2 / EPL + (BS2 % EPL ? 1 : 0);
-  constexpr int TPW = 32 / TL;         // blocks updated per pass in phase 2
-  constexpr int SPAN = 32 / TPW;
-  constexpr int GU = 32 / BS;          // U blocks per pass (lane = column)
-  int lane = threadIdx.x & 31;
-  int team = lane / SPAN, tl = lane - team * SPAN;
-  bool team_on = team < TPW && tl < TL;
-  int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
-  for (int pk = rs; pk < dI; ++pk) {
-    int K = __ldg(col + pk);
-    if (WAIT && !warp_wait(ss.flags + K, ss.err, ss.spin)) return false;
-    int dK = __ldg(diag + K), ke = __ldg(row + K + 1);
-    double* L = val + (long long)pk * BS2;
-    const double* Ukk = val + (long long)dK * BS2;
-    // phase 1: lane r owns row r of A_IK
-    if (lane < BS) {
-      double a[BS];
-#pragma unroll
-      for (int c = 0; c < BS; ++c) a[c] = L[lane * BS + c];
-#pragma unroll
-      for (int k = 0; k < BS; ++k) {
-        a[k] = a[k] / __ldcg(Ukk + k * BS + k);
-#pragma unroll
-        for (int c = k + 1; c < BS; ++c) a[c] -= a[k] * __ldcg(Ukk + k * BS + c);
-      }
-#pragma unroll
-      for (int c = 0; c < BS; ++c) L[lane * BS + c] = a[c];
-    }
-    __syncwarp();
-    // phase 2: A_IJ -= L_IK U_KJ for J > K in rows I and K.  The shorter
-    // of the two column lists supplies the candidates, 32 at a time, each
-    // lane binary-searching one of them in the other list (hub rows of
-    // power-law matrices hold thousands of blocks); then the teams update
-    // the matched blocks.  Every block is updated once per K, so the
-    // update order of each element is the same either way.
-    {
-      const bool from_i = (re - pk - 1) <= (ke - dK - 1);
-      const int cs = from_i ? pk + 1 : dK + 1, ce = from_i ? re : ke;
-      const int ss_ = from_i ? dK + 1 : pk + 1, se = from_i ? ke : re;
-      for (int c0 = cs; c0 < ce; c0 += 32) {
-        int pc = c0 + lane, other = -1;
-        if (pc < ce) other = find_in_row(col, ss_, se, __ldg(col + pc));
-        unsigned found = __ballot_sync(FULL, other >= 0);
-        while (found) {
-          // the next TPW matches go to the TPW teams
-          int src = -1;
-#pragma unroll
-          for (int t = 0; t < TPW; ++t) {
-            int bit = found ? __ffs(found) - 1 : -1;
-            if (bit >= 0) found &= found - 1;
-            if (t == team) src = bit;
-          }
-          int o = __shfl_sync(FULL, other, src < 0 ? 0 : src);
-          if (team_on && src >= 0) {
-            int pj = from_i ? c0 + src : o;
-            int pos = from_i ? o : c0 + src;
-            double* Aij = val + (long long)pj * BS2;
-            const double* Ukj = val + (long long)pos * BS2;
-#pragma unroll
-            for (int q = 0; q < EPL; ++q) {
-              int e = tl * EPL + q;
-              if (e < BS2) {
-                int r = e / BS, c = e - r * BS;
-                double v = Aij[e];
-#pragma unroll
-                for (int k = 0; k < BS; ++k) v -= L[r * BS + k] * __ldcg(Ukj + k * BS + c);
-                Aij[e] = v;
-              }
-            }
-          }
-        }
-      }
-    }
-    __syncwarp();
-  }
-  // diagonal block: lane c owns column c
-  double* D = val + (long long)dI * BS2;
-  double dc[BS];
-  if (lane < BS) {
-#pragma unroll
-    for (int r = 0; r < BS; ++r) dc[r] = D[r * BS + lane];
-  } else {
-#pragma unroll
-    for (int r = 0; r < BS; ++r) dc[r] = 1.0;
-  }
-#pragma unroll
-  for (int r = 1; r < BS; ++r) {
-#pragma unroll
-    for (int k = 0; k < r; ++k) {
-      double lk = dc[r] / dc[k];  // meaningful on lane k
-      double l = __shfl_sync(FULL, lk, k);
-      if (lane == k) dc[r] = l;
-      else if (lane > k && lane < BS) dc[r] -= l * dc[k];
-    }
-  }
-  if (lane < BS) {
-    if (dc[lane] == 0.0) atomicMin(ss.zp, I);
-#pragma unroll
-    for (int r = 0; r < BS; ++r) D[r * BS + lane] = dc[r];
-  }
-  __syncwarp();
-  // U blocks right of the diagonal: U_IJ = L_II^-1 A_IJ, lane per column
-  for (int pj0 = dI + 1; pj0 < re; pj0 += GU) {
-    int slot = lane / BS, c = lane - slot * BS;
-    int pj = pj0 + slot;
-    if (slot < GU && pj < re) {
-      double* U = val + (long long)pj * BS2;
-      double u[BS];
-#pragma unroll
-      for (int r = 0; r < BS; ++r) u[r] = U[r * BS + c];
-#pragma unroll
-      for (int r = 1; r < BS; ++r)
-#pragma unroll
-        for (int k = 0; k < r; ++k) u[r] -= D[r * BS + k] * u[k];
-#pragma unroll
-      for (int r = 1; r < BS; ++r) U[r * BS + c] = u[r];
-    }
-  }
-  return true;
-}
-
-template <int BS>
-__global__ void __launch_bounds__(128) k_bilu0(int nb, const int* __restrict__ row,
-                                               const int* __restrict__ col,
-                                               const int* __restrict__ diag, double* val,
-                                               SyncState ss) {
-  int lane = threadIdx.x & 31;
-  while (true) {
-    int I = 0;
-    if (lane == 0) I = atomicAdd(ss.ticket, 1);
-    I = __shfl_sync(FULL, I, 0);
-    if (I >= nb) return;
-    if (ss.order) I = __ldg(ss.order + I);
-    if (__any_sync(FULL, ld_relaxed(ss.err) != 0)) return;
-    if (!bilu0_row<BS, true>(I, row, col, diag, val, ss)) return;
-    __threadfence();
-    __syncwarp();
-    if (lane == 0 && I != ss.withhold) st_release(ss.flags + I, 1);
-  }
-}
-
 // ------------------------------------------------------------------ SpTRSV
 // Block-row solve on a packed factor.  LOWER: x_I = b_I - sum_{K<I} B_IK x_K
 // then the diagonal block's lower part; otherwise the upper part and J > I
@@ -288,7 +117,7 @@ struct RowPre {
   int K;              // this lane's block column in the first pass, or -1
   double a[BS];       // row r of that block
   double dq[BS];      // lanes q < BS: row q of the diagonal block
-  double bq, rq;      // lanes q < BS: b_q and 1 / D_qq (1 when UNIT)
+  double bq;          // lanes q < BS: b_q
 };
 
 template <int BS, bool LOWER, bool UNIT>
@@ -313,18 +142,13 @@ __device__ __forceinline__ void sptrsv_prefetch(int I, const int* __restrict__ r
 #pragma unroll
     for (int c = 0; c < BS; ++c) p.a[c] = __ldg(blk + c);
   }
-  // the diagonal block row, b and the pivot reciprocal do not depend on x:
-  // the division (a long FP64 sequence on this GPU) leaves the critical path
+  // the diagonal block row and b do not depend on x
   p.bq = 0.0;
-  p.rq = 1.0;
   if (lane < BS) {
     const double* D = val + (long long)dI * BS * BS + lane * BS;
 #pragma unroll
     for (int c = 0; c < BS; ++c) p.dq[c] = __ldg(D + c);
     p.bq = __ldg(b + (long long)I * BS + lane);
-#pragma unroll
-    for (int c = 0; c < BS; ++c)
-      if (c == lane && !UNIT) p.rq = 1.0 / p.dq[c];
   } else {
 #pragma unroll
     for (int c = 0; c < BS; ++c) p.dq[c] = 1.0;
@@ -347,38 +171,58 @@ __device__ __forceinline__ bool sptrsv_finish(const RowPre<BS>& p, const int* __
   constexpr int BS2 = BS * BS;
   constexpr int G = 32 / BS;
   const int lane = threadIdx.x & 31, slot = lane / BS, r = lane - slot * BS;
-  double s = 0.0;
+  // Blocks are summed in row order: each block's partial starts from zero
+  // and the partials of a pass are added in slot order, so the total is
+  // the same as a sequential sum over the row's blocks (the level schedule
+  // sums that way and gives bit-identical x).
+  double tot = 0.0, rq = 1.0;
   bool ok = true;
-  if (p.K >= 0) {
-    if (WAIT) ok = lane_wait(ss.flags + p.K, ss.err, ss.spin);
-    if (ok) {
-      const double* xk = x + (long long)p.K * BS;
+  {
+    double d = p.dq[0];  // pivot of row `lane` (lanes < BS), one division per lane
 #pragma unroll
-      for (int c = 0; c < BS; ++c) s = fma(p.a[c], __ldcg(xk + c), s);
+    for (int c = 1; c < BS; ++c)
+      if (c == lane) d = p.dq[c];
+    double sp = 0.0;
+    if (p.K >= 0) {
+      if (WAIT) ok = lane_wait(ss.flags + p.K, ss.err, ss.spin);
+      if (ok) {
+        const double* xk = x + (long long)p.K * BS;
+        double xv[BS];
+#pragma unroll
+        for (int c = 0; c < BS; ++c) xv[c] = __ldcg(xk + c);
+        if (!UNIT) rq = 1.0 / d;  // overlaps the x reads
+#pragma unroll
+        for (int c = 0; c < BS; ++c) sp = fma(p.a[c], xv[c], sp);
+      }
+    } else if (!UNIT) {
+      rq = 1.0 / d;
     }
+    if (WAIT && __any_sync(FULL, !ok)) return false;
+#pragma unroll
+    for (int g = 0; g < G; ++g) tot += __shfl_sync(FULL, sp, g * BS + r);
   }
   for (int p0 = p.ps + G; p0 < p.pe; p0 += G) {  // rows with more than G blocks
     int q = p0 + slot;
-    if (slot < G && q < p.pe && ok) {
+    double sp = 0.0;
+    if (slot < G && q < p.pe) {
       int K = __ldg(col + q);
       if (WAIT) ok = lane_wait(ss.flags + K, ss.err, ss.spin);
       if (ok) {
         const double* blk = val + (long long)q * BS2 + r * BS;
         const double* xk = x + (long long)K * BS;
 #pragma unroll
-        for (int c = 0; c < BS; ++c) s = fma(__ldg(blk + c), __ldcg(xk + c), s);
+        for (int c = 0; c < BS; ++c) sp = fma(__ldg(blk + c), __ldcg(xk + c), sp);
       }
     }
-  }
-  if (WAIT && __any_sync(FULL, !ok)) return false;
-  double tot = 0.0;
+    if (WAIT && __any_sync(FULL, !ok)) return false;
 #pragma unroll
-  for (int g = 0; g < G; ++g) tot += __shfl_sync(FULL, s, g * BS + r);
+    for (int g = 0; g < G; ++g) tot += __shfl_sync(FULL, sp, g * BS + r);
+  }
   double v = p.bq - tot, xv = 0.0;
 #pragma unroll
   for (int k = 0; k < BS; ++k) {
     const int c = LOWER ? k : BS - 1 - k;
-    double mine = (UNIT || lane != c) ? v : v * p.rq;
+    double mine = (UNIT || lane != c) ? v : v * rq;
     double xc = __shfl_sync(FULL, mine, c);
     if (lane == c) xv = xc;
     if (LOWER ? (lane > c && lane < BS) : (lane < c)) v -= p.dq[c] * xc;
@@ -671,61 +515,267 @@ __global__ void __launch_bounds__(256) k_bfs_levels(int nb, const int* __restric
 
 constexpr int kLvlThreads = 256;
 
-// Level-scheduled solve.  Each warp keeps the structural part of its first
-// row of the next level in registers, loaded before the barrier; after the
-// barrier only the x reads of that row remain.
+// Level-scheduled solve with a group of BS lanes per block row (32/BS rows
+// per warp; lane r of a group owns scalar row r).  On GB300 an FP64 warp
+// instruction costs the same whatever the number of active lanes, so packing
+// rows is what makes the per-level FP64 work small; rows of one level are
+// independent, so groups of a warp never wait on each other.  The structural
+// part of each group's first row of the next level (indices, first block,
+// diagonal row, b) is loaded before the barrier.
+template <int BS>
+struct GRowPre {
+  int I, ps, pe, K0;  // I < 0: no row for this group
+  double a0[BS];      // row r of the first block
+  double dq[BS];      // row r of the diagonal block
+  double bq;          // b_r
+};
+
+template <int BS, bool LOWER>
+__device__ __forceinline__ void grow_prefetch(int I, const int* __restrict__ row,
+                                              const int* __restrict__ col,
+                                              const int* __restrict__ diag,
+                                              const double* __restrict__ val,
+                                              const double* __restrict__ b, GRowPre<BS>& p) {
+  constexpr int BS2 = BS * BS;
+  const int r = (threadIdx.x & 31) % BS;
+  p.I = I;
+  p.K0 = -1;
+  p.ps = p.pe = 0;
+  if (I < 0) return;
+  int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
+  p.ps = LOWER ? rs : dI + 1;
+  p.pe = LOWER ? dI : re;
+  if (p.ps < p.pe) {
+    p.K0 = __ldg(col + p.ps);
+    const double* blk = val + (long long)p.ps * BS2 + r * BS;
+#pragma unroll
+    for (int c = 0; c < BS; ++c) p.a0[c] = __ldg(blk + c);
+  }
+  const double* D = val + (long long)dI * BS2 + r * BS;
+#pragma unroll
+  for (int c = 0; c < BS; ++c) p.dq[c] = __ldg(D + c);
+  p.bq = __ldg(b + (long long)I * BS + r);
+}
+
+// Called by all 32 lanes (the diagonal solve shuffles inside each group).
 template <int BS, bool LOWER, bool UNIT>
-__global__ void __launch_bounds__(kLvlThreads, BS == 8 ? 2 : (BS == 5 ? 3 : 4)) k_sptrsv_levels(
+__device__ __forceinline__ void grow_finish(const GRowPre<BS>& p, const int* __restrict__ col,
+                                            const double* __restrict__ val, double* x) {
+  constexpr int BS2 = BS * BS;
+  const int lane = threadIdx.x & 31, r = lane % BS, gb = lane - r;
+  double tot = 0.0, rq = 1.0;
+  if (p.I >= 0) {
+    double d = p.dq[0];
+#pragma unroll
+    for (int c = 1; c < BS; ++c)
+      if (c == r) d = p.dq[c];
+    if (p.K0 >= 0) {
+      const double* xk = x + (long long)p.K0 * BS;
+      double xv[BS];
+#pragma unroll
+      for (int c = 0; c < BS; ++c) xv[c] = __ldcg(xk + c);
+      if (!UNIT) rq = 1.0 / d;  // overlaps the x reads
+      double sp = 0.0;
+#pragma unroll
+      for (int c = 0; c < BS; ++c) sp = fma(p.a0[c], xv[c], sp);
+      tot += sp;
+      for (int q = p.ps + 1; q < p.pe; ++q) {
+        const int K = __ldg(col + q);
+        const double* blk = val + (long long)q * BS2 + r * BS;
+        const double* xq = x + (long long)K * BS;
+        sp = 0.0;
+#pragma unroll
+        for (int c = 0; c < BS; ++c) sp = fma(__ldg(blk + c), __ldcg(xq + c), sp);
+        tot += sp;
+      }
+    } else if (!UNIT) {
+      rq = 1.0 / d;
+    }
+  }
+  double v = p.bq - tot, xr = 0.0;
+#pragma unroll
+  for (int k = 0; k < BS; ++k) {
+    const int c = LOWER ? k : BS - 1 - k;
+    double mine = (UNIT || r != c) ? v : v * rq;
+    double xc = __shfl_sync(FULL, mine, (gb + c) & 31);
+    if (r == c) xr = xc;
+    if (LOWER ? (r > c) : (r < c)) v -= p.dq[c] * xc;
+  }
+  if (p.I >= 0) x[(long long)p.I * BS + r] = xr;
+}
+
+template <int BS, bool LOWER, bool UNIT>
+__global__ void __launch_bounds__(kLvlThreads, 2) k_sptrsv_levels(
     const int* __restrict__ row, const int* __restrict__ col, const int* __restrict__ diag,
     const double* __restrict__ val, const double* __restrict__ b, double* x,
     const int* __restrict__ order, const int* __restrict__ lvl_ptr, const int* __restrict__ nlev_p,
     SyncState ss, GridSync gs) {
+  constexpr int G = 32 / BS;
   // generation at launch: no barrier completes before every CTA has read it,
   // so consecutive launches need no reset of the barrier words
   unsigned gen = threadIdx.x == 0 ? ld_relaxed_u(gs.gen) : 0u;
+  const int g = (threadIdx.x & 31) / BS;
   const int warp = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int nw = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+  const long long ngrp = (long long)nw * G;
+  const long long mygrp = (long long)warp * G + g;  // groups g >= G (bs 5: lanes 30, 31) idle
   const int nlev = __ldg(nlev_p);
   if (nlev <= 0) return;
-  RowPre<BS> pre;
+  GRowPre<BS> pre;
   {
-    int t = __ldg(lvl_ptr) + warp;
-    sptrsv_prefetch<BS, LOWER, UNIT>(t < __ldg(lvl_ptr + 1) ? __ldg(order + t) : -1, row, col,
-                                     diag, val, b, pre);
+    long long t = __ldg(lvl_ptr) + mygrp;
+    grow_prefetch<BS, LOWER>(g < G && t < __ldg(lvl_ptr + 1) ? __ldg(order + t) : -1, row, col,
+                             diag, val, b, pre);
   }
   for (int l = 0; l < nlev; ++l) {
-    int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
-    if (pre.I >= 0) sptrsv_finish<BS, LOWER, UNIT, false, false>(pre, col, val, x, ss);
-    for (int t = s + warp + nw; t < e; t += nw) {
-      RowPre<BS> q;
-      sptrsv_prefetch<BS, LOWER, UNIT>(__ldg(order + t), row, col, diag, val, b, q);
-      sptrsv_finish<BS, LOWER, UNIT, false, false>(q, col, val, x, ss);
+    const int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
+    grow_finish<BS, LOWER, UNIT>(pre, col, val, x);
+    // further rows of a wide level, G at a time per warp (warp-uniform loop)
+    for (long long t0 = s + (long long)warp * G + ngrp; t0 < e; t0 += ngrp) {
+      GRowPre<BS> q;
+      long long t = t0 + g;
+      grow_prefetch<BS, LOWER>(g < G && t < e ? __ldg(order + t) : -1, row, col, diag, val, b, q);
+      grow_finish<BS, LOWER, UNIT>(q, col, val, x);
     }
     if (l + 1 < nlev) {
-      int t = e + warp;
-      sptrsv_prefetch<BS, LOWER, UNIT>(t < __ldg(lvl_ptr + l + 2) ? __ldg(order + t) : -1, row,
-                                       col, diag, val, b, pre);
+      long long t = e + mygrp;
+      grow_prefetch<BS, LOWER>(g < G && t < __ldg(lvl_ptr + l + 2) ? __ldg(order + t) : -1, row,
+                               col, diag, val, b, pre);
       if (!grid_sync(gs, gen, NoOp{})) return;
     }
+  }
+  (void)ss;
+}
+
+// ------------------------------------------------------------------ BILU(0)
+// Scalar ILU(0) on the block pattern in IKJ order, blockwise:
+//   for K < I in row I:  L_IK = A_IK U_KK^-1 (row-wise forward elimination),
+//                        A_IJ -= L_IK U_KJ for J > K present in rows I and K;
+//   then LU of the diagonal block (no pivoting) and U_IJ = L_II^-1 A_IJ.
+// Each element sees the same sequence of a -= l*u updates as the scalar IKJ
+// loop, with ascending k.
+//
+// One block row with a group of BS lanes (level schedule: rows of one level
+// are independent, so groups of a warp never wait on each other; the
+// group's shuffles and ballots use its own lane mask).  Lane r of the group
+// owns scalar row r of L_IK and of the updates, and column r of the
+// diagonal LU and of the U blocks.  Phase 2 takes its candidates from the
+// shorter of the two column lists (power-law hub rows hold thousands of
+// blocks), BS at a time, each lane binary-searching one in the other list;
+// every block is updated once per K, so the update order of each element
+// does not depend on which list is scanned.
+template <int BS>
+__device__ __forceinline__ void bilu0_grow(int I, const int* __restrict__ row,
+                                           const int* __restrict__ col,
+                                           const int* __restrict__ diag, double* val,
+                                           const SyncState& ss, unsigned gmask, int r, int gb) {
+  constexpr int BS2 = BS * BS;
+  const int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
+  for (int pk = rs; pk < dI; ++pk) {
+    const int K = __ldg(col + pk);
+    const int dK = __ldg(diag + K), ke = __ldg(row + K + 1);
+    double* L = val + (long long)pk * BS2;
+    const double* Ukk = val + (long long)dK * BS2;
+    // phase 1: row r of L_IK = A_IK U_KK^-1 (forward elimination)
+    double a[BS];
+#pragma unroll
+    for (int c = 0; c < BS; ++c) a[c] = L[r * BS + c];
+#pragma unroll
+    for (int k = 0; k < BS; ++k) {
+      a[k] = a[k] / __ldcg(Ukk + k * BS + k);
+#pragma unroll
+      for (int c = k + 1; c < BS; ++c) a[c] -= a[k] * __ldcg(Ukk + k * BS + c);
+    }
+#pragma unroll
+    for (int c = 0; c < BS; ++c) L[r * BS + c] = a[c];
+    // phase 2: A_IJ -= L_IK U_KJ for J > K in rows I and K; the shorter
+    // column list supplies the candidates, BS at a time
+    const bool from_i = (re - pk - 1) <= (ke - dK - 1);
+    const int cs = from_i ? pk + 1 : dK + 1, ce = from_i ? re : ke;
+    const int ss_ = from_i ? dK + 1 : pk + 1, se = from_i ? ke : re;
+    for (int c0 = cs; c0 < ce; c0 += BS) {
+      int pc = c0 + r, other = -1;
+      if (pc < ce) other = find_in_row(col, ss_, se, __ldg(col + pc));
+      unsigned found = (__ballot_sync(gmask, other >= 0) >> gb) & ((1u << BS) - 1u);
+      while (found) {
+        const int bit = __ffs(found) - 1;
+        found &= found - 1;
+        const int o = __shfl_sync(gmask, other, gb + bit);
+        const int pj = from_i ? c0 + bit : o, pos = from_i ? o : c0 + bit;
+        double* Aij = val + (long long)pj * BS2 + r * BS;
+        const double* Ukj = val + (long long)pos * BS2;
+#pragma unroll
+        for (int c = 0; c < BS; ++c) {
+          double v = Aij[c];
+#pragma unroll
+          for (int k = 0; k < BS; ++k) v -= a[k] * __ldcg(Ukj + k * BS + c);
+          Aij[c] = v;
+        }
+      }
+    }
+  }
+  __syncwarp(gmask);
+  // diagonal block: lane c = r owns column c
+  double* D = val + (long long)dI * BS2;
+  double dc[BS];
+#pragma unroll
+  for (int q = 0; q < BS; ++q) dc[q] = D[q * BS + r];
+#pragma unroll
+  for (int q = 1; q < BS; ++q) {
+#pragma unroll
+    for (int k = 0; k < q; ++k) {
+      double lk = dc[q] / dc[k];  // meaningful on lane k
+      double l = __shfl_sync(gmask, lk, gb + k);
+      if (r == k) dc[q] = l;
+      else if (r > k) dc[q] -= l * dc[k];
+    }
+  }
+  double piv = dc[0];  // this lane's diagonal element of U_II
+#pragma unroll
+  for (int q = 1; q < BS; ++q)
+    if (q == r) piv = dc[q];
+  if (piv == 0.0) atomicMin(ss.zp, I);
+#pragma unroll
+  for (int q = 0; q < BS; ++q) D[q * BS + r] = dc[q];
+  __syncwarp(gmask);
+  // U blocks right of the diagonal: U_IJ = L_II^-1 A_IJ, lane per column
+  for (int pj = dI + 1; pj < re; ++pj) {
+    double* U = val + (long long)pj * BS2;
+    double u[BS];
+#pragma unroll
+    for (int q = 0; q < BS; ++q) u[q] = U[q * BS + r];
+#pragma unroll
+    for (int q = 1; q < BS; ++q)
+#pragma unroll
+      for (int k = 0; k < q; ++k) u[q] -= D[q * BS + k] * u[k];
+#pragma unroll
+    for (int q = 1; q < BS; ++q) U[q * BS + r] = u[q];
   }
 }
 
 template <int BS>
-__global__ void __launch_bounds__(kLvlThreads) k_bilu0_levels(
+__global__ void __launch_bounds__(kLvlThreads, 2) k_bilu0_levels(
     const int* __restrict__ row, const int* __restrict__ col, const int* __restrict__ diag,
     double* val, const int* __restrict__ order, const int* __restrict__ lvl_ptr,
     const int* __restrict__ nlev_p, SyncState ss, GridSync gs) {
+  constexpr int G = 32 / BS;
   unsigned gen = threadIdx.x == 0 ? ld_relaxed_u(gs.gen) : 0u;
+  const int lane = threadIdx.x & 31, g = lane / BS, r = lane - g * BS, gb = g * BS;
+  const unsigned gmask = g < G ? (((1u << BS) - 1u) << gb) : 0u;
   const int warp = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int nw = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+  const long long ngrp = (long long)nw * G;
+  const long long mygrp = (long long)warp * G + g;
   const int nlev = __ldg(nlev_p);
   for (int l = 0; l < nlev; ++l) {
-    int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
-    for (int t = s + warp; t < e; t += nw)
-      bilu0_row<BS, false>(__ldg(order + t), row, col, diag, val, ss);
+    const int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
+    if (g < G)
+      for (long long t = s + mygrp; t < e; t += ngrp)
+        bilu0_grow<BS>(__ldg(order + t), row, col, diag, val, ss, gmask, r, gb);
     if (l + 1 < nlev && !grid_sync(gs, gen, NoOp{})) return;
   }
 }
+
 
 int occupancy_grid(const void* fn, int threads) {
   static int sms = 0;
@@ -796,16 +846,6 @@ int build_order(int nb, const int* row, const int* col, const int* diag, int low
   BILU_LAUNCH_CHECK();
   BILU_TRY(scan_exclusive(cnt, cnt, nb, nullptr, ws, st));
   k_level_scatter<<<ceil_div(nb, 256), 256, 0, st>>>(nb, level, cnt, order);
-  BILU_LAUNCH_CHECK();
-  return BILU_OK;
-}
-
-template <int BS>
-int launch_bilu0(int nb, const int* row, const int* col, const int* diag, double* val,
-                 SyncState ss, cudaStream_t st) {
-  int grid = occupancy_grid((const void*)k_bilu0<BS>, 128);
-  grid = std::min<long long>(grid, (nb + 3) / 4 + 1);
-  k_bilu0<BS><<<grid, 128, 0, st>>>(nb, row, col, diag, val, ss);
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }
@@ -911,9 +951,9 @@ int launch_sptrsv_levels(int nb, const int* row, const int* col, const int* diag
                                  : (const void*)k_sptrsv_levels<BS, true, false>)
                          : (unit ? (const void*)k_sptrsv_levels<BS, false, true>
                                  : (const void*)k_sptrsv_levels<BS, false, false>);
-  // no more warps than rows; fewer CTAs make the barrier cheaper
+  // no more lane groups than rows; fewer CTAs make the barrier cheaper
   int grid = std::min<long long>(coop_grid(fn, kLvlThreads),
-                                 ceil_div(nb, kLvlThreads / 32));
+                                 ceil_div(nb, (kLvlThreads / 32) * (32 / BS)));
   (void)nlev;
   void* args[] = {&row, &col, &diag, &val, &b, &x, &order, &lvl_ptr, &nlev_d, &ss, &gs};
   return launch_coop(fn, grid, kLvlThreads, args, st);
@@ -924,7 +964,8 @@ int launch_bilu0_levels(int nb, const int* row, const int* col, const int* diag,
                         const int* order, const int* lvl_ptr, const int* nlev_d, SyncState ss,
                         GridSync gs, cudaStream_t st) {
   const void* fn = (const void*)k_bilu0_levels<BS>;
-  int grid = std::min<long long>(coop_grid(fn, kLvlThreads), ceil_div(nb, kLvlThreads / 32));
+  int grid = std::min<long long>(coop_grid(fn, kLvlThreads),
+                                 ceil_div(nb, (kLvlThreads / 32) * (32 / BS)));
   void* args[] = {&row, &col, &diag, &val, &order, &lvl_ptr, &nlev_d, &ss, &gs};
   return launch_coop(fn, grid, kLvlThreads, args, st);
 }

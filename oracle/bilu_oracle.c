@@ -152,6 +152,39 @@ int orc_isai_pattern_fill(int nb, const int* Arow, const int* Acol, int lower,
   return ORC_OK;
 }
 
+/* Symbolic product C = pattern(X A) (ISAI(k) patterns; no counterpart in
+ * the reference): row i of C is the sorted union of the rows of A named by
+ * row i of X.  Ccol == NULL: counts only (Crow[nb] = nnz). */
+int orc_pattern_product(int nb, const int* Xrow, const int* Xcol, const int* Arow,
+                        const int* Acol, int* Crow, int* Ccol) {
+  int cap = 64;
+  int* buf = (int*)malloc(sizeof(int) * (size_t)cap);
+  Crow[0] = 0;
+  for (int i = 0; i < nb; ++i) {
+    int m = 0;
+    for (int p = Xrow[i]; p < Xrow[i + 1]; ++p) {
+      int c = Xcol[p];
+      for (int q = Arow[c]; q < Arow[c + 1]; ++q) {
+        if (m == cap) {
+          cap *= 2;
+          buf = (int*)realloc(buf, sizeof(int) * (size_t)cap);
+        }
+        buf[m++] = Acol[q];
+      }
+    }
+    qsort(buf, (size_t)m, sizeof(int), cmp_int);
+    int u = 0;
+    for (int t = 0; t < m; ++t)
+      if (t == 0 || buf[t] != buf[t - 1]) {
+        if (Ccol) Ccol[Crow[i] + u] = buf[t];
+        ++u;
+      }
+    Crow[i + 1] = Crow[i] + u;
+  }
+  free(buf);
+  return ORC_OK;
+}
+
 /* bcsc2bcsr.h:11-30 */
 int orc_tri_pattern_count(int nb, const int* Arow, const int* Acol, int lower,
                           int* Trow) {

@@ -44,6 +44,11 @@ int orc_isai_pattern_count(int nb, const int* Arow, const int* Acol, int lower,
 int orc_isai_pattern_fill(int nb, const int* Arow, const int* Acol, int lower,
                           const int* Mptr, int* Mind);
 
+/* Symbolic product C = pattern(X A), rows sorted and distinct (ISAI(k));
+ * Ccol == NULL counts only. */
+int orc_pattern_product(int nb, const int* Xrow, const int* Xcol, const int* Arow,
+                        const int* Acol, int* Crow, int* Ccol);
+
 /* bcsc2bcsr.h:11-30 */
 int orc_tri_pattern_count(int nb, const int* Arow, const int* Acol, int lower,
                           int* Trow /* nb+1 */);

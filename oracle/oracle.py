@@ -100,6 +100,27 @@ def isai_pattern(nb, Arow, Acol, lower):
     return mp, mi
 
 
+def pattern_product(nb, Xrow, Xcol, Arow, Acol):
+    """Symbolic C = pattern(X A), rows sorted and distinct -> (Crow, Ccol)."""
+    Xrow, Xcol, Arow, Acol = _i(Xrow), _i(Xcol), _i(Arow), _i(Acol)
+    cr = np.zeros(nb + 1, np.int32)
+    f = lib().orc_pattern_product
+    f.restype = ctypes.c_int
+    _chk("pattern_product", f(nb, _ptr(Xrow), _ptr(Xcol), _ptr(Arow), _ptr(Acol), _ptr(cr), None))
+    cc = np.zeros(int(cr[-1]), np.int32)
+    _chk("pattern_product", f(nb, _ptr(Xrow), _ptr(Xcol), _ptr(Arow), _ptr(Acol), _ptr(cr),
+                              _ptr(cc)))
+    return cr, cc
+
+
+def pattern_power(nb, Arow, Acol, k):
+    """pattern(A^k) as (rowptr, colind) (k = 1: A's own pattern)."""
+    pr, pc = _i(Arow), _i(Acol)
+    for _ in range(k - 1):
+        pr, pc = pattern_product(nb, pr, pc, Arow, Acol)
+    return pr, pc
+
+
 def tri_pattern(nb, Arow, Acol, lower):
     """bcsc2bcsr.h:11 build_triangular_bcsr_pattern_from_A -> (Trow, Tcol)."""
     Arow, Acol = _i(Arow), _i(Acol)
@@ -271,15 +292,17 @@ def gmres(A, L, U, b, precond=1, restart=30, tol=1e-10, maxit=3000):
     return x, it.value, rr.value, hist[: it.value + 1], st
 
 
-def isai_setup(A):
+def isai_setup(A, level=1):
     """Full oracle setup on a BSRMatrix: BILU(0), patterns, pairs, Dinv,
-    ISAI-L/U and BCSR reorder.  Returns a dict of every intermediate."""
+    ISAI-L/U and BCSR reorder.  level k > 1: ISAI(k), the M patterns taken
+    from pattern(A^k).  Returns a dict of every intermediate."""
     nb, bs = A.nb, A.bs
     LU, zp = bsrilu0(nb, bs, A.rowptr, A.colind, A.val)
     out = {"LU": LU, "zero_pivot": zp}
+    Pr, Pc = pattern_power(nb, A.rowptr, A.colind, level)
     for lower, tag in ((True, "L"), (False, "U")):
-        mp, mi = isai_pattern(nb, A.rowptr, A.colind, lower)
-        tr, tc = tri_pattern(nb, A.rowptr, A.colind, lower)
+        mp, mi = isai_pattern(nb, Pr, Pc, lower)
+        tr, tc = tri_pattern(nb, Pr, Pc, lower)
         mp_map = map_bcsc2bcsr(nb, mp, mi, tr, tc)
         D = dinv(nb, bs, A.rowptr, A.colind, LU, lower)
         if lower:

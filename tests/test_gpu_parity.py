@@ -477,6 +477,51 @@ def test_gmres_exact_ilu_and_switch(cuda, orc, name):
     q.close()
 
 
+@pytest.mark.parametrize("name,level", [("c2_s6", 2), ("c2_s6", 3), ("c1_s16", 2),
+                                        ("c3_nb200", 2), ("bs5_s7", 2)])
+def test_isai_level_k(cuda, orc, name, level):
+    """ISAI(k): pattern(A^k) by the symbolic product kernel equals the
+    oracle's bit for bit; the engine's M_L / M_U (patterns bit-exact, values
+    within 1e-12) equal the oracle's ISAI(k); FP64 GMRES takes the oracle's
+    iteration count."""
+    from isai_kernel_gb300 import api
+
+    A = mats()[name]
+    row, col = T(A.rowptr, cuda), T(A.colind, cuda)
+    pr, pc = row, col
+    for _ in range(level - 1):
+        pr, pc = api.pattern_product(A.nb, pr, pc, row, col)
+    opr, opc = orc.pattern_power(A.nb, A.rowptr, A.colind, level)
+    assert np.array_equal(N(pr), opr) and np.array_equal(N(pc), opc)
+    S = orc.isai_setup(A, level=level)
+    p = api.Preconditioner(A.nb, A.bs, row, col, T(A.val, cuda), isai_level=level)
+    lu, Lf, Uf = p.factors()
+    assert np.array_equal(N(Lf[0]), S["TrowL"]) and np.array_equal(N(Lf[1]), S["TcolL"])
+    assert np.array_equal(N(Uf[0]), S["TrowU"]) and np.array_equal(N(Uf[1]), S["TcolU"])
+    assert relerr(N(Lf[2]), S["McsrL"]) < 1e-12 and relerr(N(Uf[2]), S["McsrU"]) < 1e-12
+    b = gen.rhs(A.n, 0)
+    _, ito, _, _, st = orc.gmres((A.rowptr, A.colind, A.val), (S["TrowL"], S["TcolL"], S["McsrL"]),
+                                 (S["TrowU"], S["TcolU"], S["McsrU"]), b, precond=1, maxit=3000)
+    assert st == 0
+    x, res = p.solve(T(b, cuda), prec=0, maxit=3000)
+    assert res.converged and res.iters == ito
+    p.close()
+
+
+def test_pattern_product_too_dense_is_reported(cuda):
+    """A row of pattern(A^3) of the power-law system gathers more than 1024
+    candidate columns: the kernel reports BILU_ERR_UNSUPPORTED (no
+    truncation)."""
+    from isai_kernel_gb300 import api
+
+    A = mats()["c3_nb200"]
+    row, col = T(A.rowptr, cuda), T(A.colind, cuda)
+    p2, c2 = api.pattern_product(A.nb, row, col, row, col)
+    with pytest.raises(api.BiluError) as e:
+        api.pattern_product(A.nb, p2, c2, row, col)
+    assert e.value.status == -8
+
+
 def test_solve_host_end_to_end(cuda, orc):
     from isai_kernel_gb300 import api
 
