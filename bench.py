@@ -124,6 +124,27 @@ def apply_bytes(nb, bs, nnzL, nnzU, s_val, s_tmp):
     return (nnzL + nnzU) * (bs * bs * s_val + 4) + 2 * (nb + 1) * 4 + n * (8 + 2 * s_tmp + 8)
 
 
+def apply_bytes_staged(nb, bs, nnzL, nnzU):
+    """Algorithmic bytes of the FP32 apply as the solver runs it (input is
+    the FP32 copy of the basis vector written by the normalisation): FP32
+    values + column indices, row pointers, read x32, write and read y32,
+    write z (FP64)."""
+    n = nb * bs
+    return (nnzL + nnzU) * (bs * bs * 4 + 4) + 2 * (nb + 1) * 4 + n * (4 + 2 * 4 + 8)
+
+
+def measured_traffic(side):
+    """DRAM bytes per FP32 apply from the committed ncu summary of the same
+    workload (profiles/roofline_traffic.json), or None."""
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if not os.path.exists(p):
+        return None, None
+    d = json.load(open(p))
+    if d.get("side") != side:
+        return None, None
+    return float(d["dram_bytes_per_apply"]), d.get("source")
+
+
 def spmv_bytes(nb, bs, nnzb):
     n = nb * bs
     return nnzb * (bs * bs * 8 + 4) + (nb + 1) * 4 + 2 * n * 8
@@ -283,6 +304,22 @@ def run_ours(args):
     e1.synchronize()
     t_f32i = e0.elapsed_time(e1) / 1e3
 
+    # exact BILU(0) preconditioner (two level-scheduled triangular solves
+    # per apply), FP64: reported beside the ISAI paths
+    Pi = api.Preconditioner(nb, bs, row, col, val, fp32=False, ilu=True)
+    xi = torch.empty_like(b)
+    _, ri = Pi.solve(b, xi, prec=api.BILU_ILU, restart=args.restart, tol=args.tol,
+                     maxit=args.maxit)
+    e0.record(stream)
+    _, ri = Pi.solve(b, xi, prec=api.BILU_ILU, restart=args.restart, tol=args.tol,
+                     maxit=args.maxit)
+    e1.record(stream)
+    e1.synchronize()
+    t_ilu = e0.elapsed_time(e1) / 1e3
+    ilu_setup = Pi.setup_ms["total"]
+    Pi.close()
+    del Pi, xi
+
     # preconditioner apply kernels, timed alone with CUDA events on the
     # launching stream (inputs: 1.1-1.9 GB of factors, larger than L2)
     lu, Lf, Uf = P.factors()
@@ -304,13 +341,28 @@ def run_ours(args):
     t_apply64 = time_it(lambda: api.isai_apply(nb, bs, Lf, Uf, b, prec=0), reps)
     t_apply32 = time_it(lambda: api.isai_apply(nb, bs, (Lf[0], Lf[1], L32), (Uf[0], Uf[1], U32),
                                                b, prec=1), reps)
+    # the apply as the solver launches it: two k_bsr_spmv, FP32 input and
+    # intermediate, FP64 output
+    b32 = b.float()
+    y32 = torch.empty(n, dtype=torch.float32, device=dev)
+    z = torch.empty_like(b)
+
+    def apply_staged():
+        L.bilu_bcsr_spmv_f32(nb, bs, api._p(Lf[0]), api._p(Lf[1]), api._p(L32), api._p(b32), 1,
+                             api._p(y32), 1, api._s())
+        L.bilu_bcsr_spmv_f32(nb, bs, api._p(Uf[0]), api._p(Uf[1]), api._p(U32), api._p(y32), 1,
+                             api._p(z), 0, api._s())
+    t_apply32s = time_it(apply_staged, reps)
     y = torch.empty_like(b)
     t_spmvA = time_it(lambda: api.bcsr_spmv(nb, bs, row, col, val, b, y), reps)
     B64 = apply_bytes(nb, bs, nnzL, nnzU, 8, 8)
     B32 = apply_bytes(nb, bs, nnzL, nnzU, 4, 4)
     BA = spmv_bytes(nb, bs, nnzb)
+    B32s = apply_bytes_staged(nb, bs, nnzL, nnzU)
     peak, peak_kind = peaks()
     gbs32 = B32 / t_apply32 / 1e9
+    gbs32s = B32s / t_apply32s / 1e9
+    traffic, traffic_src = measured_traffic(args.side)
     rates = (ctypes.c_double * 3)()
     _lib.check("bilu_probe_rates", L.bilu_probe_rates(rates))
     dfma_tf = rates[0]
@@ -367,17 +419,25 @@ def run_ours(args):
         "restart_cycles": {"mixed": restarts_mixed, "fp64": r64.restarts},
         "relres": {"mixed": relres_mixed, "fp64": r64.relres},
         "fp64_solve_s": t_fp64, "speedup_mixed_vs_fp64": t_fp64 / t_mixed,
+        "exact_ilu": {"s": t_ilu, "iters": ri.iters, "relres": ri.relres,
+                      "setup_ms": ilu_setup, "speedup_vs_fp64_isai": t_fp64 / t_ilu,
+                      "what": "FP64 FGMRES(30) with the exact BILU(0) applied by two "
+                              "level-scheduled block triangular solves"},
         "fp32_inner": {"s": t_f32i, "iters": r32i.iters, "relres": r32i.relres,
                        "restart_cycles": r32i.restarts, "speedup_vs_fp64": t_fp64 / t_f32i,
                        "what": "FP32 ISAI + FP32-stored A in the Arnoldi products; FP64 "
                                "orthogonalisation, true residual and restarts"},
         "setup_ms": setup_ms,
         "apply": {"fp32_s": t_apply32, "fp64_s": t_apply64, "fp32_GBs": gbs32,
+                  "fp32_solver_s": t_apply32s, "fp32_solver_GBs": gbs32s,
                   "fp64_GBs": B64 / t_apply64 / 1e9, "bytes_fp32": B32, "bytes_fp64": B64,
                   "A_spmv_s": t_spmvA, "A_spmv_GBs": BA / t_spmvA / 1e9},
-        "roofline": {"bound": "hbm", "achieved": gbs32, "peak": peak, "unit": "GB/s",
-                     "frac": gbs32 / peak, "traffic": None,
-                     "kernel": "FP32-stored ISAI apply (k_bsr_spmv x2)",
+        "roofline": {"bound": "hbm", "achieved": gbs32s, "peak": peak, "unit": "GB/s",
+                     "frac": gbs32s / peak, "traffic": traffic,
+                     "algorithmic_bytes": B32s, "duration_s": t_apply32s,
+                     "kernel": "FP32-stored ISAI apply as run in the solver (k_bsr_spmv x2: "
+                               "M_L on the FP32 basis vector, M_U to FP64)",
+                     "traffic_source": traffic_src,
                      "peak_source": f"{peak_kind} hbm_gbs"},
         "fp64_compute_roofline": {
             "dfma_tflops": dfma_tf, "dmma_tflops": rates[1], "ffma_tflops": rates[2],
@@ -504,7 +564,13 @@ def run_sptrsv(args):
         e1.record()
         e1.synchronize()
         out[f"{tag}_analysis_ms"] = e0.elapsed_time(e1)
-        for fn, name in (("bilu_sptrsv_solve", "level"), ("bilu_sptrsv_solve_syncfree", "syncfree")):
+        words = info.view(torch.int32).cpu().numpy()
+        carve = lambda k: ((k * 4 + 255) // 256) * 64
+        o_nlev = 2 * carve(nb + 1) + carve(nb + 2)
+        out[f"{tag}_levels"] = int(words[o_nlev])
+        out[f"{tag}_recommended"] = "syncfree" if int(words[o_nlev + 2]) == 1 else "level"
+        for fn, name in (("bilu_sptrsv_solve_level", "level"),
+                         ("bilu_sptrsv_solve_syncfree", "syncfree")):
             def solve():
                 api.call(fn, nb, bs, P(row), P(col), P(lu), lower, lower, P(info), P(b), P(x),
                          P(ws), ws.numel(), api._s())

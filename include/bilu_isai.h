@@ -143,10 +143,13 @@ int bilu_bcsc_to_bcsr(int mb, int nbcol, int bs, const int* d_cscPtr, const int*
 /* ------------------------------------------------------------------ */
 
 /* Replaces bsrilu02_inplace (bsrilu.h:20; cuSPARSE bsrilu02, row direction,
- * no level information): BILU(0) in place, scheduled by dependency level
- * (level analysis of the lower DAG, then one cooperative launch with a
- * bounded grid barrier per level).  h_info[0] receives the first block row
- * with a zero pivot (or -1); BILU_ERR_ZERO_PIVOT then. */
+ * no level information): BILU(0) in place.  A level analysis of the lower
+ * DAG picks the schedule: wide levels and short rows -> one cooperative
+ * launch with a bounded grid barrier per level (a bs-lane group per row);
+ * narrow levels or rows with more than 32 dependencies -> sync-free (warp
+ * per row, atomic tickets in level order, bounded waits on ready flags).
+ * h_info[0] receives the first block row with a zero pivot (or -1);
+ * BILU_ERR_ZERO_PIVOT then. */
 size_t bilu_bsrilu0_ws_bytes(int nb, int nnzb);
 int bilu_bsrilu0(int nb, int nnzb, int bs, const int* d_row, const int* d_col, double* d_val,
                  int* h_info, void* d_ws, size_t ws_bytes, bilu_stream_t stream);
@@ -220,8 +223,7 @@ int bilu_isai_apply(int nb, int bs, int prec, const int* d_Lrow, const int* d_Lc
 /* Replaces spTrSolveL / spTrSolveU (cape_sptrsv.h:8,55) and
  * csr_cape_SpTRSV (cape_sptrsv.h:105), blockwise on the packed BILU(0):
  * lower: unit-lower L x = b; upper: U x = b.  One-shot form: level analysis
- * then the level-scheduled solve (warp per block row, one bounded grid
- * barrier per dependency level). */
+ * then the schedule it recommends (see the analysis / solve split below). */
 size_t bilu_sptrsv_ws_bytes(int nb, int nnzb);
 int bilu_sptrsv(int nb, int nnzb, int bs, const int* d_row, const int* d_col, const double* d_val,
                 int lower, const double* d_b, double* d_x, void* d_ws, size_t ws_bytes,
@@ -230,11 +232,15 @@ int bilu_sptrsv(int nb, int nnzb, int bs, const int* d_row, const int* d_col, co
  * BILU_cusparse.h:203-220): the analysis (diagonal positions, dependency
  * levels and the rows in level order; bilu_sptrsv_analysis_bytes(nb) bytes
  * in d_info, scratch bilu_sptrsv_analysis_ws_bytes) is computed once per
- * pattern and triangle.  bilu_sptrsv_solve then runs the level-scheduled
- * kernel; bilu_sptrsv_solve_syncfree runs the sync-free kernel of the
- * reference's design on the same analysis (block rows taken by atomic
- * tickets in level order, per-row ready flags polled by the dependent rows,
- * every wait bounded: BILU_ERR_TIMEOUT).  Both give identical x. */
+ * pattern and triangle, together with a schedule recommendation: the level
+ * schedule when a level holds at least 1024 block rows on average and no
+ * row has more than 32 dependencies, the sync-free schedule otherwise.  bilu_sptrsv_solve runs the recommended
+ * schedule; bilu_sptrsv_solve_level forces the level-scheduled kernel (one
+ * cooperative launch, a bounded grid barrier per level);
+ * bilu_sptrsv_solve_syncfree forces the sync-free kernel of the reference's
+ * design (block rows taken by atomic tickets in level order, per-row ready
+ * flags polled by the dependent rows, every wait bounded:
+ * BILU_ERR_TIMEOUT).  All give identical x. */
 size_t bilu_sptrsv_analysis_bytes(int nb);
 size_t bilu_sptrsv_analysis_ws_bytes(int nb, int nnzb);
 size_t bilu_sptrsv_solve_ws_bytes(int nb);
@@ -243,6 +249,10 @@ int bilu_sptrsv_analysis(int nb, int nnzb, int bs, const int* d_row, const int* 
 int bilu_sptrsv_solve(int nb, int bs, const int* d_row, const int* d_col, const double* d_val,
                       int lower, int unit, const void* d_info, const double* d_b, double* d_x,
                       void* d_ws, size_t ws_bytes, bilu_stream_t stream);
+int bilu_sptrsv_solve_level(int nb, int bs, const int* d_row, const int* d_col,
+                            const double* d_val, int lower, int unit, const void* d_info,
+                            const double* d_b, double* d_x, void* d_ws, size_t ws_bytes,
+                            bilu_stream_t stream);
 int bilu_sptrsv_solve_syncfree(int nb, int bs, const int* d_row, const int* d_col,
                                const double* d_val, int lower, int unit, const void* d_info,
                                const double* d_b, double* d_x, void* d_ws, size_t ws_bytes,

@@ -45,7 +45,11 @@ int pattern_product_fill(int n, const int* Xrow, const int* Xcol, const int* Aro
                          cudaStream_t st);
 int level_analysis(int nb, long long nnzb, const int* row, const int* col, const int* diag,
                    int lower, int* order, int* lvl, int* nlev_d, int* h_nlev, Carver& ws,
-                   cudaStream_t st);
+                   cudaStream_t st, int* h_sched);
+int sptrsv_syncfree_async(int nb, int bs, const int* row, const int* col, const int* diag,
+                          const int* order, const double* val, int lower, int unit,
+                          const double* b, double* x, int* flags, int* ticket, int* err,
+                          cudaStream_t st);
 int sptrsv_levels_async(int nb, int bs, const int* row, const int* col, const int* diag,
                         const int* order, const int* lvl, const int* nlev_d, const double* val,
                         int lower, int unit, const double* b, double* x, unsigned* words,
@@ -102,6 +106,8 @@ struct bilu_ctx {
   int *ordU = nullptr, *lvlU = nullptr, *nlevU = nullptr;
   unsigned* ilu_words = nullptr;
   int nlev_host[2] = {0, 0};
+  int ilu_sched[2] = {0, 0};    // per triangle: 0 level schedule, 1 sync-free
+  int* ilu_flags = nullptr;     // ready flags + ticket of the sync-free solves
   // solver buffers
   int m_alloc = 0;
   long long ldv = 0;  // stride of the basis vectors in V and Z (n rounded up to 32)
@@ -122,6 +128,7 @@ struct bilu_ctx {
     Lval32 = Uval32 = nullptr;
     Aval32 = nullptr;
     ordL = lvlL = nlevL = ordU = lvlU = nlevU = nullptr;
+    ilu_flags = nullptr;
     Prow = Pcol = nullptr;
     ilu_words = nullptr;
     ready = false;
@@ -357,11 +364,12 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
           **nl = lower ? &c->nlevL : &c->nlevU;
       BILU_TRY(c->alloc(ord, (size_t)nb + 1));
       BILU_TRY(c->alloc(lvl, (size_t)nb + 2));
-      BILU_TRY(c->alloc(nl, 2));
+      BILU_TRY(c->alloc(nl, 4));
       Carver w2 = ws;
       BILU_TRY(level_analysis(nb, nnzb, c->Arow, c->Acol, c->diag, lower, *ord, *lvl, *nl,
-                              &c->nlev_host[lower ? 0 : 1], w2, st));
+                              &c->nlev_host[lower ? 0 : 1], w2, st, &c->ilu_sched[lower ? 0 : 1]));
     }
+    BILU_TRY(c->alloc(&c->ilu_flags, (size_t)nb + 2));
     BILU_TRY(c->alloc(&c->ilu_words, 4));
     BILU_TRY_CUDA(cudaMemsetAsync(c->ilu_words, 0, sizeof(unsigned) * 4, st));
   }
@@ -445,11 +453,22 @@ int norm2(bilu_ctx* c, const double* v, double* dslot, double* host) {
 
 int apply_prec(bilu_ctx* c, int prec, const double* v, double* z) {
   if (prec == BILU_ILU) {
-    // z = U^-1 (L^-1 v): unit-lower then upper solve on the packed factor
-    BILU_TRY(sptrsv_levels_async(c->nb, c->bs, c->Arow, c->Acol, c->diag, c->ordL, c->lvlL,
-                                 c->nlevL, c->LU, 1, 1, v, c->tmp, c->ilu_words, c->st));
-    return sptrsv_levels_async(c->nb, c->bs, c->Arow, c->Acol, c->diag, c->ordU, c->lvlU,
-                               c->nlevU, c->LU, 0, 0, c->tmp, z, c->ilu_words, c->st);
+    // z = U^-1 (L^-1 v): unit-lower then upper solve on the packed factor,
+    // each with the schedule its level analysis recommends
+    for (int lower = 1; lower >= 0; --lower) {
+      const double* in = lower ? v : c->tmp;
+      double* out = lower ? c->tmp : z;
+      const int* ord = lower ? c->ordL : c->ordU;
+      if (c->ilu_sched[lower ? 0 : 1] == 1)
+        BILU_TRY(sptrsv_syncfree_async(c->nb, c->bs, c->Arow, c->Acol, c->diag, ord, c->LU,
+                                       lower, lower, in, out, c->ilu_flags,
+                                       c->ilu_flags + c->nb + 1, (int*)c->ilu_words + 2, c->st));
+      else
+        BILU_TRY(sptrsv_levels_async(c->nb, c->bs, c->Arow, c->Acol, c->diag, ord,
+                                     lower ? c->lvlL : c->lvlU, lower ? c->nlevL : c->nlevU,
+                                     c->LU, lower, lower, in, out, c->ilu_words, c->st));
+    }
+    return BILU_OK;
   }
   if (prec < 0) {
     BILU_TRY_CUDA(cudaMemcpyAsync(z, v, sizeof(double) * c->n, cudaMemcpyDeviceToDevice, c->st));

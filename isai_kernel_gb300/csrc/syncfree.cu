@@ -58,6 +58,25 @@ __device__ __forceinline__ void fence_acquire() {
   asm volatile("fence.acq_rel.gpu;" ::: "memory");
 }
 
+// Warp-wide wait until flags[K] != 0.  Returns false if the launch aborted.
+__device__ __forceinline__ bool warp_wait(const int* flag, int* err, long long spin) {
+  long long n = 0;
+  unsigned ns = 32;
+  while (true) {
+    int v = ld_relaxed(flag);
+    if (__all_sync(FULL, v != 0)) {
+      fence_acquire();
+      return true;
+    }
+    if (__any_sync(FULL, ld_relaxed(err) != 0)) return false;
+    if (++n > spin) {
+      if ((threadIdx.x & 31) == 0) atomicCAS(err, 0, (int)BILU_ERR_TIMEOUT);
+      return false;
+    }
+    backoff(ns);
+  }
+}
+
 // Single-lane wait (lanes of a warp may wait on different rows).
 __device__ __forceinline__ bool lane_wait(const int* flag, int* err, long long spin) {
   long long n = 0;
@@ -457,11 +476,12 @@ struct NoOp {
 // columns in (diag[I], row[I+1]).  cnt[K] += 1 per dependent of K.
 __global__ void k_dep_count(int nb, const int* __restrict__ row, const int* __restrict__ col,
                             const int* __restrict__ diag, int lower, int* __restrict__ cnt,
-                            int* __restrict__ indeg) {
+                            int* __restrict__ indeg, int* maxdeg) {
   int I = blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= nb) return;
   int ps = lower ? row[I] : diag[I] + 1, pe = lower ? diag[I] : row[I + 1];
   indeg[I] = pe - ps;
+  if (pe - ps > 0) atomicMax(maxdeg, pe - ps);
   for (int p = ps; p < pe; ++p) atomicAdd(cnt + col[p], 1);
 }
 
@@ -514,6 +534,13 @@ __global__ void __launch_bounds__(256) k_bfs_levels(int nb, const int* __restric
 }
 
 constexpr int kLvlThreads = 256;
+// rows with more dependencies than this make the level kernels give each
+// row a whole warp instead of a bs-lane group
+constexpr int kLongRow = 32;
+// level analysis recommendation: the level schedule when a level holds at
+// least this many rows on average, the sync-free schedule otherwise (a
+// level costs a grid barrier; narrow levels are cheaper without one)
+constexpr int kMinLevelWidth = 1024;
 
 // Level-scheduled solve with a group of BS lanes per block row (32/BS rows
 // per warp; lane r of a group owns scalar row r).  On GB300 an FP64 warp
@@ -621,6 +648,31 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_sptrsv_levels(
   const long long mygrp = (long long)warp * G + g;  // groups g >= G (bs 5: lanes 30, 31) idle
   const int nlev = __ldg(nlev_p);
   if (nlev <= 0) return;
+  if (__ldg(nlev_p + 1) > kLongRow) {
+    // long rows (nlev_p[1] = the largest dependency count): a warp per row
+    RowPre<BS> wp;
+    {
+      int t = __ldg(lvl_ptr) + warp;
+      sptrsv_prefetch<BS, LOWER, UNIT>(t < __ldg(lvl_ptr + 1) ? __ldg(order + t) : -1, row, col,
+                                       diag, val, b, wp);
+    }
+    for (int l = 0; l < nlev; ++l) {
+      const int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
+      if (wp.I >= 0) sptrsv_finish<BS, LOWER, UNIT, false, false>(wp, col, val, x, ss);
+      for (int t = s + warp + nw; t < e; t += nw) {
+        RowPre<BS> q;
+        sptrsv_prefetch<BS, LOWER, UNIT>(__ldg(order + t), row, col, diag, val, b, q);
+        sptrsv_finish<BS, LOWER, UNIT, false, false>(q, col, val, x, ss);
+      }
+      if (l + 1 < nlev) {
+        int t = e + warp;
+        sptrsv_prefetch<BS, LOWER, UNIT>(t < __ldg(lvl_ptr + l + 2) ? __ldg(order + t) : -1, row,
+                                         col, diag, val, b, wp);
+        if (!grid_sync(gs, gen, NoOp{})) return;
+      }
+    }
+    return;
+  }
   GRowPre<BS> pre;
   {
     long long t = __ldg(lvl_ptr) + mygrp;
@@ -753,6 +805,196 @@ __device__ __forceinline__ void bilu0_grow(int I, const int* __restrict__ row,
   }
 }
 
+// One block row with a whole warp (the sync-free factorisation, used for
+// matrices with long rows or narrow levels).  WAIT: the rows K it reads may
+// still be in progress and are waited for through their flags.  Phase 1 on
+// lanes r < BS (row r of L_IK), phase 2 with teams of lanes per updated
+// block, the diagonal LU with lane = column, U blocks with 32/BS blocks per
+// pass.  The same operations per element as bilu0_grow.  Returns false if
+// the launch aborted.
+// Column index p of row I (rs = first position of the row): from the
+// shared-memory copy when the row was staged there.
+__device__ __forceinline__ int row_col(const int* __restrict__ col, const int* stage, int rs,
+                                       int p) {
+  return stage ? stage[p - rs] : __ldg(col + p);
+}
+
+// Binary search for key among positions [s, e) of row I (staged or not).
+__device__ __forceinline__ int find_in_row_staged(const int* __restrict__ col, const int* stage,
+                                                  int rs, int s, int e, int key) {
+  int lo = s, hi = e - 1;
+  while (lo <= hi) {
+    int m = (lo + hi) >> 1;
+    int v = row_col(col, stage, rs, m);
+    if (v == key) return m;
+    if (v < key) lo = m + 1; else hi = m - 1;
+  }
+  return -1;
+}
+
+constexpr int kRowStage = 2048;  // column indices of a long row kept in shared memory
+
+__device__ __forceinline__ unsigned dynamic_smem_bytes() {
+  unsigned v;
+  asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(v));
+  return v;
+}
+
+template <int BS, bool WAIT>
+__device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
+                                          const int* __restrict__ col,
+                                          const int* __restrict__ diag, double* val,
+                                          const SyncState& ss, int* stage_buf) {
+  constexpr int BS2 = BS * BS;
+  constexpr int EPL = BS2 > 32 ? 2 : 1;
+  constexpr int TL = BS2 / EPL + (BS2 % EPL ? 1 : 0);
+  constexpr int TPW = 32 / TL;         // blocks updated per pass in phase 2
+  constexpr int SPAN = 32 / TPW;
+  constexpr int GU = 32 / BS;          // U blocks per pass (lane = column)
+  int lane = threadIdx.x & 31;
+  int team = lane / SPAN, tl = lane - team * SPAN;
+  bool team_on = team < TPW && tl < TL;
+  int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
+  // a hub row searches its own column list once per K: keep it in shared
+  // memory (one L2 round trip per search step otherwise)
+  const int* stage = nullptr;
+  if (stage_buf && re - rs > 64 && re - rs <= kRowStage) {
+    for (int t = lane; t < re - rs; t += 32) stage_buf[t] = __ldg(col + rs + t);
+    __syncwarp();
+    stage = stage_buf;
+  }
+  // structural data of the next K, loaded one step ahead
+  int Kn = rs < dI ? row_col(col, stage, rs, rs) : 0;
+  int dKn = rs < dI ? __ldg(diag + Kn) : 0, ken = rs < dI ? __ldg(row + Kn + 1) : 0;
+  for (int pk = rs; pk < dI; ++pk) {
+    const int K = Kn, dK = dKn, ke = ken;
+    if (pk + 1 < dI) {
+      Kn = row_col(col, stage, rs, pk + 1);
+      dKn = __ldg(diag + Kn);
+      ken = __ldg(row + Kn + 1);
+    }
+    // sync-free schedule: row K may still be in progress
+    if (WAIT && !warp_wait(ss.flags + K, ss.err, ss.spin)) return false;
+    double* L = val + (long long)pk * BS2;
+    const double* Ukk = val + (long long)dK * BS2;
+    // phase 1: lane r owns row r of A_IK
+    if (lane < BS) {
+      double a[BS];
+#pragma unroll
+      for (int c = 0; c < BS; ++c) a[c] = L[lane * BS + c];
+#pragma unroll
+      for (int k = 0; k < BS; ++k) {
+        a[k] = a[k] / __ldcg(Ukk + k * BS + k);
+#pragma unroll
+        for (int c = k + 1; c < BS; ++c) a[c] -= a[k] * __ldcg(Ukk + k * BS + c);
+      }
+#pragma unroll
+      for (int c = 0; c < BS; ++c) L[lane * BS + c] = a[c];
+    }
+    __syncwarp();
+    // phase 2: A_IJ -= L_IK U_KJ for J > K in rows I and K.  The shorter
+    // of the two column lists supplies the candidates, 32 at a time, each
+    // lane binary-searching one of them in the other list (hub rows of
+    // power-law matrices hold thousands of blocks); then the teams update
+    // the matched blocks.  Every block is updated once per K, so the
+    // update order of each element is the same either way.
+    {
+      const bool from_i = (re - pk - 1) <= (ke - dK - 1);
+      const int cs = from_i ? pk + 1 : dK + 1, ce = from_i ? re : ke;
+      const int ss_ = from_i ? dK + 1 : pk + 1, se = from_i ? ke : re;
+      for (int c0 = cs; c0 < ce; c0 += 32) {
+        int pc = c0 + lane, other = -1;
+        if (pc < ce) {
+          // candidates from row I come from the staged copy, searches in row
+          // I run on it too; row K is read from global memory
+          const int key = from_i ? row_col(col, stage, rs, pc) : __ldg(col + pc);
+          other = from_i ? find_in_row(col, ss_, se, key)
+                         : find_in_row_staged(col, stage, rs, ss_, se, key);
+        }
+        unsigned found = __ballot_sync(FULL, other >= 0);
+        while (found) {
+          // the next TPW matches go to the TPW teams
+          int src = -1;
+#pragma unroll
+          for (int t = 0; t < TPW; ++t) {
+            int bit = found ? __ffs(found) - 1 : -1;
+            if (bit >= 0) found &= found - 1;
+            if (t == team) src = bit;
+          }
+          int o = __shfl_sync(FULL, other, src < 0 ? 0 : src);
+          if (team_on && src >= 0) {
+            int pj = from_i ? c0 + src : o;
+            int pos = from_i ? o : c0 + src;
+            double* Aij = val + (long long)pj * BS2;
+            const double* Ukj = val + (long long)pos * BS2;
+#pragma unroll
+            for (int q = 0; q < EPL; ++q) {
+              int e = tl * EPL + q;
+              if (e < BS2) {
+                int r = e / BS, c = e - r * BS;
+                double v = Aij[e];
+#pragma unroll
+                for (int k = 0; k < BS; ++k) v -= L[r * BS + k] * __ldcg(Ukj + k * BS + c);
+                Aij[e] = v;
+              }
+            }
+          }
+        }
+      }
+    }
+    __syncwarp();
+  }
+  // diagonal block: lane c owns column c
+  double* D = val + (long long)dI * BS2;
+  double dc[BS];
+  if (lane < BS) {
+#pragma unroll
+    for (int r = 0; r < BS; ++r) dc[r] = D[r * BS + lane];
+  } else {
+#pragma unroll
+    for (int r = 0; r < BS; ++r) dc[r] = 1.0;
+  }
+#pragma unroll
+  for (int r = 1; r < BS; ++r) {
+#pragma unroll
+    for (int k = 0; k < r; ++k) {
+      double lk = dc[r] / dc[k];  // meaningful on lane k
+      double l = __shfl_sync(FULL, lk, k);
+      if (lane == k) dc[r] = l;
+      else if (lane > k && lane < BS) dc[r] -= l * dc[k];
+    }
+  }
+  if (lane < BS) {
+    double piv = dc[0];  // this lane's diagonal element of U_II
+#pragma unroll
+    for (int q = 1; q < BS; ++q)
+      if (q == lane) piv = dc[q];
+    if (piv == 0.0) atomicMin(ss.zp, I);
+#pragma unroll
+    for (int r = 0; r < BS; ++r) D[r * BS + lane] = dc[r];
+  }
+  __syncwarp();
+  // U blocks right of the diagonal: U_IJ = L_II^-1 A_IJ, lane per column
+  for (int pj0 = dI + 1; pj0 < re; pj0 += GU) {
+    int slot = lane / BS, c = lane - slot * BS;
+    int pj = pj0 + slot;
+    if (slot < GU && pj < re) {
+      double* U = val + (long long)pj * BS2;
+      double u[BS];
+#pragma unroll
+      for (int r = 0; r < BS; ++r) u[r] = U[r * BS + c];
+#pragma unroll
+      for (int r = 1; r < BS; ++r)
+#pragma unroll
+        for (int k = 0; k < r; ++k) u[r] -= D[r * BS + k] * u[k];
+#pragma unroll
+      for (int r = 1; r < BS; ++r) U[r * BS + c] = u[r];
+    }
+  }
+  return true;
+}
+
+
 template <int BS>
 __global__ void __launch_bounds__(kLvlThreads, 2) k_bilu0_levels(
     const int* __restrict__ row, const int* __restrict__ col, const int* __restrict__ diag,
@@ -767,6 +1009,7 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_bilu0_levels(
   const long long ngrp = (long long)nw * G;
   const long long mygrp = (long long)warp * G + g;
   const int nlev = __ldg(nlev_p);
+  // (matrices with long rows or narrow levels take the sync-free kernel)
   for (int l = 0; l < nlev; ++l) {
     const int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
     if (g < G)
@@ -777,7 +1020,7 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_bilu0_levels(
 }
 
 
-int occupancy_grid(const void* fn, int threads) {
+int occupancy_grid(const void* fn, int threads, size_t smem = 0) {
   static int sms = 0;
   if (!sms) {
     int dev = 0;
@@ -786,7 +1029,8 @@ int occupancy_grid(const void* fn, int threads) {
     if (sms <= 0) sms = 1;
   }
   int per = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0) != cudaSuccess || per < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, smem) != cudaSuccess ||
+      per < 1)
     per = 1;
   return sms * per;
 }
@@ -868,8 +1112,36 @@ int launch_sptrsv(int nb, const int* row, const int* col, const int* diag, const
   return BILU_OK;
 }
 
+// Sync-free BILU(0) (matrices with narrow levels or long rows): block rows
+// taken by atomic tickets in level order, a warp per row, bounded waits on
+// the rows it reads, the row's flag released when it is final.  Hub rows of
+// a power-law matrix then no longer hold up a whole level.
+template <int BS>
+__global__ void __launch_bounds__(kLvlThreads, 2) k_bilu0_syncfree(
+    int nb, const int* __restrict__ row, const int* __restrict__ col,
+    const int* __restrict__ diag, double* val, SyncState ss) {
+  extern __shared__ int stage_smem[];
+  const bool staged = dynamic_smem_bytes() >= (blockDim.x >> 5) * kRowStage * sizeof(int);
+  int* stage = staged ? stage_smem + (threadIdx.x >> 5) * kRowStage : nullptr;
+  const int lane = threadIdx.x & 31;
+  while (true) {
+    int t = 0;
+    if (lane == 0) t = atomicAdd(ss.ticket, 1);
+    t = __shfl_sync(FULL, t, 0);
+    if (t >= nb) return;
+    const int I = __ldg(ss.order + t);
+    if (__any_sync(FULL, ld_relaxed(ss.err) != 0)) return;
+    if (!bilu0_wrow<BS, true>(I, row, col, diag, val, ss, stage)) return;
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) st_release(ss.flags + I, 1);
+  }
+}
+
 // ---------------------------------------------------------------- level schedule (host)
-int coop_grid(const void* fn, int threads) { return occupancy_grid(fn, threads); }
+int coop_grid(const void* fn, int threads, size_t smem = 0) {
+  return occupancy_grid(fn, threads, smem);
+}
 
 // misc words of a level-scheduled launch: count, gen, err, spare
 int grid_sync_init(GridSync& gs, Carver& ws, cudaStream_t st) {
@@ -890,9 +1162,10 @@ int grid_sync_finish(const GridSync& gs, cudaStream_t st) {
   return herr;
 }
 
-int launch_coop(const void* fn, int grid, int threads, void** args, cudaStream_t st) {
+int launch_coop(const void* fn, int grid, int threads, void** args, cudaStream_t st,
+                size_t smem = 0) {
   BILU_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3((unsigned)grid), dim3((unsigned)threads),
-                                            args, 0, st));
+                                            args, smem, st));
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }
@@ -902,7 +1175,7 @@ int launch_coop(const void* fn, int grid, int threads, void** args, cudaStream_t
 // lvl_ptr[nb+2] and *nlev_d on the device; *h_nlev on the host.
 int build_levels(int nb, const int* row, const int* col, const int* diag, int lower,
                  long long ndeps_max, int* order, int* lvl_ptr, int* nlev_d, int* h_nlev,
-                 Carver& ws, cudaStream_t st) {
+                 Carver& ws, cudaStream_t st, int* h_sched = nullptr) {
   int* sptr = ws.take<int>((size_t)nb + 1);
   int* cursor = ws.take<int>((size_t)nb + 1);
   int* indeg = ws.take<int>((size_t)nb + 1);
@@ -914,13 +1187,14 @@ int build_levels(int nb, const int* row, const int* col, const int* diag, int lo
   BILU_TRY_CUDA(cudaMemsetAsync(sptr, 0, sizeof(int) * ((size_t)nb + 1), st));
   BILU_TRY_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * ((size_t)nb + 1), st));
   BILU_TRY_CUDA(cudaMemsetAsync(tail, 0, sizeof(int) * 2, st));
-  BILU_TRY_CUDA(cudaMemsetAsync(nlev_d, 0, sizeof(int), st));
+  BILU_TRY_CUDA(cudaMemsetAsync(nlev_d, 0, sizeof(int) * 4, st));
   BILU_TRY_CUDA(cudaMemsetAsync(lvl_ptr, 0, sizeof(int) * ((size_t)nb + 2), st));
   if (nb == 0) {
     if (h_nlev) *h_nlev = 0;
     return BILU_OK;
   }
-  k_dep_count<<<ceil_div(nb, 256), 256, 0, st>>>(nb, row, col, diag, lower, sptr, indeg);
+  k_dep_count<<<ceil_div(nb, 256), 256, 0, st>>>(nb, row, col, diag, lower, sptr, indeg,
+                                                  tail + 1);
   BILU_LAUNCH_CHECK();
   int total = 0;
   BILU_TRY(scan_exclusive(sptr, sptr, nb, &total, ws, st));
@@ -939,6 +1213,16 @@ int build_levels(int nb, const int* row, const int* col, const int* diag, int lo
   BILU_TRY_CUDA(cudaStreamSynchronize(st));
   if (h[1] != nb) return BILU_ERR_PATTERN;  // a row was never reached
   if (h_nlev) *h_nlev = h[0];
+  // nlev_d[1] = the largest dependency count (picks warp or group rows);
+  // nlev_d[2] = the recommended schedule (0 level, 1 sync-free)
+  BILU_TRY_CUDA(cudaMemcpyAsync(nlev_d + 1, tail + 1, sizeof(int), cudaMemcpyDeviceToDevice, st));
+  int maxdeg = 0;
+  BILU_TRY_CUDA(cudaMemcpy(&maxdeg, tail + 1, sizeof(int), cudaMemcpyDeviceToHost));
+  // level schedule only when levels are wide and no row is long: a level
+  // costs a grid barrier and waits for its slowest row
+  int sched = ((long long)nb < (long long)kMinLevelWidth * h[0] || maxdeg > kLongRow) ? 1 : 0;
+  BILU_TRY_CUDA(cudaMemcpy(nlev_d + 2, &sched, sizeof(int), cudaMemcpyHostToDevice));
+  if (h_sched) *h_sched = sched;
   return BILU_OK;
 }
 
@@ -957,6 +1241,26 @@ int launch_sptrsv_levels(int nb, const int* row, const int* col, const int* diag
   (void)nlev;
   void* args[] = {&row, &col, &diag, &val, &b, &x, &order, &lvl_ptr, &nlev_d, &ss, &gs};
   return launch_coop(fn, grid, kLvlThreads, args, st);
+}
+
+template <int BS>
+int launch_bilu0_syncfree(int nb, const int* row, const int* col, const int* diag, double* val,
+                          SyncState ss, cudaStream_t st) {
+  const void* fn = (const void*)k_bilu0_syncfree<BS>;
+  const size_t smem = (size_t)(kLvlThreads / 32) * kRowStage * sizeof(int);
+  static bool attr_set = false;
+  if (!attr_set) {
+    BILU_TRY_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+    attr_set = true;
+  }
+  // every warp resident at once is not required (tickets), but more warps
+  // than rows would only spin
+  int grid = std::min<long long>(occupancy_grid(fn, kLvlThreads, smem),
+                                 ceil_div(nb, kLvlThreads / 32));
+  k_bilu0_syncfree<BS><<<grid, kLvlThreads, smem, st>>>(nb, row, col, diag, val, ss);
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
 }
 
 template <int BS>
@@ -1031,13 +1335,22 @@ int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, c
                double* val, int* h_zp, Carver& ws, cudaStream_t st) {
   int* order = ws.take<int>((size_t)nb + 1);
   int* lvl = ws.take<int>((size_t)nb + 2);
-  int* nlev_d = ws.take<int>(2);
+  int* nlev_d = ws.take<int>(4);
   if (!order || !lvl || !nlev_d) return BILU_ERR_WORKSPACE;
-  int nlev = 0;
+  int nlev = 0, sched = 0;
   {
     Carver w2 = ws;
     BILU_TRY(build_levels(nb, row, col, diag, 1, std::max(nnzb - nb, 0ll), order, lvl, nlev_d,
-                          &nlev, w2, st));
+                          &nlev, w2, st, &sched));
+  }
+  if (sched == 1) {
+    // narrow levels or long rows: sync-free, tickets in level order
+    SyncState ss;
+    BILU_TRY(sync_init(ss, nb, ws, st));
+    ss.order = order;
+    if (nb > 0)
+      BILU_TRY(BILU_DISPATCH_BS(bs, launch_bilu0_syncfree, nb, row, col, diag, val, ss, st));
+    return sync_finish(ss, h_zp, st);
   }
   SyncState ss;
   BILU_TRY(sync_init_words(ss, ws, st));
@@ -1086,19 +1399,35 @@ int sptrsv_levels(int nb, int bs, const int* row, const int* col, const int* dia
   return grid_sync_finish(gs, st);
 }
 
-// One-shot level-scheduled solve: analysis then solve.
+// Sync-free solve on a level order (ticket order = order[]).
+int sptrsv_syncfree_ordered(int nb, int bs, const int* row, const int* col, const int* diag,
+                            const int* order, const double* val, int lower, int unit,
+                            const double* b, double* x, Carver& ws, cudaStream_t st) {
+  SyncState ss;
+  BILU_TRY(sync_init(ss, nb, ws, st));
+  ss.order = order;
+  if (nb > 0)
+    BILU_TRY(BILU_DISPATCH_BS(bs, launch_sptrsv, nb, row, col, diag, val, lower, unit, b, x, ss,
+                              st));
+  return sync_finish(ss, nullptr, st);
+}
+
+// One-shot solve: level analysis, then the schedule it recommends.
 int sptrsv_level_impl(int nb, long long nnzb, int bs, const int* row, const int* col,
                       const int* diag, const double* val, int lower, int unit, const double* b,
                       double* x, Carver& ws, cudaStream_t st) {
   int* order = ws.take<int>((size_t)nb + 1);
   int* lvl = ws.take<int>((size_t)nb + 2);
-  int* nlev_d = ws.take<int>(2);
+  int* nlev_d = ws.take<int>(4);
   if (!order || !lvl || !nlev_d) return BILU_ERR_WORKSPACE;
+  int sched = 0;
   {
     Carver w2 = ws;
     BILU_TRY(build_levels(nb, row, col, diag, lower, std::max(nnzb - nb, 0ll), order, lvl,
-                          nlev_d, nullptr, w2, st));
+                          nlev_d, nullptr, w2, st, &sched));
   }
+  if (sched == 1)
+    return sptrsv_syncfree_ordered(nb, bs, row, col, diag, order, val, lower, unit, b, x, ws, st);
   return sptrsv_levels(nb, bs, row, col, diag, order, lvl, nlev_d, val, lower, unit, b, x, ws,
                        st);
 }
@@ -1106,9 +1435,23 @@ int sptrsv_level_impl(int nb, long long nnzb, int bs, const int* row, const int*
 // Level analysis into caller-owned arrays (order[nb+1], lvl[nb+2], nlev[2]).
 int level_analysis(int nb, long long nnzb, const int* row, const int* col, const int* diag,
                    int lower, int* order, int* lvl, int* nlev_d, int* h_nlev, Carver& ws,
-                   cudaStream_t st) {
+                   cudaStream_t st, int* h_sched) {
   return build_levels(nb, row, col, diag, lower, std::max(nnzb - nb, 0ll), order, lvl, nlev_d,
-                      h_nlev, ws, st);
+                      h_nlev, ws, st, h_sched);
+}
+
+// Launch-only sync-free solve for use inside a solver: flags and ticket
+// (nb + 1 and 1 ints, caller-owned) are cleared on the stream before the
+// launch; failures land in *err for a later check.
+int sptrsv_syncfree_async(int nb, int bs, const int* row, const int* col, const int* diag,
+                          const int* order, const double* val, int lower, int unit,
+                          const double* b, double* x, int* flags, int* ticket, int* err,
+                          cudaStream_t st) {
+  if (nb == 0) return BILU_OK;
+  BILU_TRY_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * ((size_t)nb + 1), st));
+  BILU_TRY_CUDA(cudaMemsetAsync(ticket, 0, sizeof(int), st));
+  SyncState ss{flags, ticket, err, err, kSpinLimit, -1, order};
+  return BILU_DISPATCH_BS(bs, launch_sptrsv, nb, row, col, diag, val, lower, unit, b, x, ss, st);
 }
 
 // Launch-only level-scheduled solve for use inside a solver: no host
@@ -1141,7 +1484,7 @@ struct AnalysisView {
     diag = c.take<int>((size_t)nb + 1);
     order = c.take<int>((size_t)nb + 1);
     lvl = c.take<int>((size_t)nb + 2);
-    nlev = c.take<int>(2);
+    nlev = c.take<int>(4);  // levels, largest dependency count, schedule, spare
   }
 };
 
@@ -1150,7 +1493,7 @@ struct AnalysisView {
 extern "C" size_t bilu_sptrsv_analysis_bytes(int nb) {
   if (nb < 0) return 0;
   return 2 * carve_size(sizeof(int) * ((size_t)nb + 1)) +
-         carve_size(sizeof(int) * ((size_t)nb + 2)) + carve_size(sizeof(int) * 2);
+         carve_size(sizeof(int) * ((size_t)nb + 2)) + carve_size(sizeof(int) * 4);
 }
 
 extern "C" size_t bilu_sptrsv_analysis_ws_bytes(int nb, int nnzb) {
@@ -1184,6 +1527,28 @@ extern "C" int bilu_sptrsv_solve(int nb, int bs, const int* d_row, const int* d_
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   AnalysisView a(const_cast<void*>(d_info), nb);
   Carver ws(d_ws, ws_bytes);
+  int sched = 0;
+  if (nb > 0) {
+    BILU_TRY_CUDA(cudaMemcpyAsync(&sched, a.nlev + 2, sizeof(int), cudaMemcpyDeviceToHost,
+                                  S(stream)));
+    BILU_TRY_CUDA(cudaStreamSynchronize(S(stream)));
+  }
+  if (sched == 1)
+    return sptrsv_syncfree_ordered(nb, bs, d_row, d_col, a.diag, a.order, d_val, lower != 0,
+                                   unit != 0, d_b, d_x, ws, S(stream));
+  return sptrsv_levels(nb, bs, d_row, d_col, a.diag, a.order, a.lvl, a.nlev, d_val, lower != 0,
+                       unit != 0, d_b, d_x, ws, S(stream));
+}
+
+extern "C" int bilu_sptrsv_solve_level(int nb, int bs, const int* d_row, const int* d_col,
+                                       const double* d_val, int lower, int unit,
+                                       const void* d_info, const double* d_b, double* d_x,
+                                       void* d_ws, size_t ws_bytes, bilu_stream_t stream) {
+  if (nb < 0 || !d_info || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)))
+    return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  AnalysisView a(const_cast<void*>(d_info), nb);
+  Carver ws(d_ws, ws_bytes);
   return sptrsv_levels(nb, bs, d_row, d_col, a.diag, a.order, a.lvl, a.nlev, d_val, lower != 0,
                        unit != 0, d_b, d_x, ws, S(stream));
 }
@@ -1197,13 +1562,8 @@ extern "C" int bilu_sptrsv_solve_syncfree(int nb, int bs, const int* d_row, cons
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   AnalysisView a(const_cast<void*>(d_info), nb);
   Carver ws(d_ws, ws_bytes);
-  SyncState ss;
-  BILU_TRY(sync_init(ss, nb, ws, S(stream)));
-  ss.order = a.order;
-  if (nb > 0)
-    BILU_TRY(BILU_DISPATCH_BS(bs, launch_sptrsv, nb, d_row, d_col, a.diag, d_val, lower != 0,
-                              unit != 0, d_b, d_x, ss, S(stream)));
-  return sync_finish(ss, nullptr, S(stream));
+  return sptrsv_syncfree_ordered(nb, bs, d_row, d_col, a.diag, a.order, d_val, lower != 0,
+                                 unit != 0, d_b, d_x, ws, S(stream));
 }
 
 extern "C" size_t bilu_bsrilu0_ws_bytes(int nb, int nnzb) {

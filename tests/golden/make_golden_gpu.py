@@ -177,6 +177,11 @@ def main():
         np.savez_compressed(os.path.join(out_dir, f"refgpu_{name}.npz"), nb=A.nb, bs=bs,
                             row=A.rowptr, col=A.colind, LU=LU, **res)
         print("wrote", name)
+    if "--time-powerlaw" in sys.argv:
+        nbp = int(sys.argv[sys.argv.index("--time-powerlaw") + 1])
+        A = gen.powerlaw(nbp, bs=8, seed=0)
+        print(json.dumps({"workload": f"powerlaw nb={nbp} bs8 nnzb={A.nnzb}",
+                          "factor_and_solve_ms": time_factor_and_solves(A)}))
     if "--time" in sys.argv:
         side = int(sys.argv[sys.argv.index("--time") + 1])
         A = gen.convdiff3d(side, bs=4, seed=0)
@@ -265,7 +270,8 @@ def time_our_isai_steps(A, LU, reps=5):
 def time_factor_and_solves(A, reps=5):
     """cuSPARSE bsrilu02 / bsrsv2 with the reference's settings (bsrilu.h:20,
     BILU_cusparse.h:110-224) beside this library's BILU(0) and sync-free
-    solves on the same matrix (CUDA events, GPU time only)."""
+    solves (level-scheduled and sync-free) on the same matrix (CUDA events,
+    GPU time only)."""
     import torch
 
     from isai_kernel_gb300 import _lib, api
@@ -319,15 +325,15 @@ def time_factor_and_solves(A, reps=5):
         e1.synchronize()
         out[f"ours_sptrsv_{tag}_analysis_ms"] = e0.elapsed_time(e1)
         y = torch.empty_like(b)
-        L.bilu_sptrsv_solve(A.nb, A.bs, P(row), P(col), P(lu_ref), lower, lower, P(info), P(b),
-                            P(y), P(ws), ws.numel(), api._s())
+        L.bilu_sptrsv_solve_level(A.nb, A.bs, P(row), P(col), P(lu_ref), lower, lower, P(info),
+                                  P(b), P(y), P(ws), ws.numel(), api._s())
         e0.record()
         for _ in range(reps):
-            L.bilu_sptrsv_solve(A.nb, A.bs, P(row), P(col), P(lu_ref), lower, lower, P(info),
-                                P(b), P(y), P(ws), ws.numel(), api._s())
+            L.bilu_sptrsv_solve_level(A.nb, A.bs, P(row), P(col), P(lu_ref), lower, lower,
+                                      P(info), P(b), P(y), P(ws), ws.numel(), api._s())
         e1.record()
         e1.synchronize()
-        out[f"ours_sptrsv_{tag}_solve_ms"] = e0.elapsed_time(e1) / reps
+        out[f"ours_sptrsv_{tag}_level_solve_ms"] = e0.elapsed_time(e1) / reps
         y2 = torch.empty_like(b)
         L.bilu_sptrsv_solve_syncfree(A.nb, A.bs, P(row), P(col), P(lu_ref), lower, lower, P(info),
                                      P(b), P(y2), P(ws), ws.numel(), api._s())

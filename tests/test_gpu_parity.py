@@ -282,11 +282,12 @@ def test_sptrsv_level_and_syncfree_schedules(cuda, orc, name):
         api.call("bilu_sptrsv_analysis", nb, nnzb, bs, api._p(row), api._p(col), lower,
                  api._p(info), api._p(ws), ws.numel(), api._s())
         bd = T(b, cuda)
-        x1, x2 = torch.empty_like(bd), torch.empty_like(bd)
-        for fn, x in (("bilu_sptrsv_solve", x1), ("bilu_sptrsv_solve_syncfree", x2)):
+        x1, x2, x3 = torch.empty_like(bd), torch.empty_like(bd), torch.empty_like(bd)
+        for fn, x in (("bilu_sptrsv_solve_level", x1), ("bilu_sptrsv_solve_syncfree", x2),
+                      ("bilu_sptrsv_solve", x3)):
             api.call(fn, nb, bs, api._p(row), api._p(col), api._p(lu), lower, lower, api._p(info),
                      api._p(bd), api._p(x), api._p(ws), ws.numel(), api._s())
-        assert torch.equal(x1, x2)
+        assert torch.equal(x1, x2) and torch.equal(x1, x3)
         ref = (orc.sptrsv_lower if lower else orc.sptrsv_upper)(nb, bs, d["row"], d["col"],
                                                                 LU, b)
         assert relerr(N(x1), ref) < 1e-12
@@ -308,6 +309,41 @@ def test_sptrsv_level_and_syncfree_schedules(cuda, orc, name):
         ptr = words[o_lvl:o_lvl + nlev + 1]
         assert nlev == lv.max() and ptr[-1] == nb
         assert np.array_equal(np.diff(ptr), np.bincount(lv - 1, minlength=nlev))
+
+
+def test_long_rows_take_the_warp_path(cuda, orc):
+    """A power-law system with rows of more than 32 dependencies (up to 126
+    here): the level kernels switch to a warp per row.  BILU(0) within 1e-12
+    of the oracle, level and sync-free solves bit-identical and within 1e-12
+    of the oracle's."""
+    import torch
+
+    from isai_kernel_gb300 import _lib, api
+
+    A = gen.powerlaw(400, bs=8, seed=5, kmax=150)
+    LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    row, col = T(A.rowptr, cuda), T(A.colind, cuda)
+    lu = T(A.val, cuda).clone()
+    assert api.bsrilu02_inplace(A.nb, A.nnzb, A.bs, row, col, lu) == -1
+    assert relerr(N(lu), LU) < 1e-12
+    L = _lib.lib()
+    b = gen.rhs(A.n, 7)
+    bd = T(b, cuda)
+    for lower in (1, 0):
+        info = api._ws(L.bilu_sptrsv_analysis_bytes(A.nb), cuda)
+        ws = api._ws(max(L.bilu_sptrsv_analysis_ws_bytes(A.nb, A.nnzb),
+                         L.bilu_sptrsv_solve_ws_bytes(A.nb)), cuda)
+        api.call("bilu_sptrsv_analysis", A.nb, A.nnzb, A.bs, api._p(row), api._p(col), lower,
+                 api._p(info), api._p(ws), ws.numel(), api._s())
+        x1, x2, x3 = torch.empty_like(bd), torch.empty_like(bd), torch.empty_like(bd)
+        for fn, x in (("bilu_sptrsv_solve_level", x1), ("bilu_sptrsv_solve_syncfree", x2),
+                      ("bilu_sptrsv_solve", x3)):
+            api.call(fn, A.nb, A.bs, api._p(row), api._p(col), api._p(lu), lower, lower,
+                     api._p(info), api._p(bd), api._p(x), api._p(ws), ws.numel(), api._s())
+        assert torch.equal(x1, x2) and torch.equal(x1, x3)
+        ref = (orc.sptrsv_lower if lower else orc.sptrsv_upper)(A.nb, A.bs, A.rowptr, A.colind,
+                                                                LU, b)
+        assert relerr(N(x1), ref) < 1e-12
 
 
 def test_sptrsv_timeout_path(cuda, orc):
