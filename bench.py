@@ -6,10 +6,17 @@ A step is one solve to 1e-10 relative residual from x0 = 0 with the
 mixed-precision path (FP32-stored ISAI inside FP64 flexible GMRES(30) with
 FP64 residuals, orthogonalisation and restarts); the preconditioner setup
 (BILU(0) + ISAI on the GPU) runs once before the timed region and is
-reported separately, as is the plain FP64 path.  `value` is the mean solve
+reported separately, as are the plain FP64 ISAI path, the FP32-operator
+variant (`fp32_inner`) and GMRES with the exact BILU(0) applied by
+level-scheduled triangular solves (`exact_ilu`).  `value` is the mean solve
 time (s) with the matrix resident in HBM (1.9 GB of values, larger than L2).
 `e2e` is the same metric through the C ABI call with host buffers
-(bilu_solve_host: H2D of A and b, setup, solve, D2H of x).
+(bilu_solve_host: H2D of A and b, setup, solve, D2H of x).  `roofline`
+rates the FP32 apply as the solver launches it (two k_bsr_spmv, FP32 basis
+vector in) against the measured copy bandwidth; `traffic` is the DRAM bytes
+of the same launches from the committed ncu capture.  `cpu_baseline` is the
+oracle on the host cores, plus the serial (one core) BILU(0) and triangular
+solves.  Secondary lines: --workload sptrsv | powerlaw | batch.
 
     python bench.py [--steps K] [--warmup W] [--side 128] [--impl reference]
     torchrun --nproc-per-node N bench.py --gpus N   (N independent replicas)
@@ -202,11 +209,29 @@ def cpu_baseline(side, iters_full, gmres_iters=3, seed=0):
     _, it, _, _, _ = oracle.gmres(Ab, L, U, b, precond=2, restart=30, maxit=gmres_iters)
     t_it = (time.perf_counter() - t0) / max(it, 1)
     est = t_setup + t_it * iters_full
-    return {"value": est, "unit": "s", "cores": oracle.num_threads(), "kind": "port",
+    cores = oracle.num_threads()
+    # the serial CPU BILU(0) + triangular-solve path on one core (the
+    # reference has no CPU ILU / SpTRSV; its GPU sync-free solve is the
+    # restated algorithm), next to the GPU factor and solves
+    oracle.set_threads(1)
+    try:
+        t0 = time.perf_counter()
+        LU, _ = oracle.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+        t_f1 = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        y = oracle.sptrsv_lower(A.nb, A.bs, A.rowptr, A.colind, LU, b)
+        t_l1 = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        oracle.sptrsv_upper(A.nb, A.bs, A.rowptr, A.colind, LU, y)
+        t_u1 = time.perf_counter() - t0
+    finally:
+        oracle.set_threads(cores)
+    return {"value": est, "unit": "s", "cores": cores, "kind": "port",
             "sample": (f"oracle on the full {side}^3 system: setup {t_setup:.2f} s measured, "
                        f"{it} FGMRES(30) iterations measured at {t_it:.3f} s each, scaled to "
                        f"{iters_full} iterations"),
-            "setup_s": t_setup, "per_iter_s": t_it}
+            "setup_s": t_setup, "per_iter_s": t_it,
+            "serial_1_core": {"bilu0_s": t_f1, "sptrsv_L_s": t_l1, "sptrsv_U_s": t_u1}}
 
 
 def run_reference(args):
@@ -398,7 +423,8 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu_baseline:
         try:
             cpu = cpu_baseline(args.side, int(statistics.mean(iters)), gmres_iters=args.cpu_iters)
-            cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "setup_s",
+                                       "per_iter_s", "serial_1_core")}
         except Exception as exc:  # report, never hide
             cpu = {"value": None, "unit": "s", "cores": 0, "kind": "port",
                    "sample": f"failed: {exc}"}

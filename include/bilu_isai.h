@@ -153,6 +153,10 @@ int bilu_bcsc_to_bcsr(int mb, int nbcol, int bs, const int* d_cscPtr, const int*
 size_t bilu_bsrilu0_ws_bytes(int nb, int nnzb);
 int bilu_bsrilu0(int nb, int nnzb, int bs, const int* d_row, const int* d_col, double* d_val,
                  int* h_info, void* d_ws, size_t ws_bytes, bilu_stream_t stream);
+/* Same with the schedule chosen by the caller: -1 as recommended by the
+ * analysis, 0 level schedule, 1 sync-free (both give identical factors). */
+int bilu_bsrilu0_ex(int nb, int nnzb, int bs, const int* d_row, const int* d_col, double* d_val,
+                    int schedule, int* h_info, void* d_ws, size_t ws_bytes, bilu_stream_t stream);
 
 /* ------------------------------------------------------------------ */
 /* ISAI setup                                                          */
@@ -330,6 +334,9 @@ int bilu_ctx_setup(bilu_ctx* ctx, int nb, int nnzb, int bs, const int* d_row, co
  * (ISAI(k): denser approximate inverses, fewer iterations, a costlier
  * apply). */
 int bilu_ctx_set_isai_level(bilu_ctx* ctx, int k);
+/* Schedule of the next setup's BILU(0) and of the exact-ILU solves: -1 (the
+ * default) as the level analyses recommend, 0 level schedule, 1 sync-free. */
+int bilu_ctx_set_schedule(bilu_ctx* ctx, int schedule);
 
 /* Right-preconditioned restarted (F)GMRES(restart) with modified
  * Gram-Schmidt and Givens rotations, x0 = 0: prec BILU_FP64 applies the FP64 ISAI, BILU_FP32 the

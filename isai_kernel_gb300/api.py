@@ -182,13 +182,15 @@ def bsr_transpose(mb: int, bs: int, row, col, val):
 
 
 # ------------------------------------------------------------ factorisation
-def bsrilu02_inplace(nb: int, nnzb: int, bs: int, bsrRow, bsrCol, bsrVal) -> int:
-    """bsrilu.h:20 bsrilu02_inplace: BILU(0) in place.  Returns the first
+def bsrilu02_inplace(nb: int, nnzb: int, bs: int, bsrRow, bsrCol, bsrVal,
+                     schedule: int = -1) -> int:
+    """bsrilu.h:20 bsrilu02_inplace: BILU(0) in place (schedule: -1 as the
+    level analysis recommends, 0 level, 1 sync-free).  Returns the first
     zero-pivot block row or -1 (the reference prints it)."""
     dev = _dev(bsrVal)
     info = ctypes.c_int(-1)
     ws = _ws(lib().bilu_bsrilu0_ws_bytes(nb, nnzb), dev)
-    call("bilu_bsrilu0", nb, nnzb, bs, _p(_ci(bsrRow)), _p(_ci(bsrCol)), _p(bsrVal),
+    call("bilu_bsrilu0_ex", nb, nnzb, bs, _p(_ci(bsrRow)), _p(_ci(bsrCol)), _p(bsrVal), schedule,
          ctypes.byref(info), _p(ws), ws.numel(), _s(), ok=(0, -3))
     return info.value
 
@@ -344,12 +346,14 @@ class Preconditioner:
     preconditioner from a BSR matrix, then preconditioned (F)GMRES solves."""
 
     def __init__(self, nb: int, bs: int, row, col, val, fp32: bool = True, ilu: bool = False,
-                 fp32_inner: bool = False, isai_level: int = 1, stream=None):
+                 fp32_inner: bool = False, isai_level: int = 1, schedule: int = -1,
+                 stream=None):
         self._h = ctypes.c_void_p()
         self.nb, self.bs = nb, bs
         self.stream = stream
         call("bilu_ctx_create", ctypes.byref(self._h), _s(stream))
         call("bilu_ctx_set_isai_level", self._h, isai_level)
+        call("bilu_ctx_set_schedule", self._h, schedule)
         self._keep = (row, col, val)
         times = (ctypes.c_double * 4)()
         call("bilu_ctx_setup", self._h, nb, int(col.numel()), bs, _p(_ci(row)), _p(_ci(col)),

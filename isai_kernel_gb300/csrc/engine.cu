@@ -55,7 +55,7 @@ int sptrsv_levels_async(int nb, int bs, const int* row, const int* col, const in
                         int lower, int unit, const double* b, double* x, unsigned* words,
                         cudaStream_t st);
 int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, const int* diag,
-               double* val, int* h_zp, Carver& ws, cudaStream_t st);
+               double* val, int* h_zp, Carver& ws, cudaStream_t st, int schedule);
 int dinv_impl(int nb, int bs, const int* row, const int* col, const double* val, int lower,
               double* Dinv, int* d_fail, cudaStream_t st);
 size_t pairs_ws(long long mnnz);
@@ -97,6 +97,7 @@ struct bilu_ctx {
   float* Aval32 = nullptr;  // FP32 copy of A for the Arnoldi products (BILU_FP32_INNER)
   int nnzL = 0, nnzU = 0;
   int isai_level = 1;                     // ISAI(k): M patterns from pattern(A^k)
+  int schedule = -1;  // BILU(0) and exact-ILU solves: -1 recommended, 0 level, 1 sync-free
   int *Prow = nullptr, *Pcol = nullptr;   // pattern(A^k) when isai_level > 1
   int nnzP = 0;
   bool ready = false;
@@ -308,7 +309,8 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   {
     Carver w2 = ws;
     int zp = -1;
-    int rc = bilu0_impl(nb, nnzb, bs, c->Arow, c->Acol, c->diag, c->LU, &zp, w2, st);
+    int rc = bilu0_impl(nb, nnzb, bs, c->Arow, c->Acol, c->diag, c->LU, &zp, w2, st,
+                        c->schedule);
     if (rc != BILU_OK) return rc;
   }
   tm.mark(2);
@@ -368,6 +370,7 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
       Carver w2 = ws;
       BILU_TRY(level_analysis(nb, nnzb, c->Arow, c->Acol, c->diag, lower, *ord, *lvl, *nl,
                               &c->nlev_host[lower ? 0 : 1], w2, st, &c->ilu_sched[lower ? 0 : 1]));
+      if (c->schedule == 0 || c->schedule == 1) c->ilu_sched[lower ? 0 : 1] = c->schedule;
     }
     BILU_TRY(c->alloc(&c->ilu_flags, (size_t)nb + 2));
     BILU_TRY(c->alloc(&c->ilu_words, 4));
@@ -384,6 +387,12 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
     h_times[3] = t_total;
   }
   c->ready = true;
+  return BILU_OK;
+}
+
+extern "C" int bilu_ctx_set_schedule(bilu_ctx* c, int schedule) {
+  if (!c || schedule < -1 || schedule > 1) return BILU_ERR_ARG;
+  c->schedule = schedule;
   return BILU_OK;
 }
 

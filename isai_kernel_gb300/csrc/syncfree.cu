@@ -1332,7 +1332,7 @@ int sync_init_words(SyncState& ss, Carver& ws, cudaStream_t st) {
 // BILU(0) in place, level scheduled (one cooperative launch, one grid
 // barrier per dependency level of the lower DAG).
 int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, const int* diag,
-               double* val, int* h_zp, Carver& ws, cudaStream_t st) {
+               double* val, int* h_zp, Carver& ws, cudaStream_t st, int schedule) {
   int* order = ws.take<int>((size_t)nb + 1);
   int* lvl = ws.take<int>((size_t)nb + 2);
   int* nlev_d = ws.take<int>(4);
@@ -1343,6 +1343,7 @@ int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, c
     BILU_TRY(build_levels(nb, row, col, diag, 1, std::max(nnzb - nb, 0ll), order, lvl, nlev_d,
                           &nlev, w2, st, &sched));
   }
+  if (schedule == 0 || schedule == 1) sched = schedule;  // caller's choice
   if (sched == 1) {
     // narrow levels or long rows: sync-free, tickets in level order
     SyncState ss;
@@ -1575,8 +1576,15 @@ extern "C" size_t bilu_bsrilu0_ws_bytes(int nb, int nnzb) {
 extern "C" int bilu_bsrilu0(int nb, int nnzb, int bs, const int* d_row, const int* d_col,
                             double* d_val, int* h_info, void* d_ws, size_t ws_bytes,
                             bilu_stream_t stream) {
+  return bilu_bsrilu0_ex(nb, nnzb, bs, d_row, d_col, d_val, -1, h_info, d_ws, ws_bytes, stream);
+}
+
+extern "C" int bilu_bsrilu0_ex(int nb, int nnzb, int bs, const int* d_row, const int* d_col,
+                               double* d_val, int schedule, int* h_info, void* d_ws,
+                               size_t ws_bytes, bilu_stream_t stream) {
   if (h_info) *h_info = -1;
   if (nb < 0 || nnzb < 0 || (nb > 0 && (!d_row || !d_col || !d_val))) return BILU_ERR_ARG;
+  if (schedule < -1 || schedule > 1) return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   Carver ws(d_ws, ws_bytes);
   int* diag = ws.take<int>((size_t)nb + 1);
@@ -1587,7 +1595,7 @@ extern "C" int bilu_bsrilu0(int nb, int nnzb, int bs, const int* d_row, const in
     if (h_info) *h_info = bad;
     return rc;
   }
-  return bilu0_impl(nb, nnzb, bs, d_row, d_col, diag, d_val, h_info, ws, S(stream));
+  return bilu0_impl(nb, nnzb, bs, d_row, d_col, diag, d_val, h_info, ws, S(stream), schedule);
 }
 
 extern "C" size_t bilu_sptrsv_ws_bytes(int nb, int nnzb) {

@@ -311,6 +311,51 @@ def test_sptrsv_level_and_syncfree_schedules(cuda, orc, name):
         assert np.array_equal(np.diff(ptr), np.bincount(lv - 1, minlength=nlev))
 
 
+@pytest.mark.parametrize("name", ["c1_s16", "c2_s6", "c3_nb200", "bs5_s7", "long_rows"])
+def test_bilu0_both_schedules(cuda, orc, name):
+    """BILU(0) under the level schedule (a bs-lane group per row) and the
+    sync-free one (a warp per row, tickets in level order): identical
+    factors, within 1e-12 of the oracle."""
+    from isai_kernel_gb300 import api
+
+    A = gen.powerlaw(400, bs=8, seed=5, kmax=150) if name == "long_rows" else mats()[name]
+    LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    row, col = T(A.rowptr, cuda), T(A.colind, cuda)
+    out = []
+    for sched in (0, 1):
+        lu = T(A.val, cuda).clone()
+        assert api.bsrilu02_inplace(A.nb, A.nnzb, A.bs, row, col, lu, schedule=sched) == -1
+        out.append(N(lu))
+    assert np.array_equal(out[0], out[1])
+    assert relerr(out[0], LU) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["c2_s6", "c3_nb200"])
+def test_exact_ilu_gmres_both_schedules(cuda, orc, name):
+    """GMRES with the exact BILU(0) under both schedules of the factor and
+    the triangular solves: the same iterations and the same x bit for bit,
+    equal to the oracle's iteration count."""
+    from isai_kernel_gb300 import api
+
+    A = mats()[name]
+    b = T(gen.rhs(A.n, 0), cuda)
+    LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    _, ito, _, _, st = orc.gmres((A.rowptr, A.colind, A.val), (A.rowptr, A.colind, LU), None,
+                                 N(b), precond=3, maxit=3000)
+    assert st == 0
+    xs, its = [], []
+    for sched in (0, 1):
+        p = api.Preconditioner(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda),
+                               ilu=True, schedule=sched)
+        x, res = p.solve(b, prec=api.BILU_ILU, maxit=3000)
+        assert res.converged
+        xs.append(N(x))
+        its.append(res.iters)
+        p.close()
+    assert its[0] == its[1] == ito
+    assert np.array_equal(xs[0], xs[1])
+
+
 def test_long_rows_take_the_warp_path(cuda, orc):
     """A power-law system with rows of more than 32 dependencies (up to 126
     here): the level kernels switch to a warp per row.  BILU(0) within 1e-12
