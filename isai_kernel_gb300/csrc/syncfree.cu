@@ -419,6 +419,7 @@ struct GridSync {
   unsigned* gen;    // barriers completed
   int* err;         // 0 or a bilu_status; set on a barrier timeout
   long long spin;   // polls before a waiting CTA gives up
+  int per_sm = 1;   // CTAs of the launch resident on one SM
 };
 
 __device__ __forceinline__ unsigned ld_relaxed_u(const unsigned* p) {
@@ -480,6 +481,53 @@ __device__ __forceinline__ bool grid_sync(const GridSync& g, unsigned& gen_seen,
 struct NoOp {
   __device__ void operator()() const {}
 };
+
+// Counting grid barrier, for kernels with no last-arriver action: the
+// arrival count grows through the launch (barrier b is complete when it
+// reaches (b + 1) x gridDim.x) and every CTA polls the count itself, so the
+// release reaches the waiting CTAs with the last arrival's atomic instead
+// of a generation word written after it returns.  `passed` counts the
+// barriers this CTA has passed (thread 0's copy is the one used).  The
+// comparison is modulo 2^32.  g.gen counts CTAs that have left the kernel
+// (grid_exit_count); both words are 0 between launches.
+__device__ __forceinline__ bool grid_sync_count(const GridSync& g, unsigned& passed) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned target = (passed + 1u) * gridDim.x;
+    unsigned v = atom_add_acq_rel_u(g.count, 1u) + 1u;
+    long long n = 0;
+    unsigned ns = 32;
+    while ((int)(v - target) < 0) {
+      if (ld_relaxed(g.err) != 0) { ok = 0; break; }
+      if (++n > g.spin) {
+        atomicCAS(g.err, 0, (int)BILU_ERR_TIMEOUT);
+        ok = 0;
+        break;
+      }
+      backoff(ns);
+      v = ld_relaxed_u(g.count);
+    }
+    fence_acquire();
+    passed += 1u;
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// End of a launch that used grid_sync_count: a CTA arrives here only after
+// passing every barrier, so when the last one arrives no CTA polls the
+// count any more and both words can go back to 0 for the next launch.  (A
+// launch that aborted skips this; its error word is set and the caller
+// clears the words before the next solve.)
+__device__ __forceinline__ void grid_exit_count(const GridSync& g) {
+  if (threadIdx.x == 0 && atomicAdd(g.gen, 1u) == gridDim.x - 1u) {
+    atomicExch(g.count, 0u);
+    atomicExch(g.gen, 0u);
+  }
+}
 
 // Dependencies of row I: lower -> columns in [row[I], diag[I]); upper ->
 // columns in (diag[I], row[I+1]).  cnt[K] += 1 per dependent of K.
@@ -543,6 +591,35 @@ __global__ void __launch_bounds__(256) k_bfs_levels(int nb, const int* __restric
 }
 
 constexpr int kLvlThreads = 256;
+
+// Warp rank for level work.  Consecutive ranks sit in different CTAs (the
+// CTAs of a co-resident launch are spread over the SMs), so a level narrower
+// than the grid is spread over every SM instead of filling the first CTAs'
+// warps while the other SMs wait at the barrier.  Within a CTA, which warp
+// serves which round of ranks is rotated by the CTA's slot on its SM, so
+// that the CTAs sharing an SM start on different sub-partitions: each of
+// the four has its own FP64 unit, about 80 cycles per warp instruction
+// whatever the number of active lanes.  The slot comes from a per-SM
+// counter that is never reset (consecutive CTAs on one SM get consecutive
+// values); any rotation is a permutation of the CTA's warps, so only the
+// spread, not the set of ranks, depends on it.  Called by every thread of
+// the CTA before any of them returns.
+__device__ unsigned g_sm_slot[1024];
+
+__device__ __forceinline__ int spread_warp(int per_sm) {
+  __shared__ int rot_s;
+  const int nwc = (int)(blockDim.x >> 5);
+  if (threadIdx.x == 0) {
+    unsigned sm;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+    const int c = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
+    const int k = (int)(atomicAdd(&g_sm_slot[sm & 1023u], 1u) % (unsigned)c);
+    rot_s = (k * (4 / c)) % nwc;  // per_sm 2: warps 0 and 2 open the rounds
+  }
+  __syncthreads();
+  const int round = ((int)(threadIdx.x >> 5) - rot_s + nwc) % nwc;
+  return (int)(round * gridDim.x + blockIdx.x);
+}
 // rows with more dependencies than this make the level kernels give each
 // row a whole warp instead of a bs-lane group
 constexpr int kLongRow = 32;
@@ -555,16 +632,65 @@ constexpr int kMinLevelWidth = 1024;
 // per warp; lane r of a group owns scalar row r).  On GB300 an FP64 warp
 // instruction costs the same whatever the number of active lanes, so packing
 // rows is what makes the per-level FP64 work small; rows of one level are
-// independent, so groups of a warp never wait on each other.  The structural
-// part of each group's first row of the next level (indices, first block,
-// diagonal row, b) is loaded before the barrier.
+// independent, so groups of a warp never wait on each other.
+//
+// A level's critical path is its x reads (rows of earlier levels), a short
+// FP64 chain and the grid barrier; everything else is loaded ahead in three
+// stages.  While level l is solved, a group holds: the row index it will
+// take at level l+2 (read from the level order), the row pointers and
+// diagonal position of its level-(l+1) row (issued before the level-l
+// arithmetic), and, issued just before the barrier, that row's first
+// kPreDeps column indices and blocks, its diagonal row and b.  After the
+// barrier only x is read, and the x reads of those blocks are independent.
 template <int BS>
 struct GRowPre {
-  int I, ps, pe, K0;  // I < 0: no row for this group
-  double a0[BS];      // row r of the first block
-  double dq[BS];      // row r of the diagonal block
-  double bq;          // b_r
+  // blocks held in registers (bs 8: one, within 128 registers a thread)
+  static constexpr int D = BS <= 5 ? 16 / BS : 1;
+  int I, ps, pe;   // I < 0: no row for this group
+  int K[D];        // columns of the first D dependencies (-1 past the row)
+  double a[D][BS]; // row r of those blocks
+  double dq[BS];   // row r of the diagonal block
+  double bq;       // b_r
 };
+
+// structural words of row I: dependency range and diagonal position
+struct GRowMeta {
+  int rs, re, dI;
+};
+
+__device__ __forceinline__ void grow_meta(int I, const int* __restrict__ row,
+                                          const int* __restrict__ diag, GRowMeta& m) {
+  m.rs = m.re = m.dI = 0;
+  if (I < 0) return;
+  m.rs = __ldg(row + I);
+  m.re = __ldg(row + I + 1);
+  m.dI = __ldg(diag + I);
+}
+
+template <int BS, bool LOWER>
+__device__ __forceinline__ void grow_load(int I, const GRowMeta& m, const int* __restrict__ col,
+                                          const double* __restrict__ val,
+                                          const double* __restrict__ b, GRowPre<BS>& p) {
+  constexpr int BS2 = BS * BS, D = GRowPre<BS>::D;
+  const int r = (threadIdx.x & 31) % BS;
+  p.I = I;
+  p.ps = LOWER ? m.rs : m.dI + 1;
+  p.pe = LOWER ? m.dI : m.re;
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    const int q = p.ps + j;
+    const bool has = I >= 0 && q < p.pe;
+    p.K[j] = has ? __ldg(col + q) : -1;
+    const double* blk = val + (long long)(has ? q : 0) * BS2 + r * BS;
+#pragma unroll
+    for (int c = 0; c < BS; ++c) p.a[j][c] = has ? __ldg(blk + c) : 0.0;
+  }
+  if (I < 0) return;
+  const double* Dg = val + (long long)m.dI * BS2 + r * BS;
+#pragma unroll
+  for (int c = 0; c < BS; ++c) p.dq[c] = __ldg(Dg + c);
+  p.bq = __ldg(b + (long long)I * BS + r);
+}
 
 template <int BS, bool LOWER>
 __device__ __forceinline__ void grow_prefetch(int I, const int* __restrict__ row,
@@ -572,32 +698,18 @@ __device__ __forceinline__ void grow_prefetch(int I, const int* __restrict__ row
                                               const int* __restrict__ diag,
                                               const double* __restrict__ val,
                                               const double* __restrict__ b, GRowPre<BS>& p) {
-  constexpr int BS2 = BS * BS;
-  const int r = (threadIdx.x & 31) % BS;
-  p.I = I;
-  p.K0 = -1;
-  p.ps = p.pe = 0;
-  if (I < 0) return;
-  int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
-  p.ps = LOWER ? rs : dI + 1;
-  p.pe = LOWER ? dI : re;
-  if (p.ps < p.pe) {
-    p.K0 = __ldg(col + p.ps);
-    const double* blk = val + (long long)p.ps * BS2 + r * BS;
-#pragma unroll
-    for (int c = 0; c < BS; ++c) p.a0[c] = __ldg(blk + c);
-  }
-  const double* D = val + (long long)dI * BS2 + r * BS;
-#pragma unroll
-  for (int c = 0; c < BS; ++c) p.dq[c] = __ldg(D + c);
-  p.bq = __ldg(b + (long long)I * BS + r);
+  GRowMeta m;
+  grow_meta(I, row, diag, m);
+  grow_load<BS, LOWER>(I, m, col, val, b, p);
 }
 
 // Called by all 32 lanes (the diagonal solve shuffles inside each group).
+// Sum order: the row's blocks in storage order, each block's row r as an
+// FMA chain from zero, added to a running total from zero.
 template <int BS, bool LOWER, bool UNIT>
 __device__ __forceinline__ void grow_finish(const GRowPre<BS>& p, const int* __restrict__ col,
                                             const double* __restrict__ val, double* x) {
-  constexpr int BS2 = BS * BS;
+  constexpr int BS2 = BS * BS, D = GRowPre<BS>::D;
   const int lane = threadIdx.x & 31, r = lane % BS, gb = lane - r;
   double tot = 0.0, rq = 1.0;
   if (p.I >= 0) {
@@ -605,27 +717,31 @@ __device__ __forceinline__ void grow_finish(const GRowPre<BS>& p, const int* __r
 #pragma unroll
     for (int c = 1; c < BS; ++c)
       if (c == r) d = p.dq[c];
-    if (p.K0 >= 0) {
-      const double* xk = x + (long long)p.K0 * BS;
-      double xv[BS];
+    double xv[D][BS];
 #pragma unroll
-      for (int c = 0; c < BS; ++c) xv[c] = __ldcg(xk + c);
-      if (!UNIT) rq = 1.0 / d;  // overlaps the x reads
-      double sp = 0.0;
+    for (int j = 0; j < D; ++j) {
+      const double* xk = x + (long long)(p.K[j] >= 0 ? p.K[j] : 0) * BS;
 #pragma unroll
-      for (int c = 0; c < BS; ++c) sp = fma(p.a0[c], xv[c], sp);
-      tot += sp;
-      for (int q = p.ps + 1; q < p.pe; ++q) {
-        const int K = __ldg(col + q);
-        const double* blk = val + (long long)q * BS2 + r * BS;
-        const double* xq = x + (long long)K * BS;
-        sp = 0.0;
+      for (int c = 0; c < BS; ++c) xv[j][c] = p.K[j] >= 0 ? __ldcg(xk + c) : 0.0;
+    }
+    if (!UNIT) rq = 1.0 / d;  // overlaps the x reads
 #pragma unroll
-        for (int c = 0; c < BS; ++c) sp = fma(__ldg(blk + c), __ldcg(xq + c), sp);
+    for (int j = 0; j < D; ++j) {
+      if (p.K[j] >= 0) {
+        double sp = 0.0;
+#pragma unroll
+        for (int c = 0; c < BS; ++c) sp = fma(p.a[j][c], xv[j][c], sp);
         tot += sp;
       }
-    } else if (!UNIT) {
-      rq = 1.0 / d;
+    }
+    for (int q = p.ps + D; q < p.pe; ++q) {
+      const int K = __ldg(col + q);
+      const double* blk = val + (long long)q * BS2 + r * BS;
+      const double* xq = x + (long long)K * BS;
+      double sp = 0.0;
+#pragma unroll
+      for (int c = 0; c < BS; ++c) sp = fma(__ldg(blk + c), __ldcg(xq + c), sp);
+      tot += sp;
     }
   }
   double v = p.bq - tot, xr = 0.0;
@@ -640,6 +756,15 @@ __device__ __forceinline__ void grow_finish(const GRowPre<BS>& p, const int* __r
   if (p.I >= 0) x[(long long)p.I * BS + r] = xr;
 }
 
+// level-order row of this group at level l (-1 if the level is narrower)
+__device__ __forceinline__ int group_row(int l, int nlev, long long mygrp, bool active,
+                                         const int* __restrict__ order,
+                                         const int* __restrict__ lvl_ptr) {
+  if (!active || l >= nlev) return -1;
+  const long long t = __ldg(lvl_ptr + l) + mygrp;
+  return t < __ldg(lvl_ptr + l + 1) ? __ldg(order + t) : -1;
+}
+
 template <int BS, bool LOWER, bool UNIT>
 __global__ void __launch_bounds__(kLvlThreads, 2) k_sptrsv_levels(
     const int* __restrict__ row, const int* __restrict__ col, const int* __restrict__ diag,
@@ -647,11 +772,9 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_sptrsv_levels(
     const int* __restrict__ order, const int* __restrict__ lvl_ptr, const int* __restrict__ nlev_p,
     SyncState ss, GridSync gs) {
   constexpr int G = 32 / BS;
-  // generation at launch: no barrier completes before every CTA has read it,
-  // so consecutive launches need no reset of the barrier words
-  unsigned gen = threadIdx.x == 0 ? ld_relaxed_u(gs.gen) : 0u;
+  unsigned passed = 0;
   const int g = (threadIdx.x & 31) / BS;
-  const int warp = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int warp = spread_warp(gs.per_sm);
   const int nw = (int)(((long long)gridDim.x * blockDim.x) >> 5);
   const long long ngrp = (long long)nw * G;
   const long long mygrp = (long long)warp * G + g;  // groups g >= G (bs 5: lanes 30, 31) idle
@@ -677,34 +800,38 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_sptrsv_levels(
         int t = e + warp;
         sptrsv_prefetch<BS, LOWER, UNIT>(t < __ldg(lvl_ptr + l + 2) ? __ldg(order + t) : -1, row,
                                          col, diag, val, b, wp);
-        if (!grid_sync(gs, gen, NoOp{})) return;
+        if (!grid_sync_count(gs, passed)) return;
       }
     }
+    grid_exit_count(gs);
     return;
   }
+  const bool active = g < G;
   GRowPre<BS> pre;
-  {
-    long long t = __ldg(lvl_ptr) + mygrp;
-    grow_prefetch<BS, LOWER>(g < G && t < __ldg(lvl_ptr + 1) ? __ldg(order + t) : -1, row, col,
-                             diag, val, b, pre);
-  }
+  grow_prefetch<BS, LOWER>(group_row(0, nlev, mygrp, active, order, lvl_ptr), row, col, diag,
+                           val, b, pre);
+  int I1 = group_row(1, nlev, mygrp, active, order, lvl_ptr);
   for (int l = 0; l < nlev; ++l) {
-    const int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
+    // loads for later levels first: they do not depend on x
+    GRowMeta m1;
+    grow_meta(I1, row, diag, m1);
+    const int I2 = group_row(l + 2, nlev, mygrp, active, order, lvl_ptr);
     grow_finish<BS, LOWER, UNIT>(pre, col, val, x);
     // further rows of a wide level, G at a time per warp (warp-uniform loop)
+    const int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
     for (long long t0 = s + (long long)warp * G + ngrp; t0 < e; t0 += ngrp) {
       GRowPre<BS> q;
       long long t = t0 + g;
-      grow_prefetch<BS, LOWER>(g < G && t < e ? __ldg(order + t) : -1, row, col, diag, val, b, q);
+      grow_prefetch<BS, LOWER>(active && t < e ? __ldg(order + t) : -1, row, col, diag, val, b, q);
       grow_finish<BS, LOWER, UNIT>(q, col, val, x);
     }
     if (l + 1 < nlev) {
-      long long t = e + mygrp;
-      grow_prefetch<BS, LOWER>(g < G && t < __ldg(lvl_ptr + l + 2) ? __ldg(order + t) : -1, row,
-                               col, diag, val, b, pre);
-      if (!grid_sync(gs, gen, NoOp{})) return;
+      grow_load<BS, LOWER>(I1, m1, col, val, b, pre);
+      if (!grid_sync_count(gs, passed)) return;
     }
+    I1 = I2;
   }
+  grid_exit_count(gs);
   (void)ss;
 }
 
@@ -1010,10 +1137,10 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_bilu0_levels(
     double* val, const int* __restrict__ order, const int* __restrict__ lvl_ptr,
     const int* __restrict__ nlev_p, SyncState ss, GridSync gs) {
   constexpr int G = 32 / BS;
-  unsigned gen = threadIdx.x == 0 ? ld_relaxed_u(gs.gen) : 0u;
+  unsigned passed = 0;
   const int lane = threadIdx.x & 31, g = lane / BS, r = lane - g * BS, gb = g * BS;
   const unsigned gmask = g < G ? (((1u << BS) - 1u) << gb) : 0u;
-  const int warp = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int warp = spread_warp(gs.per_sm);
   const int nw = (int)(((long long)gridDim.x * blockDim.x) >> 5);
   const long long ngrp = (long long)nw * G;
   const long long mygrp = (long long)warp * G + g;
@@ -1024,12 +1151,13 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_bilu0_levels(
     if (g < G)
       for (long long t = s + mygrp; t < e; t += ngrp)
         bilu0_grow<BS>(__ldg(order + t), row, col, diag, val, ss, gmask, r, gb);
-    if (l + 1 < nlev && !grid_sync(gs, gen, NoOp{})) return;
+    if (l + 1 < nlev && !grid_sync_count(gs, passed)) return;
   }
+  grid_exit_count(gs);
 }
 
 
-int occupancy_grid(const void* fn, int threads, size_t smem = 0) {
+int sm_count() {
   static int sms = 0;
   if (!sms) {
     int dev = 0;
@@ -1037,11 +1165,19 @@ int occupancy_grid(const void* fn, int threads, size_t smem = 0) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
   }
+  return sms;
+}
+
+int occupancy_per_sm(const void* fn, int threads, size_t smem = 0) {
   int per = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, smem) != cudaSuccess ||
       per < 1)
     per = 1;
-  return sms * per;
+  return per;
+}
+
+int occupancy_grid(const void* fn, int threads, size_t smem = 0) {
+  return sm_count() * occupancy_per_sm(fn, threads, smem);
 }
 
 int sync_init(SyncState& ss, int nb, Carver& ws, cudaStream_t st, long long spin = kSpinLimit,
@@ -1247,6 +1383,7 @@ int launch_sptrsv_levels(int nb, const int* row, const int* col, const int* diag
   // no more lane groups than rows; fewer CTAs make the barrier cheaper
   int grid = std::min<long long>(coop_grid(fn, kLvlThreads),
                                  ceil_div(nb, (kLvlThreads / 32) * (32 / BS)));
+  gs.per_sm = std::max(1, std::min(occupancy_per_sm(fn, kLvlThreads), (int)ceil_div(grid, sm_count())));
   (void)nlev;
   void* args[] = {&row, &col, &diag, &val, &b, &x, &order, &lvl_ptr, &nlev_d, &ss, &gs};
   return launch_coop(fn, grid, kLvlThreads, args, st);
@@ -1279,6 +1416,7 @@ int launch_bilu0_levels(int nb, const int* row, const int* col, const int* diag,
   const void* fn = (const void*)k_bilu0_levels<BS>;
   int grid = std::min<long long>(coop_grid(fn, kLvlThreads),
                                  ceil_div(nb, (kLvlThreads / 32) * (32 / BS)));
+  gs.per_sm = std::max(1, std::min(occupancy_per_sm(fn, kLvlThreads), (int)ceil_div(grid, sm_count())));
   void* args[] = {&row, &col, &diag, &val, &order, &lvl_ptr, &nlev_d, &ss, &gs};
   return launch_coop(fn, grid, kLvlThreads, args, st);
 }
@@ -1465,8 +1603,8 @@ int sptrsv_syncfree_async(int nb, int bs, const int* row, const int* col, const 
 }
 
 // Launch-only level-scheduled solve for use inside a solver: no host
-// synchronisation.  words: [0] barrier count (0 between launches), [1]
-// barrier generation, [2] error word (0 or a bilu_status, read by the caller
+// synchronisation.  words: [0] barrier count, [1] exit count (both 0
+// between launches), [2] error word (0 or a bilu_status, read by the caller
 // later), [3] zero-pivot word.
 int sptrsv_levels_async(int nb, int bs, const int* row, const int* col, const int* diag,
                         const int* order, const int* lvl, const int* nlev_d, const double* val,
