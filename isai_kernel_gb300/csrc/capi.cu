@@ -169,7 +169,9 @@ extern "C" int bilu_sptrsv_transpose(int nb, int bs, const int* d_row, const int
                                      const double* d_val, int lower, const double* d_b,
                                      double* d_x, void* d_ws, size_t ws_bytes,
                                      bilu_stream_t stream) {
-  if (nb < 0 || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x))) return BILU_ERR_ARG;
+  if (nb < 0 || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)) ||
+      (nb > 0 && (const void*)d_b == (const void*)d_x))
+    return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   cudaStream_t st = S(stream);
   int nnzb = 0;

@@ -45,17 +45,18 @@ int pattern_product_fill(int n, const int* Xrow, const int* Xcol, const int* Aro
                          cudaStream_t st);
 int level_analysis(int nb, long long nnzb, const int* row, const int* col, const int* diag,
                    int lower, int* order, int* lvl, int* nlev_d, int* h_nlev, Carver& ws,
-                   cudaStream_t st, int* h_sched);
+                   cudaStream_t st, int* h_sched, int* h_maxdeg);
 int sptrsv_syncfree_async(int nb, int bs, const int* row, const int* col, const int* diag,
                           const int* order, const double* val, int lower, int unit,
                           const double* b, double* x, int* flags, int* ticket, int* err,
-                          cudaStream_t st);
+                          cudaStream_t st, const double* rdiag);
 int sptrsv_levels_async(int nb, int bs, const int* row, const int* col, const int* diag,
                         const int* order, const int* lvl, const int* nlev_d, const double* val,
                         int lower, int unit, const double* b, double* x, unsigned* words,
-                        cudaStream_t st);
+                        cudaStream_t st, const double* rdiag, int maxdeg);
 int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, const int* diag,
-               double* val, int* h_zp, Carver& ws, cudaStream_t st, int schedule);
+               double* val, int* h_zp, Carver& ws, cudaStream_t st, int schedule,
+               double* rdiag);
 int dinv_impl(int nb, int bs, const int* row, const int* col, const double* val, int lower,
               double* Dinv, int* d_fail, cudaStream_t st);
 size_t pairs_ws(long long mnnz);
@@ -91,6 +92,7 @@ struct bilu_ctx {
   long long n = 0;
   int *Arow = nullptr, *Acol = nullptr, *diag = nullptr;
   double *Aval = nullptr, *LU = nullptr;
+  double* rdiag = nullptr;  // 1 / pivots of the factor's U_II (nb x bs), written by BILU(0)
   int *Lrow = nullptr, *Lcol = nullptr, *Urow = nullptr, *Ucol = nullptr;
   double *Lval = nullptr, *Uval = nullptr;
   float *Lval32 = nullptr, *Uval32 = nullptr;
@@ -108,6 +110,7 @@ struct bilu_ctx {
   unsigned* ilu_words = nullptr;
   int nlev_host[2] = {0, 0};
   int ilu_sched[2] = {0, 0};    // per triangle: 0 level schedule, 1 sync-free
+  int ilu_maxdeg[2] = {0, 0};   // per triangle: largest dependency count
   int* ilu_flags = nullptr;     // ready flags + ticket of the sync-free solves
   // solver buffers
   int m_alloc = 0;
@@ -126,6 +129,7 @@ struct bilu_ctx {
     setup_bufs.clear();
     Arow = Acol = diag = Lrow = Lcol = Urow = Ucol = nullptr;
     Aval = LU = Lval = Uval = nullptr;
+    rdiag = nullptr;
     Lval32 = Uval32 = nullptr;
     Aval32 = nullptr;
     ordL = lvlL = nlevL = ordU = lvlU = nlevU = nullptr;
@@ -290,6 +294,7 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   BILU_TRY(c->alloc(&c->Aval, nnzb * bs2));
   BILU_TRY(c->alloc(&c->LU, nnzb * bs2));
   BILU_TRY(c->alloc(&c->diag, nb + 1));
+  BILU_TRY(c->alloc(&c->rdiag, (size_t)nb * bs + 1));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->Arow, d_row, sizeof(int) * (nb + 1), cudaMemcpyDeviceToDevice, st));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->Acol, d_col, sizeof(int) * nnzb, cudaMemcpyDeviceToDevice, st));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->Aval, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
@@ -310,7 +315,7 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
     Carver w2 = ws;
     int zp = -1;
     int rc = bilu0_impl(nb, nnzb, bs, c->Arow, c->Acol, c->diag, c->LU, &zp, w2, st,
-                        c->schedule);
+                        c->schedule, c->rdiag);
     if (rc != BILU_OK) return rc;
   }
   tm.mark(2);
@@ -369,7 +374,8 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
       BILU_TRY(c->alloc(nl, 4));
       Carver w2 = ws;
       BILU_TRY(level_analysis(nb, nnzb, c->Arow, c->Acol, c->diag, lower, *ord, *lvl, *nl,
-                              &c->nlev_host[lower ? 0 : 1], w2, st, &c->ilu_sched[lower ? 0 : 1]));
+                              &c->nlev_host[lower ? 0 : 1], w2, st, &c->ilu_sched[lower ? 0 : 1],
+                              &c->ilu_maxdeg[lower ? 0 : 1]));
       if (c->schedule == 0 || c->schedule == 1) c->ilu_sched[lower ? 0 : 1] = c->schedule;
     }
     BILU_TRY(c->alloc(&c->ilu_flags, (size_t)nb + 2));
@@ -471,11 +477,13 @@ int apply_prec(bilu_ctx* c, int prec, const double* v, double* z) {
       if (c->ilu_sched[lower ? 0 : 1] == 1)
         BILU_TRY(sptrsv_syncfree_async(c->nb, c->bs, c->Arow, c->Acol, c->diag, ord, c->LU,
                                        lower, lower, in, out, c->ilu_flags,
-                                       c->ilu_flags + c->nb + 1, (int*)c->ilu_words + 2, c->st));
+                                       c->ilu_flags + c->nb + 1, (int*)c->ilu_words + 2, c->st,
+                                       lower ? nullptr : c->rdiag));
       else
         BILU_TRY(sptrsv_levels_async(c->nb, c->bs, c->Arow, c->Acol, c->diag, ord,
                                      lower ? c->lvlL : c->lvlU, lower ? c->nlevL : c->nlevU,
-                                     c->LU, lower, lower, in, out, c->ilu_words, c->st));
+                                     c->LU, lower, lower, in, out, c->ilu_words, c->st,
+                                     lower ? nullptr : c->rdiag, c->ilu_maxdeg[lower ? 0 : 1]));
     }
     return BILU_OK;
   }

@@ -40,6 +40,9 @@ struct SyncState {
   long long spin;     // polls before a wait gives up
   int withhold;       // test hook: this row never publishes (-1: none)
   const int* order;   // ticket -> block row (dependency-level order), or null
+  // reciprocal pivots 1 / u_rr of the block rows (nb x bs): written by the
+  // factorisation, read by upper solves instead of dividing (null: divide)
+  double* rdiag = nullptr;
 };
 
 // Exponential back-off between polls (32 ns doubling to 256 ns): waiters that
@@ -139,6 +142,15 @@ struct RowPre {
   double bq;          // lanes q < BS: b_q
 };
 
+// 1 / d for scalar row (lane % BS) of block row I: the factorisation's
+// stored reciprocal when there is one (the same correctly rounded
+// quotient), else the division.
+template <int BS>
+__device__ __forceinline__ double recip_pivot(const double* rdiag, int I, double d) {
+  if (rdiag) return __ldg(rdiag + (long long)I * BS + (threadIdx.x & 31) % BS);
+  return 1.0 / d;
+}
+
 template <int BS, bool LOWER, bool UNIT>
 __device__ __forceinline__ void sptrsv_prefetch(int I, const int* __restrict__ row,
                                                 const int* __restrict__ col,
@@ -209,12 +221,12 @@ __device__ __forceinline__ bool sptrsv_finish(const RowPre<BS>& p, const int* __
         double xv[BS];
 #pragma unroll
         for (int c = 0; c < BS; ++c) xv[c] = __ldcg(xk + c);
-        if (!UNIT) rq = 1.0 / d;  // overlaps the x reads
+        if (!UNIT) rq = recip_pivot<BS>(ss.rdiag, p.I, d);  // overlaps the x reads
 #pragma unroll
         for (int c = 0; c < BS; ++c) sp = fma(p.a[c], xv[c], sp);
       }
     } else if (!UNIT) {
-      rq = 1.0 / d;
+      rq = recip_pivot<BS>(ss.rdiag, p.I, d);
     }
     if (WAIT && __any_sync(FULL, !ok)) return false;
 #pragma unroll
@@ -478,9 +490,6 @@ __device__ __forceinline__ bool grid_sync(const GridSync& g, unsigned& gen_seen,
   return ok_s != 0;
 }
 
-struct NoOp {
-  __device__ void operator()() const {}
-};
 
 // Counting grid barrier, for kernels with no last-arriver action: the
 // arrival count grows through the launch (barrier b is complete when it
@@ -628,20 +637,19 @@ constexpr int kLongRow = 32;
 // level costs a grid barrier; narrow levels are cheaper without one)
 constexpr int kMinLevelWidth = 1024;
 
-// Level-scheduled solve with a group of BS lanes per block row (32/BS rows
+// Rows of the flow schedule: a group of BS lanes per block row (32/BS rows
 // per warp; lane r of a group owns scalar row r).  On GB300 an FP64 warp
 // instruction costs the same whatever the number of active lanes, so packing
-// rows is what makes the per-level FP64 work small; rows of one level are
+// rows is what makes the per-row FP64 work small; rows of one level are
 // independent, so groups of a warp never wait on each other.
 //
-// A level's critical path is its x reads (rows of earlier levels), a short
-// FP64 chain and the grid barrier; everything else is loaded ahead in three
-// stages.  While level l is solved, a group holds: the row index it will
-// take at level l+2 (read from the level order), the row pointers and
-// diagonal position of its level-(l+1) row (issued before the level-l
-// arithmetic), and, issued just before the barrier, that row's first
-// kPreDeps column indices and blocks, its diagonal row and b.  After the
-// barrier only x is read, and the x reads of those blocks are independent.
+// A row's critical path is its x reads (rows of earlier levels) and a short
+// FP64 chain; everything else is loaded ahead in three stages.  While one
+// row is solved, a group holds: the index of its row after next (read from
+// the level order), the row pointers and diagonal position of its next row
+// (issued before the current row's arithmetic), and, issued right after it,
+// the next row's first D column indices and blocks, its diagonal row and b.
+// The x reads of those D blocks are then independent of each other.
 template <int BS>
 struct GRowPre {
   // blocks held in registers (bs 8: one, within 128 registers a thread)
@@ -651,6 +659,7 @@ struct GRowPre {
   double a[D][BS]; // row r of those blocks
   double dq[BS];   // row r of the diagonal block
   double bq;       // b_r
+  double rq;       // 1 / pivot of row r, when the factorisation stored it
 };
 
 // structural words of row I: dependency range and diagonal position
@@ -670,7 +679,8 @@ __device__ __forceinline__ void grow_meta(int I, const int* __restrict__ row,
 template <int BS, bool LOWER>
 __device__ __forceinline__ void grow_load(int I, const GRowMeta& m, const int* __restrict__ col,
                                           const double* __restrict__ val,
-                                          const double* __restrict__ b, GRowPre<BS>& p) {
+                                          const double* __restrict__ b,
+                                          const double* __restrict__ rdiag, GRowPre<BS>& p) {
   constexpr int BS2 = BS * BS, D = GRowPre<BS>::D;
   const int r = (threadIdx.x & 31) % BS;
   p.I = I;
@@ -690,6 +700,7 @@ __device__ __forceinline__ void grow_load(int I, const GRowMeta& m, const int* _
 #pragma unroll
   for (int c = 0; c < BS; ++c) p.dq[c] = __ldg(Dg + c);
   p.bq = __ldg(b + (long long)I * BS + r);
+  p.rq = (!LOWER && rdiag) ? __ldg(rdiag + (long long)I * BS + r) : 0.0;
 }
 
 template <int BS, bool LOWER>
@@ -697,53 +708,183 @@ __device__ __forceinline__ void grow_prefetch(int I, const int* __restrict__ row
                                               const int* __restrict__ col,
                                               const int* __restrict__ diag,
                                               const double* __restrict__ val,
-                                              const double* __restrict__ b, GRowPre<BS>& p) {
+                                              const double* __restrict__ b,
+                                              const double* __restrict__ rdiag, GRowPre<BS>& p) {
   GRowMeta m;
   grow_meta(I, row, diag, m);
-  grow_load<BS, LOWER>(I, m, col, val, b, p);
+  grow_load<BS, LOWER>(I, m, col, val, b, rdiag, p);
 }
 
-// Called by all 32 lanes (the diagonal solve shuffles inside each group).
-// Sum order: the row's blocks in storage order, each block's row r as an
-// FMA chain from zero, added to a running total from zero.
+// Level-scheduled solve for rows with long dependency lists (more than
+// kLongRow blocks): a warp per row, the slots of the warp summing the row's
+// blocks as in the sync-free kernel (bit-identical x), a counting grid
+// barrier after each level.  The first row of a warp's next level is
+// loaded before the barrier.
 template <int BS, bool LOWER, bool UNIT>
-__device__ __forceinline__ void grow_finish(const GRowPre<BS>& p, const int* __restrict__ col,
-                                            const double* __restrict__ val, double* x) {
+__global__ void __launch_bounds__(kLvlThreads, 2) k_sptrsv_levels(
+    const int* __restrict__ row, const int* __restrict__ col, const int* __restrict__ diag,
+    const double* __restrict__ val, const double* __restrict__ b, double* x,
+    const int* __restrict__ order, const int* __restrict__ lvl_ptr, const int* __restrict__ nlev_p,
+    SyncState ss, GridSync gs) {
+  unsigned passed = 0;
+  const int warp = spread_warp(gs.per_sm);
+  const int nw = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+  const int nlev = __ldg(nlev_p);
+  if (nlev <= 0) return;
+  RowPre<BS> wp;
+  {
+    int t = __ldg(lvl_ptr) + warp;
+    sptrsv_prefetch<BS, LOWER, UNIT>(t < __ldg(lvl_ptr + 1) ? __ldg(order + t) : -1, row, col,
+                                     diag, val, b, wp);
+  }
+  for (int l = 0; l < nlev; ++l) {
+    const int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
+    if (wp.I >= 0) sptrsv_finish<BS, LOWER, UNIT, false, false>(wp, col, val, x, ss);
+    for (int t = s + warp + nw; t < e; t += nw) {
+      RowPre<BS> q;
+      sptrsv_prefetch<BS, LOWER, UNIT>(__ldg(order + t), row, col, diag, val, b, q);
+      sptrsv_finish<BS, LOWER, UNIT, false, false>(q, col, val, x, ss);
+    }
+    if (l + 1 < nlev) {
+      int t = e + warp;
+      sptrsv_prefetch<BS, LOWER, UNIT>(t < __ldg(lvl_ptr + l + 2) ? __ldg(order + t) : -1, row,
+                                       col, diag, val, b, wp);
+      if (!grid_sync_count(gs, passed)) return;
+    }
+  }
+  grid_exit_count(gs);
+}
+
+// ------------------------------------------------------------------ flow schedule
+// Level-order solve without grid barriers.  Every group keeps the rows the
+// level schedule gives it (the same static assignment and the same
+// arithmetic as k_sptrsv_levels), but instead of meeting the whole grid at
+// a barrier after each level it waits only for the x entries its row reads.
+// x is self-flagging: before the launch every entry holds kXPending, a
+// signalling-NaN pattern; a row's entries are written once, with single
+// 64-bit stores, and FP64 arithmetic only ever yields quiet NaNs, so an
+// entry that no longer reads kXPending holds its final value and no flag,
+// fence or barrier is needed.  Each dependent entry is read with a strong
+// (L2) load; a pending one is polled with bounded back-off.  All warps are
+// co-resident (cooperative launch) and each processes its rows in level
+// order, so every wait ends: rows of level 0 wait for nothing, rows of
+// level l only for rows of lower levels.  The solve then advances as a
+// wavefront at the latency of one dependency chain per level rather than
+// at that of the slowest CTA plus a grid barrier.
+constexpr unsigned long long kXPending = 0x7FF0A5A5A5A5A5A5ull;  // signalling NaN
+constexpr int kFlowSpin = 64;  // polling rounds without sleeping
+
+__device__ __forceinline__ unsigned long long ld_strong_u64(const double* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p));
+  return v;
+}
+
+// Stores a computed entry; a value with the pending pattern (impossible
+// for an arithmetic result) would be stored as the canonical quiet NaN.
+__device__ __forceinline__ void st_strong_f64(double* p, double v) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  if (u == kXPending) u = 0x7FF8000000000000ull;
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(u));
+}
+
+// Re-reads the entries of u[] that are still pending (x entries of rows of
+// earlier levels that other warps are computing) until none is: the first
+// kFlowSpin rounds back to back (most waits end within a few hundred
+// nanoseconds, and a sleep, however short it is asked to be, was measured to
+// cost more than that on GB300), then with bounded back-off.  u[j * BS + c] is entry c of block row K[j] (absent
+// dependencies have K[j] < 0 and u = 0, never pending).  The addresses are
+// rebuilt from K each round (through an opaque move, so the compiler does
+// not keep D * BS addresses live across the loop).  Per lane, no warp
+// collectives (groups of a warp wait for different rows).  false: the
+// launch aborted.
+template <int BS, int D>
+__device__ __forceinline__ bool poll_pending(unsigned long long (&u)[D * BS], const int (&K)[D],
+                                             const double* x, const SyncState& ss) {
+  bool pend = false;
+#pragma unroll
+  for (int i = 0; i < D * BS; ++i) pend |= u[i] == kXPending;
+  long long n = 0;
+  unsigned ns = 32;
+  while (pend) {
+    if (n >= kFlowSpin) backoff(ns);
+    pend = false;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      int k;
+      asm volatile("mov.b32 %0, %1;" : "=r"(k) : "r"(K[j]));
+      const double* xk = x + (long long)k * BS;
+#pragma unroll
+      for (int c = 0; c < BS; ++c) {
+        if (u[j * BS + c] == kXPending) {
+          u[j * BS + c] = ld_strong_u64(xk + c);
+          pend |= u[j * BS + c] == kXPending;
+        }
+      }
+    }
+    if (!pend) break;
+    if (++n > ss.spin) {
+      atomicCAS(ss.err, 0, (int)BILU_ERR_TIMEOUT);
+      return false;
+    }
+    if ((n & 31) == 0 && ld_relaxed(ss.err) != 0) return false;
+  }
+  return true;
+}
+
+// grow_finish with waits on the entries read; the same operations in the
+// same order.  Called by all 32 lanes; false in every lane if the launch
+// aborted.
+template <int BS, bool LOWER, bool UNIT>
+__device__ __forceinline__ bool grow_finish_flow(const GRowPre<BS>& p, const int* __restrict__ col,
+                                                 const double* __restrict__ val, double* x,
+                                                 bool have_rq, const SyncState& ss) {
   constexpr int BS2 = BS * BS, D = GRowPre<BS>::D;
   const int lane = threadIdx.x & 31, r = lane % BS, gb = lane - r;
   double tot = 0.0, rq = 1.0;
+  bool ok = true;
   if (p.I >= 0) {
     double d = p.dq[0];
 #pragma unroll
     for (int c = 1; c < BS; ++c)
       if (c == r) d = p.dq[c];
-    double xv[D][BS];
+    // entries of absent dependencies read as 0 (never pending)
+    unsigned long long u[D * BS];
 #pragma unroll
     for (int j = 0; j < D; ++j) {
       const double* xk = x + (long long)(p.K[j] >= 0 ? p.K[j] : 0) * BS;
 #pragma unroll
-      for (int c = 0; c < BS; ++c) xv[j][c] = p.K[j] >= 0 ? __ldcg(xk + c) : 0.0;
+      for (int c = 0; c < BS; ++c) u[j * BS + c] = p.K[j] >= 0 ? ld_strong_u64(xk + c) : 0ull;
     }
-    if (!UNIT) rq = 1.0 / d;  // overlaps the x reads
+    if (!UNIT) rq = have_rq ? p.rq : 1.0 / d;  // overlaps the x reads
+    ok = poll_pending<BS, D>(u, p.K, x, ss);
 #pragma unroll
     for (int j = 0; j < D; ++j) {
       if (p.K[j] >= 0) {
         double sp = 0.0;
 #pragma unroll
-        for (int c = 0; c < BS; ++c) sp = fma(p.a[j][c], xv[j][c], sp);
+        for (int c = 0; c < BS; ++c)
+          sp = fma(p.a[j][c], __longlong_as_double((long long)u[j * BS + c]), sp);
         tot += sp;
       }
     }
-    for (int q = p.ps + D; q < p.pe; ++q) {
+    for (int q = p.ps + D; ok && q < p.pe; ++q) {
       const int K = __ldg(col + q);
       const double* blk = val + (long long)q * BS2 + r * BS;
       const double* xq = x + (long long)K * BS;
+      unsigned long long uq[BS];
+#pragma unroll
+      for (int c = 0; c < BS; ++c) uq[c] = ld_strong_u64(xq + c);
+      const int Kq[1] = {K};
+      ok = poll_pending<BS, 1>(uq, Kq, x, ss);
       double sp = 0.0;
 #pragma unroll
-      for (int c = 0; c < BS; ++c) sp = fma(__ldg(blk + c), __ldcg(xq + c), sp);
+      for (int c = 0; c < BS; ++c)
+        sp = fma(__ldg(blk + c), __longlong_as_double((long long)uq[c]), sp);
       tot += sp;
     }
   }
+  if (__any_sync(FULL, !ok)) return false;
   double v = p.bq - tot, xr = 0.0;
 #pragma unroll
   for (int k = 0; k < BS; ++k) {
@@ -753,86 +894,97 @@ __device__ __forceinline__ void grow_finish(const GRowPre<BS>& p, const int* __r
     if (r == c) xr = xc;
     if (LOWER ? (r > c) : (r < c)) v -= p.dq[c] * xc;
   }
-  if (p.I >= 0) x[(long long)p.I * BS + r] = xr;
+  if (p.I >= 0) st_strong_f64(x + (long long)p.I * BS + r, xr);
+  return true;
 }
 
-// level-order row of this group at level l (-1 if the level is narrower)
-__device__ __forceinline__ int group_row(int l, int nlev, long long mygrp, bool active,
-                                         const int* __restrict__ order,
-                                         const int* __restrict__ lvl_ptr) {
-  if (!active || l >= nlev) return -1;
-  const long long t = __ldg(lvl_ptr + l) + mygrp;
-  return t < __ldg(lvl_ptr + l + 1) ? __ldg(order + t) : -1;
+// Row cursor of a warp in the flow kernel: level l and the position t0 of
+// group 0's row in the level order.  Pass 0 of every level is visited, also
+// where the warp has no row (a cheap skip); further passes of a wide level
+// follow while group 0's position is inside the level.
+struct RowCursor {
+  int l;
+  long long t0;
+};
+
+__device__ __forceinline__ void cursor_next(RowCursor& c, int nlev, long long first,
+                                            long long ngrp, const int* __restrict__ lvl_ptr) {
+  if (c.l >= nlev) return;
+  c.t0 += ngrp;
+  if (c.t0 >= __ldg(lvl_ptr + c.l + 1)) {
+    ++c.l;
+    c.t0 = c.l < nlev ? __ldg(lvl_ptr + c.l) + first : 0;
+  }
 }
 
+__device__ __forceinline__ int cursor_row(const RowCursor& c, int g, bool active, int nlev,
+                                          const int* __restrict__ order,
+                                          const int* __restrict__ lvl_ptr) {
+  if (!active || c.l >= nlev) return -1;
+  const long long t = c.t0 + g;
+  return t < __ldg(lvl_ptr + c.l + 1) ? __ldg(order + t) : -1;
+}
+
+// One row per group and iteration.  The rows ahead of the cursor are staged
+// so that nothing but x is read on a row's critical path: the next row's
+// blocks, diagonal row and b are loaded before the current row waits, the
+// structure of the row after it (row pointers, diagonal position) and the
+// index of the one after that one step earlier still.  Two staged rows
+// need about 180 registers a thread, so one 256-thread CTA runs per SM (two
+// warps a sub-partition; more warps only queue on its FP64 unit).
 template <int BS, bool LOWER, bool UNIT>
-__global__ void __launch_bounds__(kLvlThreads, 2) k_sptrsv_levels(
+__global__ void __launch_bounds__(kLvlThreads, 1) k_sptrsv_flow(
     const int* __restrict__ row, const int* __restrict__ col, const int* __restrict__ diag,
     const double* __restrict__ val, const double* __restrict__ b, double* x,
     const int* __restrict__ order, const int* __restrict__ lvl_ptr, const int* __restrict__ nlev_p,
-    SyncState ss, GridSync gs) {
+    SyncState ss, int per_sm) {
   constexpr int G = 32 / BS;
-  unsigned passed = 0;
   const int g = (threadIdx.x & 31) / BS;
-  const int warp = spread_warp(gs.per_sm);
+  const int warp = spread_warp(per_sm);
   const int nw = (int)(((long long)gridDim.x * blockDim.x) >> 5);
   const long long ngrp = (long long)nw * G;
-  const long long mygrp = (long long)warp * G + g;  // groups g >= G (bs 5: lanes 30, 31) idle
+  const long long first = (long long)warp * G;
   const int nlev = __ldg(nlev_p);
   if (nlev <= 0) return;
-  if (__ldg(nlev_p + 1) > kLongRow) {
-    // long rows (nlev_p[1] = the largest dependency count): a warp per row
-    RowPre<BS> wp;
-    {
-      int t = __ldg(lvl_ptr) + warp;
-      sptrsv_prefetch<BS, LOWER, UNIT>(t < __ldg(lvl_ptr + 1) ? __ldg(order + t) : -1, row, col,
-                                       diag, val, b, wp);
-    }
-    for (int l = 0; l < nlev; ++l) {
-      const int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
-      if (wp.I >= 0) sptrsv_finish<BS, LOWER, UNIT, false, false>(wp, col, val, x, ss);
-      for (int t = s + warp + nw; t < e; t += nw) {
-        RowPre<BS> q;
-        sptrsv_prefetch<BS, LOWER, UNIT>(__ldg(order + t), row, col, diag, val, b, q);
-        sptrsv_finish<BS, LOWER, UNIT, false, false>(q, col, val, x, ss);
-      }
-      if (l + 1 < nlev) {
-        int t = e + warp;
-        sptrsv_prefetch<BS, LOWER, UNIT>(t < __ldg(lvl_ptr + l + 2) ? __ldg(order + t) : -1, row,
-                                         col, diag, val, b, wp);
-        if (!grid_sync_count(gs, passed)) return;
-      }
-    }
-    grid_exit_count(gs);
-    return;
-  }
   const bool active = g < G;
+  const double* rdiag = LOWER ? nullptr : ss.rdiag;
+  RowCursor c0{0, __ldg(lvl_ptr) + first};
+  RowCursor c1 = c0;
+  cursor_next(c1, nlev, first, ngrp, lvl_ptr);
+  RowCursor c2 = c1;
+  cursor_next(c2, nlev, first, ngrp, lvl_ptr);
+  RowCursor c3 = c2;
+  cursor_next(c3, nlev, first, ngrp, lvl_ptr);
   GRowPre<BS> pre;
-  grow_prefetch<BS, LOWER>(group_row(0, nlev, mygrp, active, order, lvl_ptr), row, col, diag,
-                           val, b, pre);
-  int I1 = group_row(1, nlev, mygrp, active, order, lvl_ptr);
-  for (int l = 0; l < nlev; ++l) {
-    // loads for later levels first: they do not depend on x
-    GRowMeta m1;
-    grow_meta(I1, row, diag, m1);
-    const int I2 = group_row(l + 2, nlev, mygrp, active, order, lvl_ptr);
-    grow_finish<BS, LOWER, UNIT>(pre, col, val, x);
-    // further rows of a wide level, G at a time per warp (warp-uniform loop)
-    const int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
-    for (long long t0 = s + (long long)warp * G + ngrp; t0 < e; t0 += ngrp) {
-      GRowPre<BS> q;
-      long long t = t0 + g;
-      grow_prefetch<BS, LOWER>(active && t < e ? __ldg(order + t) : -1, row, col, diag, val, b, q);
-      grow_finish<BS, LOWER, UNIT>(q, col, val, x);
-    }
-    if (l + 1 < nlev) {
-      grow_load<BS, LOWER>(I1, m1, col, val, b, pre);
-      if (!grid_sync_count(gs, passed)) return;
-    }
+  grow_prefetch<BS, LOWER>(cursor_row(c0, g, active, nlev, order, lvl_ptr), row, col, diag, val,
+                           b, rdiag, pre);
+  int I1 = cursor_row(c1, g, active, nlev, order, lvl_ptr);
+  GRowMeta m1;
+  grow_meta(I1, row, diag, m1);
+  int I2 = cursor_row(c2, g, active, nlev, order, lvl_ptr);
+  while (c0.l < nlev) {
+    // loads for the rows ahead first: they do not depend on x
+    GRowPre<BS> nxt;
+    if (c1.l < nlev) grow_load<BS, LOWER>(I1, m1, col, val, b, rdiag, nxt);
+    GRowMeta m2;
+    grow_meta(I2, row, diag, m2);
+    const int I3 = cursor_row(c3, g, active, nlev, order, lvl_ptr);
+    if (!grow_finish_flow<BS, LOWER, UNIT>(pre, col, val, x, rdiag != nullptr, ss)) return;
+    pre = nxt;
+    m1 = m2;
     I1 = I2;
+    I2 = I3;
+    c0 = c1;
+    c1 = c2;
+    c2 = c3;
+    cursor_next(c3, nlev, first, ngrp, lvl_ptr);
   }
-  grid_exit_count(gs);
-  (void)ss;
+}
+
+__global__ void k_fill_pending(unsigned long long* x, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] = kXPending;
 }
 
 // ------------------------------------------------------------------ BILU(0)
@@ -841,7 +993,12 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_sptrsv_levels(
 //                        A_IJ -= L_IK U_KJ for J > K present in rows I and K;
 //   then LU of the diagonal block (no pivoting) and U_IJ = L_II^-1 A_IJ.
 // Each element sees the same sequence of a -= l*u updates as the scalar IKJ
-// loop, with ascending k.
+// loop, with ascending k.  Multipliers are formed as a * (1 / u_kk): each
+// row stores the reciprocals of its BS pivots once (SyncState::rdiag) and
+// the rows below it multiply by them, so a row costs BS FP64 divisions
+// instead of BS per dependency plus BS(BS-1)/2 (a division is a chain of
+// FP64 instructions, each ~80 cycles of a sub-partition's FP64 unit on
+// GB300).  The factor differs from the divided one by rounding only.
 //
 // One block row with a group of BS lanes (level schedule: rows of one level
 // are independent, so groups of a warp never wait on each other; the
@@ -852,6 +1009,31 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_sptrsv_levels(
 // blocks), BS at a time, each lane binary-searching one in the other list;
 // every block is updated once per K, so the update order of each element
 // does not depend on which list is scanned.
+// LU without pivoting of a diagonal block, right-looking, in the registers
+// of a group of BS lanes: lane c holds column c (dc[q] = D[q][c]) on entry
+// and the packed L\U column on exit.  Step k takes the reciprocal of the
+// final pivot u_kk on lane k, scales the rest of column k into the
+// multipliers l_qk = d_qk * (1 / u_kk), broadcasts them and updates the
+// columns right of it.  Each element receives its updates in ascending k,
+// as in the scalar IKJ loop.  Returns 1 / u_cc on lane c (the reciprocal
+// pivots that later rows and the upper solves multiply by).
+template <int BS>
+__device__ __forceinline__ double bilu0_diag_lu(double (&dc)[BS], int c, unsigned gmask, int gb) {
+  double rp = 0.0;
+#pragma unroll
+  for (int k = 0; k < BS; ++k) {
+    const double rk = 1.0 / dc[k];  // meaningful on lane k
+    if (c == k) rp = rk;
+#pragma unroll
+    for (int q = k + 1; q < BS; ++q) {
+      const double l = __shfl_sync(gmask, dc[q] * rk, gb + k);
+      if (c == k) dc[q] = l;
+      else if (c > k) dc[q] -= l * dc[k];
+    }
+  }
+  return rp;
+}
+
 template <int BS>
 __device__ __forceinline__ void bilu0_grow(int I, const int* __restrict__ row,
                                            const int* __restrict__ col,
@@ -864,13 +1046,14 @@ __device__ __forceinline__ void bilu0_grow(int I, const int* __restrict__ row,
     const int dK = __ldg(diag + K), ke = __ldg(row + K + 1);
     double* L = val + (long long)pk * BS2;
     const double* Ukk = val + (long long)dK * BS2;
+    const double* rK = ss.rdiag + (long long)K * BS;  // 1 / pivots of U_KK
     // phase 1: row r of L_IK = A_IK U_KK^-1 (forward elimination)
     double a[BS];
 #pragma unroll
     for (int c = 0; c < BS; ++c) a[c] = L[r * BS + c];
 #pragma unroll
     for (int k = 0; k < BS; ++k) {
-      a[k] = a[k] / __ldcg(Ukk + k * BS + k);
+      a[k] = a[k] * __ldcg(rK + k);
 #pragma unroll
       for (int c = k + 1; c < BS; ++c) a[c] -= a[k] * __ldcg(Ukk + k * BS + c);
     }
@@ -903,21 +1086,12 @@ __device__ __forceinline__ void bilu0_grow(int I, const int* __restrict__ row,
     }
   }
   __syncwarp(gmask);
-  // diagonal block: lane c = r owns column c
+  // diagonal block, lane c = r owns column c: bilu0_diag_lu
   double* D = val + (long long)dI * BS2;
   double dc[BS];
 #pragma unroll
   for (int q = 0; q < BS; ++q) dc[q] = D[q * BS + r];
-#pragma unroll
-  for (int q = 1; q < BS; ++q) {
-#pragma unroll
-    for (int k = 0; k < q; ++k) {
-      double lk = dc[q] / dc[k];  // meaningful on lane k
-      double l = __shfl_sync(gmask, lk, gb + k);
-      if (r == k) dc[q] = l;
-      else if (r > k) dc[q] -= l * dc[k];
-    }
-  }
+  const double rp = bilu0_diag_lu<BS>(dc, r, gmask, gb);
   double piv = dc[0];  // this lane's diagonal element of U_II
 #pragma unroll
   for (int q = 1; q < BS; ++q)
@@ -925,6 +1099,7 @@ __device__ __forceinline__ void bilu0_grow(int I, const int* __restrict__ row,
   if (piv == 0.0) atomicMin(ss.zp, I);
 #pragma unroll
   for (int q = 0; q < BS; ++q) D[q * BS + r] = dc[q];
+  ss.rdiag[(long long)I * BS + r] = rp;
   __syncwarp(gmask);
   // U blocks right of the diagonal: U_IJ = L_II^-1 A_IJ, lane per column
   for (int pj = dI + 1; pj < re; ++pj) {
@@ -1013,6 +1188,7 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
     if (WAIT && !warp_wait(ss.flags + K, ss.err, ss.spin)) return false;
     double* L = val + (long long)pk * BS2;
     const double* Ukk = val + (long long)dK * BS2;
+    const double* rK = ss.rdiag + (long long)K * BS;  // 1 / pivots of U_KK
     // phase 1: lane r owns row r of A_IK
     if (lane < BS) {
       double a[BS];
@@ -1020,7 +1196,7 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
       for (int c = 0; c < BS; ++c) a[c] = L[lane * BS + c];
 #pragma unroll
       for (int k = 0; k < BS; ++k) {
-        a[k] = a[k] / __ldcg(Ukk + k * BS + k);
+        a[k] = a[k] * __ldcg(rK + k);
 #pragma unroll
         for (int c = k + 1; c < BS; ++c) a[c] -= a[k] * __ldcg(Ukk + k * BS + c);
       }
@@ -1090,16 +1266,9 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
 #pragma unroll
     for (int r = 0; r < BS; ++r) dc[r] = 1.0;
   }
-#pragma unroll
-  for (int r = 1; r < BS; ++r) {
-#pragma unroll
-    for (int k = 0; k < r; ++k) {
-      double lk = dc[r] / dc[k];  // meaningful on lane k
-      double l = __shfl_sync(FULL, lk, k);
-      if (lane == k) dc[r] = l;
-      else if (lane > k && lane < BS) dc[r] -= l * dc[k];
-    }
-  }
+  // lanes >= BS take part as columns right of the block (their updates are
+  // discarded)
+  const double rp = bilu0_diag_lu<BS>(dc, lane, FULL, 0);
   if (lane < BS) {
     double piv = dc[0];  // this lane's diagonal element of U_II
 #pragma unroll
@@ -1108,6 +1277,7 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
     if (piv == 0.0) atomicMin(ss.zp, I);
 #pragma unroll
     for (int r = 0; r < BS; ++r) D[r * BS + lane] = dc[r];
+    ss.rdiag[(long long)I * BS + lane] = rp;
   }
   __syncwarp();
   // U blocks right of the diagonal: U_IJ = L_II^-1 A_IJ, lane per column
@@ -1283,6 +1453,42 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_bilu0_syncfree(
   }
 }
 
+// Rows of each level in ascending index order.  The order inside a level
+// is free (its rows are independent); sorted, the rows a warp takes at
+// consecutive levels of a structured problem depend on rows of a few
+// neighbouring warps instead of rows all over the previous level, which
+// the flow schedule turns into shorter waits.  One CTA per level, bitonic
+// sort in shared memory; a level wider than kSortCap keeps its breadth-first
+// order (only the speed depends on it).
+constexpr int kSortCap = 16384;
+
+__global__ void __launch_bounds__(512) k_sort_levels(int* order, const int* __restrict__ lvl_ptr) {
+  extern __shared__ int sbuf[];
+  const int l = blockIdx.x;
+  const int s = __ldg(lvl_ptr + l), n = __ldg(lvl_ptr + l + 1) - s;
+  if (n <= 1 || n > kSortCap) return;
+  int m2 = 1;
+  while (m2 < n) m2 <<= 1;
+  for (int t = threadIdx.x; t < m2; t += blockDim.x) sbuf[t] = t < n ? order[s + t] : INT_MAX;
+  __syncthreads();
+  for (int k = 2; k <= m2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = threadIdx.x; t < m2; t += blockDim.x) {
+        const int u = t ^ j;
+        if (u > t) {
+          const int a = sbuf[t], c = sbuf[u];
+          if ((a > c) == ((t & k) == 0)) {
+            sbuf[t] = c;
+            sbuf[u] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int t = threadIdx.x; t < n; t += blockDim.x) order[s + t] = sbuf[t];
+}
+
 // ---------------------------------------------------------------- level schedule (host)
 int coop_grid(const void* fn, int threads, size_t smem = 0) {
   return occupancy_grid(fn, threads, smem);
@@ -1320,7 +1526,7 @@ int launch_coop(const void* fn, int grid, int threads, void** args, cudaStream_t
 // lvl_ptr[nb+2] and *nlev_d on the device; *h_nlev on the host.
 int build_levels(int nb, const int* row, const int* col, const int* diag, int lower,
                  long long ndeps_max, int* order, int* lvl_ptr, int* nlev_d, int* h_nlev,
-                 Carver& ws, cudaStream_t st, int* h_sched = nullptr) {
+                 Carver& ws, cudaStream_t st, int* h_sched = nullptr, int* h_maxdeg = nullptr) {
   int* sptr = ws.take<int>((size_t)nb + 1);
   int* cursor = ws.take<int>((size_t)nb + 1);
   int* indeg = ws.take<int>((size_t)nb + 1);
@@ -1336,6 +1542,7 @@ int build_levels(int nb, const int* row, const int* col, const int* diag, int lo
   BILU_TRY_CUDA(cudaMemsetAsync(lvl_ptr, 0, sizeof(int) * ((size_t)nb + 2), st));
   if (nb == 0) {
     if (h_nlev) *h_nlev = 0;
+    if (h_maxdeg) *h_maxdeg = 0;
     return BILU_OK;
   }
   k_dep_count<<<ceil_div(nb, 256), 256, 0, st>>>(nb, row, col, diag, lower, sptr, indeg,
@@ -1358,6 +1565,17 @@ int build_levels(int nb, const int* row, const int* col, const int* diag, int lo
   BILU_TRY_CUDA(cudaStreamSynchronize(st));
   if (h[1] != nb) return BILU_ERR_PATTERN;  // a row was never reached
   if (h_nlev) *h_nlev = h[0];
+  if (h[0] > 0) {
+    static bool attr_set = false;
+    if (!attr_set) {
+      BILU_TRY_CUDA(cudaFuncSetAttribute((const void*)k_sort_levels,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(kSortCap * sizeof(int))));
+      attr_set = true;
+    }
+    k_sort_levels<<<(unsigned)h[0], 512, kSortCap * sizeof(int), st>>>(order, lvl_ptr);
+    BILU_LAUNCH_CHECK();
+  }
   // nlev_d[1] = the largest dependency count (picks warp or group rows);
   // nlev_d[2] = the recommended schedule (0 level, 1 sync-free)
   BILU_TRY_CUDA(cudaMemcpyAsync(nlev_d + 1, tail + 1, sizeof(int), cudaMemcpyDeviceToDevice, st));
@@ -1368,6 +1586,7 @@ int build_levels(int nb, const int* row, const int* col, const int* diag, int lo
   int sched = ((long long)nb < (long long)kMinLevelWidth * h[0] || maxdeg > kLongRow) ? 1 : 0;
   BILU_TRY_CUDA(cudaMemcpy(nlev_d + 2, &sched, sizeof(int), cudaMemcpyHostToDevice));
   if (h_sched) *h_sched = sched;
+  if (h_maxdeg) *h_maxdeg = maxdeg;
   return BILU_OK;
 }
 
@@ -1386,6 +1605,28 @@ int launch_sptrsv_levels(int nb, const int* row, const int* col, const int* diag
   gs.per_sm = std::max(1, std::min(occupancy_per_sm(fn, kLvlThreads), (int)ceil_div(grid, sm_count())));
   (void)nlev;
   void* args[] = {&row, &col, &diag, &val, &b, &x, &order, &lvl_ptr, &nlev_d, &ss, &gs};
+  return launch_coop(fn, grid, kLvlThreads, args, st);
+}
+
+// Flow-scheduled solve: x is filled with the pending pattern on the stream,
+// then one cooperative launch (every warp resident, so every wait ends).
+template <int BS>
+int launch_sptrsv_flow(int nb, const int* row, const int* col, const int* diag,
+                       const double* val, int lower, int unit, const double* b, double* x,
+                       const int* order, const int* lvl_ptr, const int* nlev_d, SyncState ss,
+                       cudaStream_t st) {
+  const void* fn = lower ? (unit ? (const void*)k_sptrsv_flow<BS, true, true>
+                                 : (const void*)k_sptrsv_flow<BS, true, false>)
+                         : (unit ? (const void*)k_sptrsv_flow<BS, false, true>
+                                 : (const void*)k_sptrsv_flow<BS, false, false>);
+  int grid = std::min<long long>(coop_grid(fn, kLvlThreads),
+                                 ceil_div(nb, (kLvlThreads / 32) * (32 / BS)));
+  int per_sm = std::max(1, std::min(occupancy_per_sm(fn, kLvlThreads), (int)ceil_div(grid, sm_count())));
+  const long long n = (long long)nb * BS;
+  k_fill_pending<<<(unsigned)std::min<long long>(ceil_div(n, 256), (long long)sm_count() * 16),
+                   256, 0, st>>>((unsigned long long*)x, n);
+  BILU_LAUNCH_CHECK();
+  void* args[] = {&row, &col, &diag, &val, &b, &x, &order, &lvl_ptr, &nlev_d, &ss, &per_sm};
   return launch_coop(fn, grid, kLvlThreads, args, st);
 }
 
@@ -1477,13 +1718,16 @@ int sync_init_words(SyncState& ss, Carver& ws, cudaStream_t st) {
 }  // namespace
 
 // BILU(0) in place, level scheduled (one cooperative launch, one grid
-// barrier per dependency level of the lower DAG).
+// barrier per dependency level of the lower DAG) or sync-free.  rdiag
+// (nb x bs) receives the reciprocal pivots; null: carved from ws.
 int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, const int* diag,
-               double* val, int* h_zp, Carver& ws, cudaStream_t st, int schedule) {
+               double* val, int* h_zp, Carver& ws, cudaStream_t st, int schedule,
+               double* rdiag) {
   int* order = ws.take<int>((size_t)nb + 1);
   int* lvl = ws.take<int>((size_t)nb + 2);
   int* nlev_d = ws.take<int>(4);
-  if (!order || !lvl || !nlev_d) return BILU_ERR_WORKSPACE;
+  if (!rdiag) rdiag = ws.take<double>((size_t)nb * bs + 1);
+  if (!order || !lvl || !nlev_d || !rdiag) return BILU_ERR_WORKSPACE;
   int nlev = 0, sched = 0;
   {
     Carver w2 = ws;
@@ -1496,12 +1740,14 @@ int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, c
     SyncState ss;
     BILU_TRY(sync_init(ss, nb, ws, st));
     ss.order = order;
+    ss.rdiag = rdiag;
     if (nb > 0)
       BILU_TRY(BILU_DISPATCH_BS(bs, launch_bilu0_syncfree, nb, row, col, diag, val, ss, st));
     return sync_finish(ss, h_zp, st);
   }
   SyncState ss;
   BILU_TRY(sync_init_words(ss, ws, st));
+  ss.rdiag = rdiag;
   GridSync gs;
   BILU_TRY(grid_sync_init(gs, ws, st));
   if (nb > 0)
@@ -1533,17 +1779,28 @@ int sptrsv_impl(int nb, int bs, const int* row, const int* col, const int* diag,
   return sync_finish(ss, nullptr, st);
 }
 
-// Level-scheduled solve with a level analysis (order, lvl_ptr, nlev_d).
+// Level-scheduled solve with a level analysis (order, lvl_ptr, nlev_d):
+// the flow kernel (waits on the x entries read) when no row has more than
+// kLongRow dependencies (maxdeg, from the analysis), else the barrier
+// kernel with a warp per row.  x must not alias b (the flow kernel marks x
+// pending before it starts).
 int sptrsv_levels(int nb, int bs, const int* row, const int* col, const int* diag,
                   const int* order, const int* lvl, const int* nlev_d, const double* val,
-                  int lower, int unit, const double* b, double* x, Carver& ws, cudaStream_t st) {
+                  int lower, int unit, const double* b, double* x, Carver& ws, cudaStream_t st,
+                  int maxdeg) {
   SyncState ss;
   BILU_TRY(sync_init_words(ss, ws, st));
   GridSync gs;
   BILU_TRY(grid_sync_init(gs, ws, st));
-  if (nb > 0)
-    BILU_TRY(BILU_DISPATCH_BS(bs, launch_sptrsv_levels, nb, row, col, diag, val, lower, unit, b,
-                              x, order, lvl, nlev_d, 0, ss, gs, st));
+  ss.err = gs.err;  // one error word for either kernel
+  if (nb > 0) {
+    if (maxdeg <= kLongRow)
+      BILU_TRY(BILU_DISPATCH_BS(bs, launch_sptrsv_flow, nb, row, col, diag, val, lower, unit, b,
+                                x, order, lvl, nlev_d, ss, st));
+    else
+      BILU_TRY(BILU_DISPATCH_BS(bs, launch_sptrsv_levels, nb, row, col, diag, val, lower, unit,
+                                b, x, order, lvl, nlev_d, 0, ss, gs, st));
+  }
   return grid_sync_finish(gs, st);
 }
 
@@ -1568,24 +1825,24 @@ int sptrsv_level_impl(int nb, long long nnzb, int bs, const int* row, const int*
   int* lvl = ws.take<int>((size_t)nb + 2);
   int* nlev_d = ws.take<int>(4);
   if (!order || !lvl || !nlev_d) return BILU_ERR_WORKSPACE;
-  int sched = 0;
+  int sched = 0, maxdeg = 0;
   {
     Carver w2 = ws;
     BILU_TRY(build_levels(nb, row, col, diag, lower, std::max(nnzb - nb, 0ll), order, lvl,
-                          nlev_d, nullptr, w2, st, &sched));
+                          nlev_d, nullptr, w2, st, &sched, &maxdeg));
   }
   if (sched == 1)
     return sptrsv_syncfree_ordered(nb, bs, row, col, diag, order, val, lower, unit, b, x, ws, st);
   return sptrsv_levels(nb, bs, row, col, diag, order, lvl, nlev_d, val, lower, unit, b, x, ws,
-                       st);
+                       st, maxdeg);
 }
 
 // Level analysis into caller-owned arrays (order[nb+1], lvl[nb+2], nlev[2]).
 int level_analysis(int nb, long long nnzb, const int* row, const int* col, const int* diag,
                    int lower, int* order, int* lvl, int* nlev_d, int* h_nlev, Carver& ws,
-                   cudaStream_t st, int* h_sched) {
+                   cudaStream_t st, int* h_sched, int* h_maxdeg) {
   return build_levels(nb, row, col, diag, lower, std::max(nnzb - nb, 0ll), order, lvl, nlev_d,
-                      h_nlev, ws, st, h_sched);
+                      h_nlev, ws, st, h_sched, h_maxdeg);
 }
 
 // Launch-only sync-free solve for use inside a solver: flags and ticket
@@ -1594,11 +1851,11 @@ int level_analysis(int nb, long long nnzb, const int* row, const int* col, const
 int sptrsv_syncfree_async(int nb, int bs, const int* row, const int* col, const int* diag,
                           const int* order, const double* val, int lower, int unit,
                           const double* b, double* x, int* flags, int* ticket, int* err,
-                          cudaStream_t st) {
+                          cudaStream_t st, const double* rdiag) {
   if (nb == 0) return BILU_OK;
   BILU_TRY_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * ((size_t)nb + 1), st));
   BILU_TRY_CUDA(cudaMemsetAsync(ticket, 0, sizeof(int), st));
-  SyncState ss{flags, ticket, err, err, kSpinLimit, -1, order};
+  SyncState ss{flags, ticket, err, err, kSpinLimit, -1, order, const_cast<double*>(rdiag)};
   return BILU_DISPATCH_BS(bs, launch_sptrsv, nb, row, col, diag, val, lower, unit, b, x, ss, st);
 }
 
@@ -1609,10 +1866,14 @@ int sptrsv_syncfree_async(int nb, int bs, const int* row, const int* col, const 
 int sptrsv_levels_async(int nb, int bs, const int* row, const int* col, const int* diag,
                         const int* order, const int* lvl, const int* nlev_d, const double* val,
                         int lower, int unit, const double* b, double* x, unsigned* words,
-                        cudaStream_t st) {
+                        cudaStream_t st, const double* rdiag, int maxdeg) {
   if (nb == 0) return BILU_OK;
   int* w = (int*)words;
-  SyncState ss{nullptr, nullptr, w + 2, w + 3, kSpinLimit, -1, nullptr};
+  SyncState ss{nullptr, nullptr, w + 2, w + 3, kSpinLimit, -1, nullptr,
+               const_cast<double*>(rdiag)};
+  if (maxdeg <= kLongRow)
+    return BILU_DISPATCH_BS(bs, launch_sptrsv_flow, nb, row, col, diag, val, lower, unit, b, x,
+                            order, lvl, nlev_d, ss, st);
   GridSync gs{words, words + 1, w + 2, kSpinLimit};
   return BILU_DISPATCH_BS(bs, launch_sptrsv_levels, nb, row, col, diag, val, lower, unit, b, x,
                           order, lvl, nlev_d, 0, ss, gs, st);
@@ -1635,6 +1896,14 @@ struct AnalysisView {
     nlev = c.take<int>(4);  // levels, largest dependency count, schedule, spare
   }
 };
+
+// The analysis record's four words on the host (a synchronising read).
+int read_analysis_words(int nb, const AnalysisView& a, int* h, cudaStream_t st) {
+  if (nb == 0) return BILU_OK;
+  BILU_TRY_CUDA(cudaMemcpyAsync(h, a.nlev, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
+  BILU_TRY_CUDA(cudaStreamSynchronize(st));
+  return BILU_OK;
+}
 
 }  // namespace
 
@@ -1670,42 +1939,43 @@ extern "C" int bilu_sptrsv_solve(int nb, int bs, const int* d_row, const int* d_
                                  const double* d_val, int lower, int unit, const void* d_info,
                                  const double* d_b, double* d_x, void* d_ws, size_t ws_bytes,
                                  bilu_stream_t stream) {
-  if (nb < 0 || !d_info || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)))
+  if (nb < 0 || !d_info || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)) ||
+      (nb > 0 && (const void*)d_b == (const void*)d_x))
     return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   AnalysisView a(const_cast<void*>(d_info), nb);
   Carver ws(d_ws, ws_bytes);
-  int sched = 0;
-  if (nb > 0) {
-    BILU_TRY_CUDA(cudaMemcpyAsync(&sched, a.nlev + 2, sizeof(int), cudaMemcpyDeviceToHost,
-                                  S(stream)));
-    BILU_TRY_CUDA(cudaStreamSynchronize(S(stream)));
-  }
-  if (sched == 1)
+  int h[4] = {0, 0, 0, 0};  // levels, largest dependency count, schedule, spare
+  BILU_TRY(read_analysis_words(nb, a, h, S(stream)));
+  if (h[2] == 1)
     return sptrsv_syncfree_ordered(nb, bs, d_row, d_col, a.diag, a.order, d_val, lower != 0,
                                    unit != 0, d_b, d_x, ws, S(stream));
   return sptrsv_levels(nb, bs, d_row, d_col, a.diag, a.order, a.lvl, a.nlev, d_val, lower != 0,
-                       unit != 0, d_b, d_x, ws, S(stream));
+                       unit != 0, d_b, d_x, ws, S(stream), h[1]);
 }
 
 extern "C" int bilu_sptrsv_solve_level(int nb, int bs, const int* d_row, const int* d_col,
                                        const double* d_val, int lower, int unit,
                                        const void* d_info, const double* d_b, double* d_x,
                                        void* d_ws, size_t ws_bytes, bilu_stream_t stream) {
-  if (nb < 0 || !d_info || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)))
+  if (nb < 0 || !d_info || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)) ||
+      (nb > 0 && (const void*)d_b == (const void*)d_x))
     return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   AnalysisView a(const_cast<void*>(d_info), nb);
   Carver ws(d_ws, ws_bytes);
+  int h[4] = {0, 0, 0, 0};
+  BILU_TRY(read_analysis_words(nb, a, h, S(stream)));
   return sptrsv_levels(nb, bs, d_row, d_col, a.diag, a.order, a.lvl, a.nlev, d_val, lower != 0,
-                       unit != 0, d_b, d_x, ws, S(stream));
+                       unit != 0, d_b, d_x, ws, S(stream), h[1]);
 }
 
 extern "C" int bilu_sptrsv_solve_syncfree(int nb, int bs, const int* d_row, const int* d_col,
                                           const double* d_val, int lower, int unit,
                                           const void* d_info, const double* d_b, double* d_x,
                                           void* d_ws, size_t ws_bytes, bilu_stream_t stream) {
-  if (nb < 0 || !d_info || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)))
+  if (nb < 0 || !d_info || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)) ||
+      (nb > 0 && (const void*)d_b == (const void*)d_x))
     return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   AnalysisView a(const_cast<void*>(d_info), nb);
@@ -1716,8 +1986,9 @@ extern "C" int bilu_sptrsv_solve_syncfree(int nb, int bs, const int* d_row, cons
 
 extern "C" size_t bilu_bsrilu0_ws_bytes(int nb, int nnzb) {
   if (nb < 0 || nnzb < 0) return 0;
+  // diag, bad-row word, reciprocal pivots (largest block size), level scratch
   return carve_size(sizeof(int) * ((size_t)nb + 1)) + carve_size(sizeof(int) * 2) +
-         level_sched_ws(nb, nnzb);
+         carve_size(sizeof(double) * ((size_t)nb * 8 + 1)) + level_sched_ws(nb, nnzb);
 }
 
 extern "C" int bilu_bsrilu0(int nb, int nnzb, int bs, const int* d_row, const int* d_col,
@@ -1742,7 +2013,8 @@ extern "C" int bilu_bsrilu0_ex(int nb, int nnzb, int bs, const int* d_row, const
     if (h_info) *h_info = bad;
     return rc;
   }
-  return bilu0_impl(nb, nnzb, bs, d_row, d_col, diag, d_val, h_info, ws, S(stream), schedule);
+  return bilu0_impl(nb, nnzb, bs, d_row, d_col, diag, d_val, h_info, ws, S(stream), schedule,
+                    nullptr);
 }
 
 extern "C" size_t bilu_sptrsv_ws_bytes(int nb, int nnzb) {
@@ -1761,7 +2033,8 @@ extern "C" int bilu_sptrsv(int nb, int nnzb, int bs, const int* d_row, const int
 extern "C" int bilu_sptrsv_ex(int nb, int nnzb, int bs, const int* d_row, const int* d_col,
                               const double* d_val, int lower, int unit, const double* d_b,
                               double* d_x, void* d_ws, size_t ws_bytes, bilu_stream_t stream) {
-  if (nb < 0 || nnzb < nb || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)))
+  if (nb < 0 || nnzb < nb || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x)) ||
+      (nb > 0 && (const void*)d_b == (const void*)d_x))
     return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   Carver ws(d_ws, ws_bytes);
