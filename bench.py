@@ -575,6 +575,14 @@ def run_sptrsv(args):
     e1.synchronize()
     out = {"workload": f"sptrsv convdiff3d {args.side}^3 bs4 (nb={nb}, nnzb={nnzb})",
            "bilu0_ms_incl_analysis": e0.elapsed_time(e1), "zero_pivot": zp}
+    # what the level-order kernels are bound by (SM cycles)
+    sp = (ctypes.c_double * 8)()
+    _lib.check("bilu_probe_sync", L.bilu_probe_sync(sp))
+    out["sync_probe_cycles"] = {
+        "dfma_interval_per_sm_1_4_16_warps": [round(sp[0], 1), round(sp[1], 1), round(sp[2], 1)],
+        "dfma_interval_per_sm_4_warps_4_lanes": round(sp[3], 1),
+        "store_to_load_one_way_min_max": [round(sp[4]), round(sp[5])],
+        "release_acquire_one_way": round(sp[6]), "l2_hit_load": round(sp[7])}
     b = torch.from_numpy(gen.rhs(A.n, 1)).to(dev)
     x = torch.empty_like(b)
     P = api._p

@@ -64,6 +64,14 @@ unsigned long long bilu_kernel_launches(void);
  * h_out[1] DMMA (mma.sync m8n8k4 f64), h_out[2] FFMA.  Sets the compute
  * roofline of the FP64 kernels (allocates and frees a scratch buffer). */
 int bilu_probe_rates(double* h_out);
+/* What the level-order kernels are bound by, in SM cycles: h_out[0..3] the
+ * interval between DFMA warp instructions on one SM with 1, 4 and 16 warps
+ * per SM and with 4 warps of 4 active lanes; h_out[4..5] the one-way
+ * store -> load visibility between two SMs (relaxed; smallest and largest
+ * of four SM pairs); h_out[6] the same with st.release / ld.acquire;
+ * h_out[7] a dependent L2-hit load.  Every wait is bounded
+ * (BILU_ERR_TIMEOUT). */
+int bilu_probe_sync(double* h_out);
 
 /* ------------------------------------------------------------------ */
 /* Format conversions and patterns                                     */
@@ -227,7 +235,9 @@ int bilu_isai_apply(int nb, int bs, int prec, const int* d_Lrow, const int* d_Lc
 /* Replaces spTrSolveL / spTrSolveU (cape_sptrsv.h:8,55) and
  * csr_cape_SpTRSV (cape_sptrsv.h:105), blockwise on the packed BILU(0):
  * lower: unit-lower L x = b; upper: U x = b.  One-shot form: level analysis
- * then the schedule it recommends (see the analysis / solve split below). */
+ * then the schedule it recommends (see the analysis / solve split below).
+ * d_x must not be d_b (BILU_ERR_ARG): the level-order solve marks every x
+ * entry pending before it starts. */
 size_t bilu_sptrsv_ws_bytes(int nb, int nnzb);
 int bilu_sptrsv(int nb, int nnzb, int bs, const int* d_row, const int* d_col, const double* d_val,
                 int lower, const double* d_b, double* d_x, void* d_ws, size_t ws_bytes,
@@ -238,9 +248,12 @@ int bilu_sptrsv(int nb, int nnzb, int bs, const int* d_row, const int* d_col, co
  * in d_info, scratch bilu_sptrsv_analysis_ws_bytes) is computed once per
  * pattern and triangle, together with a schedule recommendation: the level
  * schedule when a level holds at least 1024 block rows on average and no
- * row has more than 32 dependencies, the sync-free schedule otherwise.  bilu_sptrsv_solve runs the recommended
- * schedule; bilu_sptrsv_solve_level forces the level-scheduled kernel (one
- * cooperative launch, a bounded grid barrier per level);
+ * row has more than 32 dependencies, the sync-free schedule otherwise.
+ * bilu_sptrsv_solve runs the recommended schedule; bilu_sptrsv_solve_level
+ * forces the level-order kernel (one cooperative launch; rows taken in level
+ * order by lane groups, each waiting only for the x entries it reads, which
+ * start as a signalling-NaN pattern; rows with more than 32 dependencies
+ * instead take a warp each and a bounded grid barrier per level);
  * bilu_sptrsv_solve_syncfree forces the sync-free kernel of the reference's
  * design (block rows taken by atomic tickets in level order, per-row ready
  * flags polled by the dependent rows, every wait bounded:
