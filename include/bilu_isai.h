@@ -152,10 +152,11 @@ int bilu_bcsc_to_bcsr(int mb, int nbcol, int bs, const int* d_cscPtr, const int*
 
 /* Replaces bsrilu02_inplace (bsrilu.h:20; cuSPARSE bsrilu02, row direction,
  * no level information): BILU(0) in place.  A level analysis of the lower
- * DAG picks the schedule: wide levels and short rows -> one cooperative
- * launch with a bounded grid barrier per level (a bs-lane group per row);
- * narrow levels or rows with more than 32 dependencies -> sync-free (warp
- * per row, atomic tickets in level order, bounded waits on ready flags).
+ * DAG picks the schedule: levels of at least 4096 block rows on average and
+ * no row with more than 32 dependencies -> one cooperative launch with a
+ * bounded grid barrier per level (a bs-lane group per row); otherwise
+ * sync-free (warp per row, atomic tickets in level order, bounded waits on
+ * ready flags).
  * h_info[0] receives the first block row with a zero pivot (or -1);
  * BILU_ERR_ZERO_PIVOT then. */
 size_t bilu_bsrilu0_ws_bytes(int nb, int nnzb);
@@ -247,8 +248,8 @@ int bilu_sptrsv(int nb, int nnzb, int bs, const int* d_row, const int* d_col, co
  * levels and the rows in level order; bilu_sptrsv_analysis_bytes(nb) bytes
  * in d_info, scratch bilu_sptrsv_analysis_ws_bytes) is computed once per
  * pattern and triangle, together with a schedule recommendation: the level
- * schedule when a level holds at least 1024 block rows on average and no
- * row has more than 32 dependencies, the sync-free schedule otherwise.
+ * order when no row has more than 8 dependencies, the sync-free schedule
+ * otherwise (the record's fourth word holds BILU(0)'s recommendation).
  * bilu_sptrsv_solve runs the recommended schedule; bilu_sptrsv_solve_level
  * forces the level-order kernel (one cooperative launch; rows taken in level
  * order by lane groups, each waiting only for the x entries it reads, which
@@ -491,6 +492,14 @@ int bilu_debug_sptrsv_withhold(int nb, int bs, const int* d_row, const int* d_co
                                const double* d_val, int lower, const double* d_b, double* d_x,
                                int withhold_row, long long spin_limit, void* d_ws,
                                size_t ws_bytes, bilu_stream_t stream);
+/* The same for the level-order (flow) solve: block row withhold_row never
+ * stores its x entries, the rows reading them give up after spin_limit
+ * polls, BILU_ERR_TIMEOUT.  Workspace bilu_sptrsv_ws_bytes(nb, nnzb);
+ * patterns with rows of more than 32 dependencies: BILU_ERR_UNSUPPORTED. */
+int bilu_debug_sptrsv_withhold_flow(int nb, int nnzb, int bs, const int* d_row, const int* d_col,
+                                    const double* d_val, int lower, const double* d_b,
+                                    double* d_x, int withhold_row, long long spin_limit,
+                                    void* d_ws, size_t ws_bytes, bilu_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -632,10 +632,16 @@ __device__ __forceinline__ int spread_warp(int per_sm) {
 // rows with more dependencies than this make the level kernels give each
 // row a whole warp instead of a bs-lane group
 constexpr int kLongRow = 32;
-// level analysis recommendation: the level schedule when a level holds at
-// least this many rows on average, the sync-free schedule otherwise (a
-// level costs a grid barrier; narrow levels are cheaper without one)
-constexpr int kMinLevelWidth = 1024;
+// Level analysis recommendations (measured on GB300, stencil and power-law
+// systems).  Solves: the level order (flow kernel) when no row has more than
+// kFlowMaxDeps dependencies, whatever the level width (it was 4-10x faster
+// than the sync-free kernel on 2D and 3D stencils down to 32 rows per
+// level), the sync-free kernel otherwise (a lane group walks a long row's
+// dependencies one after the other).  BILU(0): the level order (a barrier
+// per level) when a level holds at least kFactorLevelWidth rows on average
+// and no row has more than kLongRow dependencies, sync-free otherwise.
+constexpr int kFlowMaxDeps = 8;
+constexpr int kFactorLevelWidth = 4096;
 
 // Rows of the flow schedule: a group of BS lanes per block row (32/BS rows
 // per warp; lane r of a group owns scalar row r).  On GB300 an FP64 warp
@@ -894,7 +900,7 @@ __device__ __forceinline__ bool grow_finish_flow(const GRowPre<BS>& p, const int
     if (r == c) xr = xc;
     if (LOWER ? (r > c) : (r < c)) v -= p.dq[c] * xc;
   }
-  if (p.I >= 0) st_strong_f64(x + (long long)p.I * BS + r, xr);
+  if (p.I >= 0 && p.I != ss.withhold) st_strong_f64(x + (long long)p.I * BS + r, xr);
   return true;
 }
 
@@ -1526,7 +1532,8 @@ int launch_coop(const void* fn, int grid, int threads, void** args, cudaStream_t
 // lvl_ptr[nb+2] and *nlev_d on the device; *h_nlev on the host.
 int build_levels(int nb, const int* row, const int* col, const int* diag, int lower,
                  long long ndeps_max, int* order, int* lvl_ptr, int* nlev_d, int* h_nlev,
-                 Carver& ws, cudaStream_t st, int* h_sched = nullptr, int* h_maxdeg = nullptr) {
+                 Carver& ws, cudaStream_t st, int* h_sched = nullptr, int* h_maxdeg = nullptr,
+                 int* h_fsched = nullptr) {
   int* sptr = ws.take<int>((size_t)nb + 1);
   int* cursor = ws.take<int>((size_t)nb + 1);
   int* indeg = ws.take<int>((size_t)nb + 1);
@@ -1581,11 +1588,14 @@ int build_levels(int nb, const int* row, const int* col, const int* diag, int lo
   BILU_TRY_CUDA(cudaMemcpyAsync(nlev_d + 1, tail + 1, sizeof(int), cudaMemcpyDeviceToDevice, st));
   int maxdeg = 0;
   BILU_TRY_CUDA(cudaMemcpy(&maxdeg, tail + 1, sizeof(int), cudaMemcpyDeviceToHost));
-  // level schedule only when levels are wide and no row is long: a level
-  // costs a grid barrier and waits for its slowest row
-  int sched = ((long long)nb < (long long)kMinLevelWidth * h[0] || maxdeg > kLongRow) ? 1 : 0;
-  BILU_TRY_CUDA(cudaMemcpy(nlev_d + 2, &sched, sizeof(int), cudaMemcpyHostToDevice));
-  if (h_sched) *h_sched = sched;
+  // nlev_d[2] = the recommended solve schedule, nlev_d[3] the recommended
+  // factorisation schedule (0 level order, 1 sync-free)
+  int sched[2] = {maxdeg > kFlowMaxDeps ? 1 : 0,
+                  ((long long)nb < (long long)kFactorLevelWidth * h[0] || maxdeg > kLongRow) ? 1
+                                                                                            : 0};
+  BILU_TRY_CUDA(cudaMemcpy(nlev_d + 2, sched, sizeof(sched), cudaMemcpyHostToDevice));
+  if (h_sched) *h_sched = sched[0];
+  if (h_fsched) *h_fsched = sched[1];
   if (h_maxdeg) *h_maxdeg = maxdeg;
   return BILU_OK;
 }
@@ -1732,7 +1742,7 @@ int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, c
   {
     Carver w2 = ws;
     BILU_TRY(build_levels(nb, row, col, diag, 1, std::max(nnzb - nb, 0ll), order, lvl, nlev_d,
-                          &nlev, w2, st, &sched));
+                          &nlev, w2, st, nullptr, nullptr, &sched));
   }
   if (schedule == 0 || schedule == 1) sched = schedule;  // caller's choice
   if (sched == 1) {
@@ -1885,7 +1895,7 @@ using namespace bilu;
 
 namespace {
 
-// analysis record: diag[nb+1] | order[nb+1] | lvl_ptr[nb+2] | nlev[2]
+// analysis record: diag[nb+1] | order[nb+1] | lvl_ptr[nb+2] | nlev[4]
 struct AnalysisView {
   int *diag, *order, *lvl, *nlev;
   AnalysisView(void* p, int nb) {
@@ -1893,7 +1903,7 @@ struct AnalysisView {
     diag = c.take<int>((size_t)nb + 1);
     order = c.take<int>((size_t)nb + 1);
     lvl = c.take<int>((size_t)nb + 2);
-    nlev = c.take<int>(4);  // levels, largest dependency count, schedule, spare
+    nlev = c.take<int>(4);  // levels, largest dependency count, solve and factor schedules
   }
 };
 
@@ -1945,7 +1955,7 @@ extern "C" int bilu_sptrsv_solve(int nb, int bs, const int* d_row, const int* d_
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   AnalysisView a(const_cast<void*>(d_info), nb);
   Carver ws(d_ws, ws_bytes);
-  int h[4] = {0, 0, 0, 0};  // levels, largest dependency count, schedule, spare
+  int h[4] = {0, 0, 0, 0};  // levels, largest dependency count, solve / factor schedule
   BILU_TRY(read_analysis_words(nb, a, h, S(stream)));
   if (h[2] == 1)
     return sptrsv_syncfree_ordered(nb, bs, d_row, d_col, a.diag, a.order, d_val, lower != 0,
@@ -2063,4 +2073,46 @@ extern "C" int bilu_debug_sptrsv_withhold(int nb, int bs, const int* d_row, cons
   BILU_TRY(diag_positions(nb, d_row, d_col, diag, nullptr, ws, S(stream)));
   return sptrsv_impl(nb, bs, d_row, d_col, diag, d_val, lower != 0, lower != 0, d_b, d_x, ws,
                      S(stream), spin_limit, withhold_row);
+}
+
+// Test hook: the flow (level-order) solve with block row `withhold_row`
+// never storing its x entries and a spin budget of spin_limit polls, so the
+// rows that read them give up and the call returns BILU_ERR_TIMEOUT (the
+// others see the error word and leave).  Every wait is bounded; the launch
+// ends by itself and the context stays usable.  Patterns with rows of more
+// than 32 dependencies take the barrier kernel and are refused here.
+extern "C" int bilu_debug_sptrsv_withhold_flow(int nb, int nnzb, int bs, const int* d_row,
+                                               const int* d_col, const double* d_val, int lower,
+                                               const double* d_b, double* d_x, int withhold_row,
+                                               long long spin_limit, void* d_ws,
+                                               size_t ws_bytes, bilu_stream_t stream) {
+  if (nb < 1 || nnzb < nb || !d_row || !d_col || !d_val || !d_b || !d_x || d_b == d_x ||
+      spin_limit < 1 || spin_limit > kSpinLimit)
+    return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  cudaStream_t st = S(stream);
+  Carver ws(d_ws, ws_bytes);
+  int* diag = ws.take<int>((size_t)nb + 1);
+  int* order = ws.take<int>((size_t)nb + 1);
+  int* lvl = ws.take<int>((size_t)nb + 2);
+  int* nlev_d = ws.take<int>(4);
+  if (!diag || !order || !lvl || !nlev_d) return BILU_ERR_WORKSPACE;
+  BILU_TRY(diag_positions(nb, d_row, d_col, diag, nullptr, ws, st));
+  int maxdeg = 0;
+  {
+    Carver w2 = ws;
+    BILU_TRY(build_levels(nb, d_row, d_col, diag, lower != 0, (long long)nnzb - nb, order, lvl,
+                          nlev_d, nullptr, w2, st, nullptr, &maxdeg));
+  }
+  if (maxdeg > kLongRow) return BILU_ERR_UNSUPPORTED;
+  SyncState ss;
+  BILU_TRY(sync_init_words(ss, ws, st));
+  GridSync gs;
+  BILU_TRY(grid_sync_init(gs, ws, st));
+  ss.err = gs.err;
+  ss.spin = spin_limit;
+  ss.withhold = withhold_row;
+  BILU_TRY(BILU_DISPATCH_BS(bs, launch_sptrsv_flow, nb, d_row, d_col, diag, d_val, lower != 0,
+                            lower != 0, d_b, d_x, order, lvl, nlev_d, ss, st));
+  return grid_sync_finish(gs, st);
 }

@@ -413,6 +413,67 @@ def test_sptrsv_timeout_path(cuda, orc):
     assert relerr(N(y), yo) < 1e-12
 
 
+@pytest.mark.parametrize("lower", [1, 0])
+def test_flow_solve_withheld_row_times_out(cuda, orc, lower):
+    """The level-order (flow) solve with a row that never stores its x
+    entries: the rows reading them give up after a short bounded wait, the
+    call reports BILU_ERR_TIMEOUT, and the next solve is correct."""
+    import ctypes
+
+    import torch
+
+    from isai_kernel_gb300 import _lib, api
+
+    A = gen.convdiff3d(6, bs=4, seed=1)
+    LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    row, col, lu = T(A.rowptr, cuda), T(A.colind, cuda), T(LU, cuda)
+    b = T(gen.rhs(A.n, 4), cuda)
+    x = torch.empty_like(b)
+    L = _lib.lib()
+    ws = api._ws(L.bilu_sptrsv_ws_bytes(A.nb, A.nnzb), cuda)
+    st = L.bilu_debug_sptrsv_withhold_flow(
+        A.nb, A.nnzb, A.bs, api._p(row), api._p(col), api._p(lu), lower, api._p(b), api._p(x),
+        A.nb // 3, ctypes.c_longlong(1 << 12), api._p(ws), ws.numel(), api._s())
+    assert st == -4  # BILU_ERR_TIMEOUT
+    y = api.sptrsv(A.nb, A.bs, row, col, lu, b, lower=bool(lower))
+    ref = (orc.sptrsv_lower if lower else orc.sptrsv_upper)(A.nb, A.bs, A.rowptr, A.colind, LU,
+                                                             N(b))
+    assert relerr(N(y), ref) < 1e-12
+
+
+def test_nan_in_b_propagates_without_waiting(cuda, orc):
+    """A NaN in b is an ordinary value for the flow solve (only the pending
+    pattern means "not computed"): the solve finishes, the rows that depend
+    on the NaN row are NaN, and the level-order and sync-free solves agree
+    entry for entry."""
+    import torch
+
+    from isai_kernel_gb300 import _lib, api
+
+    A = gen.convdiff3d(6, bs=4, seed=2)
+    LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    row, col, lu = T(A.rowptr, cuda), T(A.colind, cuda), T(LU, cuda)
+    bh = gen.rhs(A.n, 5)
+    bh[4 * 20 + 1] = np.nan
+    b = T(bh, cuda)
+    L = _lib.lib()
+    for lower in (1, 0):
+        info = api._ws(L.bilu_sptrsv_analysis_bytes(A.nb), cuda)
+        ws = api._ws(max(L.bilu_sptrsv_analysis_ws_bytes(A.nb, A.nnzb),
+                         L.bilu_sptrsv_solve_ws_bytes(A.nb)), cuda)
+        api.call("bilu_sptrsv_analysis", A.nb, A.nnzb, A.bs, api._p(row), api._p(col), lower,
+                 api._p(info), api._p(ws), ws.numel(), api._s())
+        xs = []
+        for fn in ("bilu_sptrsv_solve_level", "bilu_sptrsv_solve_syncfree"):
+            x = torch.empty_like(b)
+            api.call(fn, A.nb, A.bs, api._p(row), api._p(col), api._p(lu), lower, lower,
+                     api._p(info), api._p(b), api._p(x), api._p(ws), ws.numel(), api._s())
+            xs.append(N(x))
+        nan0, nan1 = np.isnan(xs[0]), np.isnan(xs[1])
+        assert nan0.any() and np.array_equal(nan0, nan1)
+        assert np.array_equal(xs[0][~nan0], xs[1][~nan1])
+
+
 # ------------------------------------------------------------------ errors
 def test_pattern_errors(cuda):
     import torch
