@@ -210,9 +210,10 @@ def cpu_baseline(side, iters_full, gmres_iters=3, seed=0):
     t_it = (time.perf_counter() - t0) / max(it, 1)
     est = t_setup + t_it * iters_full
     cores = oracle.num_threads()
-    # the serial CPU BILU(0) + triangular-solve path on one core (the
-    # reference has no CPU ILU / SpTRSV; its GPU sync-free solve is the
-    # restated algorithm), next to the GPU factor and solves
+    # the serial CPU path on one core: BILU(0), the whole ISAI setup (BILU(0)
+    # again, patterns, pairs, Dinv, ISAI-L/U, reorder), one FP64 and one
+    # FP32-stored apply, the two triangular solves (the reference has no CPU
+    # ILU / ISAI / SpTRSV; its GPU kernels are the restated algorithms)
     oracle.set_threads(1)
     try:
         t0 = time.perf_counter()
@@ -224,6 +225,18 @@ def cpu_baseline(side, iters_full, gmres_iters=3, seed=0):
         t0 = time.perf_counter()
         oracle.sptrsv_upper(A.nb, A.bs, A.rowptr, A.colind, LU, y)
         t_u1 = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        oracle.isai_setup(A)
+        t_s1 = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        y = oracle.bcsr_spmv(A.nb, A.bs, L[0], L[1], L[2], b)
+        oracle.bcsr_spmv(A.nb, A.bs, U[0], U[1], U[2], y)
+        t_a64 = time.perf_counter() - t0
+        L32, U32, b32 = (a.astype(np.float32) for a in (L[2], U[2], b))
+        t0 = time.perf_counter()
+        y32 = oracle.bcsr_spmv_f32(A.nb, A.bs, L[0], L[1], L32, b32)
+        oracle.bcsr_spmv_f32(A.nb, A.bs, U[0], U[1], U32, y32)
+        t_a32 = time.perf_counter() - t0
     finally:
         oracle.set_threads(cores)
     return {"value": est, "unit": "s", "cores": cores, "kind": "port",
@@ -231,7 +244,8 @@ def cpu_baseline(side, iters_full, gmres_iters=3, seed=0):
                        f"{it} FGMRES(30) iterations measured at {t_it:.3f} s each, scaled to "
                        f"{iters_full} iterations"),
             "setup_s": t_setup, "per_iter_s": t_it,
-            "serial_1_core": {"bilu0_s": t_f1, "sptrsv_L_s": t_l1, "sptrsv_U_s": t_u1}}
+            "serial_1_core": {"bilu0_s": t_f1, "isai_setup_s": t_s1, "apply_fp64_s": t_a64,
+                              "apply_fp32_s": t_a32, "sptrsv_L_s": t_l1, "sptrsv_U_s": t_u1}}
 
 
 def run_reference(args):
