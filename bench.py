@@ -524,7 +524,8 @@ def run_batch(args):
             "pair_steps_per_s": stats[2] / (stats[3] / 1e3),
             "converged_fraction": conv, "median_iters": float(np.median(iters)),
             "autotune": {"rows_per_warp_A": cfg[0], "rows_per_warp_apply": cfg[1],
-                         "candidates_ms_A": tune_ms[:3], "candidates_ms_apply": tune_ms[3:]}}
+                         "tile_rows": cfg[2], "candidates_ms_A": tune_ms[:3],
+                         "candidates_ms_apply": tune_ms[3:6]}}
     bt.close()
     print(json.dumps(line))
 

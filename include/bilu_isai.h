@@ -451,8 +451,9 @@ int bilu_batch_solve(bilu_batch* batch, int k, const double* d_B, double* d_X, i
                      double tol, int maxit, long long mem_budget, int* h_iters,
                      double* h_relres, double* h_stats);
 /* Autotuner result: h_cfg = {rows per warp of the operator SpMM, of the
- * apply SpMM, tile rows}; h_ms[6] = timed candidates (1, 2, 4 rows per warp)
- * for the operator and the apply. */
+ * apply SpMM, tile rows (fixed: tiles partition the dot products)};
+ * h_ms[6] = timed candidates (1, 2, 4 rows per warp) for the operator and
+ * the apply. */
 int bilu_batch_tuning(bilu_batch* batch, int* h_cfg, double* h_ms);
 
 /* ------------------------------------------------------------------ */

@@ -142,15 +142,45 @@ __global__ void __launch_bounds__(kBT) k_sweep(int ntiles, int k, const int* __r
   }
 }
 
-// out[s][c] = sum over the tiles of system s (in order) of partial[t][c]
-__global__ void k_segsum(int S, int k, const int* __restrict__ sys_tiles,
-                         const double* __restrict__ partial, double* __restrict__ out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= S * k) return;
-  int s = i / k, c = i - s * k;
+// out[s][c] = sum over the tiles of system s of partial[t][c].  One CTA per
+// system, lane = right-hand side: warp w sums the system's tiles w, w + W,
+// w + 2W, ... in that order (four loads in flight), then the W warp sums are
+// added in warp order.  The order depends only on a tile's index inside its
+// system, so the result does not depend on how systems are grouped into
+// waves.  (A thread per (system, rhs) walking thousands of tiles took
+// ~230 us per call on a 2M-row wave, a quarter of the solve.)
+constexpr int kSegWarps = 16;
+
+__global__ void __launch_bounds__(32 * kSegWarps) k_segsum(int S, int k,
+                                                            const int* __restrict__ sys_tiles,
+                                                            const double* __restrict__ partial,
+                                                            double* __restrict__ out) {
+  __shared__ double red[kSegWarps][32];
+  const int s = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double v = 0.0;
-  for (int t = sys_tiles[s]; t < sys_tiles[s + 1]; ++t) v += partial[(long long)t * k + c];
-  out[i] = v;
+  if (s < S && lane < k) {
+    const int t1 = sys_tiles[s + 1];
+    int t = sys_tiles[s] + warp;
+    for (; t + 3 * kSegWarps < t1; t += 4 * kSegWarps) {
+      const double a = partial[(long long)t * k + lane];
+      const double b = partial[(long long)(t + kSegWarps) * k + lane];
+      const double c = partial[(long long)(t + 2 * kSegWarps) * k + lane];
+      const double d = partial[(long long)(t + 3 * kSegWarps) * k + lane];
+      v += a;
+      v += b;
+      v += c;
+      v += d;
+    }
+    for (; t < t1; t += kSegWarps) v += partial[(long long)t * k + lane];
+  }
+  red[warp][lane] = v;
+  __syncthreads();
+  if (warp == 0 && s < S && lane < k) {
+    double r = 0.0;
+#pragma unroll
+    for (int w = 0; w < kSegWarps; ++w) r += red[w][lane];
+    out[(long long)s * k + lane] = r;
+  }
 }
 
 // y = x / sqrt(nrm2[s][c]) (0 when the norm is 0), with an FP32 copy
@@ -344,9 +374,12 @@ struct bilu_batch {
             *Urow = nullptr, *Ucol = nullptr;
   const double* Aval = nullptr;
   const float *L32 = nullptr, *U32 = nullptr;
-  int rpw_A = 1, rpw_M = 1, tile_rows = 128;  // tuned
+  // rows per warp of the SpMMs (tuned: they do not change any sum's order);
+  // scalar rows per tile of the sweeps (fixed: the tiles partition every
+  // dot product, so the tile size is part of the arithmetic)
+  int rpw_A = 1, rpw_M = 1, tile_rows = 128;
   bool tuned = false;
-  double tune_ms[3][3] = {};
+  double tune_ms[2][3] = {};
 };
 
 namespace {
@@ -511,6 +544,28 @@ struct WaveBufs {
 
 }  // namespace
 
+namespace {
+
+// Tiles of tile_rows scalar rows over systems [s0, s1), never across a system.
+void build_tiles(const bilu_batch* B, int s0, int s1, int tile_rows, std::vector<int>& trow,
+                 std::vector<int>& tsys, std::vector<int>& stile) {
+  const int r0 = B->sys[s0], bs = B->bs;
+  trow.clear();
+  tsys.clear();
+  stile.assign(s1 - s0 + 1, 0);
+  for (int s = s0; s < s1; ++s) {
+    long long a = (long long)(B->sys[s] - r0) * bs, e = (long long)(B->sys[s + 1] - r0) * bs;
+    for (long long x = a; x < e; x += tile_rows) {
+      trow.push_back((int)x);
+      tsys.push_back(s - s0);
+    }
+    stile[s - s0 + 1] = (int)tsys.size();
+  }
+  trow.push_back((int)((long long)(B->sys[s1] - r0) * bs));
+}
+
+}  // namespace
+
 // Solves every system for k right-hand sides (B, X: [n, k] row-major FP64,
 // n = nb*bs).  h_iters / h_relres: [S*k] per pair (system-major).  h_stats
 // (optional, 4): waves, graph launches, total pair-steps, solve ms.
@@ -592,31 +647,22 @@ extern "C" int bilu_batch_solve(bilu_batch* Bt, int k, const double* d_B, double
     int s0 = wv.first, s1 = wv.second, Sw = s1 - s0, Pw = Sw * k;
     int r0 = Bt->sys[s0], r1 = Bt->sys[s1];
     long long n_w = (long long)(r1 - r0) * bs;
-    // tiles of tile_rows scalar rows, never across a system
-    std::vector<int> trow, tsys, stile(Sw + 1, 0);
-    for (int s = s0; s < s1; ++s) {
-      long long a = (long long)(Bt->sys[s] - r0) * bs, e = (long long)(Bt->sys[s + 1] - r0) * bs;
-      for (long long x = a; x < e; x += Bt->tile_rows) {
-        trow.push_back((int)x);
-        tsys.push_back(s - s0);
-      }
-      stile[s - s0 + 1] = (int)tsys.size();
-    }
+    std::vector<int> trow, tsys, stile;
+    build_tiles(Bt, s0, s1, Bt->tile_rows, trow, tsys, stile);
     int nt = (int)tsys.size();
-    trow.push_back((int)n_w);
     BILU_TRY_CUDA(cudaMemcpyAsync(W.trow, trow.data(), sizeof(int) * (nt + 1), cudaMemcpyHostToDevice, st));
     BILU_TRY_CUDA(cudaMemcpyAsync(W.tsys, tsys.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st));
     BILU_TRY_CUDA(cudaMemcpyAsync(W.stile, stile.data(), sizeof(int) * (Sw + 1), cudaMemcpyHostToDevice, st));
     const double* Bw = d_B + (size_t)(r0)*bs * k;
     double* Xw = d_X + (size_t)(r0)*bs * k;
-    unsigned gp = ceil_div(Pw, 128), gs = ceil_div(Pw, 128);
+    unsigned gp = ceil_div(Pw, 128);
     if (!Bt->tuned) BILU_TRY(autotune(Bt, r0, r1, k, W.r, W.w, W.v32, W.t32));
     // x = 0, r = b, ||b||
     BILU_TRY_CUDA(cudaMemsetAsync(Xw, 0, sizeof(double) * n_w * k, st));
     BILU_TRY_CUDA(cudaMemsetAsync(W.w, 0, sizeof(double) * n_w * k, st));
     k_residual_pairs<<<nt, kBT, 0, st>>>(nt, k, W.trow, Bw, W.w, W.r, W.part);
     BILU_LAUNCH_CHECK();
-    k_segsum<<<gs, 128, 0, st>>>(Sw, k, W.stile, W.part, W.rr);
+    k_segsum<<<Sw, 32 * kSegWarps, 0, st>>>(Sw, k, W.stile, W.part, W.rr);
     BILU_LAUNCH_CHECK();
     k_bnorm<<<gp, 128, 0, st>>>(Pw, W.ps, W.rr);
     BILU_LAUNCH_CHECK();
@@ -646,7 +692,7 @@ extern "C" int bilu_batch_solve(bilu_batch* Bt, int k, const double* d_B, double
             const double* vn = i <= j ? W.V + vec * i : nullptr;
             double* out = i <= j ? W.hcol + (size_t)i * Pw : W.hn2;
             k_sweep<<<nt, kBT, 0, st>>>(nt, k, W.trow, W.tsys, vp, hp, vn, W.w, W.part);
-            k_segsum<<<gs, 128, 0, st>>>(Sw, k, W.stile, W.part, out);
+            k_segsum<<<Sw, 32 * kSegWarps, 0, st>>>(Sw, k, W.stile, W.part, out);
           }
           k_scale_pairs<<<nt, kBT, 0, st>>>(nt, k, W.trow, W.tsys, W.w, W.hn2, W.V + vec * (j + 1),
                                             W.v32);
@@ -674,7 +720,7 @@ extern "C" int bilu_batch_solve(bilu_batch* Bt, int k, const double* d_B, double
       BILU_TRY(spmm_A(Bt, Bt->rpw_A, r0, r1, k, Xw, W.w));
       k_residual_pairs<<<nt, kBT, 0, st>>>(nt, k, W.trow, Bw, W.w, W.r, W.part);
       BILU_LAUNCH_CHECK();
-      k_segsum<<<gs, 128, 0, st>>>(Sw, k, W.stile, W.part, W.rr);
+      k_segsum<<<Sw, 32 * kSegWarps, 0, st>>>(Sw, k, W.stile, W.part, W.rr);
       BILU_LAUNCH_CHECK();
       BILU_TRY_CUDA(cudaMemsetAsync(W.counters + 1, 0, sizeof(int), st));
       k_check<<<gp, 128, 0, st>>>(Pw, tol, W.ps, W.rr, W.relres, W.counters + 1);
