@@ -337,7 +337,9 @@ int bilu_ctx_destroy(bilu_ctx* ctx);
  * ISAI-L/U, BCSC->BCSR reorder, FP32 copies when prec_mask has
  * 1 << BILU_FP32, level analyses of both triangles when it has
  * 1 << BILU_ILU, FP32 copies of the ISAI factors and of A when it has
- * 1 << BILU_FP32_INNER.
+ * 1 << BILU_FP32_INNER.  A prec_mask of 1 << BILU_ILU alone builds BILU(0)
+ * and the level analyses only (no ISAI; solves in the other modes then
+ * return BILU_ERR_ARG).
  * h_times (optional, 4 doubles, milliseconds): factor, patterns, isai,
  * total. */
 int bilu_ctx_setup(bilu_ctx* ctx, int nb, int nnzb, int bs, const int* d_row, const int* d_col,

@@ -117,4 +117,12 @@ __device__ __forceinline__ float ld_stream(const float* p) {
 // Polls back off up to 256 ns, so the budget bounds a wait at a few seconds.
 constexpr long long kSpinLimit = 1ll << 22;
 
+// Caller-owned home for the level analysis of the lower DAG that BILU(0)
+// computes (order[nb+1], lvl_ptr[nb+2], nlev[4]), so that lower triangular
+// solves on the factor can reuse it; the host words are filled on return.
+struct LevelOut {
+  int *order = nullptr, *lvl = nullptr, *nlev = nullptr;
+  int h_nlev = 0, h_sched = 0, h_maxdeg = 0;  // levels, solve schedule, largest dependency count
+};
+
 }  // namespace bilu

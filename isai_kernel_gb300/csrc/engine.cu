@@ -56,7 +56,7 @@ int sptrsv_levels_async(int nb, int bs, const int* row, const int* col, const in
                         cudaStream_t st, const double* rdiag, int maxdeg);
 int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, const int* diag,
                double* val, int* h_zp, Carver& ws, cudaStream_t st, int schedule,
-               double* rdiag);
+               double* rdiag, LevelOut* keep);
 int dinv_impl(int nb, int bs, const int* row, const int* col, const double* val, int lower,
               double* Dinv, int* d_fail, cudaStream_t st);
 size_t pairs_ws(long long mnnz);
@@ -311,16 +311,30 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
     BILU_TRY(diag_positions(nb, c->Arow, c->Acol, c->diag, nullptr, w2, st));
   }
   tm.mark(1);
+  // the exact-ILU apply's lower solves reuse BILU(0)'s analysis of the
+  // lower DAG
+  const bool ilu = (prec_mask & (1 << BILU_ILU)) != 0;
+  LevelOut keepL;
+  if (ilu) {
+    BILU_TRY(c->alloc(&c->ordL, (size_t)nb + 1));
+    BILU_TRY(c->alloc(&c->lvlL, (size_t)nb + 2));
+    BILU_TRY(c->alloc(&c->nlevL, 4));
+    keepL.order = c->ordL;
+    keepL.lvl = c->lvlL;
+    keepL.nlev = c->nlevL;
+  }
   {
     Carver w2 = ws;
     int zp = -1;
     int rc = bilu0_impl(nb, nnzb, bs, c->Arow, c->Acol, c->diag, c->LU, &zp, w2, st,
-                        c->schedule, c->rdiag);
+                        c->schedule, c->rdiag, ilu ? &keepL : nullptr);
     if (rc != BILU_OK) return rc;
   }
   tm.mark(2);
   double t_pat = 0, t_isai = 0;
-  if (c->isai_level > 1) {
+  // a mask of BILU_ILU alone asks for the exact ILU apply only: no ISAI
+  const bool isai = prec_mask != (1 << BILU_ILU);
+  if (isai && c->isai_level > 1) {
     // pattern(A^k) by repeated symbolic products with A
     const int *xr = c->Arow, *xc = c->Acol;
     for (int k = 2; k <= c->isai_level; ++k) {
@@ -351,8 +365,10 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
       ws = Carver(wsq, need);
     }
   }
-  BILU_TRY(build_isai_side(c, 1, ws, &c->Lrow, &c->Lcol, &c->Lval, &c->nnzL, &t_pat, &t_isai));
-  BILU_TRY(build_isai_side(c, 0, ws, &c->Urow, &c->Ucol, &c->Uval, &c->nnzU, &t_pat, &t_isai));
+  if (isai) {
+    BILU_TRY(build_isai_side(c, 1, ws, &c->Lrow, &c->Lcol, &c->Lval, &c->nnzL, &t_pat, &t_isai));
+    BILU_TRY(build_isai_side(c, 0, ws, &c->Urow, &c->Ucol, &c->Uval, &c->nnzU, &t_pat, &t_isai));
+  }
   if (prec_mask & (1 << BILU_FP32_INNER)) {
     BILU_TRY(c->alloc(&c->Aval32, (size_t)nnzb * bs2));
     BILU_TRY(bilu_convert_f64_to_f32((size_t)nnzb * bs2, c->Aval, c->Aval32, st));
@@ -365,19 +381,21 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   }
   if (prec_mask & (1 << BILU_ILU)) {
     // level analyses of both triangles of the packed factor for the exact
-    // BILU(0) apply (two level-scheduled triangular solves per apply)
-    for (int lower = 1; lower >= 0; --lower) {
-      int **ord = lower ? &c->ordL : &c->ordU, **lvl = lower ? &c->lvlL : &c->lvlU,
-          **nl = lower ? &c->nlevL : &c->nlevU;
-      BILU_TRY(c->alloc(ord, (size_t)nb + 1));
-      BILU_TRY(c->alloc(lvl, (size_t)nb + 2));
-      BILU_TRY(c->alloc(nl, 4));
+    // BILU(0) apply (two level-order triangular solves per apply): the
+    // lower one is BILU(0)'s, the upper one is built here
+    c->nlev_host[0] = keepL.h_nlev;
+    c->ilu_sched[0] = keepL.h_sched;
+    c->ilu_maxdeg[0] = keepL.h_maxdeg;
+    BILU_TRY(c->alloc(&c->ordU, (size_t)nb + 1));
+    BILU_TRY(c->alloc(&c->lvlU, (size_t)nb + 2));
+    BILU_TRY(c->alloc(&c->nlevU, 4));
+    {
       Carver w2 = ws;
-      BILU_TRY(level_analysis(nb, nnzb, c->Arow, c->Acol, c->diag, lower, *ord, *lvl, *nl,
-                              &c->nlev_host[lower ? 0 : 1], w2, st, &c->ilu_sched[lower ? 0 : 1],
-                              &c->ilu_maxdeg[lower ? 0 : 1]));
-      if (c->schedule == 0 || c->schedule == 1) c->ilu_sched[lower ? 0 : 1] = c->schedule;
+      BILU_TRY(level_analysis(nb, nnzb, c->Arow, c->Acol, c->diag, 0, c->ordU, c->lvlU, c->nlevU,
+                              &c->nlev_host[1], w2, st, &c->ilu_sched[1], &c->ilu_maxdeg[1]));
     }
+    for (int t = 0; t < 2; ++t)
+      if (c->schedule == 0 || c->schedule == 1) c->ilu_sched[t] = c->schedule;
     BILU_TRY(c->alloc(&c->ilu_flags, (size_t)nb + 2));
     BILU_TRY(c->alloc(&c->ilu_words, 4));
     BILU_TRY_CUDA(cudaMemsetAsync(c->ilu_words, 0, sizeof(unsigned) * 4, st));
@@ -415,12 +433,12 @@ extern "C" int bilu_ctx_get(bilu_ctx* c, int which, const void** d_ptr, long lon
   long long cnt = 0;
   switch (which) {
     case 0: p = c->LU; cnt = c->nnzb * bs2; break;
-    case 1: p = c->Lrow; cnt = c->nb + 1; break;
-    case 2: p = c->Lcol; cnt = c->nnzL; break;
-    case 3: p = c->Lval; cnt = c->nnzL * bs2; break;
-    case 4: p = c->Urow; cnt = c->nb + 1; break;
-    case 5: p = c->Ucol; cnt = c->nnzU; break;
-    case 6: p = c->Uval; cnt = c->nnzU * bs2; break;
+    case 1: p = c->Lrow; cnt = p ? c->nb + 1 : 0; break;
+    case 2: p = c->Lcol; cnt = p ? c->nnzL : 0; break;
+    case 3: p = c->Lval; cnt = p ? c->nnzL * bs2 : 0; break;
+    case 4: p = c->Urow; cnt = p ? c->nb + 1 : 0; break;
+    case 5: p = c->Ucol; cnt = p ? c->nnzU : 0; break;
+    case 6: p = c->Uval; cnt = p ? c->nnzU * bs2 : 0; break;
     case 7: p = c->Lval32; cnt = c->Lval32 ? c->nnzL * bs2 : 0; break;
     case 8: p = c->Uval32; cnt = c->Uval32 ? c->nnzU * bs2 : 0; break;
     default: return BILU_ERR_ARG;
@@ -551,8 +569,8 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
   if (prec != -1 && prec != BILU_FP64 && prec != BILU_FP32 && prec != BILU_ILU &&
       prec != BILU_FP32_INNER)
     return BILU_ERR_ARG;
-  if ((prec == BILU_FP32 && !c->Lval32) || (prec == BILU_ILU && !c->ilu_words) ||
-      (prec == BILU_FP32_INNER && !c->Aval32))
+  if ((prec == BILU_FP64 && !c->Lval) || (prec == BILU_FP32 && !c->Lval32) ||
+      (prec == BILU_ILU && !c->ilu_words) || (prec == BILU_FP32_INNER && !c->Aval32))
     return BILU_ERR_ARG;  // the setup did not build this preconditioner
   BILU_TRY(ensure_solver(c, restart));
   cudaStream_t st = c->st;
@@ -677,8 +695,8 @@ extern "C" int bilu_ctx_select(bilu_ctx* c, const double* d_b, int restart, int 
   for (int p = 0; p < 4 && rc == BILU_OK; ++p) {
     if (h_rate) h_rate[p] = 0.0;
     if (!(mask & (1 << p))) continue;
-    if ((p == BILU_FP32 && !c->Lval32) || (p == BILU_ILU && !c->ilu_words) ||
-        (p == BILU_FP32_INNER && !c->Aval32))
+    if ((p == BILU_FP64 && !c->Lval) || (p == BILU_FP32 && !c->Lval32) ||
+        (p == BILU_ILU && !c->ilu_words) || (p == BILU_FP32_INNER && !c->Aval32))
       continue;
     int it = 0;
     double rr = 1.0;

@@ -1729,20 +1729,27 @@ int sync_init_words(SyncState& ss, Carver& ws, cudaStream_t st) {
 
 // BILU(0) in place, level scheduled (one cooperative launch, one grid
 // barrier per dependency level of the lower DAG) or sync-free.  rdiag
-// (nb x bs) receives the reciprocal pivots; null: carved from ws.
+// (nb x bs) receives the reciprocal pivots; null: carved from ws.  keep
+// (optional): where the level analysis of the lower DAG is built and kept.
 int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, const int* diag,
                double* val, int* h_zp, Carver& ws, cudaStream_t st, int schedule,
-               double* rdiag) {
-  int* order = ws.take<int>((size_t)nb + 1);
-  int* lvl = ws.take<int>((size_t)nb + 2);
-  int* nlev_d = ws.take<int>(4);
+               double* rdiag, LevelOut* keep) {
+  const bool kept = keep && keep->order && keep->lvl && keep->nlev;
+  int* order = kept ? keep->order : ws.take<int>((size_t)nb + 1);
+  int* lvl = kept ? keep->lvl : ws.take<int>((size_t)nb + 2);
+  int* nlev_d = kept ? keep->nlev : ws.take<int>(4);
   if (!rdiag) rdiag = ws.take<double>((size_t)nb * bs + 1);
   if (!order || !lvl || !nlev_d || !rdiag) return BILU_ERR_WORKSPACE;
-  int nlev = 0, sched = 0;
+  int nlev = 0, sched = 0, ssched = 0, maxdeg = 0;
   {
     Carver w2 = ws;
     BILU_TRY(build_levels(nb, row, col, diag, 1, std::max(nnzb - nb, 0ll), order, lvl, nlev_d,
-                          &nlev, w2, st, nullptr, nullptr, &sched));
+                          &nlev, w2, st, &ssched, &maxdeg, &sched));
+  }
+  if (kept) {
+    keep->h_nlev = nlev;
+    keep->h_sched = ssched;
+    keep->h_maxdeg = maxdeg;
   }
   if (schedule == 0 || schedule == 1) sched = schedule;  // caller's choice
   if (sched == 1) {
@@ -2024,7 +2031,7 @@ extern "C" int bilu_bsrilu0_ex(int nb, int nnzb, int bs, const int* d_row, const
     return rc;
   }
   return bilu0_impl(nb, nnzb, bs, d_row, d_col, diag, d_val, h_info, ws, S(stream), schedule,
-                    nullptr);
+                    nullptr, nullptr);
 }
 
 extern "C" size_t bilu_sptrsv_ws_bytes(int nb, int nnzb) {

@@ -356,6 +356,29 @@ def test_exact_ilu_gmres_both_schedules(cuda, orc, name):
     assert np.array_equal(xs[0], xs[1])
 
 
+def test_exact_ilu_only_handle(cuda, orc):
+    """A handle set up for the exact ILU apply alone builds no ISAI: the ILU
+    solve matches a full handle's bit for bit, and the ISAI modes report
+    BILU_ERR_ARG instead of running on missing factors."""
+    from isai_kernel_gb300 import api
+    from isai_kernel_gb300._lib import BiluError
+
+    A = mats()["c2_s6"]
+    b = T(gen.rhs(A.n, 0), cuda)
+    args = (A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda))
+    full = api.Preconditioner(*args, fp32=True, ilu=True)
+    only = api.Preconditioner(*args, fp32=False, ilu=True)
+    x1, r1 = full.solve(b, prec=api.BILU_ILU, maxit=3000)
+    x2, r2 = only.solve(b, prec=api.BILU_ILU, maxit=3000)
+    assert r1.converged and r1.iters == r2.iters and np.array_equal(N(x1), N(x2))
+    for prec in (api.BILU_FP64, api.BILU_FP32):
+        with pytest.raises(BiluError) as e:
+            only.solve(b, prec=prec, maxit=10)
+        assert e.value.status == -1
+    full.close()
+    only.close()
+
+
 def test_long_rows_take_the_warp_path(cuda, orc):
     """A power-law system with rows of more than 32 dependencies (up to 126
     here): the level kernels switch to a warp per row.  BILU(0) within 1e-12
