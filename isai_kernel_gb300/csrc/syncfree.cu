@@ -427,8 +427,8 @@ __global__ void k_level_scatter(int nb, const int* __restrict__ level, int* curs
 // grid-wide barrier; no per-row flags are polled.
 
 struct GridSync {
-  unsigned* count;  // arrivals at the current barrier
-  unsigned* gen;    // barriers completed
+  unsigned* count;  // arrivals since the launch started
+  unsigned* gen;    // CTAs that have left the kernel (grid_exit_count)
   int* err;         // 0 or a bilu_status; set on a barrier timeout
   long long spin;   // polls before a waiting CTA gives up
   int per_sm = 1;   // CTAs of the launch resident on one SM
@@ -439,9 +439,6 @@ __device__ __forceinline__ unsigned ld_relaxed_u(const unsigned* p) {
   asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release_u(unsigned* p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
 __device__ __forceinline__ unsigned atom_add_acq_rel_u(unsigned* p, unsigned v) {
   unsigned old;
@@ -450,52 +447,16 @@ __device__ __forceinline__ unsigned atom_add_acq_rel_u(unsigned* p, unsigned v) 
   return old;
 }
 
-// Grid-wide barrier.  After __syncthreads, thread 0 of each CTA arrives with
-// an acquire-release atomic (release: the CTA's writes, ordered before it by
-// the CTA barrier, become visible with it; acquire: the last arriver sees
-// every other CTA's writes); the last CTA to arrive resets the count, runs
-// last() and releases the generation that the others poll (bounded).  A
-// release atomic costs ~0.9 us less per barrier than a fence + relaxed
-// atomic at 304 CTAs on GB300.  Returns false in every thread of the CTA if
-// the launch aborted.
-template <class F>
-__device__ __forceinline__ bool grid_sync(const GridSync& g, unsigned& gen_seen, F last) {
-  __shared__ int ok_s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    unsigned target = gen_seen + 1u;
-    if (atom_add_acq_rel_u(g.count, 1u) == gridDim.x - 1u) {
-      atomicExch(g.count, 0u);
-      last();
-      st_release_u(g.gen, target);
-    } else {
-      long long n = 0;
-      unsigned ns = 32;
-      while (ld_relaxed_u(g.gen) != target) {
-        if (ld_relaxed(g.err) != 0) { ok = 0; break; }
-        if (++n > g.spin) {
-          atomicCAS(g.err, 0, (int)BILU_ERR_TIMEOUT);
-          ok = 0;
-          break;
-        }
-        backoff(ns);
-      }
-      fence_acquire();
-    }
-    gen_seen = target;
-    ok_s = ok;
-  }
-  __syncthreads();
-  return ok_s != 0;
-}
-
-
-// Counting grid barrier, for kernels with no last-arriver action: the
-// arrival count grows through the launch (barrier b is complete when it
-// reaches (b + 1) x gridDim.x) and every CTA polls the count itself, so the
-// release reaches the waiting CTAs with the last arrival's atomic instead
-// of a generation word written after it returns.  `passed` counts the
+// Counting grid barrier.  After __syncthreads, thread 0 of each CTA arrives
+// with an acquire-release atomic (release: the CTA's writes, ordered before
+// it by the CTA barrier, become visible with it); the arrival count grows
+// through the launch (barrier b is complete when it reaches
+// (b + 1) x gridDim.x) and every CTA polls the count itself with relaxed
+// loads and back-off, then takes one acquire fence, so the release reaches
+// the waiting CTAs with the last arrival's atomic.  (On GB300 an
+// acquire-release arrival costs ~0.9 us less than a fence + relaxed atomic
+// at 304 CTAs, and polling the count ~0.7 us less than a generation word
+// that the last arriver writes after its atomic returns.)  `passed` counts the
 // barriers this CTA has passed (thread 0's copy is the one used).  The
 // comparison is modulo 2^32.  g.gen counts CTAs that have left the kernel
 // (grid_exit_count); both words are 0 between launches.
@@ -564,38 +525,77 @@ __global__ void k_dep_fill(int nb, const int* __restrict__ row, const int* __res
   }
 }
 
+// Appends the rows of the warp's ready lanes to order[] with one atomic on
+// the tail per warp (ballot + prefix count).  Called by all 32 lanes.
+__device__ __forceinline__ void warp_append(bool ready, int J, int* order, int* tail) {
+  const unsigned m = __ballot_sync(FULL, ready);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(tail, __popc(m));
+  base = __shfl_sync(FULL, base, leader);
+  if (ready) order[base + __popc(m & ((1u << lane) - 1u))] = J;
+}
+
 // Breadth-first level sweep (Kahn's algorithm, one level per barrier):
 // order[] receives the rows level by level, lvl_ptr[l] the start of level l
-// (lvl_ptr[nlev] = nb), *nlev the number of levels.  The rows inside a level
-// come in atomic-append order; the level sizes do not depend on it.
+// (lvl_ptr[nlev] = nb), *nlev the number of levels.  Warps take 32
+// consecutive frontier rows, walk their successor lists in step (one slot
+// per lane and round), decrement in-degrees and append the rows that reach
+// zero with one atomic per warp; after the counting barrier every CTA reads
+// where the next frontier ends from the append counter.  The rows inside a
+// level come in append order (k_sort_levels orders them afterwards); the
+// level sizes do not depend on it.
 __global__ void __launch_bounds__(256) k_bfs_levels(int nb, const int* __restrict__ sptr,
                                                     const int* __restrict__ sidx, int* indeg,
                                                     int* order, int* lvl_ptr, int* tail,
                                                     int* nlev, GridSync gs) {
-  unsigned gen = 0;
+  __shared__ int end_s;
+  unsigned passed = 0;
+  const int lane = threadIdx.x & 31;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long wbase = tid - lane;  // first position of this warp
   const long long nthr = (long long)gridDim.x * blockDim.x;
-  for (long long I = tid; I < nb; I += nthr)
-    if (indeg[I] == 0) order[atomicAdd(tail, 1)] = (int)I;
-  if (!grid_sync(gs, gen, [&] {
-        lvl_ptr[0] = 0;
-        lvl_ptr[1] = atomicAdd(tail, 0);
-      }))
-    return;
+  for (long long I0 = wbase; I0 < nb; I0 += nthr) {
+    const long long I = I0 + lane;
+    warp_append(I < nb && indeg[I] == 0, (int)I, order, tail);
+  }
+  if (!grid_sync_count(gs, passed)) return;
+  if (threadIdx.x == 0) end_s = ld_relaxed(tail);
+  __syncthreads();
+  int s = 0, e = end_s;
+  if (tid == 0) {
+    lvl_ptr[0] = 0;
+    lvl_ptr[1] = e;
+  }
   for (int l = 0;; ++l) {
-    int s = __ldcg(lvl_ptr + l), e = __ldcg(lvl_ptr + l + 1);
     if (s == e) {
       if (tid == 0) *nlev = l;
+      grid_exit_count(gs);
       return;
     }
-    for (long long q = s + tid; q < e; q += nthr) {
-      int I = __ldcg(order + q);
-      for (int p = __ldg(sptr + I), pe = __ldg(sptr + I + 1); p < pe; ++p) {
-        int J = __ldg(sidx + p);
-        if (atomicSub(indeg + J, 1) == 1) order[atomicAdd(tail, 1)] = J;
+    for (long long q0 = s + wbase; q0 < e; q0 += nthr) {
+      const long long q = q0 + lane;
+      const int I = q < e ? __ldcg(order + q) : -1;
+      int p = I >= 0 ? __ldg(sptr + I) : 0;
+      const int pe = I >= 0 ? __ldg(sptr + I + 1) : 0;
+      while (__any_sync(FULL, p < pe)) {
+        bool ready = false;
+        int J = -1;
+        if (p < pe) {
+          J = __ldg(sidx + p);
+          ready = atomicSub(indeg + J, 1) == 1;
+          ++p;
+        }
+        warp_append(ready, J, order, tail);
       }
     }
-    if (!grid_sync(gs, gen, [&] { lvl_ptr[l + 2] = atomicAdd(tail, 0); })) return;
+    if (!grid_sync_count(gs, passed)) return;
+    if (threadIdx.x == 0) end_s = ld_relaxed(tail);
+    __syncthreads();
+    s = e;
+    e = end_s;
+    if (tid == 0) lvl_ptr[l + 2] = e;
   }
 }
 
@@ -1560,7 +1560,11 @@ int build_levels(int nb, const int* row, const int* col, const int* diag, int lo
   if (total > ndeps_max) return BILU_ERR_WORKSPACE;
   k_dep_fill<<<ceil_div(nb, 256), 256, 0, st>>>(nb, row, col, diag, lower, sptr, cursor, sidx);
   BILU_LAUNCH_CHECK();
-  int grid = std::min<long long>(coop_grid((const void*)k_bfs_levels, 256), ceil_div(nb, 256));
+  // two CTAs per SM at most: a level's frontier is small, the barrier's
+  // cost grows with the number of CTAs
+  int grid = std::min<long long>(std::min(coop_grid((const void*)k_bfs_levels, 256),
+                                          2 * sm_count()),
+                                 ceil_div(nb, 256));
   void* args[] = {&nb, &sptr, &sidx, &indeg, &order, &lvl_ptr, &tail, &nlev_d, &gs};
   BILU_TRY(launch_coop((const void*)k_bfs_levels, grid, 256, args, st));
   int herr = grid_sync_finish(gs, st);

@@ -311,6 +311,42 @@ def test_sptrsv_level_and_syncfree_schedules(cuda, orc, name):
         assert np.array_equal(np.diff(ptr), np.bincount(lv - 1, minlength=nlev))
 
 
+@pytest.mark.parametrize("bs,side", [(4, 7), (5, 6), (8, 5)])
+@pytest.mark.parametrize("kind", ["laplace2d", "convdiff3d"])
+def test_flow_solve_block_sizes(cuda, orc, kind, bs, side):
+    """The level-order (flow) solve at every built block size (16/bs
+    dependencies staged in registers: 4 at bs 4, 3 at bs 5, 1 at bs 8, the
+    rest read in the row loop): bit-identical to the sync-free solve and
+    within 1e-12 of the oracle, both triangles."""
+    import torch
+
+    from isai_kernel_gb300 import _lib, api
+
+    A = (gen.laplace2d(side * 2, bs=bs, seed=bs) if kind == "laplace2d"
+         else gen.convdiff3d(side, bs=bs, seed=bs))
+    LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    row, col, lu = T(A.rowptr, cuda), T(A.colind, cuda), T(LU, cuda)
+    bh = gen.rhs(A.n, bs)
+    b = T(bh, cuda)
+    L = _lib.lib()
+    for lower in (1, 0):
+        info = api._ws(L.bilu_sptrsv_analysis_bytes(A.nb), cuda)
+        ws = api._ws(max(L.bilu_sptrsv_analysis_ws_bytes(A.nb, A.nnzb),
+                         L.bilu_sptrsv_solve_ws_bytes(A.nb)), cuda)
+        api.call("bilu_sptrsv_analysis", A.nb, A.nnzb, bs, api._p(row), api._p(col), lower,
+                 api._p(info), api._p(ws), ws.numel(), api._s())
+        xs = []
+        for fn in ("bilu_sptrsv_solve_level", "bilu_sptrsv_solve_syncfree"):
+            x = torch.empty_like(b)
+            api.call(fn, A.nb, bs, api._p(row), api._p(col), api._p(lu), lower, lower,
+                     api._p(info), api._p(b), api._p(x), api._p(ws), ws.numel(), api._s())
+            xs.append(N(x))
+        assert np.array_equal(xs[0], xs[1])
+        ref = (orc.sptrsv_lower if lower else orc.sptrsv_upper)(A.nb, bs, A.rowptr, A.colind,
+                                                                 LU, bh)
+        assert relerr(xs[0], ref) < 1e-12
+
+
 @pytest.mark.parametrize("name", ["c1_s16", "c2_s6", "c3_nb200", "bs5_s7", "long_rows"])
 def test_bilu0_both_schedules(cuda, orc, name):
     """BILU(0) under the level schedule (a bs-lane group per row) and the
