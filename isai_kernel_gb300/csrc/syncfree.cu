@@ -1040,16 +1040,46 @@ __device__ __forceinline__ double bilu0_diag_lu(double (&dc)[BS], int c, unsigne
   return rp;
 }
 
+// Structure of a block row and of its first dependency (pattern only: read
+// ahead of the values, before the level's barrier).
+struct BRowPre {
+  int I;               // < 0: no row
+  int rs, re, dI;      // row pointers and diagonal position
+  int K, dK, ke;       // first dependency: column, its diagonal position, its row end
+};
+
+__device__ __forceinline__ void brow_prefetch(int I, const int* __restrict__ row,
+                                              const int* __restrict__ col,
+                                              const int* __restrict__ diag, BRowPre& p) {
+  p.I = I;
+  p.rs = p.re = p.dI = p.K = p.dK = p.ke = 0;
+  if (I < 0) return;
+  p.rs = __ldg(row + I);
+  p.re = __ldg(row + I + 1);
+  p.dI = __ldg(diag + I);
+  if (p.rs < p.dI) {
+    p.K = __ldg(col + p.rs);
+    p.dK = __ldg(diag + p.K);
+    p.ke = __ldg(row + p.K + 1);
+  }
+}
+
 template <int BS>
-__device__ __forceinline__ void bilu0_grow(int I, const int* __restrict__ row,
+__device__ __forceinline__ void bilu0_grow(const BRowPre& pr, const int* __restrict__ row,
                                            const int* __restrict__ col,
                                            const int* __restrict__ diag, double* val,
                                            const SyncState& ss, unsigned gmask, int r, int gb) {
   constexpr int BS2 = BS * BS;
-  const int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
+  const int I = pr.I, rs = pr.rs, re = pr.re, dI = pr.dI;
+  // structure of the next dependency, loaded one step ahead
+  int Kn = pr.K, dKn = pr.dK, ken = pr.ke;
   for (int pk = rs; pk < dI; ++pk) {
-    const int K = __ldg(col + pk);
-    const int dK = __ldg(diag + K), ke = __ldg(row + K + 1);
+    const int K = Kn, dK = dKn, ke = ken;
+    if (pk + 1 < dI) {
+      Kn = __ldg(col + pk + 1);
+      dKn = __ldg(diag + Kn);
+      ken = __ldg(row + Kn + 1);
+    }
     double* L = val + (long long)pk * BS2;
     const double* Ukk = val + (long long)dK * BS2;
     const double* rK = ss.rdiag + (long long)K * BS;  // 1 / pivots of U_KK
@@ -1322,12 +1352,28 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_bilu0_levels(
   const long long mygrp = (long long)warp * G + g;
   const int nlev = __ldg(nlev_p);
   // (matrices with long rows or narrow levels take the sync-free kernel)
+  // each group's first row of the next level is staged before the barrier
+  BRowPre pre;
+  {
+    const long long t = __ldg(lvl_ptr) + mygrp;
+    brow_prefetch(g < G && nlev > 0 && t < __ldg(lvl_ptr + 1) ? __ldg(order + t) : -1, row, col,
+                  diag, pre);
+  }
   for (int l = 0; l < nlev; ++l) {
     const int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
+    if (pre.I >= 0) bilu0_grow<BS>(pre, row, col, diag, val, ss, gmask, r, gb);
     if (g < G)
-      for (long long t = s + mygrp; t < e; t += ngrp)
-        bilu0_grow<BS>(__ldg(order + t), row, col, diag, val, ss, gmask, r, gb);
-    if (l + 1 < nlev && !grid_sync_count(gs, passed)) return;
+      for (long long t = s + mygrp + ngrp; t < e; t += ngrp) {
+        BRowPre q;
+        brow_prefetch(__ldg(order + t), row, col, diag, q);
+        bilu0_grow<BS>(q, row, col, diag, val, ss, gmask, r, gb);
+      }
+    if (l + 1 < nlev) {
+      const long long t = e + mygrp;
+      brow_prefetch(g < G && t < __ldg(lvl_ptr + l + 2) ? __ldg(order + t) : -1, row, col, diag,
+                    pre);
+      if (!grid_sync_count(gs, passed)) return;
+    }
   }
   grid_exit_count(gs);
 }
