@@ -203,7 +203,13 @@ int bilu_isai_compute(int nb, int bs, const double* d_Aval, const int* d_Mptr, c
 /* ------------------------------------------------------------------ */
 
 /* Replaces bcsr_spmv (bcsc2bcsrAndSpMV.h:49) and bsr_SpMV_tensorcore
- * (bsr_tensor_SpMV.h:402): y = M x.  FP64 values and vectors. */
+ * (bsr_tensor_SpMV.h:402): y = M x.  FP64 values and vectors.  Rows of more
+ * than 64 blocks are summed by a whole CTA instead of one lane group; the
+ * first call with a given d_row array (and mb) finds out whether there are
+ * such rows with a synchronising reduction over d_row, later calls reuse
+ * the answer (a stale answer after reusing d_row for another pattern only
+ * costs speed).  The same holds for bilu_bcsr_spmv_f32 and
+ * bilu_isai_apply. */
 int bilu_bcsr_spmv(int mb, int bs, const int* d_row, const int* d_col, const double* d_val,
                    const double* d_x, double* d_y, bilu_stream_t stream);
 /* FP32-stored values, FP32 accumulation; x and y each FP64 or FP32

@@ -20,7 +20,7 @@ int sptrsv_level_impl(int nb, long long nnzb, int bs, const int* row, const int*
                       const int* diag, const double* val, int lower, int unit, const double* b,
                       double* x, Carver& ws, cudaStream_t st);
 int spmv_any(int mb, int bs, int prec, const int* row, const int* col, const void* val,
-             const void* x, int x32, void* y, int y32, cudaStream_t st);
+             const void* x, int x32, void* y, int y32, cudaStream_t st, int long_rows);
 
 namespace {
 
@@ -219,7 +219,7 @@ extern "C" int bilu_bcsr_spmv_transpose(int mb, int bs, const int* d_row, const 
   double* tval = ws.take<double>((size_t)nnzb * bs * bs);
   if (!trow || (nnzb && (!tcol || !tval))) return BILU_ERR_WORKSPACE;
   BILU_TRY(bsr_transpose_impl(mb, bs, d_row, d_col, d_val, nnzb, trow, tcol, tval, ws, st));
-  return spmv_any(mb, bs, BILU_FP64, trow, tcol, tval, d_x, 0, d_y, 0, st);
+  return spmv_any(mb, bs, BILU_FP64, trow, tcol, tval, d_x, 0, d_y, 0, st, -1);
 }
 
 extern "C" int bilu_masked_outer(int mb, int bs, const int* d_row, const int* d_col,
@@ -260,7 +260,7 @@ extern "C" int bilu_rel_errors(int nb, int bs, const int* d_row, const int* d_co
   double* out = ws.take<double>(8);
   if (!ax || !part || !out) return BILU_ERR_WORKSPACE;
   double h[4] = {0, 0, 0, 0};
-  BILU_TRY(spmv_any(nb, bs, BILU_FP64, d_row, d_col, d_val, d_x, 0, ax, 0, st));
+  BILU_TRY(spmv_any(nb, bs, BILU_FP64, d_row, d_col, d_val, d_x, 0, ax, 0, st, -1));
   // ||b - Ax||^2 and ||b||^2
   k_diff_sq<<<kRedCTAs, kRedThreads, 0, st>>>(n, ax, d_b, part);
   BILU_LAUNCH_CHECK();

@@ -11,6 +11,8 @@
 // segment is a broadcast within the group.
 #include <algorithm>
 
+#include <mutex>
+
 #include "common.cuh"
 
 namespace bilu {
@@ -89,14 +91,73 @@ __device__ __forceinline__ void load_row(const VT* __restrict__ val, long long p
   }
 }
 
+// Rows with more blocks than this are worth the CTA's help: power-law hub
+// rows hold up to ~2000 blocks, and a lane group alone runs one dependent
+// FMA chain over all of them while the rest of the GPU idles.
+constexpr int kLongSpmvRow = 64;
+
+// The CTA's long rows (slots in group order, -1 for none): its NG groups
+// take the blocks g, g + NG, ... of each (two accumulators, even and odd
+// turns), the NG partials are added in group order.  Out of line so that
+// the short rows' loop keeps its registers.  Called by every thread.
+template <int BS, class VT, class XT, class YT, class AccT, int NSLOT, int NG>
+__device__ __noinline__ void spmv_long_rows(const int* long_rows, const int* __restrict__ row,
+                                            const int* __restrict__ col,
+                                            const VT* __restrict__ val,
+                                            const XT* __restrict__ x, YT* __restrict__ y,
+                                            float* __restrict__ y32, AccT* red, bool in_group,
+                                            int cg, int r) {
+  for (int i = 0; i < NSLOT; ++i) {
+    const int br = long_rows[i];
+    if (br < 0) continue;  // uniform across the CTA (shared memory)
+    const int rs = __ldg(row + br), re = __ldg(row + br + 1);
+    AccT a0 = 0, a1 = 0;
+    if (in_group) {
+      int p = rs + cg;
+      for (; p + NG < re; p += 2 * NG) {
+        AccT v0[BS], v1[BS], x0[BS], x1[BS];
+        load_row<BS, VT, AccT>(val, p, r, v0);
+        load_row<BS, VT, AccT>(val, p + NG, r, v1);
+        load_x<BS, XT, AccT>(x, __ldg(col + p), x0);
+        load_x<BS, XT, AccT>(x, __ldg(col + p + NG), x1);
+#pragma unroll
+        for (int k = 0; k < BS; ++k) {
+          a0 = fma(v0[k], x0[k], a0);
+          a1 = fma(v1[k], x1[k], a1);
+        }
+      }
+      if (p < re) {
+        AccT v0[BS], x0[BS];
+        load_row<BS, VT, AccT>(val, p, r, v0);
+        load_x<BS, XT, AccT>(x, __ldg(col + p), x0);
+#pragma unroll
+        for (int k = 0; k < BS; ++k) a0 = fma(v0[k], x0[k], a0);
+      }
+      red[cg * BS + r] = a0 + a1;
+    }
+    __syncthreads();
+    if (threadIdx.x < BS) {
+      AccT t = 0;
+      for (int q = 0; q < NG; ++q) t += red[q * BS + threadIdx.x];
+      y[(long long)br * BS + threadIdx.x] = (YT)t;
+      if (y32) y32[(long long)br * BS + threadIdx.x] = (float)t;
+    }
+    __syncthreads();
+  }
+}
+
 // y = M x: lane group of BS lanes per block row, lane r owns scalar row r.
 // A group handles RPG consecutive block rows and issues the loads of the
 // first U blocks of all of them before any arithmetic, so a warp keeps
 // RPG*U independent block loads per lane in flight (the rows of the ISAI
 // factors hold about 4 blocks, so one batch usually covers them).  FP64
 // values: U = 2, RPG = 1 (the DFMA pipe, not memory, is the limit); FP32
-// values: U = 4, RPG = 2 (memory latency is the limit).
-template <int BS, class VT, class XT, class YT, class AccT, int RPG>
+// values: U = 4, RPG = 2 (memory latency is the limit).  LONG (matrices
+// with rows of more than kLongSpmvRow blocks): such a row is skipped by its
+// group and summed after the short rows by the whole CTA (dynamic shared
+// memory: the CTA's long-row slots and the group partials); the other
+// instance has no CTA barrier at all.
+template <int BS, class VT, class XT, class YT, class AccT, int RPG, bool LONG>
 __global__ void __launch_bounds__(256, sizeof(VT) == 4 ? 4 : 2) k_bsr_spmv(int mb, const int* __restrict__ row,
                                                      const int* __restrict__ col,
                                                      const VT* __restrict__ val,
@@ -108,20 +169,31 @@ __global__ void __launch_bounds__(256, sizeof(VT) == 4 ? 4 : 2) k_bsr_spmv(int m
   int lane = threadIdx.x & 31;
   int g = lane / BS, r = lane - g * BS;
   long long base = (((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G + g) * RPG;
-  if (g >= G || base >= mb) return;
+  const bool active = g < G && base < mb;
+  if (!LONG && !active) return;
   int s[RPG], e[RPG];
+  bool skip[RPG], mine_long = false;
+  extern __shared__ int long_slots[];  // LONG: [8*G*RPG] slots, then the partials
+  const int cg = (threadIdx.x >> 5) * G + g;
 #pragma unroll
   for (int q = 0; q < RPG; ++q) {
-    bool ok = base + q < mb;
+    bool ok = active && base + q < mb;
     s[q] = ok ? __ldg(row + base + q) : 0;
     e[q] = ok ? __ldg(row + base + q + 1) : 0;
+    skip[q] = false;
+    if constexpr (LONG) {
+      skip[q] = e[q] - s[q] > kLongSpmvRow;
+      if (g < G && r == 0) long_slots[cg * RPG + q] = skip[q] ? (int)(base + q) : -1;
+      if (skip[q]) e[q] = s[q];
+      mine_long |= skip[q];
+    }
   }
   AccT acc[RPG];
 #pragma unroll
   for (int q = 0; q < RPG; ++q) acc[q] = 0;
   // batches of U blocks per row; every load of a batch (column indices,
   // block rows, x segments) is issued before its FMAs
-  for (int off = 0;; off += U) {
+  for (int off = 0; active; off += U) {
     bool any = false;
 #pragma unroll
     for (int q = 0; q < RPG; ++q) any |= s[q] + off < e[q];
@@ -161,15 +233,23 @@ __global__ void __launch_bounds__(256, sizeof(VT) == 4 ? 4 : 2) k_bsr_spmv(int m
   }
 #pragma unroll
   for (int q = 0; q < RPG; ++q)
-    if (base + q < mb) {
+    if (active && base + q < mb && !skip[q]) {
       y[(base + q) * BS + r] = (YT)acc[q];
       if (y32) y32[(base + q) * BS + r] = (float)acc[q];  // optional FP32 copy
     }
+  if constexpr (LONG) {
+    constexpr int NSLOT = 8 * G * RPG;
+    // one CTA barrier, which also says whether the CTA holds a long row
+    if (__syncthreads_or(mine_long))
+      spmv_long_rows<BS, VT, XT, YT, AccT, NSLOT, 8 * G>(
+          long_slots, row, col, val, x, y, y32,
+          reinterpret_cast<AccT*>(long_slots + ((NSLOT + 1) & ~1)), g < G, cg, r);
+  }
 }
 
 template <int BS, class VT, class XT, class YT>
 int launch_spmv(int mb, const int* row, const int* col, const VT* val, const XT* x, YT* y,
-                cudaStream_t st, float* y32 = nullptr) {
+                cudaStream_t st, bool long_rows, float* y32 = nullptr) {
   using AccT = VT;
   if (mb == 0) return BILU_OK;
   constexpr int G = 32 / BS;
@@ -177,7 +257,15 @@ int launch_spmv(int mb, const int* row, const int* col, const VT* val, const XT*
   long long groups = (mb + RPG - 1) / RPG;
   long long warps = (groups + G - 1) / G;
   unsigned grid = ceil_div(warps, 8);
-  k_bsr_spmv<BS, VT, XT, YT, AccT, RPG><<<grid, 256, 0, st>>>(mb, row, col, val, x, y, y32);
+  if (long_rows) {
+    constexpr int NSLOT = 8 * G * RPG;
+    const size_t smem = sizeof(int) * ((NSLOT + 1) & ~1) + sizeof(AccT) * 8 * G * BS;
+    k_bsr_spmv<BS, VT, XT, YT, AccT, RPG, true><<<grid, 256, smem, st>>>(mb, row, col, val, x,
+                                                                         y, y32);
+  } else {
+    k_bsr_spmv<BS, VT, XT, YT, AccT, RPG, false><<<grid, 256, 0, st>>>(mb, row, col, val, x, y,
+                                                                       y32);
+  }
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }
@@ -249,30 +337,40 @@ __global__ void k_f64_to_f32(size_t n, const double* __restrict__ s, float* __re
 
 template <int BS>
 int spmv_f64(int mb, const int* row, const int* col, const double* val, const double* x,
-             double* y, cudaStream_t st) {
-  return launch_spmv<BS, double, double, double>(mb, row, col, val, x, y, st);
+             double* y, cudaStream_t st, bool lr) {
+  return launch_spmv<BS, double, double, double>(mb, row, col, val, x, y, st, lr);
 }
 
 template <int BS>
 int spmv_f32(int mb, const int* row, const int* col, const float* val, const void* x, int x32,
-             void* y, int y32, cudaStream_t st) {
+             void* y, int y32, cudaStream_t st, bool lr) {
   if (x32 && y32)
-    return launch_spmv<BS, float, float, float>(mb, row, col, val, (const float*)x, (float*)y, st);
+    return launch_spmv<BS, float, float, float>(mb, row, col, val, (const float*)x, (float*)y, st,
+                                                lr);
   if (x32)
     return launch_spmv<BS, float, float, double>(mb, row, col, val, (const float*)x, (double*)y,
-                                                 st);
+                                                 st, lr);
   if (y32)
     return launch_spmv<BS, float, double, float>(mb, row, col, val, (const double*)x, (float*)y,
-                                                 st);
+                                                 st, lr);
   return launch_spmv<BS, float, double, double>(mb, row, col, val, (const double*)x, (double*)y,
-                                                st);
+                                                st, lr);
 }
 
 // FP32 values and x, FP64 y plus its FP32 copy y32
 template <int BS>
 int spmv_f32_dual(int mb, const int* row, const int* col, const float* val, const float* x,
-                  double* y, float* y32, cudaStream_t st) {
-  return launch_spmv<BS, float, float, double>(mb, row, col, val, x, y, st, y32);
+                  double* y, float* y32, cudaStream_t st, bool lr) {
+  return launch_spmv<BS, float, float, double>(mb, row, col, val, x, y, st, lr, y32);
+}
+
+__global__ void k_row_len_max(int mb, const int* __restrict__ row, int* out) {
+  int m = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < mb;
+       i += (long long)gridDim.x * blockDim.x)
+    m = max(m, __ldg(row + i + 1) - __ldg(row + i));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(out, m);
 }
 
 template <int BS>
@@ -288,15 +386,70 @@ int spmm_f32(int mb, int k, const int* row, const int* col, const float* val, co
 
 }  // namespace
 
-// internal entry points used by the solver
+// Whether a block pattern has rows of more than kLongSpmvRow blocks: one
+// reduction over the row pointers into d_word (one device int) and a
+// synchronising read.  The engine calls it once per matrix at setup.
+int spmv_long_rows_of(int mb, const int* row, int* d_word, cudaStream_t st, int* h_long) {
+  *h_long = 0;
+  if (mb <= 0) return BILU_OK;
+  int h = 0;
+  BILU_TRY_CUDA(cudaMemsetAsync(d_word, 0, sizeof(int), st));
+  k_row_len_max<<<(unsigned)std::min<long long>(ceil_div(mb, 256), 152 * 8), 256, 0, st>>>(
+      mb, row, d_word);
+  BILU_LAUNCH_CHECK();
+  BILU_TRY_CUDA(cudaMemcpyAsync(&h, d_word, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BILU_TRY_CUDA(cudaStreamSynchronize(st));
+  *h_long = h > kLongSpmvRow ? 1 : 0;
+  return BILU_OK;
+}
+
+namespace {
+
+__device__ int g_row_len_word;  // scratch of the cached check (used under its lock)
+
+// The standalone entry points do not know the pattern: the answer is cached
+// per (row pointer array, block rows), most recent first.  A stale entry (a
+// buffer reused for another pattern) can only cost speed: both kernels are
+// exact for any row length.
+int long_rows_cached(int mb, const int* row, cudaStream_t st, bool* out) {
+  struct Entry {
+    const int* row;
+    int mb, flag;
+  };
+  static std::mutex mu;
+  static Entry cache[16] = {};
+  static int next = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  for (const Entry& e : cache)
+    if (e.row == row && e.mb == mb && row) {
+      *out = e.flag != 0;
+      return BILU_OK;
+    }
+  int* word = nullptr;
+  BILU_TRY_CUDA(cudaGetSymbolAddress((void**)&word, g_row_len_word));
+  int flag = 0;
+  BILU_TRY(spmv_long_rows_of(mb, row, word, st, &flag));
+  cache[next] = Entry{row, mb, flag};
+  next = (next + 1) % 16;
+  *out = flag != 0;
+  return BILU_OK;
+}
+
+}  // namespace
+
+// internal entry point used by the solver; long_rows: 1 / 0 when the
+// caller knows whether the pattern has rows of more than kLongSpmvRow
+// blocks, -1 to look it up
 int spmv_any(int mb, int bs, int prec, const int* row, const int* col, const void* val,
-             const void* x, int x32, void* y, int y32, cudaStream_t st) {
+             const void* x, int x32, void* y, int y32, cudaStream_t st, int long_rows) {
+  bool lr = long_rows > 0;
+  if (long_rows < 0) BILU_TRY(long_rows_cached(mb, row, st, &lr));
   if (prec == BILU_FP64) {
     if (x32 || y32) return BILU_ERR_ARG;
     return BILU_DISPATCH_BS(bs, spmv_f64, mb, row, col, (const double*)val, (const double*)x,
-                            (double*)y, st);
+                            (double*)y, st, lr);
   }
-  return BILU_DISPATCH_BS(bs, spmv_f32, mb, row, col, (const float*)val, x, x32, y, y32, st);
+  return BILU_DISPATCH_BS(bs, spmv_f32, mb, row, col, (const float*)val, x, x32, y, y32, st, lr);
 }
 
 int convert_f64_f32(size_t count, const double* src, float* dst, cudaStream_t st) {
@@ -313,26 +466,30 @@ int convert_f64_f32(size_t count, const double* src, float* dst, cudaStream_t st
 // then y32 = M_L b32 and x = M_U y32 with FP32 accumulation.
 int isai_apply_impl(int nb, int bs, int prec, const int* Lrow, const int* Lcol, const void* Lval,
                     const int* Urow, const int* Ucol, const void* Uval, const double* b,
-                    void* tmp, double* x, cudaStream_t st) {
+                    void* tmp, double* x, cudaStream_t st, int longL, int longU) {
   if (prec == BILU_FP32) {
     float* b32 = reinterpret_cast<float*>(x);
     BILU_TRY(convert_f64_f32((size_t)nb * bs, b, b32, st));
-    BILU_TRY(spmv_any(nb, bs, prec, Lrow, Lcol, Lval, b32, 1, tmp, 1, st));
-    return spmv_any(nb, bs, prec, Urow, Ucol, Uval, tmp, 1, x, 0, st);
+    BILU_TRY(spmv_any(nb, bs, prec, Lrow, Lcol, Lval, b32, 1, tmp, 1, st, longL));
+    return spmv_any(nb, bs, prec, Urow, Ucol, Uval, tmp, 1, x, 0, st, longU);
   }
-  BILU_TRY(spmv_any(nb, bs, prec, Lrow, Lcol, Lval, b, 0, tmp, 0, st));
-  return spmv_any(nb, bs, prec, Urow, Ucol, Uval, tmp, 0, x, 0, st);
+  BILU_TRY(spmv_any(nb, bs, prec, Lrow, Lcol, Lval, b, 0, tmp, 0, st, longL));
+  return spmv_any(nb, bs, prec, Urow, Ucol, Uval, tmp, 0, x, 0, st, longU);
 }
 
 // Solver form: the FP32 copy of the input is already there (written by the
 // kernel that produced the FP64 basis vector).
 int isai_apply_f32_staged(int nb, int bs, const int* Lrow, const int* Lcol, const float* Lval,
                           const int* Urow, const int* Ucol, const float* Uval, const float* b32,
-                          float* tmp, double* x, cudaStream_t st, float* x32) {
-  BILU_TRY(spmv_any(nb, bs, BILU_FP32, Lrow, Lcol, Lval, b32, 1, tmp, 1, st));
-  if (x32)  // x also in FP32 (input of an FP32 operator product)
-    return BILU_DISPATCH_BS(bs, spmv_f32_dual, nb, Urow, Ucol, Uval, tmp, x, x32, st);
-  return spmv_any(nb, bs, BILU_FP32, Urow, Ucol, Uval, tmp, 1, x, 0, st);
+                          float* tmp, double* x, cudaStream_t st, float* x32, int longL,
+                          int longU) {
+  BILU_TRY(spmv_any(nb, bs, BILU_FP32, Lrow, Lcol, Lval, b32, 1, tmp, 1, st, longL));
+  if (x32) {  // x also in FP32 (input of an FP32 operator product)
+    bool lr = longU > 0;
+    if (longU < 0) BILU_TRY(long_rows_cached(nb, Urow, st, &lr));
+    return BILU_DISPATCH_BS(bs, spmv_f32_dual, nb, Urow, Ucol, Uval, tmp, x, x32, st, lr);
+  }
+  return spmv_any(nb, bs, BILU_FP32, Urow, Ucol, Uval, tmp, 1, x, 0, st, longU);
 }
 
 }  // namespace bilu
@@ -344,7 +501,7 @@ extern "C" int bilu_bcsr_spmv(int mb, int bs, const int* d_row, const int* d_col
                               bilu_stream_t stream) {
   if (mb < 0 || (mb > 0 && (!d_row || !d_col || !d_val || !d_x || !d_y))) return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
-  return spmv_any(mb, bs, BILU_FP64, d_row, d_col, d_val, d_x, 0, d_y, 0, S(stream));
+  return spmv_any(mb, bs, BILU_FP64, d_row, d_col, d_val, d_x, 0, d_y, 0, S(stream), -1);
 }
 
 extern "C" int bilu_bcsr_spmv_f32(int mb, int bs, const int* d_row, const int* d_col,
@@ -353,7 +510,7 @@ extern "C" int bilu_bcsr_spmv_f32(int mb, int bs, const int* d_row, const int* d
   if (mb < 0 || (mb > 0 && (!d_row || !d_col || !d_val || !d_x || !d_y))) return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   return spmv_any(mb, bs, BILU_FP32, d_row, d_col, d_val, d_x, x_fp32 != 0, d_y, y_fp32 != 0,
-                  S(stream));
+                  S(stream), -1);
 }
 
 extern "C" int bilu_bcsr_spmm(int mb, int bs, int k, const int* d_row, const int* d_col,
@@ -389,5 +546,5 @@ extern "C" int bilu_isai_apply(int nb, int bs, int prec, const int* d_Lrow, cons
   if (nb < 0 || (prec != BILU_FP64 && prec != BILU_FP32)) return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   return isai_apply_impl(nb, bs, prec, d_Lrow, d_Lcol, d_Lval, d_Urow, d_Ucol, d_Uval, d_b,
-                         d_tmp, d_x, S(stream));
+                         d_tmp, d_x, S(stream), -1, -1);
 }

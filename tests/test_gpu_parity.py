@@ -415,6 +415,37 @@ def test_exact_ilu_only_handle(cuda, orc):
     only.close()
 
 
+@pytest.mark.parametrize("bs", [4, 5, 8])
+def test_spmv_long_rows(cuda, orc, bs):
+    """SpMV on a power-law pattern with rows of up to ~150 blocks (rows over
+    64 blocks are summed by the whole CTA): FP64 within 1e-12 of the
+    oracle's row-order sum, FP32-stored values within FP32 rounding, and the
+    result does not depend on whether the row-length check is cached."""
+    import torch
+
+    from isai_kernel_gb300 import api
+
+    A = gen.powerlaw(600, bs=bs, seed=9, kmax=150)
+    lens = np.diff(A.rowptr)
+    assert lens.max() > 64
+    x = gen.rhs(A.n, 11)
+    row, col = T(A.rowptr, cuda), T(A.colind, cuda)
+    y = torch.empty(A.n, dtype=torch.float64, device="cuda")
+    for _ in range(2):  # the second call uses the cached check
+        api.call("bilu_bcsr_spmv", A.nb, bs, api._p(row), api._p(col), api._p(T(A.val, cuda)),
+                 api._p(T(x, cuda)), api._p(y), api._s())
+        ref = orc.bcsr_spmv(A.nb, bs, A.rowptr, A.colind, A.val, x)
+        assert relerr(N(y), ref) < 1e-12
+    v32 = T(A.val.astype(np.float32), cuda)
+    x32 = T(x.astype(np.float32), cuda)
+    y32 = torch.empty(A.n, dtype=torch.float32, device="cuda")
+    api.call("bilu_bcsr_spmv_f32", A.nb, bs, api._p(row), api._p(col), api._p(v32),
+             api._p(x32), 1, api._p(y32), 1, api._s())
+    ref32 = orc.bcsr_spmv(A.nb, bs, A.rowptr, A.colind, A.val.astype(np.float32).astype(np.float64),
+                          x.astype(np.float32).astype(np.float64))
+    assert relerr(N(y32).astype(np.float64), ref32) < 1e-5
+
+
 def test_long_rows_take_the_warp_path(cuda, orc):
     """A power-law system with rows of more than 32 dependencies (up to 126
     here): the level kernels switch to a warp per row.  BILU(0) within 1e-12
