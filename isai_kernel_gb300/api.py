@@ -39,18 +39,33 @@ def _dev(*ts):
     return ts[0].device
 
 
-def _ci(t):
-    t = t.contiguous()
-    if t.dtype != _I32:
-        raise TypeError("index arrays must be int32")
+# Contiguous copies made for a call stay referenced until the next call
+# built from them: arguments are evaluated before the launch, and a copy
+# freed in between could hand its memory to the next argument's copy.  (Once
+# the kernel is queued, the stream-ordered allocator makes the release safe.)
+_held: list = []
+
+
+def _hold(t, orig):
+    if t.data_ptr() != orig.data_ptr():
+        if len(_held) > 64:
+            del _held[:32]
+        _held.append(t)
     return t
+
+
+def _ci(t):
+    c = t.contiguous()
+    if c.dtype != _I32:
+        raise TypeError("index arrays must be int32")
+    return _hold(c, t)
 
 
 def _cf(t, dtype=_F64):
-    t = t.contiguous()
-    if t.dtype != dtype:
+    c = t.contiguous()
+    if c.dtype != dtype:
         raise TypeError(f"values must be {dtype}")
-    return t
+    return _hold(c, t)
 
 
 # ------------------------------------------------------------ conversions

@@ -429,11 +429,12 @@ def test_spmv_long_rows(cuda, orc, bs):
     lens = np.diff(A.rowptr)
     assert lens.max() > 64
     x = gen.rhs(A.n, 11)
-    row, col = T(A.rowptr, cuda), T(A.colind, cuda)
+    # every device buffer stays referenced until the kernels have run
+    row, col, val, xd = T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda), T(x, cuda)
     y = torch.empty(A.n, dtype=torch.float64, device="cuda")
     for _ in range(2):  # the second call uses the cached check
-        api.call("bilu_bcsr_spmv", A.nb, bs, api._p(row), api._p(col), api._p(T(A.val, cuda)),
-                 api._p(T(x, cuda)), api._p(y), api._s())
+        api.call("bilu_bcsr_spmv", A.nb, bs, api._p(row), api._p(col), api._p(val), api._p(xd),
+                 api._p(y), api._s())
         ref = orc.bcsr_spmv(A.nb, bs, A.rowptr, A.colind, A.val, x)
         assert relerr(N(y), ref) < 1e-12
     v32 = T(A.val.astype(np.float32), cuda)
