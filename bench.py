@@ -357,7 +357,20 @@ def run_ours(args):
     t_ilu = e0.elapsed_time(e1) / 1e3
     ilu_setup = Pi.setup_ms["total"]
     Pi.close()
-    del Pi, xi
+    del Pi
+    # the same with the triangular solves in FP32 on an FP32 copy of the factor
+    Pf = api.Preconditioner(nb, bs, row, col, val, fp32=False, ilu_fp32=True)
+    _, rf = Pf.solve(b, xi, prec=api.BILU_ILU_FP32, restart=args.restart, tol=args.tol,
+                     maxit=args.maxit)
+    e0.record(stream)
+    _, rf = Pf.solve(b, xi, prec=api.BILU_ILU_FP32, restart=args.restart, tol=args.tol,
+                     maxit=args.maxit)
+    e1.record(stream)
+    e1.synchronize()
+    t_iluf = e0.elapsed_time(e1) / 1e3
+    iluf_setup = Pf.setup_ms["total"]
+    Pf.close()
+    del Pf, xi
 
     # preconditioner apply kernels, timed alone with CUDA events on the
     # launching stream (inputs: 1.1-1.9 GB of factors, larger than L2)
@@ -462,7 +475,11 @@ def run_ours(args):
         "exact_ilu": {"s": t_ilu, "iters": ri.iters, "relres": ri.relres,
                       "setup_ms": ilu_setup, "speedup_vs_fp64_isai": t_fp64 / t_ilu,
                       "what": "FP64 FGMRES(30) with the exact BILU(0) applied by two "
-                              "level-scheduled block triangular solves"},
+                              "level-order block triangular solves"},
+        "exact_ilu_fp32": {"s": t_iluf, "iters": rf.iters, "relres": rf.relres,
+                           "setup_ms": iluf_setup, "speedup_vs_fp64_isai": t_fp64 / t_iluf,
+                           "what": "FP64 FGMRES(30) with the exact BILU(0) applied in FP32 "
+                                   "(FP32 copy of the factor, FP32 level-order solves)"},
         "fp32_inner": {"s": t_f32i, "iters": r32i.iters, "relres": r32i.relres,
                        "restart_cycles": r32i.restarts, "speedup_vs_fp64": t_fp64 / t_f32i,
                        "what": "FP32 ISAI + FP32-stored A in the Arnoldi products; FP64 "
@@ -636,8 +653,9 @@ def run_sptrsv(args):
             out[f"{tag}_{name}_GBs"] = nbytes / ms / 1e6
     # GMRES(30) with the exact BILU(0) (two level-scheduled solves per apply)
     # against the FP32 ISAI apply, and the measured switch between them
-    Pc = api.Preconditioner(nb, bs, row, col, val, fp32=True, ilu=True)
-    for prec, tag in ((api.BILU_ILU, "ilu"), (api.BILU_FP32, "isai_fp32")):
+    Pc = api.Preconditioner(nb, bs, row, col, val, fp32=True, ilu=True, ilu_fp32=True)
+    for prec, tag in ((api.BILU_ILU, "ilu"), (api.BILU_ILU_FP32, "ilu_fp32"),
+                      (api.BILU_FP32, "isai_fp32")):
         e0.record()
         _, res = Pc.solve(b, x, prec=prec, maxit=args.maxit)
         e1.record()
@@ -656,7 +674,8 @@ def run_sptrsv(args):
                                "setup_ms": P2.setup_ms["total"]}
     P2.close()
     choice, rate = Pc.select(b, cycles=3)
-    out["switch"] = {"choice": {0: "isai_fp64", 1: "isai_fp32", 2: "ilu", 3: "fp32_inner"}[choice],
+    out["switch"] = {"choice": {0: "isai_fp64", 1: "isai_fp32", 2: "ilu", 3: "fp32_inner",
+                                4: "ilu_fp32"}[choice],
                      "digits_per_s": rate}
     Pc.close()
     print(json.dumps(out))

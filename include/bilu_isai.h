@@ -21,9 +21,10 @@
  *   - Supported block sizes: 4, 5, 8.  Preconditioner choice: BILU_FP64
  *     (plain ISAI), BILU_FP32 (FP32-stored ISAI factors, FP32
  *     accumulation), BILU_ILU (exact BILU(0): two block triangular solves
- *     per apply, FP64) or BILU_FP32_INNER (FP32 ISAI and an FP32-stored A in
+ *     per apply, FP64), BILU_FP32_INNER (FP32 ISAI and an FP32-stored A in
  *     the Arnoldi products; orthogonalisation, true residuals and restarts
- *     stay FP64).
+ *     stay FP64) or BILU_ILU_FP32 (exact BILU(0) applied in FP32 on an
+ *     FP32 copy of the factor; FP64 operator product and Krylov vectors).
  *   - stream may be NULL (legacy default stream).  Calls are asynchronous
  *     unless documented to return a host value (h_ outputs synchronise).
  */
@@ -52,7 +53,13 @@ enum bilu_status {
   BILU_ERR_IO = -9             /* file missing, unreadable, malformed or corrupt */
 };
 
-enum bilu_precision { BILU_FP64 = 0, BILU_FP32 = 1, BILU_ILU = 2, BILU_FP32_INNER = 3 };
+enum bilu_precision {
+  BILU_FP64 = 0,
+  BILU_FP32 = 1,
+  BILU_ILU = 2,
+  BILU_FP32_INNER = 3,
+  BILU_ILU_FP32 = 4
+};
 
 const char* bilu_status_string(int status);
 int bilu_version(void);
@@ -343,9 +350,11 @@ int bilu_ctx_destroy(bilu_ctx* ctx);
  * ISAI-L/U, BCSC->BCSR reorder, FP32 copies when prec_mask has
  * 1 << BILU_FP32, level analyses of both triangles when it has
  * 1 << BILU_ILU, FP32 copies of the ISAI factors and of A when it has
- * 1 << BILU_FP32_INNER.  A prec_mask of 1 << BILU_ILU alone builds BILU(0)
- * and the level analyses only (no ISAI; solves in the other modes then
- * return BILU_ERR_ARG).
+ * 1 << BILU_FP32_INNER, an FP32 copy of the factor and of its reciprocal
+ * pivots when it has 1 << BILU_ILU_FP32 (built when no row of either
+ * triangle has more than 32 dependencies).  A prec_mask of exact-ILU bits
+ * alone builds BILU(0) and the level analyses only (no ISAI; solves in the
+ * other modes then return BILU_ERR_ARG).
  * h_times (optional, 4 doubles, milliseconds): factor, patterns, isai,
  * total. */
 int bilu_ctx_setup(bilu_ctx* ctx, int nb, int nnzb, int bs, const int* d_row, const int* d_col,
@@ -380,11 +389,12 @@ int bilu_ctx_stats(bilu_ctx* ctx, long long* h_out);
 /* Preconditioner switch by measurement (SpTRSV apply vs SpMV apply):
  * runs up to `cycles` restart cycles (fewer when it reaches tol) from x0 = 0
  * with each choice whose bit
- * (1 << BILU_FP64 / BILU_FP32 / BILU_ILU / BILU_FP32_INNER) is in `mask`
- * and that the setup built, and returns in *h_choice the one with the
- * largest residual reduction per second over its last cycle (restarted
- * GMRES gains most in its first cycle); h_rate (optional, 4 doubles)
- * receives the scores in decimal digits per second, indexed by choice. */
+ * (1 << BILU_FP64 / BILU_FP32 / BILU_ILU / BILU_FP32_INNER / BILU_ILU_FP32)
+ * is in `mask` and that the setup built, and returns in *h_choice the one
+ * with the largest residual reduction per second over its last cycle
+ * (restarted GMRES gains most in its first cycle); h_rate (optional, 4
+ * doubles, 5 when mask has 1 << BILU_ILU_FP32) receives the scores in
+ * decimal digits per second, indexed by choice. */
 int bilu_ctx_select(bilu_ctx* ctx, const double* d_b, int restart, int cycles, double tol,
                     int mask, int* h_choice, double* h_rate);
 

@@ -50,6 +50,10 @@ int sptrsv_syncfree_async(int nb, int bs, const int* row, const int* col, const 
                           const int* order, const double* val, int lower, int unit,
                           const double* b, double* x, int* flags, int* ticket, int* err,
                           cudaStream_t st, const double* rdiag);
+int sptrsv_flow_f32_async(int nb, int bs, const int* row, const int* col, const int* diag,
+                          const int* order, const int* lvl, const int* nlev_d, const float* val,
+                          int lower, int unit, const float* b32, float* x32, double* y64,
+                          unsigned* words, cudaStream_t st, const float* rdiag32, int maxdeg);
 int sptrsv_levels_async(int nb, int bs, const int* row, const int* col, const int* diag,
                         const int* order, const int* lvl, const int* nlev_d, const double* val,
                         int lower, int unit, const double* b, double* x, unsigned* words,
@@ -95,6 +99,7 @@ struct bilu_ctx {
   int *Arow = nullptr, *Acol = nullptr, *diag = nullptr;
   double *Aval = nullptr, *LU = nullptr;
   double* rdiag = nullptr;  // 1 / pivots of the factor's U_II (nb x bs), written by BILU(0)
+  float *LU32 = nullptr, *rdiag32 = nullptr;  // FP32 copies for the mixed exact-ILU apply
   // A, M_L, M_U: 1 if the pattern has rows of more than 64 blocks (their
   // SpMVs then take the kernel in which the CTA shares such rows), from the
   // setup
@@ -136,6 +141,7 @@ struct bilu_ctx {
     Arow = Acol = diag = Lrow = Lcol = Urow = Ucol = nullptr;
     Aval = LU = Lval = Uval = nullptr;
     rdiag = nullptr;
+    LU32 = rdiag32 = nullptr;
     Lval32 = Uval32 = nullptr;
     Aval32 = nullptr;
     ordL = lvlL = nlevL = ordU = lvlU = nlevU = nullptr;
@@ -319,7 +325,8 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   tm.mark(1);
   // the exact-ILU apply's lower solves reuse BILU(0)'s analysis of the
   // lower DAG
-  const bool ilu = (prec_mask & (1 << BILU_ILU)) != 0;
+  const int ilu_bits = (1 << BILU_ILU) | (1 << BILU_ILU_FP32);
+  const bool ilu = (prec_mask & ilu_bits) != 0;
   LevelOut keepL;
   if (ilu) {
     BILU_TRY(c->alloc(&c->ordL, (size_t)nb + 1));
@@ -338,8 +345,8 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   }
   tm.mark(2);
   double t_pat = 0, t_isai = 0;
-  // a mask of BILU_ILU alone asks for the exact ILU apply only: no ISAI
-  const bool isai = prec_mask != (1 << BILU_ILU);
+  // a mask of exact-ILU modes alone builds no ISAI
+  const bool isai = (prec_mask & ~ilu_bits) != 0 || (prec_mask & ilu_bits) == 0;
   if (isai && c->isai_level > 1) {
     // pattern(A^k) by repeated symbolic products with A
     const int *xr = c->Arow, *xc = c->Acol;
@@ -396,7 +403,7 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
     BILU_TRY(bilu_convert_f64_to_f32((size_t)c->nnzL * bs2, c->Lval, c->Lval32, st));
     BILU_TRY(bilu_convert_f64_to_f32((size_t)c->nnzU * bs2, c->Uval, c->Uval32, st));
   }
-  if (prec_mask & (1 << BILU_ILU)) {
+  if (ilu) {
     // level analyses of both triangles of the packed factor for the exact
     // BILU(0) apply (two level-order triangular solves per apply): the
     // lower one is BILU(0)'s, the upper one is built here
@@ -416,6 +423,14 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
     BILU_TRY(c->alloc(&c->ilu_flags, (size_t)nb + 2));
     BILU_TRY(c->alloc(&c->ilu_words, 4));
     BILU_TRY_CUDA(cudaMemsetAsync(c->ilu_words, 0, sizeof(unsigned) * 4, st));
+    // FP32 factor for the mixed exact-ILU apply (the level-order kernel has
+    // an FP32 form for rows of up to 32 dependencies)
+    if ((prec_mask & (1 << BILU_ILU_FP32)) && c->ilu_maxdeg[0] <= 32 && c->ilu_maxdeg[1] <= 32) {
+      BILU_TRY(c->alloc(&c->LU32, (size_t)nnzb * bs2));
+      BILU_TRY(c->alloc(&c->rdiag32, (size_t)nb * bs));
+      BILU_TRY(bilu_convert_f64_to_f32((size_t)nnzb * bs2, c->LU, c->LU32, st));
+      BILU_TRY(bilu_convert_f64_to_f32((size_t)nb * bs, c->rdiag, c->rdiag32, st));
+    }
   }
 
   tm.mark(3);
@@ -501,7 +516,38 @@ int norm2(bilu_ctx* c, const double* v, double* dslot, double* host) {
   return BILU_OK;
 }
 
+// whether the setup built what a preconditioner mode needs (-1: none)
+bool mode_built(const bilu_ctx* c, int prec) {
+  switch (prec) {
+    case -1: return true;
+    case BILU_FP64: return c->Lval != nullptr;
+    case BILU_FP32: return c->Lval32 != nullptr;
+    case BILU_ILU: return c->ilu_words != nullptr;
+    case BILU_FP32_INNER: return c->Aval32 != nullptr;
+    case BILU_ILU_FP32: return c->LU32 != nullptr;
+    default: return false;
+  }
+}
+
+// modes whose apply starts from the FP32 copy of the basis vector
+bool uses_v32(int prec) {
+  return prec == BILU_FP32 || prec == BILU_FP32_INNER || prec == BILU_ILU_FP32;
+}
+
 int apply_prec(bilu_ctx* c, int prec, const double* v, double* z) {
+  if (prec == BILU_ILU_FP32) {
+    // z = U^-1 (L^-1 v) in FP32 on the FP32 factor: L from the FP32 copy of
+    // v (written with v by the normalisation kernel) into t32, U from t32
+    // into x32 with z as its FP64 copy (tmp holds n doubles = 2n floats)
+    float* t32 = reinterpret_cast<float*>(c->tmp);
+    float* x32 = t32 + c->n;
+    BILU_TRY(sptrsv_flow_f32_async(c->nb, c->bs, c->Arow, c->Acol, c->diag, c->ordL, c->lvlL,
+                                   c->nlevL, c->LU32, 1, 1, c->v32, t32, nullptr, c->ilu_words,
+                                   c->st, nullptr, c->ilu_maxdeg[0]));
+    return sptrsv_flow_f32_async(c->nb, c->bs, c->Arow, c->Acol, c->diag, c->ordU, c->lvlU,
+                                 c->nlevU, c->LU32, 0, 0, t32, x32, z, c->ilu_words, c->st,
+                                 c->rdiag32, c->ilu_maxdeg[1]);
+  }
   if (prec == BILU_ILU) {
     // z = U^-1 (L^-1 v): unit-lower then upper solve on the packed factor,
     // each with the schedule its level analysis recommends
@@ -572,7 +618,7 @@ int arnoldi_back(bilu_ctx* c, int j, int prec) {
   BILU_TRY(mgs_sweep(n, V + ld * j, s + j, nullptr, c->w, c->partial, c->counter,
                      s + kPartStride, st));
   BILU_TRY(scale_rsqrt(n, c->w, s + kPartStride, c->V + ld * (j + 1), st,
-                       (prec == BILU_FP32 || prec == BILU_FP32_INNER) ? c->v32 : nullptr));
+                       uses_v32(prec) ? c->v32 : nullptr));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->hpin, s, sizeof(double) * (kPartStride + 1),
                                 cudaMemcpyDeviceToHost, st));
   return BILU_OK;
@@ -586,14 +632,13 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
   if (!c || !c->ready || !d_b || !d_x || restart < 1 || restart > kMaxVec - 1 || maxit < 0)
     return BILU_ERR_ARG;
   if (prec != -1 && prec != BILU_FP64 && prec != BILU_FP32 && prec != BILU_ILU &&
-      prec != BILU_FP32_INNER)
+      prec != BILU_FP32_INNER && prec != BILU_ILU_FP32)
     return BILU_ERR_ARG;
-  if ((prec == BILU_FP64 && !c->Lval) || (prec == BILU_FP32 && !c->Lval32) ||
-      (prec == BILU_ILU && !c->ilu_words) || (prec == BILU_FP32_INNER && !c->Aval32))
-    return BILU_ERR_ARG;  // the setup did not build this preconditioner
+  if (!mode_built(c, prec)) return BILU_ERR_ARG;  // the setup did not build this preconditioner
   BILU_TRY(ensure_solver(c, restart));
   cudaStream_t st = c->st;
-  if (prec == BILU_ILU) BILU_TRY_CUDA(cudaMemsetAsync(c->ilu_words, 0, sizeof(unsigned) * 4, st));
+  const bool ilu_mode = prec == BILU_ILU || prec == BILU_ILU_FP32;
+  if (ilu_mode) BILU_TRY_CUDA(cudaMemsetAsync(c->ilu_words, 0, sizeof(unsigned) * 4, st));
   const int m = restart;
   const long long n = c->n;
   double* s = c->dscal;
@@ -618,7 +663,7 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
   while (status != BILU_OK && total < maxit) {
     // V_0 = r / beta (beta^2 sits in s[5*kPartStride])
     BILU_TRY(scale_rsqrt(n, c->r, s + 5 * kPartStride, c->V, st,
-                         (prec == BILU_FP32 || prec == BILU_FP32_INNER) ? c->v32 : nullptr));
+                         uses_v32(prec) ? c->v32 : nullptr));
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int jlast = -1;
@@ -671,7 +716,7 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
     BILU_TRY(reduce_partials(c->partial, 1, s + 5 * kPartStride, st));
     BILU_TRY_CUDA(cudaMemcpyAsync(&rr, s + 5 * kPartStride, sizeof(double), cudaMemcpyDeviceToHost, st));
     int ilu_err = 0;
-    if (prec == BILU_ILU)
+    if (ilu_mode)
       BILU_TRY_CUDA(cudaMemcpyAsync(&ilu_err, c->ilu_words + 2, sizeof(int),
                                     cudaMemcpyDeviceToHost, st));
     BILU_TRY_CUDA(cudaStreamSynchronize(st));
@@ -712,12 +757,12 @@ extern "C" int bilu_ctx_select(bilu_ctx* c, const double* d_b, int restart, int 
   std::vector<double> hist((size_t)restart * cycles + 1);
   int best = -1, rc = BILU_OK;
   double best_rate = -1.0;
-  for (int p = 0; p < 4 && rc == BILU_OK; ++p) {
+  // h_rate has an entry for BILU_ILU_FP32 only when the mask asks for it
+  const int nrate = (mask >> BILU_ILU_FP32) ? 5 : 4;
+  for (int p = 0; p < nrate && rc == BILU_OK; ++p) {
     if (h_rate) h_rate[p] = 0.0;
     if (!(mask & (1 << p))) continue;
-    if ((p == BILU_FP64 && !c->Lval) || (p == BILU_FP32 && !c->Lval32) ||
-        (p == BILU_ILU && !c->ilu_words) || (p == BILU_FP32_INNER && !c->Aval32))
-      continue;
+    if (!mode_built(c, p)) continue;
     int it = 0;
     double rr = 1.0;
     cudaEventRecord(e0, c->st);

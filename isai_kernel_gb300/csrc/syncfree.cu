@@ -656,16 +656,18 @@ constexpr int kFactorLevelWidth = 4096;
 // (issued before the current row's arithmetic), and, issued right after it,
 // the next row's first D column indices and blocks, its diagonal row and b.
 // The x reads of those D blocks are then independent of each other.
-template <int BS>
+// T: the arithmetic and storage type of the solve (double, or float for
+// the FP32-stored factor of the mixed exact-ILU apply).
+template <int BS, class T>
 struct GRowPre {
-  // blocks held in registers (bs 8: one, within 128 registers a thread)
+  // blocks held in registers (bs 8: one, within the register budget)
   static constexpr int D = BS <= 5 ? 16 / BS : 1;
   int I, ps, pe;   // I < 0: no row for this group
   int K[D];        // columns of the first D dependencies (-1 past the row)
-  double a[D][BS]; // row r of those blocks
-  double dq[BS];   // row r of the diagonal block
-  double bq;       // b_r
-  double rq;       // 1 / pivot of row r, when the factorisation stored it
+  T a[D][BS];      // row r of those blocks
+  T dq[BS];        // row r of the diagonal block
+  T bq;            // b_r
+  T rq;            // 1 / pivot of row r, when the factorisation stored it
 };
 
 // structural words of row I: dependency range and diagonal position
@@ -682,12 +684,11 @@ __device__ __forceinline__ void grow_meta(int I, const int* __restrict__ row,
   m.dI = __ldg(diag + I);
 }
 
-template <int BS, bool LOWER>
+template <int BS, bool LOWER, class T>
 __device__ __forceinline__ void grow_load(int I, const GRowMeta& m, const int* __restrict__ col,
-                                          const double* __restrict__ val,
-                                          const double* __restrict__ b,
-                                          const double* __restrict__ rdiag, GRowPre<BS>& p) {
-  constexpr int BS2 = BS * BS, D = GRowPre<BS>::D;
+                                          const T* __restrict__ val, const T* __restrict__ b,
+                                          const T* __restrict__ rdiag, GRowPre<BS, T>& p) {
+  constexpr int BS2 = BS * BS, D = GRowPre<BS, T>::D;
   const int r = (threadIdx.x & 31) % BS;
   p.I = I;
   p.ps = LOWER ? m.rs : m.dI + 1;
@@ -697,28 +698,27 @@ __device__ __forceinline__ void grow_load(int I, const GRowMeta& m, const int* _
     const int q = p.ps + j;
     const bool has = I >= 0 && q < p.pe;
     p.K[j] = has ? __ldg(col + q) : -1;
-    const double* blk = val + (long long)(has ? q : 0) * BS2 + r * BS;
+    const T* blk = val + (long long)(has ? q : 0) * BS2 + r * BS;
 #pragma unroll
-    for (int c = 0; c < BS; ++c) p.a[j][c] = has ? __ldg(blk + c) : 0.0;
+    for (int c = 0; c < BS; ++c) p.a[j][c] = has ? __ldg(blk + c) : T(0);
   }
   if (I < 0) return;
-  const double* Dg = val + (long long)m.dI * BS2 + r * BS;
+  const T* Dg = val + (long long)m.dI * BS2 + r * BS;
 #pragma unroll
   for (int c = 0; c < BS; ++c) p.dq[c] = __ldg(Dg + c);
   p.bq = __ldg(b + (long long)I * BS + r);
-  p.rq = (!LOWER && rdiag) ? __ldg(rdiag + (long long)I * BS + r) : 0.0;
+  p.rq = (!LOWER && rdiag) ? __ldg(rdiag + (long long)I * BS + r) : T(0);
 }
 
-template <int BS, bool LOWER>
+template <int BS, bool LOWER, class T>
 __device__ __forceinline__ void grow_prefetch(int I, const int* __restrict__ row,
                                               const int* __restrict__ col,
                                               const int* __restrict__ diag,
-                                              const double* __restrict__ val,
-                                              const double* __restrict__ b,
-                                              const double* __restrict__ rdiag, GRowPre<BS>& p) {
+                                              const T* __restrict__ val, const T* __restrict__ b,
+                                              const T* __restrict__ rdiag, GRowPre<BS, T>& p) {
   GRowMeta m;
   grow_meta(I, row, diag, m);
-  grow_load<BS, LOWER>(I, m, col, val, b, rdiag, p);
+  grow_load<BS, LOWER, T>(I, m, col, val, b, rdiag, p);
 }
 
 // Level-scheduled solve for rows with long dependency lists (more than
@@ -766,32 +766,61 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_sptrsv_levels(
 // level schedule gives it (the same static assignment and the same
 // arithmetic as k_sptrsv_levels), but instead of meeting the whole grid at
 // a barrier after each level it waits only for the x entries its row reads.
-// x is self-flagging: before the launch every entry holds kXPending, a
-// signalling-NaN pattern; a row's entries are written once, with single
-// 64-bit stores, and FP64 arithmetic only ever yields quiet NaNs, so an
-// entry that no longer reads kXPending holds its final value and no flag,
-// fence or barrier is needed.  Each dependent entry is read with a strong
+// x is self-flagging: before the launch every entry holds a signalling-NaN
+// pattern (XBits::kPending); a row's entries are written once, each with a
+// single 64-bit (FP32 solve: 32-bit) store, and floating-point arithmetic
+// only ever yields quiet NaNs, so an entry that no longer reads the pattern
+// holds its final value and no flag, fence or barrier is needed.  Each dependent entry is read with a strong
 // (L2) load; a pending one is polled with bounded back-off.  All warps are
 // co-resident (cooperative launch) and each processes its rows in level
 // order, so every wait ends: rows of level 0 wait for nothing, rows of
 // level l only for rows of lower levels.  The solve then advances as a
 // wavefront at the latency of one dependency chain per level rather than
 // at that of the slowest CTA plus a grid barrier.
-constexpr unsigned long long kXPending = 0x7FF0A5A5A5A5A5A5ull;  // signalling NaN
+// Bit patterns of x entries: kPending (a signalling NaN) and the quiet NaN
+// stored instead of a result that happened to carry the pending pattern.
+template <class T>
+struct XBits;
+template <>
+struct XBits<double> {
+  using U = unsigned long long;
+  static constexpr U kPending = 0x7FF0A5A5A5A5A5A5ull;
+  static constexpr U kQuiet = 0x7FF8000000000000ull;
+};
+template <>
+struct XBits<float> {
+  using U = unsigned;
+  static constexpr U kPending = 0x7FA5A5A5u;
+  static constexpr U kQuiet = 0x7FC00000u;
+};
 constexpr int kFlowSpin = 64;  // polling rounds without sleeping
 
-__device__ __forceinline__ unsigned long long ld_strong_u64(const double* p) {
+__device__ __forceinline__ unsigned long long ld_strong_bits(const double* p) {
   unsigned long long v;
   asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p));
   return v;
 }
+__device__ __forceinline__ unsigned ld_strong_bits(const float* p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ double from_bits(unsigned long long u, double) {
+  return __longlong_as_double((long long)u);
+}
+__device__ __forceinline__ float from_bits(unsigned u, float) { return __uint_as_float(u); }
 
 // Stores a computed entry; a value with the pending pattern (impossible
 // for an arithmetic result) would be stored as the canonical quiet NaN.
-__device__ __forceinline__ void st_strong_f64(double* p, double v) {
+__device__ __forceinline__ void st_strong(double* p, double v) {
   unsigned long long u = (unsigned long long)__double_as_longlong(v);
-  if (u == kXPending) u = 0x7FF8000000000000ull;
+  if (u == XBits<double>::kPending) u = XBits<double>::kQuiet;
   asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(u));
+}
+__device__ __forceinline__ void st_strong(float* p, float v) {
+  unsigned u = __float_as_uint(v);
+  if (u == XBits<float>::kPending) u = XBits<float>::kQuiet;
+  asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(u));
 }
 
 // Re-reads the entries of u[] that are still pending (x entries of rows of
@@ -804,12 +833,13 @@ __device__ __forceinline__ void st_strong_f64(double* p, double v) {
 // not keep D * BS addresses live across the loop).  Per lane, no warp
 // collectives (groups of a warp wait for different rows).  false: the
 // launch aborted.
-template <int BS, int D>
-__device__ __forceinline__ bool poll_pending(unsigned long long (&u)[D * BS], const int (&K)[D],
-                                             const double* x, const SyncState& ss) {
+template <int BS, int D, class T>
+__device__ __forceinline__ bool poll_pending(typename XBits<T>::U (&u)[D * BS], const int (&K)[D],
+                                             const T* x, const SyncState& ss) {
+  constexpr typename XBits<T>::U kP = XBits<T>::kPending;
   bool pend = false;
 #pragma unroll
-  for (int i = 0; i < D * BS; ++i) pend |= u[i] == kXPending;
+  for (int i = 0; i < D * BS; ++i) pend |= u[i] == kP;
   long long n = 0;
   unsigned ns = 32;
   while (pend) {
@@ -819,12 +849,12 @@ __device__ __forceinline__ bool poll_pending(unsigned long long (&u)[D * BS], co
     for (int j = 0; j < D; ++j) {
       int k;
       asm volatile("mov.b32 %0, %1;" : "=r"(k) : "r"(K[j]));
-      const double* xk = x + (long long)k * BS;
+      const T* xk = x + (long long)k * BS;
 #pragma unroll
       for (int c = 0; c < BS; ++c) {
-        if (u[j * BS + c] == kXPending) {
-          u[j * BS + c] = ld_strong_u64(xk + c);
-          pend |= u[j * BS + c] == kXPending;
+        if (u[j * BS + c] == kP) {
+          u[j * BS + c] = ld_strong_bits(xk + c);
+          pend |= u[j * BS + c] == kP;
         }
       }
     }
@@ -839,68 +869,72 @@ __device__ __forceinline__ bool poll_pending(unsigned long long (&u)[D * BS], co
 }
 
 // grow_finish with waits on the entries read; the same operations in the
-// same order.  Called by all 32 lanes; false in every lane if the launch
-// aborted.
-template <int BS, bool LOWER, bool UNIT>
-__device__ __forceinline__ bool grow_finish_flow(const GRowPre<BS>& p, const int* __restrict__ col,
-                                                 const double* __restrict__ val, double* x,
+// same order, in T.  y64 (optional): x is also stored there as FP64 (the
+// FP32 solve's output in the precision its consumer wants).  Called by all
+// 32 lanes; false in every lane if the launch aborted.
+template <int BS, bool LOWER, bool UNIT, class T>
+__device__ __forceinline__ bool grow_finish_flow(const GRowPre<BS, T>& p,
+                                                 const int* __restrict__ col,
+                                                 const T* __restrict__ val, T* x, double* y64,
                                                  bool have_rq, const SyncState& ss) {
-  constexpr int BS2 = BS * BS, D = GRowPre<BS>::D;
+  constexpr int BS2 = BS * BS, D = GRowPre<BS, T>::D;
+  using U = typename XBits<T>::U;
   const int lane = threadIdx.x & 31, r = lane % BS, gb = lane - r;
-  double tot = 0.0, rq = 1.0;
+  T tot = T(0), rq = T(1);
   bool ok = true;
   if (p.I >= 0) {
-    double d = p.dq[0];
+    T d = p.dq[0];
 #pragma unroll
     for (int c = 1; c < BS; ++c)
       if (c == r) d = p.dq[c];
     // entries of absent dependencies read as 0 (never pending)
-    unsigned long long u[D * BS];
+    U u[D * BS];
 #pragma unroll
     for (int j = 0; j < D; ++j) {
-      const double* xk = x + (long long)(p.K[j] >= 0 ? p.K[j] : 0) * BS;
+      const T* xk = x + (long long)(p.K[j] >= 0 ? p.K[j] : 0) * BS;
 #pragma unroll
-      for (int c = 0; c < BS; ++c) u[j * BS + c] = p.K[j] >= 0 ? ld_strong_u64(xk + c) : 0ull;
+      for (int c = 0; c < BS; ++c) u[j * BS + c] = p.K[j] >= 0 ? ld_strong_bits(xk + c) : U(0);
     }
-    if (!UNIT) rq = have_rq ? p.rq : 1.0 / d;  // overlaps the x reads
-    ok = poll_pending<BS, D>(u, p.K, x, ss);
+    if (!UNIT) rq = have_rq ? p.rq : T(1) / d;  // overlaps the x reads
+    ok = poll_pending<BS, D, T>(u, p.K, x, ss);
 #pragma unroll
     for (int j = 0; j < D; ++j) {
       if (p.K[j] >= 0) {
-        double sp = 0.0;
+        T sp = T(0);
 #pragma unroll
-        for (int c = 0; c < BS; ++c)
-          sp = fma(p.a[j][c], __longlong_as_double((long long)u[j * BS + c]), sp);
+        for (int c = 0; c < BS; ++c) sp = fma(p.a[j][c], from_bits(u[j * BS + c], T()), sp);
         tot += sp;
       }
     }
     for (int q = p.ps + D; ok && q < p.pe; ++q) {
       const int K = __ldg(col + q);
-      const double* blk = val + (long long)q * BS2 + r * BS;
-      const double* xq = x + (long long)K * BS;
-      unsigned long long uq[BS];
+      const T* blk = val + (long long)q * BS2 + r * BS;
+      const T* xq = x + (long long)K * BS;
+      U uq[BS];
 #pragma unroll
-      for (int c = 0; c < BS; ++c) uq[c] = ld_strong_u64(xq + c);
+      for (int c = 0; c < BS; ++c) uq[c] = ld_strong_bits(xq + c);
       const int Kq[1] = {K};
-      ok = poll_pending<BS, 1>(uq, Kq, x, ss);
-      double sp = 0.0;
+      ok = poll_pending<BS, 1, T>(uq, Kq, x, ss);
+      T sp = T(0);
 #pragma unroll
-      for (int c = 0; c < BS; ++c)
-        sp = fma(__ldg(blk + c), __longlong_as_double((long long)uq[c]), sp);
+      for (int c = 0; c < BS; ++c) sp = fma(__ldg(blk + c), from_bits(uq[c], T()), sp);
       tot += sp;
     }
   }
   if (__any_sync(FULL, !ok)) return false;
-  double v = p.bq - tot, xr = 0.0;
+  T v = p.bq - tot, xr = T(0);
 #pragma unroll
   for (int k = 0; k < BS; ++k) {
     const int c = LOWER ? k : BS - 1 - k;
-    double mine = (UNIT || r != c) ? v : v * rq;
-    double xc = __shfl_sync(FULL, mine, (gb + c) & 31);
+    T mine = (UNIT || r != c) ? v : v * rq;
+    T xc = __shfl_sync(FULL, mine, (gb + c) & 31);
     if (r == c) xr = xc;
     if (LOWER ? (r > c) : (r < c)) v -= p.dq[c] * xc;
   }
-  if (p.I >= 0 && p.I != ss.withhold) st_strong_f64(x + (long long)p.I * BS + r, xr);
+  if (p.I >= 0 && p.I != ss.withhold) {
+    st_strong(x + (long long)p.I * BS + r, xr);
+    if (y64) y64[(long long)p.I * BS + r] = (double)xr;
+  }
   return true;
 }
 
@@ -938,12 +972,12 @@ __device__ __forceinline__ int cursor_row(const RowCursor& c, int g, bool active
 // index of the one after that one step earlier still.  Two staged rows
 // need about 180 registers a thread, so one 256-thread CTA runs per SM (two
 // warps a sub-partition; more warps only queue on its FP64 unit).
-template <int BS, bool LOWER, bool UNIT>
+template <int BS, bool LOWER, bool UNIT, class T>
 __global__ void __launch_bounds__(kLvlThreads, 1) k_sptrsv_flow(
     const int* __restrict__ row, const int* __restrict__ col, const int* __restrict__ diag,
-    const double* __restrict__ val, const double* __restrict__ b, double* x,
-    const int* __restrict__ order, const int* __restrict__ lvl_ptr, const int* __restrict__ nlev_p,
-    SyncState ss, int per_sm) {
+    const T* __restrict__ val, const T* __restrict__ b, T* x, double* y64,
+    const T* __restrict__ rdiag_in, const int* __restrict__ order,
+    const int* __restrict__ lvl_ptr, const int* __restrict__ nlev_p, SyncState ss, int per_sm) {
   constexpr int G = 32 / BS;
   const int g = (threadIdx.x & 31) / BS;
   const int warp = spread_warp(per_sm);
@@ -953,7 +987,7 @@ __global__ void __launch_bounds__(kLvlThreads, 1) k_sptrsv_flow(
   const int nlev = __ldg(nlev_p);
   if (nlev <= 0) return;
   const bool active = g < G;
-  const double* rdiag = LOWER ? nullptr : ss.rdiag;
+  const T* rdiag = LOWER ? nullptr : rdiag_in;
   RowCursor c0{0, __ldg(lvl_ptr) + first};
   RowCursor c1 = c0;
   cursor_next(c1, nlev, first, ngrp, lvl_ptr);
@@ -961,8 +995,8 @@ __global__ void __launch_bounds__(kLvlThreads, 1) k_sptrsv_flow(
   cursor_next(c2, nlev, first, ngrp, lvl_ptr);
   RowCursor c3 = c2;
   cursor_next(c3, nlev, first, ngrp, lvl_ptr);
-  GRowPre<BS> pre;
-  grow_prefetch<BS, LOWER>(cursor_row(c0, g, active, nlev, order, lvl_ptr), row, col, diag, val,
+  GRowPre<BS, T> pre;
+  grow_prefetch<BS, LOWER, T>(cursor_row(c0, g, active, nlev, order, lvl_ptr), row, col, diag, val,
                            b, rdiag, pre);
   int I1 = cursor_row(c1, g, active, nlev, order, lvl_ptr);
   GRowMeta m1;
@@ -970,12 +1004,13 @@ __global__ void __launch_bounds__(kLvlThreads, 1) k_sptrsv_flow(
   int I2 = cursor_row(c2, g, active, nlev, order, lvl_ptr);
   while (c0.l < nlev) {
     // loads for the rows ahead first: they do not depend on x
-    GRowPre<BS> nxt;
-    if (c1.l < nlev) grow_load<BS, LOWER>(I1, m1, col, val, b, rdiag, nxt);
+    GRowPre<BS, T> nxt;
+    if (c1.l < nlev) grow_load<BS, LOWER, T>(I1, m1, col, val, b, rdiag, nxt);
     GRowMeta m2;
     grow_meta(I2, row, diag, m2);
     const int I3 = cursor_row(c3, g, active, nlev, order, lvl_ptr);
-    if (!grow_finish_flow<BS, LOWER, UNIT>(pre, col, val, x, rdiag != nullptr, ss)) return;
+    if (!grow_finish_flow<BS, LOWER, UNIT, T>(pre, col, val, x, y64, rdiag != nullptr, ss))
+      return;
     pre = nxt;
     m1 = m2;
     I1 = I2;
@@ -987,10 +1022,11 @@ __global__ void __launch_bounds__(kLvlThreads, 1) k_sptrsv_flow(
   }
 }
 
-__global__ void k_fill_pending(unsigned long long* x, long long n) {
+template <class T>
+__global__ void k_fill_pending(typename XBits<T>::U* x, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    x[i] = kXPending;
+    x[i] = XBits<T>::kPending;
 }
 
 // ------------------------------------------------------------------ BILU(0)
@@ -1670,24 +1706,45 @@ int launch_sptrsv_levels(int nb, const int* row, const int* col, const int* diag
 
 // Flow-scheduled solve: x is filled with the pending pattern on the stream,
 // then one cooperative launch (every warp resident, so every wait ends).
+// rdiag: reciprocal pivots for the upper solve (null: divide); y64: an
+// FP64 copy of x (null: none).
+template <int BS, class T>
+int launch_sptrsv_flow_t(int nb, const int* row, const int* col, const int* diag, const T* val,
+                         int lower, int unit, const T* b, T* x, double* y64, const T* rdiag,
+                         const int* order, const int* lvl_ptr, const int* nlev_d, SyncState ss,
+                         cudaStream_t st) {
+  const void* fn = lower ? (unit ? (const void*)k_sptrsv_flow<BS, true, true, T>
+                                 : (const void*)k_sptrsv_flow<BS, true, false, T>)
+                         : (unit ? (const void*)k_sptrsv_flow<BS, false, true, T>
+                                 : (const void*)k_sptrsv_flow<BS, false, false, T>);
+  int grid = std::min<long long>(coop_grid(fn, kLvlThreads),
+                                 ceil_div(nb, (kLvlThreads / 32) * (32 / BS)));
+  int per_sm = std::max(1, std::min(occupancy_per_sm(fn, kLvlThreads), (int)ceil_div(grid, sm_count())));
+  const long long n = (long long)nb * BS;
+  k_fill_pending<T><<<(unsigned)std::min<long long>(ceil_div(n, 256), (long long)sm_count() * 16),
+                      256, 0, st>>>((typename XBits<T>::U*)x, n);
+  BILU_LAUNCH_CHECK();
+  void* args[] = {&row, &col,   &diag,    &val,     &b,      &x,  &y64,
+                  &rdiag, &order, &lvl_ptr, &nlev_d, &ss, &per_sm};
+  return launch_coop(fn, grid, kLvlThreads, args, st);
+}
+
 template <int BS>
 int launch_sptrsv_flow(int nb, const int* row, const int* col, const int* diag,
                        const double* val, int lower, int unit, const double* b, double* x,
                        const int* order, const int* lvl_ptr, const int* nlev_d, SyncState ss,
                        cudaStream_t st) {
-  const void* fn = lower ? (unit ? (const void*)k_sptrsv_flow<BS, true, true>
-                                 : (const void*)k_sptrsv_flow<BS, true, false>)
-                         : (unit ? (const void*)k_sptrsv_flow<BS, false, true>
-                                 : (const void*)k_sptrsv_flow<BS, false, false>);
-  int grid = std::min<long long>(coop_grid(fn, kLvlThreads),
-                                 ceil_div(nb, (kLvlThreads / 32) * (32 / BS)));
-  int per_sm = std::max(1, std::min(occupancy_per_sm(fn, kLvlThreads), (int)ceil_div(grid, sm_count())));
-  const long long n = (long long)nb * BS;
-  k_fill_pending<<<(unsigned)std::min<long long>(ceil_div(n, 256), (long long)sm_count() * 16),
-                   256, 0, st>>>((unsigned long long*)x, n);
-  BILU_LAUNCH_CHECK();
-  void* args[] = {&row, &col, &diag, &val, &b, &x, &order, &lvl_ptr, &nlev_d, &ss, &per_sm};
-  return launch_coop(fn, grid, kLvlThreads, args, st);
+  return launch_sptrsv_flow_t<BS, double>(nb, row, col, diag, val, lower, unit, b, x, nullptr,
+                                          ss.rdiag, order, lvl_ptr, nlev_d, ss, st);
+}
+
+template <int BS>
+int launch_sptrsv_flow_f32(int nb, const int* row, const int* col, const int* diag,
+                           const float* val, int lower, int unit, const float* b, float* x,
+                           double* y64, const float* rdiag, const int* order, const int* lvl_ptr,
+                           const int* nlev_d, SyncState ss, cudaStream_t st) {
+  return launch_sptrsv_flow_t<BS, float>(nb, row, col, diag, val, lower, unit, b, x, y64, rdiag,
+                                         order, lvl_ptr, nlev_d, ss, st);
 }
 
 template <int BS>
@@ -1944,6 +2001,23 @@ int sptrsv_levels_async(int nb, int bs, const int* row, const int* col, const in
   GridSync gs{words, words + 1, w + 2, kSpinLimit};
   return BILU_DISPATCH_BS(bs, launch_sptrsv_levels, nb, row, col, diag, val, lower, unit, b, x,
                           order, lvl, nlev_d, 0, ss, gs, st);
+}
+
+// Launch-only FP32 level-order solve for the mixed exact-ILU apply: FP32
+// factor values, b and x (x32 must not be b32), FP32 reciprocal pivots for
+// the upper solve, an optional FP64 copy of x (y64).  Only the flow kernel
+// has an FP32 form: patterns with rows of more than kLongRow dependencies
+// return BILU_ERR_UNSUPPORTED.  words as sptrsv_levels_async.
+int sptrsv_flow_f32_async(int nb, int bs, const int* row, const int* col, const int* diag,
+                          const int* order, const int* lvl, const int* nlev_d, const float* val,
+                          int lower, int unit, const float* b32, float* x32, double* y64,
+                          unsigned* words, cudaStream_t st, const float* rdiag32, int maxdeg) {
+  if (nb == 0) return BILU_OK;
+  if (maxdeg > kLongRow) return BILU_ERR_UNSUPPORTED;
+  int* w = (int*)words;
+  SyncState ss{nullptr, nullptr, w + 2, w + 3, kSpinLimit, -1, nullptr, nullptr};
+  return BILU_DISPATCH_BS(bs, launch_sptrsv_flow_f32, nb, row, col, diag, val, lower, unit, b32,
+                          x32, y64, rdiag32, order, lvl, nlev_d, ss, st);
 }
 
 }  // namespace bilu

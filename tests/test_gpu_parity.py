@@ -684,7 +684,7 @@ def test_gmres_exact_ilu_and_switch(cuda, orc, name):
                                      maxit=3000)
     assert st == 0
     p = api.Preconditioner(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda),
-                           ilu=True, fp32_inner=True)
+                           ilu=True, fp32_inner=True, ilu_fp32=True)
     x, res = p.solve(T(b, cuda), prec=api.BILU_ILU, maxit=3000, history=True)
     assert res.converged and res.iters == ito
     assert relerr(N(x), xo) < 1e-8
@@ -698,8 +698,13 @@ def test_gmres_exact_ilu_and_switch(cuda, orc, name):
     assert st4 == 0
     x4, res4 = p.solve(T(b, cuda), prec=api.BILU_FP32_INNER, maxit=3000)
     assert res4.converged and res4.relres <= 1e-10 and abs(res4.iters - it4) <= 3
+    # exact BILU(0) applied in FP32 on the FP32 factor: FP64 true residual
+    # 1e-10 within 3 iterations of the FP64 exact ILU
+    x5, res5 = p.solve(T(b, cuda), prec=api.BILU_ILU_FP32, maxit=3000)
+    assert res5.converged and res5.relres <= 1e-10 and abs(res5.iters - ito) <= 3
+    assert relerr(N(x5), xo) < 1e-8
     choice, rate = p.select(T(b, cuda), cycles=1)
-    assert choice in (0, 1, 2, 3) and all(r > 0 for r in rate)
+    assert choice in (0, 1, 2, 3, 4) and len(rate) == 5 and all(r > 0 for r in rate)
     xa, resa = p.solve(T(b, cuda), prec="auto", maxit=3000)
     assert resa.converged
     p.close()
