@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -91,6 +92,43 @@ namespace {
 
 using namespace bilu;
 
+namespace bilu {
+namespace {
+
+// The library's device buffers come from a private stream-ordered memory
+// pool per device whose release threshold keeps freed memory reserved:
+// the host-buffer entry point creates and destroys a handle (several GB of
+// factor, ISAI and Krylov storage at 128^3) per call, and mapping that
+// memory anew each time is a visible part of the call.  Other users of the
+// default pool in the process are not affected.
+cudaMemPool_t lib_pool(int dev) {
+  static std::mutex mu;
+  static std::vector<cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)pools.size() <= dev) pools.resize(dev + 1, nullptr);
+  if (!pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    if (cudaMemPoolCreate(&p, &props) != cudaSuccess) return nullptr;
+    unsigned long long keep = ~0ull;
+    cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[dev] = p;
+  }
+  return pools[dev];
+}
+
+cudaError_t dev_alloc(void** p, size_t bytes, int dev, cudaStream_t st) {
+  cudaMemPool_t pool = lib_pool(dev);
+  if (!pool) return cudaMalloc(p, bytes);
+  return cudaMallocFromPoolAsync(p, bytes, pool, st);
+}
+
+}  // namespace
+}  // namespace bilu
+
 struct bilu_ctx {
   int dev = 0;
   cudaStream_t st = nullptr;
@@ -136,7 +174,7 @@ struct bilu_ctx {
   long long steps = 0, restarts = 0;  // Arnoldi steps and cycles of the last solve
   std::vector<void*> setup_bufs;
   void free_setup() {
-    for (void* p : setup_bufs) cudaFree(p);
+    for (void* p : setup_bufs) cudaFreeAsync(p, st);
     setup_bufs.clear();
     Arow = Acol = diag = Lrow = Lcol = Urow = Ucol = nullptr;
     Aval = LU = Lval = Uval = nullptr;
@@ -151,11 +189,11 @@ struct bilu_ctx {
     ready = false;
   }
   void free_solver() {
-    cudaFree(V); cudaFree(Z); cudaFree(w); cudaFree(r); cudaFree(tmp); cudaFree(v32);
-    cudaFree(z32);
+    for (void* p : {(void*)V, (void*)Z, (void*)w, (void*)r, (void*)tmp, (void*)v32, (void*)z32,
+                    (void*)partial, (void*)dscal, (void*)dcoef, (void*)counter})
+      if (p) cudaFreeAsync(p, st);
     v32 = nullptr;
     z32 = nullptr;
-    cudaFree(partial); cudaFree(dscal); cudaFree(dcoef); cudaFree(counter);
     counter = nullptr;
     if (hpin) cudaFreeHost(hpin);
     if (ev) cudaEventDestroy(ev);
@@ -167,7 +205,7 @@ struct bilu_ctx {
   int alloc(T** p, size_t count) {
     *p = nullptr;
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+    cudaError_t e = bilu::dev_alloc((void**)p, sizeof(T) * count, dev, st);
     if (e != cudaSuccess) return cuda_status(e);
     setup_bufs.push_back(*p);
     return BILU_OK;
@@ -488,18 +526,21 @@ int ensure_solver(bilu_ctx* c, int m) {
   size_t n = (size_t)c->n;
   // basis vectors start on 256-byte boundaries (16-byte vector loads)
   c->ldv = (long long)((n + 31) & ~(size_t)31);
-  BILU_TRY_CUDA(cudaMalloc(&c->V, sizeof(double) * c->ldv * (m + 1)));
-  BILU_TRY_CUDA(cudaMalloc(&c->Z, sizeof(double) * c->ldv * m));
-  BILU_TRY_CUDA(cudaMalloc(&c->w, sizeof(double) * n));
-  BILU_TRY_CUDA(cudaMalloc(&c->r, sizeof(double) * n));
-  BILU_TRY_CUDA(cudaMalloc(&c->tmp, sizeof(double) * n));
-  BILU_TRY_CUDA(cudaMalloc(&c->v32, sizeof(float) * n));
-  BILU_TRY_CUDA(cudaMalloc(&c->z32, sizeof(float) * n));
-  BILU_TRY_CUDA(cudaMalloc(&c->partial, sizeof(double) * kRedCTAs * kPartStride));
-  BILU_TRY_CUDA(cudaMalloc(&c->dscal, sizeof(double) * 6 * kPartStride));
-  BILU_TRY_CUDA(cudaMalloc(&c->dcoef, sizeof(double) * kPartStride));
+  auto get = [&](auto** p, size_t bytes) {
+    return dev_alloc((void**)p, bytes, c->dev, c->st);
+  };
+  BILU_TRY_CUDA(get(&c->V, sizeof(double) * c->ldv * (m + 1)));
+  BILU_TRY_CUDA(get(&c->Z, sizeof(double) * c->ldv * m));
+  BILU_TRY_CUDA(get(&c->w, sizeof(double) * n));
+  BILU_TRY_CUDA(get(&c->r, sizeof(double) * n));
+  BILU_TRY_CUDA(get(&c->tmp, sizeof(double) * n));
+  BILU_TRY_CUDA(get(&c->v32, sizeof(float) * n));
+  BILU_TRY_CUDA(get(&c->z32, sizeof(float) * n));
+  BILU_TRY_CUDA(get(&c->partial, sizeof(double) * kRedCTAs * kPartStride));
+  BILU_TRY_CUDA(get(&c->dscal, sizeof(double) * 6 * kPartStride));
+  BILU_TRY_CUDA(get(&c->dcoef, sizeof(double) * kPartStride));
   BILU_TRY_CUDA(cudaMallocHost(&c->hpin, sizeof(double) * 6 * kPartStride));
-  BILU_TRY_CUDA(cudaMalloc(&c->counter, sizeof(unsigned)));
+  BILU_TRY_CUDA(get(&c->counter, sizeof(unsigned)));
   BILU_TRY_CUDA(cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->st));
   c->m_alloc = m;
   return BILU_OK;
@@ -813,11 +854,13 @@ extern "C" int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const
   auto cu = [&](cudaError_t e) {
     if (rc == BILU_OK && e != cudaSuccess) rc = cuda_status(e);
   };
-  cu(cudaMallocAsync(&row, sizeof(int) * (nb + 1), st));
-  cu(cudaMallocAsync(&col, sizeof(int) * nnzb, st));
-  cu(cudaMallocAsync(&val, sizeof(double) * nnzb * bs2, st));
-  cu(cudaMallocAsync(&b, sizeof(double) * n, st));
-  cu(cudaMallocAsync(&x, sizeof(double) * n, st));
+  int dev = 0;
+  cu(cudaGetDevice(&dev));
+  cu(dev_alloc((void**)&row, sizeof(int) * (nb + 1), dev, st));
+  cu(dev_alloc((void**)&col, sizeof(int) * nnzb, dev, st));
+  cu(dev_alloc((void**)&val, sizeof(double) * nnzb * bs2, dev, st));
+  cu(dev_alloc((void**)&b, sizeof(double) * n, dev, st));
+  cu(dev_alloc((void**)&x, sizeof(double) * n, dev, st));
   if (rc == BILU_OK) {
     cu(cudaMemcpyAsync(row, h_row, sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, st));
     cu(cudaMemcpyAsync(col, h_col, sizeof(int) * nnzb, cudaMemcpyHostToDevice, st));
@@ -826,8 +869,7 @@ extern "C" int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const
   }
   if (rc == BILU_OK) rc = bilu_ctx_create(&c, stream);
   if (rc == BILU_OK)
-    rc = bilu_ctx_setup(c, nb, nnzb, bs, row, col, val,
-                        prec == BILU_FP32 ? (1 << BILU_FP32) : 0, h_times);
+    rc = bilu_ctx_setup(c, nb, nnzb, bs, row, col, val, prec > 0 ? (1 << prec) : 0, h_times);
   int src = BILU_OK;
   if (rc == BILU_OK) {
     src = bilu_ctx_solve(c, prec, b, x, restart, tol, maxit, h_iters, h_relres, nullptr);
@@ -838,11 +880,8 @@ extern "C" int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const
     cu(cudaStreamSynchronize(st));
   }
   bilu_ctx_destroy(c);
-  cudaFreeAsync(row, st);
-  cudaFreeAsync(col, st);
-  cudaFreeAsync(val, st);
-  cudaFreeAsync(b, st);
-  cudaFreeAsync(x, st);
+  for (void* p : {(void*)row, (void*)col, (void*)val, (void*)b, (void*)x})
+    if (p) cudaFreeAsync(p, st);
   cudaStreamSynchronize(st);
   return rc != BILU_OK ? rc : src;
 }
