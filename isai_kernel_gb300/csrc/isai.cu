@@ -42,148 +42,105 @@ __device__ __forceinline__ int find_in_row(const int* __restrict__ col, int s, i
 }
 
 // ---------------------------------------------------------------- Dinv
-// Team of BS lanes per block row; lane i holds row i of the work matrix and
-// of the identity.  Gauss-Jordan without pivoting, eps 1e-14, retry once
-// with 1e-12 added to the diagonal (isai_bsr.h:61-88, :114-120).
+// Inverse of each masked diagonal block (the unit lower triangle of the
+// packed factor, or its upper triangle) by the reference's Gauss-Jordan
+// without pivoting: eps 1e-14 on the pivots, one retry with 1e-12 added to
+// the diagonal (isai_bsr.h:61-88, :114-120).  On a triangular block most
+// Gauss-Jordan operations are exact no-ops (products with structural zeros,
+// scalings by a unit pivot).  A thread per block performs only the others,
+// each element receiving them in the Gauss-Jordan order:
+//   lower: every pivot is 1 and the multiplier of row i at step k stays
+//     L[i][k], so X[i][j] = 0 - L[i][j] X[j][j] - ... - L[i][i-1] X[i-1][j]
+//     (k ascending; X[k][j] is final by step k);
+//   upper: row k is untouched until step k, where it is scaled by
+//     r_k = 1 / u_kk into S[k][j] = u_kj r_k; row i's scaled entries
+//     m_j = u_ij r_i take m_j -= m_k S[k][j] for k = i+1, i+2, ..., and
+//     X[i][k] = -(m_k r_k), X[i][i] = r_i.  The pivots it tests are the
+//     u_kk themselves.
 template <int BS>
-__device__ __forceinline__ bool gauss_jordan(double* M, double* Iv, int i, int base,
-                                            unsigned mask) {
-  bool ok = true;
-#pragma unroll
-  for (int k = 0; k < BS; ++k) {
-    double piv = __shfl_sync(mask, M[k], base + k);
-    ok = ok && fabs(piv) >= 1e-14;
-    double invp = 1.0 / piv;
-    if (i == k) {
-#pragma unroll
-      for (int j = 0; j < BS; ++j) { M[j] *= invp; Iv[j] *= invp; }
-    }
-    double f = M[k];
-#pragma unroll
-    for (int j = 0; j < BS; ++j) {
-      double rm = __shfl_sync(mask, M[j], base + k);
-      double ri = __shfl_sync(mask, Iv[j], base + k);
-      if (i != k) {
-        M[j] -= f * rm;
-        Iv[j] -= f * ri;
-      }
-    }
-  }
-  return ok;
-}
-
-template <int BS>
-__global__ void __launch_bounds__(256) k_dinv(int nb, const int* __restrict__ row,
-                                              const int* __restrict__ col,
-                                              const double* __restrict__ val, int lower,
-                                              double* __restrict__ Dinv, int* fail) {
-  constexpr int G = 32 / BS;
-  int lane = threadIdx.x & 31;
-  int g = lane / BS, i = lane - g * BS;
-  long long kk = ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G + g;
-  bool active = g < G && kk < nb;
-  int k = active ? (int)kk : 0;
-  int base = g < G ? g * BS : 0;
-  double B[BS], M[BS], Iv[BS];
-  int pos = nb > 0 ? find_in_row(col, __ldg(row + k), __ldg(row + k + 1), k) : -1;
+__device__ __forceinline__ void dinv_lower(const double (&T)[BS][BS], double* __restrict__ out) {
+  // fixed trip counts with guards (triangular bounds are not always unrolled)
 #pragma unroll
   for (int j = 0; j < BS; ++j) {
-    double v = pos >= 0 ? val[((long long)pos * BS + i) * BS + j] : 0.0;
-    if (lower ? (j > i) : (j < i)) v = 0.0;
-    if (lower && j == i) v = 1.0;
-    B[j] = v;
-    M[j] = v;
-    Iv[j] = (j == i) ? 1.0 : 0.0;
-  }
-  unsigned mask = 0xffffffffu;
-  bool ok = gauss_jordan<BS>(M, Iv, i, base, mask);
-  if (__any_sync(mask, active && !ok)) {
-    bool redo = !ok;
-    double M2[BS], I2[BS];
-#pragma unroll
-    for (int j = 0; j < BS; ++j) {
-      M2[j] = B[j] + ((j == i) ? 1e-12 : 0.0);
-      I2[j] = (j == i) ? 1.0 : 0.0;
-    }
-    bool ok2 = gauss_jordan<BS>(M2, I2, i, base, mask);
-    if (redo) {
-#pragma unroll
-      for (int j = 0; j < BS; ++j) Iv[j] = I2[j];
-      if (active && !ok2) atomicMin(fail, k);
-    }
-  }
-  if (!active) return;
-#pragma unroll
-  for (int j = 0; j < BS; ++j) Dinv[((long long)k * BS + i) * BS + j] = Iv[j];
-}
-
-// Thread per block row (bs 4 and 5: the 2*bs*bs work values fit in
-// registers): the same Gauss-Jordan steps as the team version above, in the
-// same order, without the redundant per-lane divisions and shuffles.
-template <int BS>
-__device__ __forceinline__ bool gauss_jordan_t(double (&M)[BS][BS], double (&Iv)[BS][BS]) {
-  bool ok = true;
-#pragma unroll
-  for (int k = 0; k < BS; ++k) {
-    double piv = M[k][k];
-    ok = ok && fabs(piv) >= 1e-14;
-    double invp = 1.0 / piv;
-#pragma unroll
-    for (int j = 0; j < BS; ++j) {
-      M[k][j] *= invp;
-      Iv[k][j] *= invp;
-    }
+    double x[BS];
 #pragma unroll
     for (int i = 0; i < BS; ++i) {
-      if (i == k) continue;
-      double f = M[i][k];
+      double s = i == j ? 1.0 : 0.0;
 #pragma unroll
-      for (int j = 0; j < BS; ++j) {
-        M[i][j] -= f * M[k][j];
-        Iv[i][j] -= f * Iv[k][j];
-      }
+      for (int k = 0; k < BS; ++k)
+        if (k >= j && k < i) s -= T[i][k] * x[k];
+      x[i] = s;
     }
+#pragma unroll
+    for (int i = 0; i < BS; ++i) out[i * BS + j] = x[i];
   }
+}
+
+template <int BS>
+__device__ __forceinline__ bool dinv_pivots_ok(const double (&T)[BS][BS], double shift) {
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < BS; ++k) ok = ok && fabs(T[k][k] + shift) >= 1e-14;
   return ok;
 }
 
 template <int BS>
-__global__ void __launch_bounds__(128) k_dinv_t(int nb, const int* __restrict__ row,
-                                                const int* __restrict__ col,
-                                                const double* __restrict__ val, int lower,
-                                                double* __restrict__ Dinv, int* fail) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void dinv_upper(const double (&T)[BS][BS], double shift,
+                                           double* __restrict__ out) {
+  double r[BS], S[BS][BS];
+#pragma unroll
+  for (int k = 0; k < BS; ++k) {
+    r[k] = 1.0 / (T[k][k] + shift);
+#pragma unroll
+    for (int j = k + 1; j < BS; ++j) S[k][j] = T[k][j] * r[k];
+  }
+#pragma unroll
+  for (int i = 0; i < BS; ++i) {
+    double m[BS];
+#pragma unroll
+    for (int j = i + 1; j < BS; ++j) m[j] = S[i][j];
+#pragma unroll
+    for (int j = 0; j < i; ++j) out[i * BS + j] = 0.0;
+    out[i * BS + i] = r[i];
+#pragma unroll
+    for (int k = i + 1; k < BS; ++k) {
+      const double f = m[k];
+      out[i * BS + k] = -(f * r[k]);
+#pragma unroll
+      for (int j = k + 1; j < BS; ++j) m[j] -= f * S[k][j];
+    }
+  }
+}
+
+template <int BS, bool LOWER>
+__global__ void __launch_bounds__(128) k_dinv_tri(int nb, const int* __restrict__ row,
+                                                  const int* __restrict__ col,
+                                                  const double* __restrict__ val,
+                                                  double* __restrict__ Dinv, int* fail) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nb) return;
-  int pos = find_in_row(col, __ldg(row + k), __ldg(row + k + 1), k);
-  double B[BS][BS], M[BS][BS], Iv[BS][BS];
+  const int pos = find_in_row(col, __ldg(row + k), __ldg(row + k + 1), k);
+  double T[BS][BS];
 #pragma unroll
   for (int i = 0; i < BS; ++i)
 #pragma unroll
     for (int j = 0; j < BS; ++j) {
-      double v = pos >= 0 ? __ldg(val + ((long long)pos * BS + i) * BS + j) : 0.0;
-      if (lower ? (j > i) : (j < i)) v = 0.0;
-      if (lower && j == i) v = 1.0;
-      B[i][j] = v;
-      M[i][j] = v;
-      Iv[i][j] = (j == i) ? 1.0 : 0.0;
+      const bool stored = LOWER ? j < i : j >= i;
+      T[i][j] = stored ? (pos >= 0 ? __ldg(val + ((long long)pos * BS + i) * BS + j) : 0.0)
+                       : (LOWER && i == j ? 1.0 : 0.0);
     }
-  if (!gauss_jordan_t<BS>(M, Iv)) {
-#pragma unroll
-    for (int i = 0; i < BS; ++i)
-#pragma unroll
-      for (int j = 0; j < BS; ++j) {
-        M[i][j] = B[i][j] + ((j == i) ? 1e-12 : 0.0);
-        Iv[i][j] = (j == i) ? 1.0 : 0.0;
-      }
-    if (!gauss_jordan_t<BS>(M, Iv)) atomicMin(fail, k);
-  }
   double* out = Dinv + (long long)k * BS * BS;
-#pragma unroll
-  for (int i = 0; i < BS; ++i)
-#pragma unroll
-    for (int j = 0; j < BS; ++j) out[i * BS + j] = Iv[i][j];
+  if (LOWER) {
+    dinv_lower<BS>(T, out);  // unit pivots: never retried
+    return;
+  }
+  double shift = 0.0;
+  if (!dinv_pivots_ok<BS>(T, 0.0)) {
+    shift = 1e-12;
+    if (!dinv_pivots_ok<BS>(T, shift)) atomicMin(fail, k);
+  }
+  dinv_upper<BS>(T, shift, out);
 }
-
 // ---------------------------------------------------------------- pairs
 // Warp per ISAI column j; lane per entry idx.  lower: pairs p < idx with
 // A(t, S_j[p]) stored, ascending p (the reference's merge order); upper:
@@ -311,12 +268,20 @@ __global__ void __launch_bounds__(256) k_isai(int nb, const double* __restrict__
     double y[EPL];
     if (on) {
       const double* Di = Dinv + (long long)t * BS2;
+      // an entry without pairs has rhs = delta_{t,j} I: Dinv[t] I is Dinv[t]
+      // exactly (every other product is a zero), so it is copied
+      const bool copy = qb == qe;
 #pragma unroll
       for (int q = 0; q < EPL; ++q) {
         double s = 0.0;
         if (tl * EPL + q < BS2) {
+          if (copy) {
+            s = t == j ? __ldg(Di + er[q] * BS + ec[q]) : 0.0;
+          } else {
 #pragma unroll
-          for (int k = 0; k < BS; ++k) s = fma(__ldg(Di + er[q] * BS + k), sR[k * BS + ec[q]], s);
+            for (int k = 0; k < BS; ++k)
+              s = fma(__ldg(Di + er[q] * BS + k), sR[k * BS + ec[q]], s);
+          }
         }
         y[q] = s;
       }
@@ -336,13 +301,10 @@ template <int BS>
 int launch_dinv(int nb, const int* row, const int* col, const double* val, int lower,
                 double* Dinv, int* d_fail, cudaStream_t st) {
   if (nb == 0) return BILU_OK;
-  if constexpr (BS <= 5) {
-    k_dinv_t<BS><<<ceil_div(nb, 128), 128, 0, st>>>(nb, row, col, val, lower, Dinv, d_fail);
-  } else {
-    constexpr int G = 32 / BS;
-    long long warps = (nb + G - 1) / G;
-    k_dinv<BS><<<ceil_div(warps, 8), 256, 0, st>>>(nb, row, col, val, lower, Dinv, d_fail);
-  }
+  if (lower)
+    k_dinv_tri<BS, true><<<ceil_div(nb, 128), 128, 0, st>>>(nb, row, col, val, Dinv, d_fail);
+  else
+    k_dinv_tri<BS, false><<<ceil_div(nb, 128), 128, 0, st>>>(nb, row, col, val, Dinv, d_fail);
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }

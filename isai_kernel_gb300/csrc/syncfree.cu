@@ -1076,6 +1076,45 @@ __device__ __forceinline__ double bilu0_diag_lu(double (&dc)[BS], int c, unsigne
   return rp;
 }
 
+// The same LU by a whole warp: lane (c, j) holds rows j + m PL of column c
+// (PL lanes per column, so BS 8 keeps two rows a lane instead of eight on
+// a lane per column).  Step k broadcasts the reciprocal pivot from the lane
+// holding u_kk and row k of each column from the lane holding it; slots
+// whose rows are all <= k are skipped at compile time.  Every element
+// receives the operations of bilu0_diag_lu in the same order.  On the lane
+// (c, c % PL): rp = 1 / u_cc and piv = u_cc.  Lanes outside the block take
+// part in the shuffles only.
+template <int BS, int PL>
+__device__ __forceinline__ void bilu0_diag_lu_warp(double (&d)[(BS + PL - 1) / PL], int c, int j,
+                                                   double& rp, double& piv) {
+  constexpr int PC = (BS + PL - 1) / PL;
+  rp = 0.0;
+#pragma unroll
+  for (int k = 0; k < BS; ++k) {
+    const int mk = k / PL, jk = k - mk * PL;
+    // only the pivot's lane divides a block entry (a zero elsewhere would
+    // send its lane down the division's slow path)
+    const bool at_pivot = c == k && j == jk;
+    const double rk = __shfl_sync(FULL, 1.0 / (at_pivot ? d[mk] : 1.0), k * PL + jk);
+    if (at_pivot) rp = rk;
+    const double dkc = __shfl_sync(FULL, d[mk], (c * PL + jk) & 31);  // d[k][c]
+#pragma unroll
+    for (int m = 0; m < PC; ++m) {
+      if (m * PL + PL - 1 <= k) continue;  // every row of slot m is final
+      const int q = j + m * PL;
+      const double l = __shfl_sync(FULL, d[m] * rk, k * PL + j);  // l_qk from column k
+      if (q > k && q < BS) {
+        if (c == k) d[m] = l;
+        else if (c > k && c < BS) d[m] -= l * dkc;
+      }
+    }
+  }
+  piv = d[0];
+#pragma unroll
+  for (int m = 1; m < PC; ++m)
+    if (m == c / PL) piv = d[m];
+}
+
 // Structure of a block row and of its first dependency (pattern only: read
 // ahead of the values, before the level's barrier).
 struct BRowPre {
@@ -1234,9 +1273,13 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
   constexpr int TPW = 32 / TL;         // blocks updated per pass in phase 2
   constexpr int SPAN = 32 / TPW;
   constexpr int GU = 32 / BS;          // U blocks per pass (lane = column)
+  constexpr int PL = 32 / BS < BS ? 32 / BS : BS;  // phase 1: lanes per row
+  constexpr int PC = (BS + PL - 1) / PL;           // phase 1: columns per lane
   int lane = threadIdx.x & 31;
   int team = lane / SPAN, tl = lane - team * SPAN;
   bool team_on = team < TPW && tl < TL;
+  const int pr = lane / PL, pj = lane - pr * PL;
+  const bool p_on = pr < BS;
   int rs = __ldg(row + I), re = __ldg(row + I + 1), dI = __ldg(diag + I);
   // a hub row searches its own column list once per K: keep it in shared
   // memory (one L2 round trip per search step otherwise)
@@ -1261,19 +1304,43 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
     double* L = val + (long long)pk * BS2;
     const double* Ukk = val + (long long)dK * BS2;
     const double* rK = ss.rdiag + (long long)K * BS;  // 1 / pivots of U_KK
-    // phase 1: lane r owns row r of A_IK
-    if (lane < BS) {
-      double a[BS];
+    // phase 1: row pr of L_IK = A_IK U_KK^-1 on the PL lanes of row pr,
+    // lane (pr, pj) holding columns pj + m PL.  Step k scales column k by
+    // the reciprocal pivot, broadcasts it along the row and updates the
+    // columns right of it; slots whose columns are all <= k are skipped
+    // at compile time.  Per element the same operations in the same order
+    // as a lane per row, with a quarter of the FP64 instructions at BS 8.
+    {
+      // every operand is loaded up front, unpredicated (clamped columns):
+      // loads under the lane predicates of the steps would wait one L2
+      // round trip per step
+      double a[PC], rkv[PC], u[BS][PC];
 #pragma unroll
-      for (int c = 0; c < BS; ++c) a[c] = L[lane * BS + c];
+      for (int m = 0; m < PC; ++m) {
+        const int c = pj + m * PL, cc = c < BS ? c : BS - 1;
+        a[m] = (p_on && c < BS) ? L[pr * BS + c] : 0.0;
+        rkv[m] = __ldcg(rK + cc);
 #pragma unroll
-      for (int k = 0; k < BS; ++k) {
-        a[k] = a[k] * __ldcg(rK + k);
-#pragma unroll
-        for (int c = k + 1; c < BS; ++c) a[c] -= a[k] * __ldcg(Ukk + k * BS + c);
+        for (int k = 0; k < BS; ++k)
+          u[k][m] = m * PL + PL - 1 <= k ? 0.0 : __ldcg(Ukk + k * BS + cc);
       }
 #pragma unroll
-      for (int c = 0; c < BS; ++c) L[lane * BS + c] = a[c];
+      for (int k = 0; k < BS; ++k) {
+        const int mk = k / PL, jk = k - mk * PL;
+        if (pj == jk) a[mk] = a[mk] * rkv[mk];
+        const double ak = __shfl_sync(FULL, a[mk], (pr * PL + jk) & 31);
+#pragma unroll
+        for (int m = 0; m < PC; ++m) {
+          if (m * PL + PL - 1 <= k) continue;  // every column of slot m is final
+          const int c = pj + m * PL;
+          if (c > k && c < BS) a[m] -= ak * u[k][m];
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < PC; ++m) {
+        const int c = pj + m * PL;
+        if (p_on && c < BS) L[pr * BS + c] = a[m];
+      }
     }
     __syncwarp();
     // phase 2: A_IJ -= L_IK U_KJ for J > K in rows I and K.  The shorter
@@ -1328,28 +1395,28 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
     }
     __syncwarp();
   }
-  // diagonal block: lane c owns column c
+  // diagonal block: lane (c, j) = (lane / PL, lane % PL) holds rows
+  // j + m PL of column c
   double* D = val + (long long)dI * BS2;
-  double dc[BS];
-  if (lane < BS) {
+  {
+    const int c = pr, j = pj;
+    double d[PC];
 #pragma unroll
-    for (int r = 0; r < BS; ++r) dc[r] = D[r * BS + lane];
-  } else {
+    for (int m = 0; m < PC; ++m) {
+      const int q = j + m * PL;
+      d[m] = (c < BS && q < BS) ? D[q * BS + c] : 1.0;
+    }
+    double rp, piv;
+    bilu0_diag_lu_warp<BS, PL>(d, c, j, rp, piv);
 #pragma unroll
-    for (int r = 0; r < BS; ++r) dc[r] = 1.0;
-  }
-  // lanes >= BS take part as columns right of the block (their updates are
-  // discarded)
-  const double rp = bilu0_diag_lu<BS>(dc, lane, FULL, 0);
-  if (lane < BS) {
-    double piv = dc[0];  // this lane's diagonal element of U_II
-#pragma unroll
-    for (int q = 1; q < BS; ++q)
-      if (q == lane) piv = dc[q];
-    if (piv == 0.0) atomicMin(ss.zp, I);
-#pragma unroll
-    for (int r = 0; r < BS; ++r) D[r * BS + lane] = dc[r];
-    ss.rdiag[(long long)I * BS + lane] = rp;
+    for (int m = 0; m < PC; ++m) {
+      const int q = j + m * PL;
+      if (c < BS && q < BS) D[q * BS + c] = d[m];
+    }
+    if (c < BS && j == c % PL) {
+      if (piv == 0.0) atomicMin(ss.zp, I);
+      ss.rdiag[(long long)I * BS + c] = rp;
+    }
   }
   __syncwarp();
   // U blocks right of the diagonal: U_IJ = L_II^-1 A_IJ, lane per column
