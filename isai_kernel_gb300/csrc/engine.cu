@@ -36,6 +36,7 @@ size_t syncfree_ws(int nb);
 int diag_positions(int nb, const int* row, const int* col, int* diag, int* h_bad, Carver& ws,
                    cudaStream_t st);
 size_t level_sched_ws(int nb, long long nnzb);
+size_t bilu0_ws(int nb, long long nnzb);
 size_t levels_ws(int nb, long long ndeps);
 size_t pattern_product_ws(int n);
 int pattern_product_rowptr(int n, const int* Xrow, const int* Xcol, const int* Arow,
@@ -350,7 +351,7 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   BILU_TRY_CUDA(cudaMemcpyAsync(c->Aval, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->LU, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
   // scratch shared by every step
-  size_t wsb = std::max({isai_pattern_ws(nb, nnzb), level_sched_ws(nb, nnzb), pairs_ws(nnzb + nb),
+  size_t wsb = std::max({isai_pattern_ws(nb, nnzb), bilu0_ws(nb, nnzb), pairs_ws(nnzb + nb),
                          levels_ws(nb, nnzb), pattern_product_ws(nb),
                          scan_ws_bytes(nnzb + nb + 1)}) + (1 << 16);
   void* wsp = nullptr;

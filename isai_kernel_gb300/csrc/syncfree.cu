@@ -43,6 +43,9 @@ struct SyncState {
   // reciprocal pivots 1 / u_rr of the block rows (nb x bs): written by the
   // factorisation, read by upper solves instead of dividing (null: divide)
   double* rdiag = nullptr;
+  // per lower position pk of the factor: how many blocks dependency K
+  // updates in row I (null: not counted, every dependency searches)
+  const int* nmatch = nullptr;
 };
 
 // Exponential back-off between polls (32 ns doubling to 256 ns): waiters that
@@ -1292,12 +1295,14 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
   // structural data of the next K, loaded one step ahead
   int Kn = rs < dI ? row_col(col, stage, rs, rs) : 0;
   int dKn = rs < dI ? __ldg(diag + Kn) : 0, ken = rs < dI ? __ldg(row + Kn + 1) : 0;
+  int nmn = rs < dI && ss.nmatch ? __ldg(ss.nmatch + rs) : 1;
   for (int pk = rs; pk < dI; ++pk) {
-    const int K = Kn, dK = dKn, ke = ken;
+    const int K = Kn, dK = dKn, ke = ken, nm = nmn;
     if (pk + 1 < dI) {
       Kn = row_col(col, stage, rs, pk + 1);
       dKn = __ldg(diag + Kn);
       ken = __ldg(row + Kn + 1);
+      if (ss.nmatch) nmn = __ldg(ss.nmatch + pk + 1);
     }
     // sync-free schedule: row K may still be in progress
     if (WAIT && !warp_wait(ss.flags + K, ss.err, ss.spin)) return false;
@@ -1348,8 +1353,9 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
     // lane binary-searching one of them in the other list (hub rows of
     // power-law matrices hold thousands of blocks); then the teams update
     // the matched blocks.  Every block is updated once per K, so the
-    // update order of each element is the same either way.
-    {
+    // update order of each element is the same either way.  A dependency
+    // counted as updating no block skips the searches.
+    if (nm != 0) {
       const bool from_i = (re - pk - 1) <= (ke - dK - 1);
       const int cs = from_i ? pk + 1 : dK + 1, ce = from_i ? re : ke;
       const int ss_ = from_i ? dK + 1 : pk + 1, se = from_i ? ke : re;
@@ -1582,12 +1588,94 @@ int launch_sptrsv(int nb, const int* row, const int* col, const int* diag, const
   return BILU_OK;
 }
 
+// For every lower position pk = (I, K) of the pattern: the number of blocks
+// J > K present in both rows, i.e. the blocks dependency K updates in row I
+// (0 at the other positions).  Structure only and free of dependencies; the
+// same shorter-list searches as the factorisation.  On graphs with few
+// triangles most counts are 0, and the sync-free factorisation then skips
+// those searches inside its dependency chains.
+//
+// Pass 1: a thread per position (its block row found by binary search over
+// the row pointers, so that the thousand dependencies of a hub row spread
+// over many warps), counting lists of up to kMatchSerial candidates; a
+// longer list (two hub rows) is marked -1.  Pass 2: a warp per 32
+// positions takes the marked ones, 32 candidates at a time.
+constexpr int kMatchSerial = 32;
+
+struct MatchLists {
+  int cs, ce, s, e;  // candidates [cs, ce) searched for in positions [s, e)
+};
+
+__device__ __forceinline__ MatchLists match_lists(long long pk, int nb,
+                                                  const int* __restrict__ row,
+                                                  const int* __restrict__ col,
+                                                  const int* __restrict__ diag, int& I) {
+  int lo = 0, hi = nb - 1;  // last block row starting at or before pk
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(row + mid) <= pk) lo = mid; else hi = mid - 1;
+  }
+  I = lo;
+  MatchLists m{0, 0, 0, 0};
+  if (pk >= __ldg(diag + I)) return m;  // diagonal or upper position
+  const int re = __ldg(row + I + 1);
+  const int K = __ldg(col + pk), dK = __ldg(diag + K), ke = __ldg(row + K + 1);
+  const bool from_i = (re - pk - 1) <= (ke - dK - 1);
+  m.cs = from_i ? (int)pk + 1 : dK + 1;
+  m.ce = from_i ? re : ke;
+  m.s = from_i ? dK + 1 : (int)pk + 1;
+  m.e = from_i ? ke : re;
+  return m;
+}
+
+__global__ void __launch_bounds__(256) k_bilu0_nmatch(int nb, long long nnzb,
+                                                      const int* __restrict__ row,
+                                                      const int* __restrict__ col,
+                                                      const int* __restrict__ diag,
+                                                      int* __restrict__ nmatch) {
+  const long long pk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pk >= nnzb) return;
+  int I;
+  const MatchLists m = match_lists(pk, nb, row, col, diag, I);
+  if (m.ce - m.cs > kMatchSerial) {
+    nmatch[pk] = -1;
+    return;
+  }
+  int n = 0;
+  for (int c = m.cs; c < m.ce; ++c) n += find_in_row(col, m.s, m.e, __ldg(col + c)) >= 0;
+  nmatch[pk] = n;
+}
+
+__global__ void __launch_bounds__(256) k_bilu0_nmatch_long(int nb, long long nnzb,
+                                                           const int* __restrict__ row,
+                                                           const int* __restrict__ col,
+                                                           const int* __restrict__ diag,
+                                                           int* __restrict__ nmatch) {
+  const long long p0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll;
+  const int lane = threadIdx.x & 31;
+  if (p0 >= nnzb) return;
+  unsigned todo = __ballot_sync(FULL, p0 + lane < nnzb && nmatch[p0 + lane] < 0);
+  while (todo) {
+    const long long pk = p0 + __ffs(todo) - 1;
+    todo &= todo - 1;
+    int I;
+    const MatchLists m = match_lists(pk, nb, row, col, diag, I);
+    int n = 0;
+    for (int c0 = m.cs; c0 < m.ce; c0 += 32) {
+      const int c = c0 + lane;
+      const bool hit = c < m.ce && find_in_row(col, m.s, m.e, __ldg(col + c)) >= 0;
+      n += __popc(__ballot_sync(FULL, hit));
+    }
+    if (lane == 0) nmatch[pk] = n;
+  }
+}
+
 // Sync-free BILU(0) (matrices with narrow levels or long rows): block rows
 // taken by atomic tickets in level order, a warp per row, bounded waits on
 // the rows it reads, the row's flag released when it is final.  Hub rows of
 // a power-law matrix then no longer hold up a whole level.
 template <int BS>
-__global__ void __launch_bounds__(kLvlThreads, 2) k_bilu0_syncfree(
+__global__ void __launch_bounds__(kLvlThreads, 3) k_bilu0_syncfree(
     int nb, const int* __restrict__ row, const int* __restrict__ col,
     const int* __restrict__ diag, double* val, SyncState ss) {
   extern __shared__ int stage_smem[];
@@ -1869,6 +1957,12 @@ size_t level_sched_ws(int nb, long long nnzb) {
          carve_size(sizeof(int) * 4) + carve_size(sizeof(unsigned) * 4);
 }
 
+// BILU(0) scratch: the level-scheduled one plus the sync-free schedule's
+// per-position match counts.
+size_t bilu0_ws(int nb, long long nnzb) {
+  return level_sched_ws(nb, nnzb) + carve_size(sizeof(int) * (size_t)std::max(nnzb, 1ll));
+}
+
 // diagonal positions (validates the pattern); returns BILU_ERR_PATTERN with
 // the first bad row in *h_bad
 int diag_positions(int nb, const int* row, const int* col, int* diag, int* h_bad, Carver& ws,
@@ -1928,12 +2022,21 @@ int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, c
   if (schedule == 0 || schedule == 1) sched = schedule;  // caller's choice
   if (sched == 1) {
     // narrow levels or long rows: sync-free, tickets in level order
+    int* nmatch = ws.take<int>((size_t)std::max(nnzb, 1ll));
+    if (!nmatch) return BILU_ERR_WORKSPACE;
     SyncState ss;
     BILU_TRY(sync_init(ss, nb, ws, st));
     ss.order = order;
     ss.rdiag = rdiag;
-    if (nb > 0)
+    ss.nmatch = nmatch;
+    if (nb > 0) {
+      const unsigned grid = ceil_div(std::max(nnzb, 1ll), 256);
+      k_bilu0_nmatch<<<grid, 256, 0, st>>>(nb, nnzb, row, col, diag, nmatch);
+      BILU_LAUNCH_CHECK();
+      k_bilu0_nmatch_long<<<grid, 256, 0, st>>>(nb, nnzb, row, col, diag, nmatch);
+      BILU_LAUNCH_CHECK();
       BILU_TRY(BILU_DISPATCH_BS(bs, launch_bilu0_syncfree, nb, row, col, diag, val, ss, st));
+    }
     return sync_finish(ss, h_zp, st);
   }
   SyncState ss;
@@ -2196,7 +2299,7 @@ extern "C" size_t bilu_bsrilu0_ws_bytes(int nb, int nnzb) {
   if (nb < 0 || nnzb < 0) return 0;
   // diag, bad-row word, reciprocal pivots (largest block size), level scratch
   return carve_size(sizeof(int) * ((size_t)nb + 1)) + carve_size(sizeof(int) * 2) +
-         carve_size(sizeof(double) * ((size_t)nb * 8 + 1)) + level_sched_ws(nb, nnzb);
+         carve_size(sizeof(double) * ((size_t)nb * 8 + 1)) + bilu0_ws(nb, nnzb);
 }
 
 extern "C" int bilu_bsrilu0(int nb, int nnzb, int bs, const int* d_row, const int* d_col,
