@@ -154,25 +154,53 @@ void launch_multiaxpy(long long n, const double* V, long long ldv, const double*
 // One modified Gram-Schmidt step fused with the next one's dot product:
 // w -= h_prev * v_prev (h_prev read from device memory), then the partial of
 // v_next . w (or w . w).  The basis vectors stream through with evict-first
-// loads; w (one vector, 67 MB at 128^3) is left to the L2.  The CTA that
-// finishes last sums the CTA partials in index order, so the result does not
-// depend on which CTA that is.
-__global__ void __launch_bounds__(kRedThreads) k_mgs_sweep(
+// loads; w (one vector, 67 MB at 128^3) stays in the L2 (a sweep reads
+// only the two basis vectors from DRAM), which leaves the two DFMAs per
+// element as the bound.  Elements go in pairs through 16-byte accesses (the
+// basis stride is a multiple of 32 elements and every vector starts on a
+// 256-byte boundary) into two independent accumulators, so that a thread
+// has two FMA chains in flight.  The CTA that finishes last sums the CTA
+// partials in index order, so the result does not depend on which CTA
+// that is.
+__global__ void __launch_bounds__(kRedThreads, kSweepCTAs / 152) k_mgs_sweep(
     long long n, const double* __restrict__ vp, const double* __restrict__ hp,
     const double* __restrict__ vn, double* __restrict__ w, double* __restrict__ partial,
     unsigned* counter, double* out) {
-  double h = vp ? -__ldg(hp) : 0.0;
-  double acc = 0.0;
-  long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
-    double we = w[e];
+  // launched as a programmatic dependent of the previous sweep: let the
+  // next sweep's CTAs be scheduled during this one's reduction tail, and
+  // wait here until the previous grid has finished and its writes (w, h,
+  // the counter reset) are visible
+  asm volatile("griddepcontrol.launch_dependents;");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const double h = vp ? -__ldcg(hp) : 0.0;
+  double acc0 = 0.0, acc1 = 0.0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double2* w2 = reinterpret_cast<double2*>(w);
+  const double2* vp2 = reinterpret_cast<const double2*>(vp);
+  const double2* vn2 = reinterpret_cast<const double2*>(vn);
+  for (long long e = tid; e < (n >> 1); e += stride) {
+    double2 we = __ldcg(w2 + e);  // L2: w was written by the previous sweep
     if (vp) {
-      we = fma(h, __ldcs(vp + e), we);
-      w[e] = we;
+      const double2 p = __ldcs(vp2 + e);
+      we.x = fma(h, p.x, we.x);
+      we.y = fma(h, p.y, we.y);
+      w2[e] = we;
     }
-    double o = vn ? __ldcs(vn + e) : we;
-    acc = fma(o, we, acc);
+    const double2 o = vn ? __ldcs(vn2 + e) : we;
+    acc0 = fma(o.x, we.x, acc0);
+    acc1 = fma(o.y, we.y, acc1);
   }
+  if ((n & 1) && tid == 0) {  // odd length: the last element
+    double we = __ldcg(w + n - 1);
+    if (vp) {
+      we = fma(h, __ldcs(vp + n - 1), we);
+      w[n - 1] = we;
+    }
+    const double o = vn ? __ldcs(vn + n - 1) : we;
+    acc0 = fma(o, we, acc0);
+  }
+  double acc = acc0 + acc1;
   __shared__ double red[kRedThreads / 32];
   __shared__ bool last;
   int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -239,8 +267,16 @@ int scale_rsqrt(long long n, const double* x, const double* nrm2, double* y, cud
 
 int mgs_sweep(long long n, const double* vp, const double* hp, const double* vn, double* w,
               double* partial, unsigned* counter, double* out, cudaStream_t st) {
-  k_mgs_sweep<<<kSweepCTAs, kRedThreads, 0, st>>>(n, vp, hp, vn, w, partial, counter, out);
-  BILU_LAUNCH_CHECK();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kSweepCTAs);
+  cfg.blockDim = dim3(kRedThreads);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  BILU_TRY_CUDA(cudaLaunchKernelEx(&cfg, k_mgs_sweep, n, vp, hp, vn, w, partial, counter, out));
   return BILU_OK;
 }
 

@@ -9,7 +9,7 @@ constexpr int kRedCTAs = 152 * 4;  // partial-sum slots (fixed => deterministic)
 constexpr int kRedThreads = 256;
 constexpr int kMaxVec = 32;        // vectors per multi-dot / multi-axpy call
 constexpr int kPartStride = kMaxVec + 2;
-constexpr int kSweepCTAs = 152 * 8;  // CTAs of one MGS sweep (one partial each)
+constexpr int kSweepCTAs = 152 * 6;  // CTAs of one MGS sweep (one partial each, one wave)
 
 // partial[cta * kPartStride + i] = sum_e V[i][e] * w[e] (i < nv), and at
 // index nv: sum_e w[e]^2 when with_ww.  Skipped (partials left as they
