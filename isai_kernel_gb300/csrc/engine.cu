@@ -70,7 +70,7 @@ int pairs_ptr_impl(int nb, const int* Arow, const int* Acol, const int* Mptr, co
                    int lower, int* PairPtr, int mnnz, int* h_total, int* h_nmax, Carver& ws,
                    cudaStream_t st);
 int pairs_fill_impl(int nb, const int* Arow, const int* Acol, const int* Mptr, const int* Mind,
-                    int lower, const int* PairPtr, int* PL, int* PS, cudaStream_t st);
+                    int lower, const int* PairPtr, int mnnz, int* PL, int* PS, cudaStream_t st);
 int isai_impl(int nb, int bs, const double* Aval, const int* Mptr, const int* Mind, int lower,
               const int* pp, const int* pl, const int* ps, const double* Dinv, double* Mval,
               cudaStream_t st);
@@ -304,7 +304,7 @@ int build_isai_side(bilu_ctx* c, int lower, Carver& ws, int** orow, int** ocol, 
   }
   BILU_TRY(c->alloc(&pl, total));
   BILU_TRY(c->alloc(&ps, total));
-  BILU_TRY(pairs_fill_impl(nb, c->Arow, c->Acol, Mptr, Mind, lower, pp, pl, ps, st));
+  BILU_TRY(pairs_fill_impl(nb, c->Arow, c->Acol, Mptr, Mind, lower, pp, mnnz, pl, ps, st));
   double *Dinv, *Mcsc, *Mcsr;
   BILU_TRY(c->alloc(&Dinv, (size_t)nb * bs2));
   BILU_TRY(c->alloc(&Mcsc, (size_t)mnnz * bs2));

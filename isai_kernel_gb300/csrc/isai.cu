@@ -142,46 +142,52 @@ __global__ void __launch_bounds__(128) k_dinv_tri(int nb, const int* __restrict_
   dinv_upper<BS>(T, shift, out);
 }
 // ---------------------------------------------------------------- pairs
-// Warp per ISAI column j; lane per entry idx.  lower: pairs p < idx with
-// A(t, S_j[p]) stored, ascending p (the reference's merge order); upper:
-// pairs p > idx, descending p (the reference's ISAI-U loop order).
+// Thread per ISAI entry (t = S_j[idx] of column j, the column found by
+// binary search over the column pointers, so a column of a few entries does
+// not leave most of a warp idle).  lower: pairs p < idx with A(t, S_j[p])
+// stored, ascending p (the reference's merge order); upper: pairs p > idx,
+// descending p (the reference's ISAI-U loop order).
 template <bool FILL>
-__global__ void __launch_bounds__(256) k_pairs(int nb, const int* __restrict__ Arow,
+__global__ void __launch_bounds__(256) k_pairs(int nb, long long mnnz,
+                                               const int* __restrict__ Arow,
                                                const int* __restrict__ Acol,
                                                const int* __restrict__ Mptr,
                                                const int* __restrict__ Mind, int lower,
                                                int* __restrict__ cnt_or_ptr,
                                                int* __restrict__ PL, int* __restrict__ PS,
                                                int* nmax) {
-  int lane = threadIdx.x & 31;
-  int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (j >= nb) return;
-  int start = Mptr[j], end = Mptr[j + 1], N = end - start;
-  if (!FILL && lane == 0) atomicMax(nmax, N);
-  for (int idx = lane; idx < N; idx += 32) {
-    int t = Mind[start + idx];
-    int as = __ldg(Arow + t), ae = __ldg(Arow + t + 1);
-    int out = FILL ? cnt_or_ptr[start + idx] : 0;
-    int c = 0;
-    if (lower) {
-      for (int p = 0; p < idx; ++p) {
-        int pos = find_in_row(Acol, as, ae, Mind[start + p]);
-        if (pos >= 0) {
-          if (FILL) { PL[out + c] = p; PS[out + c] = pos; }
-          ++c;
-        }
-      }
-    } else {
-      for (int p = N - 1; p > idx; --p) {
-        int pos = find_in_row(Acol, as, ae, Mind[start + p]);
-        if (pos >= 0) {
-          if (FILL) { PL[out + c] = p; PS[out + c] = pos; }
-          ++c;
-        }
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= mnnz) return;
+  int lo = 0, hi = nb - 1;  // last column starting at or before q
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(Mptr + mid) <= q) lo = mid; else hi = mid - 1;
+  }
+  const int start = __ldg(Mptr + lo), N = __ldg(Mptr + lo + 1) - start;
+  const int idx = (int)(q - start);
+  if (!FILL && idx == 0) atomicMax(nmax, N);
+  const int t = __ldg(Mind + q);
+  const int as = __ldg(Arow + t), ae = __ldg(Arow + t + 1);
+  const int out = FILL ? cnt_or_ptr[q] : 0;
+  int c = 0;
+  if (lower) {
+    for (int p = 0; p < idx; ++p) {
+      const int pos = find_in_row(Acol, as, ae, __ldg(Mind + start + p));
+      if (pos >= 0) {
+        if (FILL) { PL[out + c] = p; PS[out + c] = pos; }
+        ++c;
       }
     }
-    if (!FILL) cnt_or_ptr[start + idx] = c;
+  } else {
+    for (int p = N - 1; p > idx; --p) {
+      const int pos = find_in_row(Acol, as, ae, __ldg(Mind + start + p));
+      if (pos >= 0) {
+        if (FILL) { PL[out + c] = p; PS[out + c] = pos; }
+        ++c;
+      }
+    }
   }
+  if (!FILL) cnt_or_ptr[q] = c;
 }
 
 // ---------------------------------------------------------------- ISAI solve
@@ -346,8 +352,8 @@ int pairs_ptr_impl(int nb, const int* Arow, const int* Acol, const int* Mptr, co
   if (!nmax) return BILU_ERR_WORKSPACE;
   BILU_TRY_CUDA(cudaMemsetAsync(nmax, 0, sizeof(int), st));
   if (nb > 0) {
-    k_pairs<false><<<ceil_div(nb, 8), 256, 0, st>>>(nb, Arow, Acol, Mptr, Mind, lower, PairPtr,
-                                                    nullptr, nullptr, nmax);
+    k_pairs<false><<<ceil_div(std::max(mnnz, 1), 256), 256, 0, st>>>(
+        nb, mnnz, Arow, Acol, Mptr, Mind, lower, PairPtr, nullptr, nullptr, nmax);
     BILU_LAUNCH_CHECK();
   }
   BILU_TRY(scan_exclusive(PairPtr, PairPtr, mnnz, h_total, ws, st));
@@ -359,10 +365,10 @@ int pairs_ptr_impl(int nb, const int* Arow, const int* Acol, const int* Mptr, co
 }
 
 int pairs_fill_impl(int nb, const int* Arow, const int* Acol, const int* Mptr, const int* Mind,
-                    int lower, const int* PairPtr, int* PL, int* PS, cudaStream_t st) {
-  if (nb == 0) return BILU_OK;
-  k_pairs<true><<<ceil_div(nb, 8), 256, 0, st>>>(nb, Arow, Acol, Mptr, Mind, lower,
-                                                 const_cast<int*>(PairPtr), PL, PS, nullptr);
+                    int lower, const int* PairPtr, int mnnz, int* PL, int* PS, cudaStream_t st) {
+  if (nb == 0 || mnnz == 0) return BILU_OK;
+  k_pairs<true><<<ceil_div(mnnz, 256), 256, 0, st>>>(nb, mnnz, Arow, Acol, Mptr, Mind, lower,
+                                                     const_cast<int*>(PairPtr), PL, PS, nullptr);
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }
@@ -407,8 +413,14 @@ extern "C" int bilu_pairs_fill(int nb, const int* d_Arow, const int* d_Acol, con
                                const int* d_Mind, int lower, const int* d_PairPtr,
                                int* d_PairPLocal, int* d_PairSrc, bilu_stream_t stream) {
   if (nb < 0) return BILU_ERR_ARG;
-  return pairs_fill_impl(nb, d_Arow, d_Acol, d_Mptr, d_Mind, lower != 0, d_PairPtr, d_PairPLocal,
-                         d_PairSrc, S(stream));
+  int mnnz = 0;
+  if (nb > 0) {
+    BILU_TRY_CUDA(cudaMemcpyAsync(&mnnz, d_Mptr + nb, sizeof(int), cudaMemcpyDeviceToHost,
+                                  S(stream)));
+    BILU_TRY_CUDA(cudaStreamSynchronize(S(stream)));
+  }
+  return pairs_fill_impl(nb, d_Arow, d_Acol, d_Mptr, d_Mind, lower != 0, d_PairPtr, mnnz,
+                         d_PairPLocal, d_PairSrc, S(stream));
 }
 
 extern "C" int bilu_isai_compute(int nb, int bs, const double* d_Aval, const int* d_Mptr,
