@@ -212,13 +212,18 @@ int bilu_isai_compute(int nb, int bs, const double* d_Aval, const int* d_Mptr, c
 /* Replaces bcsr_spmv (bcsc2bcsrAndSpMV.h:49) and bsr_SpMV_tensorcore
  * (bsr_tensor_SpMV.h:402): y = M x.  FP64 values and vectors.  Rows of more
  * than 64 blocks are summed by a whole CTA instead of one lane group; the
- * first call with a given d_row array (and mb) finds out whether there are
- * such rows with a synchronising reduction over d_row, later calls reuse
- * the answer (a stale answer after reusing d_row for another pattern only
- * costs speed).  The same holds for bilu_bcsr_spmv_f32 and
+ * first call with a given d_row array (and mb, bs) finds out whether there
+ * are such rows with a synchronising reduction over d_row, later calls
+ * reuse the answer (a stale answer after reusing d_row for another pattern
+ * only costs speed).  The same holds for bilu_bcsr_spmv_f32 and
  * bilu_isai_apply. */
 int bilu_bcsr_spmv(int mb, int bs, const int* d_row, const int* d_col, const double* d_val,
                    const double* d_x, double* d_y, bilu_stream_t stream);
+/* The SpMV layout word of a pattern, as cached by the entry points above:
+ * 1 when rows of more than 64 blocks are present (the kernel in which the
+ * CTA shares such rows), else 0.  Synchronises the stream on the first
+ * query of a pattern. */
+int bilu_spmv_layout(int mb, int bs, const int* d_row, bilu_stream_t stream, int* h_layout);
 /* FP32-stored values, FP32 accumulation; x and y each FP64 or FP32
  * (x_fp32 / y_fp32 flags). */
 int bilu_bcsr_spmv_f32(int mb, int bs, const int* d_row, const int* d_col, const float* d_val,
@@ -522,6 +527,11 @@ int bilu_debug_sptrsv_withhold_flow(int nb, int nnzb, int bs, const int* d_row, 
                                     const double* d_val, int lower, const double* d_b,
                                     double* d_x, int withhold_row, long long spin_limit,
                                     void* d_ws, size_t ws_bytes, bilu_stream_t stream);
+/* Sets the SpMV layout word (0 or 1, see bilu_spmv_layout) the entry points
+ * use for the pattern (d_row, mb, bs), replacing the one they found.  Both
+ * kernels give the product to within rounding for any pattern; this
+ * exercises the one the check would not pick for a given pattern. */
+int bilu_debug_spmv_layout_set(int mb, int bs, const int* d_row, int layout);
 
 #ifdef __cplusplus
 }

@@ -20,7 +20,7 @@ int sptrsv_level_impl(int nb, long long nnzb, int bs, const int* row, const int*
                       const int* diag, const double* val, int lower, int unit, const double* b,
                       double* x, Carver& ws, cudaStream_t st);
 int spmv_any(int mb, int bs, int prec, const int* row, const int* col, const void* val,
-             const void* x, int x32, void* y, int y32, cudaStream_t st, int long_rows);
+             const void* x, int x32, void* y, int y32, cudaStream_t st, int layout);
 
 namespace {
 

@@ -75,8 +75,9 @@ int isai_impl(int nb, int bs, const double* Aval, const int* Mptr, const int* Mi
               const int* pp, const int* pl, const int* ps, const double* Dinv, double* Mval,
               cudaStream_t st);
 int spmv_any(int mb, int bs, int prec, const int* row, const int* col, const void* val,
-             const void* x, int x32, void* y, int y32, cudaStream_t st, int long_rows);
-int spmv_long_rows_of(int mb, const int* row, int* d_word, cudaStream_t st, int* h_long);
+             const void* x, int x32, void* y, int y32, cudaStream_t st, int layout);
+int spmv_layout_of(int mb, int bs, const int* row, void* d_words, cudaStream_t st,
+                   int* h_layout);
 int isai_apply_impl(int nb, int bs, int prec, const int* Lrow, const int* Lcol, const void* Lval,
                     const int* Urow, const int* Ucol, const void* Uval, const double* b,
                     void* tmp, double* x, cudaStream_t st, int longL, int longU);
@@ -139,10 +140,10 @@ struct bilu_ctx {
   double *Aval = nullptr, *LU = nullptr;
   double* rdiag = nullptr;  // 1 / pivots of the factor's U_II (nb x bs), written by BILU(0)
   float *LU32 = nullptr, *rdiag32 = nullptr;  // FP32 copies for the mixed exact-ILU apply
-  // A, M_L, M_U: 1 if the pattern has rows of more than 64 blocks (their
-  // SpMVs then take the kernel in which the CTA shares such rows), from the
-  // setup
-  int long_rows[3] = {0, 0, 0};
+  // A, M_L, M_U: SpMV layout words from the setup (1 if the pattern has
+  // rows of more than 64 blocks: their SpMVs then take the kernel in which
+  // the CTA shares such rows)
+  int spmv_layout[3] = {0, 0, 0};
   int *Lrow = nullptr, *Lcol = nullptr, *Urow = nullptr, *Ucol = nullptr;
   double *Lval = nullptr, *Uval = nullptr;
   float *Lval32 = nullptr, *Uval32 = nullptr;
@@ -423,13 +424,13 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   }
   {
     Carver w2 = ws;
-    int* word = w2.take<int>(1);
-    if (!word) return BILU_ERR_WORKSPACE;
-    BILU_TRY(spmv_long_rows_of(nb, c->Arow, word, st, &c->long_rows[0]));
-    c->long_rows[1] = c->long_rows[2] = 0;
+    int* words = w2.take<int>(1);
+    if (!words) return BILU_ERR_WORKSPACE;
+    BILU_TRY(spmv_layout_of(nb, bs, c->Arow, words, st, &c->spmv_layout[0]));
+    c->spmv_layout[1] = c->spmv_layout[2] = 0;
     if (isai) {
-      BILU_TRY(spmv_long_rows_of(nb, c->Lrow, word, st, &c->long_rows[1]));
-      BILU_TRY(spmv_long_rows_of(nb, c->Urow, word, st, &c->long_rows[2]));
+      BILU_TRY(spmv_layout_of(nb, bs, c->Lrow, words, st, &c->spmv_layout[1]));
+      BILU_TRY(spmv_layout_of(nb, bs, c->Urow, words, st, &c->spmv_layout[2]));
     }
   }
   if (prec_mask & (1 << BILU_FP32_INNER)) {
@@ -619,11 +620,11 @@ int apply_prec(bilu_ctx* c, int prec, const double* v, double* z) {
     if (!c->Lval32 || !c->Uval32) return BILU_ERR_ARG;
     return isai_apply_f32_staged(c->nb, c->bs, c->Lrow, c->Lcol, c->Lval32, c->Urow, c->Ucol,
                                  c->Uval32, c->v32, (float*)c->tmp, z, c->st,
-                                 prec == BILU_FP32_INNER ? c->z32 : nullptr, c->long_rows[1],
-                                 c->long_rows[2]);
+                                 prec == BILU_FP32_INNER ? c->z32 : nullptr, c->spmv_layout[1],
+                                 c->spmv_layout[2]);
   }
   return isai_apply_impl(c->nb, c->bs, prec, c->Lrow, c->Lcol, c->Lval, c->Urow, c->Ucol,
-                         c->Uval, v, c->tmp, z, c->st, c->long_rows[1], c->long_rows[2]);
+                         c->Uval, v, c->tmp, z, c->st, c->spmv_layout[1], c->spmv_layout[2]);
 }
 
 }  // namespace
@@ -637,9 +638,9 @@ int arnoldi_front(bilu_ctx* c, int prec, int j) {
   BILU_TRY(apply_prec(c, prec, c->V + ld * j, zj));
   if (prec == BILU_FP32_INNER)  // FP32-stored A and z (written by the apply), FP64 w
     return spmv_any(c->nb, c->bs, BILU_FP32, c->Arow, c->Acol, c->Aval32, c->z32, 1, c->w, 0,
-                    c->st, c->long_rows[0]);
+                    c->st, c->spmv_layout[0]);
   return spmv_any(c->nb, c->bs, BILU_FP64, c->Arow, c->Acol, c->Aval, zj, 0, c->w, 0, c->st,
-                  c->long_rows[0]);
+                  c->spmv_layout[0]);
 }
 
 // Orthogonalises w against V_0..V_j by modified Gram-Schmidt: j+2 fused
@@ -753,7 +754,7 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
       BILU_TRY(multiaxpy_norm(n, c->Z, c->ldv, jlast + 1, c->dcoef, 1.0, d_x, nullptr, nullptr, st));
     }
     BILU_TRY(spmv_any(c->nb, c->bs, BILU_FP64, c->Arow, c->Acol, c->Aval, d_x, 0, c->w, 0, st,
-                      c->long_rows[0]));
+                      c->spmv_layout[0]));
     BILU_TRY(residual_norm(n, d_b, c->w, c->r, c->partial, st));
     BILU_TRY(reduce_partials(c->partial, 1, s + 5 * kPartStride, st));
     BILU_TRY_CUDA(cudaMemcpyAsync(&rr, s + 5 * kPartStride, sizeof(double), cudaMemcpyDeviceToHost, st));

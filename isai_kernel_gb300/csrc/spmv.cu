@@ -247,9 +247,16 @@ __global__ void __launch_bounds__(256, sizeof(VT) == 4 ? 4 : 2) k_bsr_spmv(int m
   }
 }
 
+// Layout word of a matrix for the SpMV: bit 0 = rows of more than
+// kLongSpmvRow blocks present (the LONG instance).  (Taking several blocks
+// of a row side by side, or rows in length order, was measured slower on
+// the power-law patterns: the product is latency-bound there, not bound by
+// the lanes an uneven warp leaves idle.)
+constexpr int kLayoutLong = 1;
+
 template <int BS, class VT, class XT, class YT>
 int launch_spmv(int mb, const int* row, const int* col, const VT* val, const XT* x, YT* y,
-                cudaStream_t st, bool long_rows, float* y32 = nullptr) {
+                cudaStream_t st, int layout, float* y32 = nullptr) {
   using AccT = VT;
   if (mb == 0) return BILU_OK;
   constexpr int G = 32 / BS;
@@ -257,7 +264,7 @@ int launch_spmv(int mb, const int* row, const int* col, const VT* val, const XT*
   long long groups = (mb + RPG - 1) / RPG;
   long long warps = (groups + G - 1) / G;
   unsigned grid = ceil_div(warps, 8);
-  if (long_rows) {
+  if (layout & kLayoutLong) {
     constexpr int NSLOT = 8 * G * RPG;
     const size_t smem = sizeof(int) * ((NSLOT + 1) & ~1) + sizeof(AccT) * 8 * G * BS;
     k_bsr_spmv<BS, VT, XT, YT, AccT, RPG, true><<<grid, 256, smem, st>>>(mb, row, col, val, x,
@@ -337,13 +344,13 @@ __global__ void k_f64_to_f32(size_t n, const double* __restrict__ s, float* __re
 
 template <int BS>
 int spmv_f64(int mb, const int* row, const int* col, const double* val, const double* x,
-             double* y, cudaStream_t st, bool lr) {
+             double* y, cudaStream_t st, int lr) {
   return launch_spmv<BS, double, double, double>(mb, row, col, val, x, y, st, lr);
 }
 
 template <int BS>
 int spmv_f32(int mb, const int* row, const int* col, const float* val, const void* x, int x32,
-             void* y, int y32, cudaStream_t st, bool lr) {
+             void* y, int y32, cudaStream_t st, int lr) {
   if (x32 && y32)
     return launch_spmv<BS, float, float, float>(mb, row, col, val, (const float*)x, (float*)y, st,
                                                 lr);
@@ -360,7 +367,7 @@ int spmv_f32(int mb, const int* row, const int* col, const float* val, const voi
 // FP32 values and x, FP64 y plus its FP32 copy y32
 template <int BS>
 int spmv_f32_dual(int mb, const int* row, const int* col, const float* val, const float* x,
-                  double* y, float* y32, cudaStream_t st, bool lr) {
+                  double* y, float* y32, cudaStream_t st, int lr) {
   return launch_spmv<BS, float, float, double>(mb, row, col, val, x, y, st, lr, y32);
 }
 
@@ -386,64 +393,73 @@ int spmm_f32(int mb, int k, const int* row, const int* col, const float* val, co
 
 }  // namespace
 
-// Whether a block pattern has rows of more than kLongSpmvRow blocks: one
-// reduction over the row pointers into d_word (one device int) and a
-// synchronising read.  The engine calls it once per matrix at setup.
-int spmv_long_rows_of(int mb, const int* row, int* d_word, cudaStream_t st, int* h_long) {
-  *h_long = 0;
+// SpMV layout word of a block pattern (see kLayoutLong): one reduction
+// over the row pointers into d_words (one device int) and a synchronising
+// read.  The engine calls it once per matrix at setup.
+int spmv_layout_of(int mb, int bs, const int* row, void* d_words, cudaStream_t st,
+                   int* h_layout) {
+  (void)bs;
+  *h_layout = 0;
   if (mb <= 0) return BILU_OK;
   int h = 0;
-  BILU_TRY_CUDA(cudaMemsetAsync(d_word, 0, sizeof(int), st));
+  int* d = static_cast<int*>(d_words);
+  BILU_TRY_CUDA(cudaMemsetAsync(d, 0, sizeof(int), st));
   k_row_len_max<<<(unsigned)std::min<long long>(ceil_div(mb, 256), 152 * 8), 256, 0, st>>>(
-      mb, row, d_word);
+      mb, row, d);
   BILU_LAUNCH_CHECK();
-  BILU_TRY_CUDA(cudaMemcpyAsync(&h, d_word, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BILU_TRY_CUDA(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
   BILU_TRY_CUDA(cudaStreamSynchronize(st));
-  *h_long = h > kLongSpmvRow ? 1 : 0;
+  *h_layout = h > kLongSpmvRow ? kLayoutLong : 0;
   return BILU_OK;
 }
 
 namespace {
 
-__device__ int g_row_len_word;  // scratch of the cached check (used under its lock)
+__device__ int g_layout_word;  // scratch of the cached check (under its lock)
 
 // The standalone entry points do not know the pattern: the answer is cached
-// per (row pointer array, block rows), most recent first.  A stale entry (a
-// buffer reused for another pattern) can only cost speed: both kernels are
-// exact for any row length.
-int long_rows_cached(int mb, const int* row, cudaStream_t st, bool* out) {
-  struct Entry {
-    const int* row;
-    int mb, flag;
-  };
-  static std::mutex mu;
-  static Entry cache[16] = {};
-  static int next = 0;
-  std::lock_guard<std::mutex> lock(mu);
-  for (const Entry& e : cache)
-    if (e.row == row && e.mb == mb && row) {
-      *out = e.flag != 0;
-      return BILU_OK;
-    }
-  int* word = nullptr;
-  BILU_TRY_CUDA(cudaGetSymbolAddress((void**)&word, g_row_len_word));
-  int flag = 0;
-  BILU_TRY(spmv_long_rows_of(mb, row, word, st, &flag));
-  cache[next] = Entry{row, mb, flag};
-  next = (next + 1) % 16;
-  *out = flag != 0;
+// per (row pointer array, block rows, block size), most recent first.  A
+// stale entry (a buffer reused for another pattern) can only cost speed:
+// both kernels are exact for any row length.
+struct LayoutEntry {
+  const int* row;
+  int mb, bs, layout;
+};
+std::mutex g_layout_mu;
+LayoutEntry g_layout_cache[16] = {};
+int g_layout_next = 0;
+
+// under g_layout_mu: the entry of (row, mb, bs), or null
+LayoutEntry* layout_find(int mb, int bs, const int* row) {
+  for (LayoutEntry& e : g_layout_cache)
+    if (e.row == row && e.mb == mb && e.bs == bs && row) return &e;
+  return nullptr;
+}
+
+int layout_cached(int mb, int bs, const int* row, cudaStream_t st, int* out) {
+  std::lock_guard<std::mutex> lock(g_layout_mu);
+  if (const LayoutEntry* e = layout_find(mb, bs, row)) {
+    *out = e->layout;
+    return BILU_OK;
+  }
+  void* words = nullptr;
+  BILU_TRY_CUDA(cudaGetSymbolAddress(&words, g_layout_word));
+  int layout = 0;
+  BILU_TRY(spmv_layout_of(mb, bs, row, words, st, &layout));
+  g_layout_cache[g_layout_next] = LayoutEntry{row, mb, bs, layout};
+  g_layout_next = (g_layout_next + 1) % 16;
+  *out = layout;
   return BILU_OK;
 }
 
 }  // namespace
 
-// internal entry point used by the solver; long_rows: 1 / 0 when the
-// caller knows whether the pattern has rows of more than kLongSpmvRow
-// blocks, -1 to look it up
+// internal entry point used by the solver; layout: the pattern's layout
+// word when the caller knows it (spmv_layout_of), -1 to look it up
 int spmv_any(int mb, int bs, int prec, const int* row, const int* col, const void* val,
-             const void* x, int x32, void* y, int y32, cudaStream_t st, int long_rows) {
-  bool lr = long_rows > 0;
-  if (long_rows < 0) BILU_TRY(long_rows_cached(mb, row, st, &lr));
+             const void* x, int x32, void* y, int y32, cudaStream_t st, int layout) {
+  int lr = layout;
+  if (layout < 0) BILU_TRY(layout_cached(mb, bs, row, st, &lr));
   if (prec == BILU_FP64) {
     if (x32 || y32) return BILU_ERR_ARG;
     return BILU_DISPATCH_BS(bs, spmv_f64, mb, row, col, (const double*)val, (const double*)x,
@@ -485,8 +501,8 @@ int isai_apply_f32_staged(int nb, int bs, const int* Lrow, const int* Lcol, cons
                           int longU) {
   BILU_TRY(spmv_any(nb, bs, BILU_FP32, Lrow, Lcol, Lval, b32, 1, tmp, 1, st, longL));
   if (x32) {  // x also in FP32 (input of an FP32 operator product)
-    bool lr = longU > 0;
-    if (longU < 0) BILU_TRY(long_rows_cached(nb, Urow, st, &lr));
+    int lr = longU;
+    if (longU < 0) BILU_TRY(layout_cached(nb, bs, Urow, st, &lr));
     return BILU_DISPATCH_BS(bs, spmv_f32_dual, nb, Urow, Ucol, Uval, tmp, x, x32, st, lr);
   }
   return spmv_any(nb, bs, BILU_FP32, Urow, Ucol, Uval, tmp, 1, x, 0, st, longU);
@@ -502,6 +518,26 @@ extern "C" int bilu_bcsr_spmv(int mb, int bs, const int* d_row, const int* d_col
   if (mb < 0 || (mb > 0 && (!d_row || !d_col || !d_val || !d_x || !d_y))) return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   return spmv_any(mb, bs, BILU_FP64, d_row, d_col, d_val, d_x, 0, d_y, 0, S(stream), -1);
+}
+
+extern "C" int bilu_spmv_layout(int mb, int bs, const int* d_row, bilu_stream_t stream,
+                                int* h_layout) {
+  if (mb < 0 || !h_layout || (mb > 0 && !d_row)) return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  return layout_cached(mb, bs, d_row, S(stream), h_layout);
+}
+
+extern "C" int bilu_debug_spmv_layout_set(int mb, int bs, const int* d_row, int layout) {
+  if (mb < 0 || (mb > 0 && !d_row) || layout < 0 || layout > kLayoutLong) return BILU_ERR_ARG;
+  if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_layout_mu);
+  if (LayoutEntry* e = layout_find(mb, bs, d_row)) {
+    e->layout = layout;
+  } else {
+    g_layout_cache[g_layout_next] = LayoutEntry{d_row, mb, bs, layout};
+    g_layout_next = (g_layout_next + 1) % 16;
+  }
+  return BILU_OK;
 }
 
 extern "C" int bilu_bcsr_spmv_f32(int mb, int bs, const int* d_row, const int* d_col,

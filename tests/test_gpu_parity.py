@@ -447,6 +447,38 @@ def test_spmv_long_rows(cuda, orc, bs):
     assert relerr(N(y32).astype(np.float64), ref32) < 1e-5
 
 
+@pytest.mark.parametrize("bs", [4, 5, 8])
+def test_spmv_every_layout(cuda, orc, bs):
+    """Both SpMV kernels (with and without the CTA's long-row pass) on a
+    pattern with rows of up to ~150 blocks, and the layout the check finds
+    for it and for a stencil: within 1e-12 of the oracle whichever kernel
+    runs."""
+    import ctypes
+
+    import torch
+
+    from isai_kernel_gb300 import api
+
+    A = gen.powerlaw(600, bs=bs, seed=9, kmax=150)
+    x = gen.rhs(A.n, 13)
+    row, col, val, xd = T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda), T(x, cuda)
+    ref = orc.bcsr_spmv(A.nb, bs, A.rowptr, A.colind, A.val, x)
+    lay = ctypes.c_int(-1)
+    api.call("bilu_spmv_layout", A.nb, bs, api._p(row), api._s(), ctypes.byref(lay))
+    assert lay.value == 1
+    y = torch.empty(A.n, dtype=torch.float64, device="cuda")
+    for layout in (0, 1):
+        api.call("bilu_debug_spmv_layout_set", A.nb, bs, api._p(row), layout)
+        y.fill_(float("nan"))
+        api.call("bilu_bcsr_spmv", A.nb, bs, api._p(row), api._p(col), api._p(val), api._p(xd),
+                 api._p(y), api._s())
+        assert relerr(N(y), ref) < 1e-12, layout
+    S = gen.convdiff3d(6, bs=4, seed=0) if bs == 4 else gen.laplace2d(7, bs=bs, seed=2)
+    srow = T(S.rowptr, cuda)
+    api.call("bilu_spmv_layout", S.nb, bs, api._p(srow), api._s(), ctypes.byref(lay))
+    assert lay.value == 0
+
+
 def test_long_rows_take_the_warp_path(cuda, orc):
     """A power-law system with rows of more than 32 dependencies (up to 126
     here): the level kernels switch to a warp per row.  BILU(0) within 1e-12
