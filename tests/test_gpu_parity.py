@@ -366,6 +366,55 @@ def test_bilu0_both_schedules(cuda, orc, name):
     assert relerr(out[0], LU) < 1e-12
 
 
+def test_bilu0_dense_rows_both_schedules(cuda, orc):
+    """A dense 40 x 40 block pattern: the (row, dependency) pairs whose two
+    candidate lists both hold more than 32 blocks are counted by a whole
+    warp before the sync-free factorisation; identical factors under both
+    schedules, within 1e-12 of the oracle."""
+    from isai_kernel_gb300 import api
+
+    nb, bs = 40, 4
+    rng = np.random.default_rng(17)
+    rowptr = (np.arange(nb + 1) * nb).astype(np.int32)
+    colind = np.tile(np.arange(nb, dtype=np.int32), nb)
+    val = rng.uniform(-1.0, 1.0, (nb * nb, bs, bs))
+    for i in range(nb):
+        val[i * nb + i] += np.eye(bs) * (4.0 * nb)
+    A = gen.BSRMatrix(nb, bs, rowptr, colind, val)
+    LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    row, col = T(A.rowptr, cuda), T(A.colind, cuda)
+    out = []
+    for sched in (0, 1):
+        lu = T(A.val, cuda).clone()
+        assert api.bsrilu02_inplace(A.nb, A.nnzb, A.bs, row, col, lu, schedule=sched) == -1
+        out.append(N(lu))
+    assert np.array_equal(out[0], out[1])
+    assert relerr(out[0], LU) < 1e-12
+
+
+@pytest.mark.parametrize("bs", [4, 5, 8])
+def test_dinv_retry_blocks(cuda, orc, bs):
+    """Diagonal-block inverses with an all-zero block and a 1e-15 pivot:
+    the lower inverse reads the unit lower part, the upper one retries with
+    1e-12 added to the diagonal (isai_bsr.h:114-120); every block within
+    1e-12 of the oracle's Gauss-Jordan."""
+    from isai_kernel_gb300 import api
+
+    nb = 6
+    rng = np.random.default_rng(4)
+    row = np.arange(nb + 1, dtype=np.int32)
+    col = np.arange(nb, dtype=np.int32)
+    val = rng.uniform(-1.0, 1.0, (nb, bs, bs)) + np.eye(bs) * 3.0
+    val[1] = 0.0
+    val[2][1, 1] = 1e-15
+    for lower in (True, False):
+        D = N(api.build_Dinv(nb, bs, T(row, cuda), T(col, cuda), T(val, cuda), lower))
+        ref = orc.dinv(nb, bs, row, col, val, lower)
+        for k in range(nb):
+            assert relerr(D[k], ref[k]) < 1e-12, (lower, k)
+    assert abs(ref[1][0, 0] - 1e12) < 1.0  # the upper retry ran (zero block)
+
+
 @pytest.mark.parametrize("name", ["c2_s6", "c3_nb200"])
 def test_exact_ilu_gmres_both_schedules(cuda, orc, name):
     """GMRES with the exact BILU(0) under both schedules of the factor and
