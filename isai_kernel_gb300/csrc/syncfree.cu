@@ -1314,7 +1314,8 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
     // the reciprocal pivot, broadcasts it along the row and updates the
     // columns right of it; slots whose columns are all <= k are skipped
     // at compile time.  Per element the same operations in the same order
-    // as a lane per row, with a quarter of the FP64 instructions at BS 8.
+    // as a lane per row, with half the FP64 instructions at BS 8 (18 per
+    // dependency instead of 36).
     {
       // every operand is loaded up front, unpredicated (clamped columns):
       // loads under the lane predicates of the steps would wait one L2
