@@ -1265,6 +1265,78 @@ __device__ __forceinline__ unsigned dynamic_smem_bytes() {
   return v;
 }
 
+// Wait of a group of lanes (gmask) on one flag: the group's lanes read the
+// same word; bounded like warp_wait.
+__device__ __forceinline__ bool group_wait(const int* flag, int* err, long long spin,
+                                           unsigned gmask, bool leader) {
+  long long n = 0;
+  unsigned ns = 32;
+  while (true) {
+    const int v = ld_relaxed(flag);
+    if (__all_sync(gmask, v != 0)) {
+      fence_acquire();
+      return true;
+    }
+    if (__any_sync(gmask, ld_relaxed(err) != 0)) return false;
+    if (++n > spin) {
+      if (leader) atomicCAS(err, 0, (int)BILU_ERR_TIMEOUT);
+      return false;
+    }
+    backoff(ns);
+  }
+}
+
+// Phase 1 of a run of dependencies of row I: positions pk, pk+1, ... (at
+// most 32 / BS of them, all before the diagonal) whose match count is 0,
+// so that none of them updates a block another one reads.  Group q of BS
+// lanes takes position pk + q, waits for its row K and computes
+// L_IK = A_IK U_KK^-1 with lane r owning row r, the same operations per
+// element in the same order as the warp-wide step.  A hub row of a
+// power-law matrix has about a thousand such dependencies, which one warp
+// would otherwise take one after another on the critical path.  Returns
+// how many positions were taken (0 if fewer than two qualify), -1 if a
+// wait gave up.
+template <int BS, bool WAIT>
+__device__ __forceinline__ int bilu0_run_phase1(int pk, int dI, int rs,
+                                                const int* __restrict__ col, const int* stage,
+                                                const int* __restrict__ diag, double* val,
+                                                const SyncState& ss) {
+  constexpr int G = 32 / BS, BS2 = BS * BS;
+  const int lane = threadIdx.x & 31, q = lane / BS, r = lane - q * BS;
+  const int p = pk + q;
+  const bool mine = q < G && p < dI && __ldg(ss.nmatch + p) == 0;
+  const unsigned lead = __ballot_sync(FULL, mine && r == 0);
+  int take = 0;  // the run of qualifying groups from group 0
+  while (take < G && ((lead >> (take * BS)) & 1u)) ++take;
+  if (take < 2) return 0;
+  bool ok = true;
+  if (q < take) {
+    const unsigned gmask = ((1u << BS) - 1u) << (q * BS);
+    const int K = row_col(col, stage, rs, p);
+    const int dK = __ldg(diag + K);
+    if (WAIT) ok = group_wait(ss.flags + K, ss.err, ss.spin, gmask, r == 0);
+    if (ok) {
+      double* L = val + (long long)p * BS2;
+      const double* Ukk = val + (long long)dK * BS2;
+      const double* rK = ss.rdiag + (long long)K * BS;
+      double a[BS];
+#pragma unroll
+      for (int c = 0; c < BS; ++c) a[c] = L[r * BS + c];
+#pragma unroll
+      for (int k = 0; k < BS; ++k) {
+        a[k] = a[k] * __ldcg(rK + k);
+#pragma unroll
+        for (int c = k + 1; c < BS; ++c) a[c] -= a[k] * __ldcg(Ukk + k * BS + c);
+      }
+#pragma unroll
+      for (int c = 0; c < BS; ++c) L[r * BS + c] = a[c];
+    }
+  }
+  if (!__all_sync(FULL, ok)) return -1;
+  __syncwarp();
+  return take;
+}
+
 template <int BS, bool WAIT>
 __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
                                           const int* __restrict__ col,
@@ -1292,18 +1364,20 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
     __syncwarp();
     stage = stage_buf;
   }
-  // structural data of the next K, loaded one step ahead
-  int Kn = rs < dI ? row_col(col, stage, rs, rs) : 0;
-  int dKn = rs < dI ? __ldg(diag + Kn) : 0, ken = rs < dI ? __ldg(row + Kn + 1) : 0;
-  int nmn = rs < dI && ss.nmatch ? __ldg(ss.nmatch + rs) : 1;
   for (int pk = rs; pk < dI; ++pk) {
-    const int K = Kn, dK = dKn, ke = ken, nm = nmn;
-    if (pk + 1 < dI) {
-      Kn = row_col(col, stage, rs, pk + 1);
-      dKn = __ldg(diag + Kn);
-      ken = __ldg(row + Kn + 1);
-      if (ss.nmatch) nmn = __ldg(ss.nmatch + pk + 1);
+    // a run of dependencies that update no block beyond their own L_IK
+    // (match count 0) is independent inside the row: a lane group each
+    if (ss.nmatch && dI - pk >= 2) {
+      const int took = bilu0_run_phase1<BS, WAIT>(pk, dI, rs, col, stage, diag, val, ss);
+      if (took < 0) return false;
+      if (took > 0) {
+        pk += took - 1;
+        continue;
+      }
     }
+    const int K = row_col(col, stage, rs, pk);
+    const int dK = __ldg(diag + K), ke = __ldg(row + K + 1);
+    const int nm = ss.nmatch ? __ldg(ss.nmatch + pk) : 1;
     // sync-free schedule: row K may still be in progress
     if (WAIT && !warp_wait(ss.flags + K, ss.err, ss.spin)) return false;
     double* L = val + (long long)pk * BS2;
