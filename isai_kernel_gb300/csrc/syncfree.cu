@@ -1232,11 +1232,12 @@ __device__ __forceinline__ void bilu0_grow(const BRowPre& pr, const int* __restr
 
 // One block row with a whole warp (the sync-free factorisation, used for
 // matrices with long rows or narrow levels).  WAIT: the rows K it reads may
-// still be in progress and are waited for through their flags.  Phase 1 on
-// lanes r < BS (row r of L_IK), phase 2 with teams of lanes per updated
-// block, the diagonal LU with lane = column, U blocks with 32/BS blocks per
-// pass.  The same operations per element as bilu0_grow.  Returns false if
-// the launch aborted.
+// still be in progress and are waited for through their flags.  Phase 1 by
+// the whole warp (PL lanes per row of L_IK), or for runs of dependencies
+// without updates by a lane group each; phase 2 with teams of lanes per
+// updated block; the diagonal LU by the whole warp; U blocks with 32/BS
+// blocks per pass.  The same operations per element as bilu0_grow.
+// Returns false if the launch aborted.
 // Column index p of row I (rs = first position of the row): from the
 // shared-memory copy when the row was staged there.
 __device__ __forceinline__ int row_col(const int* __restrict__ col, const int* stage, int rs,
