@@ -51,6 +51,14 @@ def test_argument_errors_without_gpu():
     assert L.bilu_bsrilu0(-2, 0, 4, None, None, None, None, None, 0, None) == -1
     assert L.bilu_isai_apply(10, 4, 7, None, None, None, None, None, None, None, None, None,
                              None) == -1
+    lay = ctypes.c_int(7)
+    assert L.bilu_spmv_layout(-1, 4, None, None, ctypes.byref(lay)) == -1
+    assert L.bilu_spmv_layout(10, 4, ctypes.c_void_p(8), None, None) == -1
+    assert L.bilu_spmv_layout(10, 6, ctypes.c_void_p(8), None, ctypes.byref(lay)) == -8
+    assert lay.value == 7  # untouched on error
+    assert L.bilu_debug_spmv_layout_set(10, 4, ctypes.c_void_p(8), 2) == -1  # only 0 or 1
+    assert L.bilu_debug_spmv_layout_set(10, 4, None, 1) == -1
+    assert L.bilu_debug_spmv_layout_set(10, 6, ctypes.c_void_p(8), 1) == -8
 
 
 def test_build_is_in_tree():
