@@ -31,7 +31,7 @@ int tri_pattern_fill_impl(int nb, const int* row, const int* col, int lower, con
 int map_impl(int nb, const int* cptr, const int* cind, const int* rrow, const int* rcol, int* map,
              int* h_bad, Carver& ws, cudaStream_t st);
 int reorder_impl(long long nnzb, int bs, const int* map, const double* src, double* dst,
-                 cudaStream_t st);
+                 cudaStream_t st, float* dst32);
 size_t syncfree_ws(int nb);
 int diag_positions(int nb, const int* row, const int* col, int* diag, int* h_bad, Carver& ws,
                    cudaStream_t st);
@@ -256,7 +256,7 @@ struct Timer {
 // One triangle of the ISAI: pattern (BCSC), BCSR pattern + map, pairs,
 // Dinv, column solves, BCSC->BCSR reorder.  Outputs BCSR rowptr/col/val.
 int build_isai_side(bilu_ctx* c, int lower, Carver& ws, int** orow, int** ocol, double** oval,
-                    int* onnz, double* t_pattern, double* t_isai) {
+                    int* onnz, double* t_pattern, double* t_isai, float** oval32) {
   cudaStream_t st = c->st;
   int nb = c->nb, bs = c->bs, bs2 = bs * bs;
   // the M patterns come from pattern(A^k) for ISAI(k); the pair lists, Dinv
@@ -312,7 +312,11 @@ int build_isai_side(bilu_ctx* c, int lower, Carver& ws, int** orow, int** ocol, 
   BILU_TRY(c->alloc(&Mcsr, (size_t)mnnz * bs2));
   BILU_TRY(dinv_impl(nb, bs, c->Arow, c->Acol, c->LU, lower, Dinv, nullptr, st));
   BILU_TRY(isai_impl(nb, bs, c->LU, Mptr, Mind, lower, pp, pl, ps, Dinv, Mcsc, st));
-  BILU_TRY(reorder_impl(mnnz, bs, map, Mcsc, Mcsr, st));
+  // the FP32 copy of the mixed apply is written by the same pass
+  float* M32 = nullptr;
+  if (oval32) BILU_TRY(c->alloc(&M32, (size_t)mnnz * bs2));
+  BILU_TRY(reorder_impl(mnnz, bs, map, Mcsc, Mcsr, st, M32));
+  if (oval32) *oval32 = M32;
   tm.mark(2);
   *t_pattern += tm.ms(0, 1);
   *t_isai += tm.ms(1, 2);
@@ -419,8 +423,11 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
     }
   }
   if (isai) {
-    BILU_TRY(build_isai_side(c, 1, ws, &c->Lrow, &c->Lcol, &c->Lval, &c->nnzL, &t_pat, &t_isai));
-    BILU_TRY(build_isai_side(c, 0, ws, &c->Urow, &c->Ucol, &c->Uval, &c->nnzU, &t_pat, &t_isai));
+    const bool want32 = (prec_mask & ((1 << BILU_FP32) | (1 << BILU_FP32_INNER))) != 0;
+    BILU_TRY(build_isai_side(c, 1, ws, &c->Lrow, &c->Lcol, &c->Lval, &c->nnzL, &t_pat, &t_isai,
+                             want32 ? &c->Lval32 : nullptr));
+    BILU_TRY(build_isai_side(c, 0, ws, &c->Urow, &c->Ucol, &c->Uval, &c->nnzU, &t_pat, &t_isai,
+                             want32 ? &c->Uval32 : nullptr));
   }
   {
     Carver w2 = ws;
@@ -436,12 +443,6 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   if (prec_mask & (1 << BILU_FP32_INNER)) {
     BILU_TRY(c->alloc(&c->Aval32, (size_t)nnzb * bs2));
     BILU_TRY(bilu_convert_f64_to_f32((size_t)nnzb * bs2, c->Aval, c->Aval32, st));
-  }
-  if (prec_mask & ((1 << BILU_FP32) | (1 << BILU_FP32_INNER))) {
-    BILU_TRY(c->alloc(&c->Lval32, (size_t)c->nnzL * bs2));
-    BILU_TRY(c->alloc(&c->Uval32, (size_t)c->nnzU * bs2));
-    BILU_TRY(bilu_convert_f64_to_f32((size_t)c->nnzL * bs2, c->Lval, c->Lval32, st));
-    BILU_TRY(bilu_convert_f64_to_f32((size_t)c->nnzU * bs2, c->Uval, c->Uval32, st));
   }
   if (ilu) {
     // level analyses of both triangles of the packed factor for the exact

@@ -129,25 +129,35 @@ __global__ void k_map(int nb, const int* __restrict__ cptr, const int* __restric
 }
 
 // dst[map[k]] = src[k], blocks of bs2 doubles copied as double2 pairs when
-// the block size allows it.
+// the block size allows it; dst32 (optional) receives the same values
+// rounded to FP32 in the same pass (the FP32-stored factors of the mixed
+// apply), instead of a second read of dst.
 __global__ void k_reorder(long long nnzb, int bs2, const int* __restrict__ map,
-                          const double* __restrict__ src, double* __restrict__ dst) {
+                          const double* __restrict__ src, double* __restrict__ dst,
+                          float* __restrict__ dst32) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long total = nnzb * bs2;
   if (t >= total) return;
   long long k = t / bs2;
   int e = (int)(t - k * bs2);
-  dst[(long long)map[k] * bs2 + e] = src[t];
+  const long long d = (long long)map[k] * bs2 + e;
+  const double v = src[t];
+  dst[d] = v;
+  if (dst32) dst32[d] = __double2float_rn(v);
 }
 
 __global__ void k_reorder_v2(long long nnzb, int half, const int* __restrict__ map,
-                             const double2* __restrict__ src, double2* __restrict__ dst) {
+                             const double2* __restrict__ src, double2* __restrict__ dst,
+                             float2* __restrict__ dst32) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long total = nnzb * half;
   if (t >= total) return;
   long long k = t / half;
   int e = (int)(t - k * half);
-  dst[(long long)map[k] * half + e] = src[t];
+  const long long d = (long long)map[k] * half + e;
+  const double2 v = src[t];
+  dst[d] = v;
+  if (dst32) dst32[d] = make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
 }
 
 // bcsc -> bcsr: count blocks per row
@@ -381,16 +391,16 @@ int map_impl(int nb, const int* cptr, const int* cind, const int* rrow, const in
 }
 
 int reorder_impl(long long nnzb, int bs, const int* map, const double* src, double* dst,
-                 cudaStream_t st) {
+                 cudaStream_t st, float* dst32 = nullptr) {
   if (nnzb == 0) return BILU_OK;
   int bs2 = bs * bs;
   if (bs2 % 2 == 0) {
     long long total = nnzb * (bs2 / 2);
     k_reorder_v2<<<ceil_div(total, kT), kT, 0, st>>>(nnzb, bs2 / 2, map, (const double2*)src,
-                                                     (double2*)dst);
+                                                     (double2*)dst, (float2*)dst32);
   } else {
     long long total = nnzb * bs2;
-    k_reorder<<<ceil_div(total, kT), kT, 0, st>>>(nnzb, bs2, map, src, dst);
+    k_reorder<<<ceil_div(total, kT), kT, 0, st>>>(nnzb, bs2, map, src, dst, dst32);
   }
   BILU_LAUNCH_CHECK();
   return BILU_OK;
