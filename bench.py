@@ -77,6 +77,16 @@ def parse():
     return a
 
 
+def probe_lib():
+    """bench_probe.so (built by __graft_entry__.build()): pipe-rate and
+    synchronisation probes reported beside the numbers."""
+    P = ctypes.CDLL(os.path.join(ROOT, "bench_probe.so"))
+    for f in (P.probe_rates, P.probe_sync):
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    return P
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -416,7 +426,8 @@ def run_ours(args):
     gbs32s = B32s / t_apply32s / 1e9
     traffic, traffic_src = measured_traffic(args.side)
     rates = (ctypes.c_double * 3)()
-    _lib.check("bilu_probe_rates", L.bilu_probe_rates(rates))
+    rc = probe_lib().probe_rates(rates)
+    assert rc == 0, f"probe_rates returned {rc}"
     dfma_tf = rates[0]
     # FP64 kernels: one DFMA per stored FP64 value, so their compute roofline
     # is 2 * (#values) / DFMA rate
@@ -616,7 +627,8 @@ def run_sptrsv(args):
            "bilu0_ms_incl_analysis": e0.elapsed_time(e1), "zero_pivot": zp}
     # what the level-order kernels are bound by (SM cycles)
     sp = (ctypes.c_double * 8)()
-    _lib.check("bilu_probe_sync", L.bilu_probe_sync(sp))
+    rc = probe_lib().probe_sync(sp)
+    assert rc == 0, f"probe_sync returned {rc}"
     out["sync_probe_cycles"] = {
         "dfma_interval_per_sm_1_4_16_warps": [round(sp[0], 1), round(sp[1], 1), round(sp[2], 1)],
         "dfma_interval_per_sm_4_warps_4_lanes": round(sp[3], 1),

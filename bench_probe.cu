@@ -1,16 +1,31 @@
-// Pipe-throughput probe used to set the compute roofline of the FP64
+// Pipe-throughput and synchronisation probes for bench.py (measurement
+// tooling, built into bench_probe.so beside bench.py; not part of
+// libbilu_isai.so).  The first probe sets the compute roofline of the FP64
 // kernels: DFMA, DMMA (mma.sync.m8n8k4.f64, the reference's tensor path) and
-// FFMA rates of the current GPU.  Register-only kernels, one store per thread.
-// A second probe measures what the level-order kernels are bound by: the
-// FP64 issue interval of one SM sub-partition, the store-to-load visibility
-// between two SMs and the latency of an L2 hit.  Every wait in it is
-// bounded.
+// FFMA rates of the current GPU, from register-only kernels with one store
+// per thread.  The second measures what the level-order kernels are bound
+// by: the FP64 issue interval of one SM sub-partition, the store-to-load
+// visibility between two SMs and the latency of an L2 hit.  Every wait in
+// it is bounded.
+//
+// Return codes: 0 ok, -1 bad argument, -4 a wait gave up, -5 CUDA error,
+// -8 unsupported device.
+#include <cuda_runtime.h>
+
 #include <algorithm>
 #include <vector>
 
-#include "common.cuh"
+namespace probe {
 
-namespace bilu {
+constexpr int kOk = 0, kErrArg = -1, kErrTimeout = -4, kErrCuda = -5, kErrUnsupported = -8;
+
+inline int cuda_status(cudaError_t e) { return e == cudaSuccess ? kOk : kErrCuda; }
+
+#define PROBE_TRY_CUDA(call)                 \
+  do {                                       \
+    if ((call) != cudaSuccess) return kErrCuda; \
+  } while (0)
+
 namespace {
 
 constexpr int kProbeIters = 4096;
@@ -129,26 +144,26 @@ __global__ void k_probe_chain(const unsigned* p, int n, long long* out) {
 }
 
 }  // namespace
-}  // namespace bilu
+}  // namespace probe
 
-using namespace bilu;
+using namespace probe;
 
 // h_out[0..2] = DFMA, DMMA, FFMA throughput in TFLOP/s (best of two runs).
-extern "C" int bilu_probe_rates(double* h_out) {
-  if (!h_out) return BILU_ERR_ARG;
+extern "C" int probe_rates(double* h_out) {
+  if (!h_out) return kErrArg;
   int dev = 0, sms = 0;
-  BILU_TRY_CUDA(cudaGetDevice(&dev));
-  BILU_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  PROBE_TRY_CUDA(cudaGetDevice(&dev));
+  PROBE_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int grid = sms * 8, block = 256;
   const double threads = (double)grid * block;
   double* buf = nullptr;
-  BILU_TRY_CUDA(cudaMalloc(&buf, sizeof(double) * (size_t)grid * block));
+  PROBE_TRY_CUDA(cudaMalloc(&buf, sizeof(double) * (size_t)grid * block));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   double best[3] = {0, 0, 0};
-  int rc = BILU_OK;
-  for (int rep = 0; rep < 2 && rc == BILU_OK; ++rep) {
+  int rc = kOk;
+  for (int rep = 0; rep < 2 && rc == kOk; ++rep) {
     float ms = 0;
     k_probe_dfma<<<grid, block>>>(buf, 64, 1.0000001, 1e-9);
     cudaEventRecord(e0);
@@ -186,29 +201,29 @@ extern "C" int bilu_probe_rates(double* h_out) {
 // between two SMs (relaxed stores and loads), smallest and largest over
 // four SM pairs; h_out[6]: the same with st.release / ld.acquire (first
 // pair); h_out[7]: cycles of a dependent L2-hit load.
-extern "C" int bilu_probe_sync(double* h_out) {
-  if (!h_out) return BILU_ERR_ARG;
+extern "C" int probe_sync(double* h_out) {
+  if (!h_out) return kErrArg;
   int dev = 0, sms = 0;
-  BILU_TRY_CUDA(cudaGetDevice(&dev));
-  BILU_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  if (sms < 2) return BILU_ERR_UNSUPPORTED;
+  PROBE_TRY_CUDA(cudaGetDevice(&dev));
+  PROBE_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  if (sms < 2) return kErrUnsupported;
   long long* cyc = nullptr;
   unsigned* words = nullptr;
   double* sink = nullptr;
   const size_t nchain = 1 << 20;
-  BILU_TRY_CUDA(cudaMalloc(&cyc, sizeof(long long) * (size_t)sms * 16));
-  BILU_TRY_CUDA(cudaMalloc(&words, sizeof(unsigned) * nchain));
-  BILU_TRY_CUDA(cudaMalloc(&sink, sizeof(double)));
-  int rc = BILU_OK;
+  PROBE_TRY_CUDA(cudaMalloc(&cyc, sizeof(long long) * (size_t)sms * 16));
+  PROBE_TRY_CUDA(cudaMalloc(&words, sizeof(unsigned) * nchain));
+  PROBE_TRY_CUDA(cudaMalloc(&sink, sizeof(double)));
+  int rc = kOk;
   std::vector<long long> h((size_t)sms * 16);
   // issue interval
   const int iters = 4096;
   const int wl[4] = {1, 4, 16, 4}, al[4] = {32, 32, 32, 4};
-  for (int c = 0; c < 4 && rc == BILU_OK; ++c) {
+  for (int c = 0; c < 4 && rc == kOk; ++c) {
     k_probe_dfma_issue<<<sms, 32 * wl[c]>>>(iters, al[c], cyc, sink);
     k_probe_dfma_issue<<<sms, 32 * wl[c]>>>(iters, al[c], cyc, sink);
     rc = cuda_status(cudaDeviceSynchronize());
-    if (rc != BILU_OK) break;
+    if (rc != kOk) break;
     rc = cuda_status(cudaMemcpy(h.data(), cyc, sizeof(long long) * (size_t)sms * wl[c],
                                 cudaMemcpyDeviceToHost));
     long long mx = 1;
@@ -220,23 +235,23 @@ extern "C" int bilu_probe_sync(double* h_out) {
   const int rounds = 2000;
   const int bs_[4] = {1, sms / 4, sms / 2, (3 * sms) / 4};
   double lo = 1e30, hi = 0, acq = 0;
-  for (int mode = 0; mode < 2 && rc == BILU_OK; ++mode) {
-    for (int k = 0; k < (mode == 0 ? 4 : 1) && rc == BILU_OK; ++k) {
+  for (int mode = 0; mode < 2 && rc == kOk; ++mode) {
+    for (int k = 0; k < (mode == 0 ? 4 : 1) && rc == kOk; ++k) {
       unsigned* X = words;
       unsigned* Y = words + 4096;  // 16 KB apart
       int b = std::max(1, std::min(sms - 1, bs_[k])), r = rounds, m = mode;
       rc = cuda_status(cudaMemset(words, 0, sizeof(unsigned) * 8192));
-      if (rc == BILU_OK) rc = cuda_status(cudaMemset(out, 0, sizeof(long long) * 3));
+      if (rc == kOk) rc = cuda_status(cudaMemset(out, 0, sizeof(long long) * 3));
       void* args[] = {&b, &r, &m, &X, &Y, &out};
-      if (rc == BILU_OK)
+      if (rc == kOk)
         rc = cuda_status(cudaLaunchCooperativeKernel((const void*)k_probe_pingpong, dim3(sms),
                                                      dim3(32), args, 0, 0));
-      if (rc == BILU_OK) rc = cuda_status(cudaDeviceSynchronize());
+      if (rc == kOk) rc = cuda_status(cudaDeviceSynchronize());
       long long o[3] = {0, 0, 0};
-      if (rc == BILU_OK) rc = cuda_status(cudaMemcpy(o, out, sizeof(o), cudaMemcpyDeviceToHost));
-      if (rc != BILU_OK) break;
+      if (rc == kOk) rc = cuda_status(cudaMemcpy(o, out, sizeof(o), cudaMemcpyDeviceToHost));
+      if (rc != kOk) break;
       if (o[0] <= 0) {
-        rc = BILU_ERR_TIMEOUT;
+        rc = kErrTimeout;
         break;
       }
       const double one_way = (double)o[0] / rounds / 2;
@@ -252,17 +267,17 @@ extern "C" int bilu_probe_sync(double* h_out) {
   h_out[5] = hi;
   h_out[6] = acq;
   // dependent L2-hit loads: p[i] = i + 32 (128-byte stride) over 4 MB
-  if (rc == BILU_OK) {
+  if (rc == kOk) {
     std::vector<unsigned> ring(nchain);
     for (size_t i = 0; i < nchain; ++i) ring[i] = (unsigned)((i + 32) % nchain);
     rc = cuda_status(cudaMemcpy(words, ring.data(), sizeof(unsigned) * nchain,
                                 cudaMemcpyHostToDevice));
-    for (int rep = 0; rep < 2 && rc == BILU_OK; ++rep) {
+    for (int rep = 0; rep < 2 && rc == kOk; ++rep) {
       k_probe_chain<<<1, 1>>>(words, 20000, cyc);
       rc = cuda_status(cudaDeviceSynchronize());
     }
     long long o = 0;
-    if (rc == BILU_OK) rc = cuda_status(cudaMemcpy(&o, cyc, sizeof(o), cudaMemcpyDeviceToHost));
+    if (rc == kOk) rc = cuda_status(cudaMemcpy(&o, cyc, sizeof(o), cudaMemcpyDeviceToHost));
     h_out[7] = (double)o / 20000;
   }
   cudaFree(cyc);

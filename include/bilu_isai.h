@@ -67,18 +67,6 @@ int bilu_version(void);
 int bilu_last_cuda_error(void);
 /* number of kernels this library has launched since it was loaded */
 unsigned long long bilu_kernel_launches(void);
-/* Measured pipe throughput of the current GPU in TFLOP/s: h_out[0] DFMA,
- * h_out[1] DMMA (mma.sync m8n8k4 f64), h_out[2] FFMA.  Sets the compute
- * roofline of the FP64 kernels (allocates and frees a scratch buffer). */
-int bilu_probe_rates(double* h_out);
-/* What the level-order kernels are bound by, in SM cycles: h_out[0..3] the
- * interval between DFMA warp instructions on one SM with 1, 4 and 16 warps
- * per SM and with 4 warps of 4 active lanes; h_out[4..5] the one-way
- * store -> load visibility between two SMs (relaxed; smallest and largest
- * of four SM pairs); h_out[6] the same with st.release / ld.acquire;
- * h_out[7] a dependent L2-hit load.  Every wait is bounded
- * (BILU_ERR_TIMEOUT). */
-int bilu_probe_sync(double* h_out);
 
 /* ------------------------------------------------------------------ */
 /* Format conversions and patterns                                     */
@@ -487,15 +475,18 @@ int bilu_batch_tuning(bilu_batch* batch, int* h_cfg, double* h_ms);
 /* ------------------------------------------------------------------ */
 
 /* No counterpart in the reference.  The sync-free block triangular solve of
- * bilu_sptrsv for callers that cannot allocate device memory (code running
- * while a CUDA graph is being captured, hosts whose device memory belongs to
- * a fixed arena or budget, plugins limited to the buffers they are handed):
- * it takes only inputs and the output and keeps its scratch in one fixed,
- * file-scope device array of about 6 MiB that every device holds from the
- * moment the library is loaded until the process exits.  It never calls
- * cudaMalloc, cudaFree or any allocating routine.
+ * bilu_sptrsv for callers that cannot allocate device memory (hosts whose
+ * device memory belongs to a fixed arena or budget, plugins limited to the
+ * buffers they are handed): it takes only inputs and the output and keeps
+ * its scratch in one fixed, file-scope device array of about 6 MiB that
+ * every device holds from the moment the library is loaded until the
+ * process exits.  It never calls cudaMalloc, cudaFree or any allocating
+ * routine.  Like bilu_sptrsv it waits on the stream before it returns (the
+ * pattern check and the error word are read back to the host).
  *   - nb may not exceed bilu_sptrsv_noalloc_max_rows() (262144 block rows);
  *     larger systems return BILU_ERR_WORKSPACE without touching the GPU.
+ *   - d_b and d_x may not be the same buffer (BILU_ERR_ARG); a block row
+ *     without a stored diagonal block returns BILU_ERR_PATTERN.
  *   - The first call on a device looks up the array's device address with
  *     cudaGetSymbolAddress (no allocation) and caches it; make that first call
  *     before any stream capture on that device.

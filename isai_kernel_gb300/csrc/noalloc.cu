@@ -1,12 +1,12 @@
 // Sync-free block triangular solve that allocates nothing.
 //
-// Callers that cannot allocate device memory -- code that runs while a CUDA
-// graph is being captured, hosts whose device memory is owned by a fixed
-// arena or budget, or plugins that may only touch the buffers they are given
-// -- cannot provide the workspace bilu_sptrsv asks for.  This variant takes
-// only the inputs and the output and keeps its scratch in one file-scope
-// device array of fixed size, so it never calls cudaMalloc, cudaFree or any
-// allocating routine.
+// Callers that cannot allocate device memory -- hosts whose device memory is
+// owned by a fixed arena or budget, or plugins that may only touch the
+// buffers they are given -- cannot provide the workspace bilu_sptrsv asks
+// for.  This variant takes only the inputs and the output and keeps its
+// scratch in one file-scope device array of fixed size, so it never calls
+// cudaMalloc, cudaFree or any allocating routine.  It waits on its stream
+// (to read the pattern check and the error word back), like bilu_sptrsv.
 #include <mutex>
 
 #include "common.cuh"
@@ -62,6 +62,8 @@ extern "C" int bilu_sptrsv_noalloc(int nb, int bs, const int* d_row, const int* 
                                    const double* d_val, int lower, const double* d_b, double* d_x,
                                    bilu_stream_t stream) {
   if (nb < 0 || (nb > 0 && (!d_row || !d_col || !d_val || !d_b || !d_x))) return BILU_ERR_ARG;
+  // b is read while x is written: they may not share memory
+  if (nb > 0 && (const void*)d_b == (const void*)d_x) return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   if (nb > kNoAllocMaxRows) return BILU_ERR_WORKSPACE;
   size_t need = syncfree_ws(nb) + carve_size(sizeof(int) * ((size_t)nb + 1));
