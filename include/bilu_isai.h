@@ -58,7 +58,8 @@ enum bilu_precision {
   BILU_FP32 = 1,
   BILU_ILU = 2,
   BILU_FP32_INNER = 3,
-  BILU_ILU_FP32 = 4
+  BILU_ILU_FP32 = 4,
+  BILU_NESTED = 5
 };
 
 const char* bilu_status_string(int status);
@@ -345,7 +346,8 @@ int bilu_ctx_destroy(bilu_ctx* ctx);
  * 1 << BILU_ILU, FP32 copies of the ISAI factors and of A when it has
  * 1 << BILU_FP32_INNER, an FP32 copy of the factor and of its reciprocal
  * pivots when it has 1 << BILU_ILU_FP32 (built when no row of either
- * triangle has more than 32 dependencies).  A prec_mask of exact-ILU bits
+ * triangle has more than 32 dependencies), FP32 copies of the ISAI factors
+ * and of A when it has 1 << BILU_NESTED.  A prec_mask of exact-ILU bits
  * alone builds BILU(0) and the level analyses only (no ISAI; solves in the
  * other modes then return BILU_ERR_ARG).
  * h_times (optional, 4 doubles, milliseconds): factor, patterns, isai,
@@ -369,7 +371,14 @@ int bilu_ctx_set_schedule(bilu_ctx* ctx, int schedule);
  * exact BILU(0) by level-scheduled triangular solves, BILU_FP32_INNER the
  * FP32 ISAI with the FP32-stored A in the Arnoldi products (the true FP64
  * residual at every restart corrects the inner precision, as in GMRES with
- * iterative refinement); prec -1 runs without preconditioner.  A choice the setup did not build returns BILU_ERR_ARG.  h_iters, h_relres: iteration count and final true
+ * iterative refinement), BILU_NESTED the nested GMRES-IR form: every
+ * preconditioned vector z_j of the FP64 flexible outer GMRES is a fixed
+ * number of steps (bilu_ctx_set_inner, default 20) of right-preconditioned
+ * GMRES in FP32 on A z = v_j with the FP32-stored A and ISAI, FP32
+ * Gram-Schmidt and the Hessenberg least squares on the device; the outer
+ * residuals, orthogonalisation and true residual at every restart stay
+ * FP64.  h_iters then counts outer steps (bilu_ctx_inner_steps gives the
+ * inner ones); prec -1 runs without preconditioner.  A choice the setup did not build returns BILU_ERR_ARG.  h_iters, h_relres: iteration count and final true
  * relative residual.  h_hist (optional, maxit+1 doubles) receives the
  * residual estimate after every iteration. */
 int bilu_ctx_solve(bilu_ctx* ctx, int prec, const double* d_b, double* d_x, int restart,
@@ -378,6 +387,11 @@ int bilu_ctx_solve(bilu_ctx* ctx, int prec, const double* d_b, double* d_x, int 
 /* Counters of the last solve: h_out[0] = Arnoldi steps, h_out[1] = restart
  * cycles. */
 int bilu_ctx_stats(bilu_ctx* ctx, long long* h_out);
+/* Inner FP32 GMRES steps per outer step of the nested mode (1..32; default
+ * 20), for the next solve; no counterpart in the reference. */
+int bilu_ctx_set_inner(bilu_ctx* ctx, int k);
+/* Inner steps the last BILU_NESTED solve took in total. */
+int bilu_ctx_inner_steps(bilu_ctx* ctx, long long* h_steps);
 
 /* Preconditioner switch by measurement (SpTRSV apply vs SpMV apply):
  * runs up to `cycles` restart cycles (fewer when it reaches tol) from x0 = 0

@@ -37,7 +37,7 @@ STATUS = {
     -8: "BILU_ERR_UNSUPPORTED",
     -9: "BILU_ERR_IO",
 }
-BILU_FP64, BILU_FP32, BILU_ILU, BILU_FP32_INNER, BILU_ILU_FP32 = 0, 1, 2, 3, 4
+BILU_FP64, BILU_FP32, BILU_ILU, BILU_FP32_INNER, BILU_ILU_FP32, BILU_NESTED = 0, 1, 2, 3, 4, 5
 
 
 def _ctype(t: str):

@@ -14,8 +14,8 @@ from dataclasses import dataclass
 
 import torch
 
-from ._lib import (BILU_FP32, BILU_FP32_INNER, BILU_FP64, BILU_ILU, BILU_ILU_FP32, BiluError, call,
-                   lib)
+from ._lib import (BILU_FP32, BILU_FP32_INNER, BILU_FP64, BILU_ILU, BILU_ILU_FP32, BILU_NESTED,
+                   BiluError, call, lib)
 
 _I32, _F64, _F32 = torch.int32, torch.float64, torch.float32
 
@@ -355,6 +355,7 @@ class SolveResult:
     converged: bool
     history: list
     restarts: int = 0
+    inner_steps: int = 0
 
 
 class Preconditioner:
@@ -363,19 +364,21 @@ class Preconditioner:
 
     def __init__(self, nb: int, bs: int, row, col, val, fp32: bool = True, ilu: bool = False,
                  fp32_inner: bool = False, isai_level: int = 1, schedule: int = -1,
-                 stream=None, ilu_fp32: bool = False):
+                 stream=None, ilu_fp32: bool = False, nested: bool = False, inner: int = 20):
         self._h = ctypes.c_void_p()
         self.nb, self.bs = nb, bs
         self.stream = stream
         call("bilu_ctx_create", ctypes.byref(self._h), _s(stream))
         call("bilu_ctx_set_isai_level", self._h, isai_level)
         call("bilu_ctx_set_schedule", self._h, schedule)
+        call("bilu_ctx_set_inner", self._h, inner)
         self._keep = (row, col, val)
         times = (ctypes.c_double * 4)()
         call("bilu_ctx_setup", self._h, nb, int(col.numel()), bs, _p(_ci(row)), _p(_ci(col)),
              _p(_cf(val)), ((1 << BILU_FP32) if fp32 else 0) | ((1 << BILU_ILU) if ilu else 0)
              | ((1 << BILU_FP32_INNER) if fp32_inner else 0)
-             | ((1 << BILU_ILU_FP32) if ilu_fp32 else 0), times)
+             | ((1 << BILU_ILU_FP32) if ilu_fp32 else 0)
+             | ((1 << BILU_NESTED) if nested else 0), times)
         self.setup_ms = {"factor": times[0], "patterns": times[1], "isai": times[2],
                          "total": times[3]}
 
@@ -409,20 +412,25 @@ class Preconditioner:
         U = (self.get(4), self.get(5), self.get(6).view(-1, bs, bs))
         return lu, L, U
 
+    def set_inner(self, k: int):
+        """Inner FP32 GMRES steps per outer step of the nested mode."""
+        call("bilu_ctx_set_inner", self._h, k)
+
     def select(self, b, restart: int = 30, cycles: int = 3, tol: float = 1e-10, mask: int = 31):
         """bilu_ctx_select: the preconditioner (BILU_FP64 / BILU_FP32 /
-        BILU_ILU / BILU_FP32_INNER / BILU_ILU_FP32) with the best measured
-        residual reduction per second over the last of up to `cycles`
-        restart cycles -> (choice, [digits/s])."""
-        choice, rate = ctypes.c_int(-1), (ctypes.c_double * 5)()
+        BILU_ILU / BILU_FP32_INNER / BILU_ILU_FP32 / BILU_NESTED) with the
+        best measured residual reduction per second over the last of up to
+        `cycles` restart cycles -> (choice, [digits/s])."""
+        choice, rate = ctypes.c_int(-1), (ctypes.c_double * 6)()
         call("bilu_ctx_select", self._h, _p(_cf(b)), restart, cycles, tol, mask,
              ctypes.byref(choice), rate)
-        return choice.value, list(rate)
+        nrate = max([4] + [p + 1 for p in (BILU_ILU_FP32, BILU_NESTED) if mask >> p])
+        return choice.value, list(rate)[:nrate]
 
     def solve(self, b, x=None, prec=BILU_FP64, restart: int = 30, tol: float = 1e-10,
               maxit: int = 10000, history: bool = False) -> tuple:
-        """prec: BILU_FP64, BILU_FP32, BILU_ILU, BILU_FP32_INNER, BILU_ILU_FP32, -1 (none) or
-        "auto" (measured choice by select())."""
+        """prec: BILU_FP64, BILU_FP32, BILU_ILU, BILU_FP32_INNER, BILU_ILU_FP32, BILU_NESTED,
+        -1 (none) or "auto" (measured choice by select())."""
         b = _cf(b)
         if prec == "auto":
             prec, _ = self.select(b, restart, tol=tol)
@@ -437,7 +445,9 @@ class Preconditioner:
         h = list(hist[: it.value + 1]) if history else []
         stats = (ctypes.c_longlong * 4)()
         call("bilu_ctx_stats", self._h, stats)
-        return x, SolveResult(it.value, rr.value, st == 0, h, int(stats[1]))
+        inner = ctypes.c_longlong(0)
+        call("bilu_ctx_inner_steps", self._h, ctypes.byref(inner))
+        return x, SolveResult(it.value, rr.value, st == 0, h, int(stats[1]), int(inner.value))
 
 
 # ------------------------------------------------------------ host ingest

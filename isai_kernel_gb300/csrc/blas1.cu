@@ -234,6 +234,192 @@ __global__ void __launch_bounds__(kRedThreads, kSweepCTAs / 152) k_mgs_sweep(
   }
 }
 
+
+// FP32 form of k_mgs_sweep for the inner solver: four elements per 16-byte
+// access, FP32 products and sums per thread, FP64 from the warp sums on.
+// w (33.5 MB at 128^3) and vn stay in the L2 (vn is read with ld.global.cg,
+// so the next sweep finds it there as vp); vp streams with evict-first
+// loads, the last use of that basis vector in this step.
+__global__ void __launch_bounds__(kRedThreads, kSweepCTAs / 152) k_mgs_sweep_f32(
+    long long n, const float* __restrict__ vp, const double* __restrict__ hp,
+    const float* __restrict__ vn, float* __restrict__ w, double* __restrict__ partial,
+    unsigned* counter, double* out) {
+  asm volatile("griddepcontrol.launch_dependents;");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const float h = vp ? -(float)__ldcg(hp) : 0.0f;
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  float4* w4 = reinterpret_cast<float4*>(w);
+  const float4* vp4 = reinterpret_cast<const float4*>(vp);
+  const float4* vn4 = reinterpret_cast<const float4*>(vn);
+  const long long n4 = n >> 2;
+  for (long long e = tid; e < n4; e += stride) {
+    float4 we = __ldcg(w4 + e);
+    if (vp) {
+      const float4 p = __ldcs(vp4 + e);
+      we.x = fmaf(h, p.x, we.x);
+      we.y = fmaf(h, p.y, we.y);
+      we.z = fmaf(h, p.z, we.z);
+      we.w = fmaf(h, p.w, we.w);
+      w4[e] = we;
+    }
+    const float4 o = vn ? __ldcg(vn4 + e) : we;
+    a0 = fmaf(o.x, we.x, a0);
+    a1 = fmaf(o.y, we.y, a1);
+    a2 = fmaf(o.z, we.z, a2);
+    a3 = fmaf(o.w, we.w, a3);
+  }
+  if (tid < (n & 3)) {  // the last n % 4 elements
+    const long long e = (n4 << 2) + tid;
+    float we = __ldcg(w + e);
+    if (vp) {
+      we = fmaf(h, __ldcs(vp + e), we);
+      w[e] = we;
+    }
+    const float o = vn ? __ldcg(vn + e) : we;
+    a0 = fmaf(o, we, a0);
+  }
+  float accf = (a0 + a1) + (a2 + a3);
+  __shared__ double red[kRedThreads / 32];
+  __shared__ bool last;
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) accf += __shfl_xor_sync(0xffffffffu, accf, o);
+  if (lane == 0) red[warp] = (double)accf;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < kRedThreads / 32; ++i) s += red[i];
+    partial[blockIdx.x] = s;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double s = 0.0;
+  for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) s += __ldcg(partial + c);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) red[warp] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+#pragma unroll
+    for (int i = 0; i < kRedThreads / 32; ++i) t += red[i];
+    *out = t;
+    *counter = 0u;
+  }
+}
+
+__global__ void k_scale_rsqrt_f32(long long n, const float* __restrict__ x,
+                                  const double* __restrict__ nrm2, float* __restrict__ y) {
+  __shared__ float a_s;
+  if (threadIdx.x == 0) {
+    const double v = *nrm2;
+    a_s = v > 0.0 ? (float)(1.0 / sqrt(v)) : 0.0f;
+  }
+  __syncthreads();
+  const float a = a_s;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long n4 = n >> 2;
+  const float4* x4 = reinterpret_cast<const float4*>(x);
+  float4* y4 = reinterpret_cast<float4*>(y);
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n4; e += stride) {
+    float4 v = x4[e];
+    v.x *= a;
+    v.y *= a;
+    v.z *= a;
+    v.w *= a;
+    y4[e] = v;
+  }
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (n & 3)) y[(n4 << 2) + t] = x[(n4 << 2) + t] * a;
+}
+
+// One thread: Givens QR of the inner Hessenberg matrix and the triangular
+// solve, as the host does for the outer one (the same rotation formulas).
+__global__ void k_inner_lsq(int k, const double* __restrict__ Hraw, const double* __restrict__ ww,
+                            double* __restrict__ y) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double H[kMaxVec + 1][kMaxVec];
+  double cs[kMaxVec], sn[kMaxVec], g[kMaxVec + 1];
+  int steps = k;
+  for (int j = 0; j < k; ++j) {
+    for (int i = 0; i <= j; ++i) H[i][j] = Hraw[i * k + j];
+    const double hn = sqrt(ww[j]);
+    H[j + 1][j] = hn;
+    if (hn == 0.0) {
+      steps = j + 1;
+      break;
+    }
+  }
+  g[0] = 1.0;
+  for (int j = 0; j < steps; ++j) {
+    for (int i = 0; i < j; ++i) {
+      const double a = H[i][j], b = H[i + 1][j];
+      H[i][j] = cs[i] * a + sn[i] * b;
+      H[i + 1][j] = -sn[i] * a + cs[i] * b;
+    }
+    const double a = H[j][j], b = H[j + 1][j];
+    const double den = sqrt(a * a + b * b);
+    cs[j] = den != 0.0 ? a / den : 1.0;
+    sn[j] = den != 0.0 ? b / den : 0.0;
+    H[j][j] = cs[j] * a + sn[j] * b;
+    g[j + 1] = -sn[j] * g[j];
+    g[j] = cs[j] * g[j];
+  }
+  for (int i = steps - 1; i >= 0; --i) {
+    double v = g[i];
+    for (int l = i + 1; l < steps; ++l) v -= H[i][l] * y[l];
+    y[i] = H[i][i] != 0.0 ? v / H[i][i] : 0.0;
+  }
+  for (int i = steps; i < k; ++i) y[i] = 0.0;
+}
+
+template <int K>
+__global__ void __launch_bounds__(kRedThreads) k_combine_f32(long long n,
+                                                             const float* __restrict__ Q,
+                                                             long long ldq,
+                                                             const double* __restrict__ y,
+                                                             double* __restrict__ z) {
+  __shared__ float ys[K > 0 ? K : 1];
+  if (threadIdx.x < K) ys[threadIdx.x] = (float)y[threadIdx.x];
+  __syncthreads();
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long n4 = n >> 2;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n4; e += stride) {
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      const float4 q = __ldcs(reinterpret_cast<const float4*>(Q + i * ldq) + e);
+      s.x = fmaf(ys[i], q.x, s.x);
+      s.y = fmaf(ys[i], q.y, s.y);
+      s.z = fmaf(ys[i], q.z, s.z);
+      s.w = fmaf(ys[i], q.w, s.w);
+    }
+    double2* z2 = reinterpret_cast<double2*>(z + (e << 2));
+    z2[0] = make_double2((double)s.x, (double)s.y);
+    z2[1] = make_double2((double)s.z, (double)s.w);
+  }
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (n & 3)) {
+    const long long e = (n4 << 2) + t;
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < K; ++i) s = fmaf(ys[i], Q[i * ldq + e], s);
+    z[e] = (double)s;
+  }
+}
+
+template <int K>
+void launch_combine(long long n, const float* Q, long long ldq, const double* y, double* z,
+                    cudaStream_t st) {
+  k_combine_f32<K><<<kRedCTAs, kRedThreads, 0, st>>>(n, Q, ldq, y, z);
+}
+
 }  // namespace
 
 int multidot(long long n, const double* V, long long ldv, int nv, const double* w, bool with_ww,
@@ -277,6 +463,45 @@ int mgs_sweep(long long n, const double* vp, const double* hp, const double* vn,
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   BILU_TRY_CUDA(cudaLaunchKernelEx(&cfg, k_mgs_sweep, n, vp, hp, vn, w, partial, counter, out));
+  __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED);
+  return BILU_OK;
+}
+
+int mgs_sweep_f32(long long n, const float* vp, const double* hp, const float* vn, float* w,
+                  double* partial, unsigned* counter, double* out, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kSweepCTAs);
+  cfg.blockDim = dim3(kRedThreads);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  BILU_TRY_CUDA(
+      cudaLaunchKernelEx(&cfg, k_mgs_sweep_f32, n, vp, hp, vn, w, partial, counter, out));
+  __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED);
+  return BILU_OK;
+}
+
+int scale_rsqrt_f32(long long n, const float* x, const double* nrm2, float* y, cudaStream_t st) {
+  k_scale_rsqrt_f32<<<kRedCTAs, kRedThreads, 0, st>>>(n, x, nrm2, y);
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
+}
+
+int inner_lsq(int k, const double* H, const double* ww, double* y, cudaStream_t st) {
+  if (k < 1 || k > kMaxVec) return BILU_ERR_ARG;
+  k_inner_lsq<<<1, 32, 0, st>>>(k, H, ww, y);
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
+}
+
+int combine_f32(long long n, const float* Q, long long ldq, int k, const double* y, double* z,
+                cudaStream_t st) {
+  const int nv = k;
+  BILU_NV_CASES(launch_combine, n, Q, ldq, y, z, st);
+  BILU_LAUNCH_CHECK();
   return BILU_OK;
 }
 

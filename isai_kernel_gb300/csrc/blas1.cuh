@@ -38,4 +38,26 @@ int residual_norm(long long n, const double* b, const double* ax, double* r, dou
 int mgs_sweep(long long n, const double* vp, const double* hp, const double* vn, double* w,
               double* partial, unsigned* counter, double* out, cudaStream_t st);
 
+// ---- FP32 inner solver of the nested (GMRES-IR) mode ----
+// The same fused sweep on FP32 vectors (vp, vn, w float; h read as double
+// and rounded to FP32): FP32 products and per-thread FP32 sums, the warp
+// sums widened to FP64 and the CTA partials added in a fixed order, so the
+// dot products are reproducible run to run.  vn is read with an L2-keeping
+// load (it is the next sweep's vp), vp with an evict-first load.
+int mgs_sweep_f32(long long n, const float* vp, const double* hp, const float* vn, float* w,
+                  double* partial, unsigned* counter, double* out, cudaStream_t st);
+// y = x * (1/sqrt(*nrm2)) in FP32 (zeros when *nrm2 == 0).
+int scale_rsqrt_f32(long long n, const float* x, const double* nrm2, float* y, cudaStream_t st);
+// Least squares of the inner Arnoldi steps on the device (one thread): H
+// holds (k+1) x k entries H[i*k + j] with the raw column entries h_ij
+// (i <= j) and, in ww[j], ||w_j||^2 (the subdiagonal squared); Givens
+// rotations in FP64 reduce H to triangular form against beta e_1 (beta = 1)
+// and y[0..k) receives the solution (zeros beyond the first zero
+// subdiagonal, where the steps found an invariant subspace).
+int inner_lsq(int k, const double* H, const double* ww, double* y, cudaStream_t st);
+// z = sum_{i<k} y_i Q_i: FP32 products and sums (i ascending), widened to
+// FP64 (z is the outer flexible-GMRES direction).
+int combine_f32(long long n, const float* Q, long long ldq, int k, const double* y, double* z,
+                cudaStream_t st);
+
 }  // namespace bilu

@@ -174,6 +174,14 @@ struct bilu_ctx {
   cudaEvent_t ev = nullptr;
   unsigned* counter = nullptr;  // arrival counter of the MGS sweep reductions
   long long steps = 0, restarts = 0;  // Arnoldi steps and cycles of the last solve
+  // nested (GMRES-IR) mode: FP32 inner GMRES of inner_k steps per outer
+  // step; its basis U32 ((k+1) vectors, U32[0] = the outer basis vector in
+  // FP32), the preconditioned vectors Q32 (k), the working vector w32 and
+  // the small FP64 arrays (raw Hessenberg (k+1) x k, ||w||^2 per step, y)
+  int inner_k = 20, inner_alloc = 0;
+  long long inner_steps = 0;  // inner steps of the last solve
+  float *U32 = nullptr, *Q32 = nullptr, *w32 = nullptr;
+  double* inner_small = nullptr;
   std::vector<void*> setup_bufs;
   void free_setup() {
     for (void* p : setup_bufs) cudaFreeAsync(p, st);
@@ -192,8 +200,12 @@ struct bilu_ctx {
   }
   void free_solver() {
     for (void* p : {(void*)V, (void*)Z, (void*)w, (void*)r, (void*)tmp, (void*)v32, (void*)z32,
-                    (void*)partial, (void*)dscal, (void*)dcoef, (void*)counter})
+                    (void*)partial, (void*)dscal, (void*)dcoef, (void*)counter, (void*)U32,
+                    (void*)Q32, (void*)w32, (void*)inner_small})
       if (p) cudaFreeAsync(p, st);
+    U32 = Q32 = w32 = nullptr;
+    inner_small = nullptr;
+    inner_alloc = 0;
     v32 = nullptr;
     z32 = nullptr;
     counter = nullptr;
@@ -423,7 +435,8 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
     }
   }
   if (isai) {
-    const bool want32 = (prec_mask & ((1 << BILU_FP32) | (1 << BILU_FP32_INNER))) != 0;
+    const bool want32 =
+        (prec_mask & ((1 << BILU_FP32) | (1 << BILU_FP32_INNER) | (1 << BILU_NESTED))) != 0;
     BILU_TRY(build_isai_side(c, 1, ws, &c->Lrow, &c->Lcol, &c->Lval, &c->nnzL, &t_pat, &t_isai,
                              want32 ? &c->Lval32 : nullptr));
     BILU_TRY(build_isai_side(c, 0, ws, &c->Urow, &c->Ucol, &c->Uval, &c->nnzU, &t_pat, &t_isai,
@@ -440,7 +453,7 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
       BILU_TRY(spmv_layout_of(nb, bs, c->Urow, words, st, &c->spmv_layout[2]));
     }
   }
-  if (prec_mask & (1 << BILU_FP32_INNER)) {
+  if (prec_mask & ((1 << BILU_FP32_INNER) | (1 << BILU_NESTED))) {
     BILU_TRY(c->alloc(&c->Aval32, (size_t)nnzb * bs2));
     BILU_TRY(bilu_convert_f64_to_f32((size_t)nnzb * bs2, c->Aval, c->Aval32, st));
   }
@@ -569,13 +582,81 @@ bool mode_built(const bilu_ctx* c, int prec) {
     case BILU_ILU: return c->ilu_words != nullptr;
     case BILU_FP32_INNER: return c->Aval32 != nullptr;
     case BILU_ILU_FP32: return c->LU32 != nullptr;
+    case BILU_NESTED: return c->Aval32 != nullptr && c->Lval32 != nullptr;
     default: return false;
   }
 }
 
 // modes whose apply starts from the FP32 copy of the basis vector
 bool uses_v32(int prec) {
-  return prec == BILU_FP32 || prec == BILU_FP32_INNER || prec == BILU_ILU_FP32;
+  return prec == BILU_FP32 || prec == BILU_FP32_INNER || prec == BILU_ILU_FP32 ||
+         prec == BILU_NESTED;
+}
+
+// where the normalisation kernel writes that FP32 copy: the nested mode's
+// inner basis starts with it
+float* v32_of(bilu_ctx* c, int prec) {
+  if (!uses_v32(prec)) return nullptr;
+  return prec == BILU_NESTED ? c->U32 : c->v32;
+}
+
+int ensure_inner(bilu_ctx* c) {
+  const int k = c->inner_k;
+  if (c->inner_alloc >= k && c->U32) return BILU_OK;
+  for (void* p : {(void*)c->U32, (void*)c->Q32, (void*)c->w32, (void*)c->inner_small})
+    if (p) cudaFreeAsync(p, c->st);
+  c->U32 = c->Q32 = c->w32 = nullptr;
+  c->inner_small = nullptr;
+  c->inner_alloc = 0;
+  const size_t ld = (size_t)c->ldv;
+  BILU_TRY_CUDA(dev_alloc((void**)&c->U32, sizeof(float) * ld * (k + 1), c->dev, c->st));
+  BILU_TRY_CUDA(dev_alloc((void**)&c->Q32, sizeof(float) * ld * k, c->dev, c->st));
+  BILU_TRY_CUDA(dev_alloc((void**)&c->w32, sizeof(float) * ld, c->dev, c->st));
+  BILU_TRY_CUDA(dev_alloc((void**)&c->inner_small,
+                          sizeof(double) * ((size_t)(k + 1) * k + 2 * (size_t)k), c->dev, c->st));
+  c->inner_alloc = k;
+  return BILU_OK;
+}
+
+// The nested mode's preconditioner: inner_k steps of right-preconditioned
+// FP32 GMRES on A z = v from z = 0, with the FP32-stored A and ISAI, the
+// basis starting from u_0 = v in FP32 (U32[0], written by the kernel that
+// normalised v; v has unit norm, so beta = 1: flexible GMRES accepts any
+// scaling of z).  Every step: q_i = M_U (M_L u_i) into Q32[i], w = A q_i,
+// i + 2 fused FP32 Gram-Schmidt sweeps writing h_0i..h_ii and ||w||^2,
+// u_{i+1} = w / ||w||.  Then the Hessenberg least-squares problem on the
+// device and z = Q y widened to FP64.  Nothing waits on the host: the
+// whole inner solve is queued on the stream.
+int inner_solve(bilu_ctx* c, double* z) {
+  cudaStream_t st = c->st;
+  const long long n = c->n;
+  const size_t ld = (size_t)c->ldv;
+  const int k = c->inner_k;
+  double* H = c->inner_small;                // (k+1) x k, H[i*k + j]
+  double* ww = H + (size_t)(k + 1) * k;      // ||w_j||^2
+  double* y = ww + k;
+  float* t32 = reinterpret_cast<float*>(c->tmp);
+  for (int j = 0; j < k; ++j) {
+    const float* uj = c->U32 + ld * j;
+    float* qj = c->Q32 + ld * j;
+    BILU_TRY(spmv_any(c->nb, c->bs, BILU_FP32, c->Lrow, c->Lcol, c->Lval32, uj, 1, t32, 1, st,
+                      c->spmv_layout[1]));
+    BILU_TRY(spmv_any(c->nb, c->bs, BILU_FP32, c->Urow, c->Ucol, c->Uval32, t32, 1, qj, 1, st,
+                      c->spmv_layout[2]));
+    BILU_TRY(spmv_any(c->nb, c->bs, BILU_FP32, c->Arow, c->Acol, c->Aval32, qj, 1, c->w32, 1, st,
+                      c->spmv_layout[0]));
+    const float* U = c->U32;
+    BILU_TRY(mgs_sweep_f32(n, nullptr, nullptr, U, c->w32, c->partial, c->counter, H + j, st));
+    for (int i = 1; i <= j; ++i)
+      BILU_TRY(mgs_sweep_f32(n, U + ld * (i - 1), H + (size_t)(i - 1) * k + j, U + ld * i,
+                             c->w32, c->partial, c->counter, H + (size_t)i * k + j, st));
+    BILU_TRY(mgs_sweep_f32(n, U + ld * j, H + (size_t)j * k + j, nullptr, c->w32, c->partial,
+                           c->counter, ww + j, st));
+    if (j + 1 < k) BILU_TRY(scale_rsqrt_f32(n, c->w32, ww + j, c->U32 + ld * (j + 1), st));
+  }
+  BILU_TRY(inner_lsq(k, H, ww, y, st));
+  c->inner_steps += k;
+  return combine_f32(n, c->Q32, (long long)ld, k, y, z, st);
 }
 
 int apply_prec(bilu_ctx* c, int prec, const double* v, double* z) {
@@ -616,6 +697,7 @@ int apply_prec(bilu_ctx* c, int prec, const double* v, double* z) {
     BILU_TRY_CUDA(cudaMemcpyAsync(z, v, sizeof(double) * c->n, cudaMemcpyDeviceToDevice, c->st));
     return BILU_OK;
   }
+  if (prec == BILU_NESTED) return inner_solve(c, z);
   if (prec == BILU_FP32 || prec == BILU_FP32_INNER) {
     // v32 (written with v by the normalisation kernel) is the FP32 copy of v
     if (!c->Lval32 || !c->Uval32) return BILU_ERR_ARG;
@@ -661,8 +743,7 @@ int arnoldi_back(bilu_ctx* c, int j, int prec) {
                        c->counter, s + i, st));
   BILU_TRY(mgs_sweep(n, V + ld * j, s + j, nullptr, c->w, c->partial, c->counter,
                      s + kPartStride, st));
-  BILU_TRY(scale_rsqrt(n, c->w, s + kPartStride, c->V + ld * (j + 1), st,
-                       uses_v32(prec) ? c->v32 : nullptr));
+  BILU_TRY(scale_rsqrt(n, c->w, s + kPartStride, c->V + ld * (j + 1), st, v32_of(c, prec)));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->hpin, s, sizeof(double) * (kPartStride + 1),
                                 cudaMemcpyDeviceToHost, st));
   return BILU_OK;
@@ -676,10 +757,12 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
   if (!c || !c->ready || !d_b || !d_x || restart < 1 || restart > kMaxVec - 1 || maxit < 0)
     return BILU_ERR_ARG;
   if (prec != -1 && prec != BILU_FP64 && prec != BILU_FP32 && prec != BILU_ILU &&
-      prec != BILU_FP32_INNER && prec != BILU_ILU_FP32)
+      prec != BILU_FP32_INNER && prec != BILU_ILU_FP32 && prec != BILU_NESTED)
     return BILU_ERR_ARG;
   if (!mode_built(c, prec)) return BILU_ERR_ARG;  // the setup did not build this preconditioner
   BILU_TRY(ensure_solver(c, restart));
+  if (prec == BILU_NESTED) BILU_TRY(ensure_inner(c));
+  c->inner_steps = 0;
   cudaStream_t st = c->st;
   const bool ilu_mode = prec == BILU_ILU || prec == BILU_ILU_FP32;
   if (ilu_mode) BILU_TRY_CUDA(cudaMemsetAsync(c->ilu_words, 0, sizeof(unsigned) * 4, st));
@@ -706,8 +789,7 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
   if (res <= tol) status = BILU_OK;
   while (status != BILU_OK && total < maxit) {
     // V_0 = r / beta (beta^2 sits in s[5*kPartStride])
-    BILU_TRY(scale_rsqrt(n, c->r, s + 5 * kPartStride, c->V, st,
-                         uses_v32(prec) ? c->v32 : nullptr));
+    BILU_TRY(scale_rsqrt(n, c->r, s + 5 * kPartStride, c->V, st, v32_of(c, prec)));
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int jlast = -1;
@@ -782,6 +864,18 @@ extern "C" int bilu_ctx_stats(bilu_ctx* c, long long* h_out) {
   return BILU_OK;
 }
 
+extern "C" int bilu_ctx_set_inner(bilu_ctx* c, int k) {
+  if (!c || k < 1 || k > kMaxVec) return BILU_ERR_ARG;
+  c->inner_k = k;
+  return BILU_OK;
+}
+
+extern "C" int bilu_ctx_inner_steps(bilu_ctx* c, long long* h_steps) {
+  if (!c || !h_steps) return BILU_ERR_ARG;
+  *h_steps = c->inner_steps;
+  return BILU_OK;
+}
+
 // Preconditioner switch by measurement: up to `cycles` restart cycles (fewer
 // if it reaches tol) of the solve from x0 = 0 with every choice in `mask` (bits 1 << BILU_FP64 /
 // BILU_FP32 / BILU_ILU / BILU_FP32_INNER that the setup built), timed with
@@ -801,8 +895,11 @@ extern "C" int bilu_ctx_select(bilu_ctx* c, const double* d_b, int restart, int 
   std::vector<double> hist((size_t)restart * cycles + 1);
   int best = -1, rc = BILU_OK;
   double best_rate = -1.0;
-  // h_rate has an entry for BILU_ILU_FP32 only when the mask asks for it
-  const int nrate = (mask >> BILU_ILU_FP32) ? 5 : 4;
+  // h_rate has entries up to the highest choice the mask asks for (at
+  // least four)
+  int nrate = 4;
+  for (int p = BILU_ILU_FP32; p <= BILU_NESTED; ++p)
+    if (mask >> p) nrate = p + 1;
   for (int p = 0; p < nrate && rc == BILU_OK; ++p) {
     if (h_rate) h_rate[p] = 0.0;
     if (!(mask & (1 << p))) continue;

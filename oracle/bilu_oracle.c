@@ -709,11 +709,110 @@ static void isai_apply(const isai_apply_t* P, int precond, const double* v,
     orc_bcsr_spmv(P->nb, P->bs, P->Lrow, P->Lcol, P->Lval, v, P->y);
     orc_bcsr_spmv(P->nb, P->bs, P->Urow, P->Ucol, P->Uval, P->y, z);
   } else {
-    for (size_t i = 0; i < n; ++i) P->v32[i] = (float)v[i];
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)n; ++i) P->v32[i] = (float)v[i];
     orc_bcsr_spmv_f32(P->nb, P->bs, P->Lrow, P->Lcol, P->Lval32, P->v32, P->y32);
     orc_bcsr_spmv_f32(P->nb, P->bs, P->Urow, P->Ucol, P->Uval32, P->y32, P->z32);
-    for (size_t i = 0; i < n; ++i) z[i] = (double)P->z32[i];
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)n; ++i) z[i] = (double)P->z32[i];
   }
+}
+
+/* FP32 dot product: float products and float sums inside each chunk, the
+ * chunk sums added in double in chunk order (thread-count independent). */
+static double dot_chunked_f32(size_t n, const float* a, const float* b) {
+  size_t nch = (n + CHUNK - 1) / CHUNK;
+  double* part = (double*)malloc(sizeof(double) * (nch > 0 ? nch : 1));
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < (long)nch; ++c) {
+    size_t lo = (size_t)c * CHUNK, hi = lo + CHUNK < n ? lo + CHUNK : n;
+    float s = 0.0f;
+    for (size_t i = lo; i < hi; ++i) s += a[i] * b[i];
+    part[c] = (double)s;
+  }
+  double s = 0.0;
+  for (size_t c = 0; c < nch; ++c) s += part[c];
+  free(part);
+  return s;
+}
+
+/* Inner solve of the nested (GMRES-IR) mode: k steps of right-preconditioned
+ * GMRES in FP32 on A s = v, from s = 0, with the FP32-stored A and the
+ * FP32-stored ISAI (M = M_U M_L), modified Gram-Schmidt in FP32 (dot
+ * products as dot_chunked_f32), the Hessenberg least-squares problem in
+ * double.  v has unit norm (the outer basis vector), so the start vector is
+ * v rounded to FP32 with beta = 1: FGMRES accepts any scaling of its
+ * preconditioned vectors.  The preconditioned vectors q_i = M u_i are kept,
+ * and z = sum_i y_i q_i (FP32 accumulation, i ascending) widened to FP64.
+ * A zero subdiagonal entry (an invariant subspace) ends the steps early.
+ * Returns the number of steps taken. */
+typedef struct {
+  int nb, bs, k;
+  const int *Arow, *Acol, *Lrow, *Lcol, *Urow, *Ucol;
+  const float *A32, *L32, *U32;
+  float *Ub, *Qb, *w, *t;    /* (k+1) n, k n, n, n */
+  double *H, *cs, *sn, *g, *y;  /* (k+1) k, k, k, k+1, k */
+} inner_t;
+
+static int inner_gmres_f32(const inner_t* I, const double* v, double* z) {
+  const size_t n = (size_t)I->nb * I->bs;
+  const int k = I->k;
+  float* u0 = I->Ub;
+#pragma omp parallel for schedule(static)
+  for (long e = 0; e < (long)n; ++e) u0[e] = (float)v[e];
+  for (int i = 0; i <= k; ++i) I->g[i] = 0.0;
+  I->g[0] = 1.0;
+  int steps = 0;
+  for (int j = 0; j < k; ++j) {
+    float* uj = I->Ub + n * (size_t)j;
+    float* qj = I->Qb + n * (size_t)j;
+    orc_bcsr_spmv_f32(I->nb, I->bs, I->Lrow, I->Lcol, I->L32, uj, I->t);
+    orc_bcsr_spmv_f32(I->nb, I->bs, I->Urow, I->Ucol, I->U32, I->t, qj);
+    orc_bcsr_spmv_f32(I->nb, I->bs, I->Arow, I->Acol, I->A32, qj, I->w);
+    for (int i = 0; i <= j; ++i) {
+      const float* ui = I->Ub + n * (size_t)i;
+      double h = dot_chunked_f32(n, ui, I->w);
+      I->H[i * k + j] = h;
+      float hf = (float)h;
+#pragma omp parallel for schedule(static)
+      for (long e = 0; e < (long)n; ++e) I->w[e] -= hf * ui[e];
+    }
+    double hn = sqrt(dot_chunked_f32(n, I->w, I->w));
+    I->H[(j + 1) * k + j] = hn;
+    if (hn != 0.0) {
+      float inv = (float)(1.0 / hn);
+      float* un = I->Ub + n * (size_t)(j + 1);
+#pragma omp parallel for schedule(static)
+      for (long e = 0; e < (long)n; ++e) un[e] = I->w[e] * inv;
+    }
+    for (int i = 0; i < j; ++i) {
+      double a = I->H[i * k + j], c = I->H[(i + 1) * k + j];
+      I->H[i * k + j] = I->cs[i] * a + I->sn[i] * c;
+      I->H[(i + 1) * k + j] = -I->sn[i] * a + I->cs[i] * c;
+    }
+    double a = I->H[j * k + j], c = I->H[(j + 1) * k + j];
+    double den = sqrt(a * a + c * c);
+    I->cs[j] = den != 0.0 ? a / den : 1.0;
+    I->sn[j] = den != 0.0 ? c / den : 0.0;
+    I->H[j * k + j] = I->cs[j] * a + I->sn[j] * c;
+    I->H[(j + 1) * k + j] = 0.0;
+    I->g[j + 1] = -I->sn[j] * I->g[j];
+    I->g[j] = I->cs[j] * I->g[j];
+    steps = j + 1;
+    if (hn == 0.0) break;
+  }
+  for (int i = steps - 1; i >= 0; --i) {
+    double s = I->g[i];
+    for (int l = i + 1; l < steps; ++l) s -= I->H[i * k + l] * I->y[l];
+    I->y[i] = I->H[i * k + i] != 0.0 ? s / I->H[i * k + i] : 0.0;
+  }
+#pragma omp parallel for schedule(static)
+  for (long e = 0; e < (long)n; ++e) {
+    float s = 0.0f;
+    for (int i = 0; i < steps; ++i) s += (float)I->y[i] * I->Qb[n * (size_t)i + e];
+    z[e] = (double)s;
+  }
+  return steps;
 }
 
 /* Restarted right-preconditioned (F)GMRES(m):
@@ -730,9 +829,21 @@ int orc_gmres(int nb, int bs, const int* Arow, const int* Acol,
               const double* Uval, int precond, const double* b, double* x,
               int restart, double tol, int maxit, int* iters, double* relres,
               double* hist) {
+  return orc_gmres_ex(nb, bs, Arow, Acol, Aval, Lrow, Lcol, Lval, Urow, Ucol, Uval, precond, 0,
+                      b, x, restart, tol, maxit, iters, NULL, relres, hist);
+}
+
+int orc_gmres_ex(int nb, int bs, const int* Arow, const int* Acol,
+                 const double* Aval, const int* Lrow, const int* Lcol,
+                 const double* Lval, const int* Urow, const int* Ucol,
+                 const double* Uval, int precond, int inner_k, const double* b,
+                 double* x, int restart, double tol, int maxit, int* iters,
+                 long long* inner_total, double* relres, double* hist) {
   size_t n = (size_t)nb * bs;
   int m = restart;
   if (m < 1 || nb < 1) return ORC_ERR_ARG;
+  if (precond == 5 && inner_k < 1) return ORC_ERR_ARG;
+  long long inner_sum = 0;
   double* V = (double*)malloc(sizeof(double) * n * (size_t)(m + 1));
   double* Z = (double*)malloc(sizeof(double) * n * (size_t)m);
   double* w = (double*)malloc(sizeof(double) * n);
@@ -744,12 +855,12 @@ int orc_gmres(int nb, int bs, const int* Arow, const int* Acol,
   isai_apply_t P = {nb, bs, Lrow, Lcol, Urow, Ucol, Lval, Uval, NULL, NULL, NULL, NULL, NULL, NULL};
   float* A32 = NULL;
   if (precond >= 1) P.y = (double*)malloc(sizeof(double) * n);
-  if (precond == 4) {
+  if (precond == 4 || precond == 5) {
     size_t na = (size_t)Arow[nb] * bs * bs;
     A32 = (float*)malloc(sizeof(float) * na);
     for (size_t i = 0; i < na; ++i) A32[i] = (float)Aval[i];
   }
-  if (precond == 2 || precond == 4) {
+  if (precond == 2 || precond == 4 || precond == 5) {
     int nL = Lrow[nb], nU = Urow[nb];
     size_t bs2 = (size_t)bs * bs;
     P.Lval32 = (float*)malloc(sizeof(float) * nL * bs2);
@@ -759,6 +870,25 @@ int orc_gmres(int nb, int bs, const int* Arow, const int* Acol,
     P.v32 = (float*)malloc(sizeof(float) * n);
     P.y32 = (float*)malloc(sizeof(float) * n);
     P.z32 = (float*)malloc(sizeof(float) * n);
+  }
+  inner_t I;
+  memset(&I, 0, sizeof(I));
+  if (precond == 5) {
+    int k = inner_k;
+    I.nb = nb;
+    I.bs = bs;
+    I.k = k;
+    I.Arow = Arow; I.Acol = Acol; I.Lrow = Lrow; I.Lcol = Lcol; I.Urow = Urow; I.Ucol = Ucol;
+    I.A32 = A32; I.L32 = P.Lval32; I.U32 = P.Uval32;
+    I.Ub = (float*)malloc(sizeof(float) * n * (size_t)(k + 1));
+    I.Qb = (float*)malloc(sizeof(float) * n * (size_t)k);
+    I.w = (float*)malloc(sizeof(float) * n);
+    I.t = (float*)malloc(sizeof(float) * n);
+    I.H = (double*)calloc((size_t)(k + 1) * k, sizeof(double));
+    I.cs = (double*)calloc((size_t)k, sizeof(double));
+    I.sn = (double*)calloc((size_t)k, sizeof(double));
+    I.g = (double*)calloc((size_t)k + 1, sizeof(double));
+    I.y = (double*)calloc((size_t)k, sizeof(double));
   }
   for (size_t i = 0; i < n; ++i) x[i] = 0.0;
   double bnorm = sqrt(dot_chunked(n, b, b));
@@ -771,20 +901,26 @@ int orc_gmres(int nb, int bs, const int* Arow, const int* Acol,
   if (res <= tol) status = ORC_OK;
   while (status != ORC_OK && total < maxit) {
     double binv = 1.0 / beta;
-    for (size_t i = 0; i < n; ++i) V[i] = r[i] * binv;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)n; ++i) V[i] = r[i] * binv;
     for (int i = 0; i <= m; ++i) g[i] = 0.0;
     g[0] = beta;
     int jlast = -1;
     for (int j = 0; j < m && total < maxit; ++j) {
       double* vj = V + n * (size_t)j;
       double* zj = Z + n * (size_t)j;
-      isai_apply(&P, precond == 4 ? 2 : precond, vj, zj, n);
+      if (precond == 5)
+        inner_sum += inner_gmres_f32(&I, vj, zj);
+      else
+        isai_apply(&P, precond == 4 ? 2 : precond, vj, zj, n);
       if (precond == 4) {
         /* FP32-stored A in the Arnoldi product: z rounded to FP32, FP32
          * accumulation, result widened to FP64 */
-        for (size_t i = 0; i < n; ++i) P.v32[i] = (float)zj[i];
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < (long)n; ++i) P.v32[i] = (float)zj[i];
         orc_bcsr_spmv_f32(nb, bs, Arow, Acol, A32, P.v32, P.y32);
-        for (size_t i = 0; i < n; ++i) w[i] = (double)P.y32[i];
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < (long)n; ++i) w[i] = (double)P.y32[i];
       } else {
         orc_bcsr_spmv(nb, bs, Arow, Acol, Aval, zj, w);
       }
@@ -801,7 +937,8 @@ int orc_gmres(int nb, int bs, const int* Arow, const int* Acol,
       double* vn = V + n * (size_t)(j + 1);
       if (hn != 0.0) {
         double inv = 1.0 / hn;
-        for (size_t e = 0; e < n; ++e) vn[e] = w[e] * inv;
+#pragma omp parallel for schedule(static)
+        for (long e = 0; e < (long)n; ++e) vn[e] = w[e] * inv;
       }
       for (int i = 0; i < j; ++i) {
         double a = H[i * m + j], c = H[(i + 1) * m + j];
@@ -834,16 +971,20 @@ int orc_gmres(int nb, int bs, const int* Arow, const int* Acol,
       x[e] = s;
     }
     orc_bcsr_spmv(nb, bs, Arow, Acol, Aval, x, w);
-    for (size_t e = 0; e < n; ++e) r[e] = b[e] - w[e];
+#pragma omp parallel for schedule(static)
+    for (long e = 0; e < (long)n; ++e) r[e] = b[e] - w[e];
     beta = sqrt(dot_chunked(n, r, r));
     res = beta / bnorm;
     if (res <= tol) status = ORC_OK;
     if (beta == 0.0) break;
   }
   if (iters) *iters = total;
+  if (inner_total) *inner_total = inner_sum;
   if (relres) *relres = res;
   free(V); free(Z); free(w); free(r); free(H); free(cs); free(sn); free(g); free(yv); free(hcol);
   free(P.y); free(P.Lval32); free(P.Uval32); free(P.v32); free(P.y32); free(P.z32);
   free(A32);
+  free(I.Ub); free(I.Qb); free(I.w); free(I.t); free(I.H); free(I.cs); free(I.sn); free(I.g);
+  free(I.y);
   return status;
 }

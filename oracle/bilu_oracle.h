@@ -131,6 +131,18 @@ int orc_gmres(int nb, int bs, const int* Arow, const int* Acol,
               const double* Uval, int precond, const double* b, double* x,
               int restart, double tol, int maxit, int* iters, double* relres,
               double* hist);
+/* The same with precond 5, the nested (GMRES-IR) mode: each z_j of the FP64
+ * outer FGMRES is inner_k steps of FP32 right-preconditioned GMRES on
+ * A z = v_j from z = 0 (FP32-stored A, FP32-stored ISAI, FP32 modified
+ * Gram-Schmidt, Hessenberg least squares in double); the outer residuals,
+ * orthogonalisation and true residual at every restart stay FP64.
+ * inner_total (optional) receives the number of inner steps taken. */
+int orc_gmres_ex(int nb, int bs, const int* Arow, const int* Acol,
+                 const double* Aval, const int* Lrow, const int* Lcol,
+                 const double* Lval, const int* Urow, const int* Ucol,
+                 const double* Uval, int precond, int inner_k, const double* b,
+                 double* x, int restart, double tol, int maxit, int* iters,
+                 long long* inner_total, double* relres, double* hist);
 
 #ifdef __cplusplus
 }

@@ -292,6 +292,25 @@ def gmres(A, L, U, b, precond=1, restart=30, tol=1e-10, maxit=3000):
     return x, it.value, rr.value, hist[: it.value + 1], st
 
 
+def gmres_nested(A, L, U, b, inner=30, restart=30, tol=1e-10, maxit=3000):
+    """FP64 outer FGMRES(restart) whose preconditioner is `inner` steps of FP32
+    ISAI-preconditioned GMRES on the FP32-stored A (the nested, GMRES-IR mode;
+    no counterpart in the reference).  Returns (x, outer iterations, inner
+    steps in total, relres, history, status)."""
+    nb = A[0].shape[0] - 1
+    bs = A[2].shape[1]
+    x = np.zeros(nb * bs)
+    it, rr, tot = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_longlong(0)
+    hist = np.zeros(maxit + 1)
+    f = lib().orc_gmres_ex
+    f.restype = ctypes.c_int
+    st = f(nb, bs, _ptr(_i(A[0])), _ptr(_i(A[1])), _ptr(_d(A[2])), _ptr(_i(L[0])),
+           _ptr(_i(L[1])), _ptr(_d(L[2])), _ptr(_i(U[0])), _ptr(_i(U[1])), _ptr(_d(U[2])),
+           5, inner, _ptr(_d(b)), _ptr(x), restart, ctypes.c_double(tol), maxit,
+           ctypes.byref(it), ctypes.byref(tot), ctypes.byref(rr), _ptr(hist))
+    return x, it.value, tot.value, rr.value, hist[: it.value + 1], st
+
+
 def isai_setup(A, level=1):
     """Full oracle setup on a BSRMatrix: BILU(0), patterns, pairs, Dinv,
     ISAI-L/U and BCSR reorder.  level k > 1: ISAI(k), the M patterns taken

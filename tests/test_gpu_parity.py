@@ -850,3 +850,39 @@ def test_solve_host_end_to_end(cuda, orc):
     assert res.converged
     r = b - A.to_dense() @ x
     assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.01e-10
+
+
+@pytest.mark.parametrize("name,inner", [("c1_s16", 10), ("c2_s6", 20), ("c3_nb200", 20),
+                                        ("bs5_s7", 8)])
+def test_gmres_nested_matches_oracle(cuda, orc, name, inner):
+    """BILU_NESTED (GMRES-IR): FP64 flexible outer GMRES(30) whose every
+    preconditioned vector is `inner` steps of FP32 ISAI-preconditioned GMRES
+    on the FP32-stored A.  The FP32 inner arithmetic differs from the
+    oracle's in rounding only (fused multiply-adds, summation order), so the
+    outer iteration count is within 1 of the oracle's nested mode; the FP64
+    true residual reaches 1e-10 and x is within 1e-8 of the oracle's FP64
+    GMRES solution.  Two solves in a row give the same x bit for bit."""
+    from isai_kernel_gb300 import api
+
+    A = mats()[name]
+    S = orc.isai_setup(A)
+    b = gen.rhs(A.n, 0)
+    Ab = (A.rowptr, A.colind, A.val)
+    Lo = (S["TrowL"], S["TcolL"], S["McsrL"])
+    Uo = (S["TrowU"], S["TcolU"], S["McsrU"])
+    x64, _, _, _, st64 = orc.gmres(Ab, Lo, Uo, b, precond=1, maxit=3000)
+    xo, ito, inno, rro, _, st = orc.gmres_nested(Ab, Lo, Uo, b, inner=inner, maxit=300)
+    assert st == 0 and st64 == 0
+    p = api.Preconditioner(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda),
+                           nested=True, inner=inner)
+    x, res = p.solve(T(b, cuda), prec=api.BILU_NESTED, maxit=300)
+    assert res.converged and res.relres <= 1e-10
+    assert abs(res.iters - ito) <= 1, (res.iters, ito)
+    assert res.inner_steps == res.iters * inner
+    assert relerr(N(x), x64) < 1e-8 and relerr(N(x), xo) < 1e-8
+    x2, res2 = p.solve(T(b, cuda), prec=api.BILU_NESTED, maxit=300)
+    assert res2.iters == res.iters and np.array_equal(N(x2), N(x))
+    r = b - A.to_dense() @ N(x) if A.n <= 4096 else None
+    if r is not None:
+        assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.01e-10
+    p.close()

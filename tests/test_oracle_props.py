@@ -101,12 +101,40 @@ def test_gmres_c1_iterations_deterministic(orc):
     assert st == 0 and rr <= 1e-10
     r = b - A.to_dense() @ x
     assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.01e-10
+    cores = orc.num_threads()
     orc.set_threads(1)
     x1, it1, rr1, _, _ = orc.gmres(Ab, L, U, b, precond=1, maxit=2000)
-    orc.set_threads(0)
+    orc.set_threads(cores)
     assert it1 == it and np.array_equal(x1, x)  # chunked reductions: thread-count independent
     x2, it2, rr2, _, st2 = orc.gmres(Ab, L, U, b, precond=2, maxit=2000)
     assert st2 == 0 and abs(it2 - it) <= 2
+
+
+def test_gmres_nested_oracle(orc):
+    """The nested (GMRES-IR) mode: FP64 outer FGMRES(30) over k-step FP32
+    inner GMRES solves.  It reaches the FP64 true residual 1e-10, its x is
+    within 1e-8 of the FP64 GMRES solution, it is thread-count independent,
+    and on the 64 x 64 Laplacian it needs far fewer inner steps in total than
+    restarted GMRES(30) needs iterations (1111): the outer space keeps what
+    each restart of the flat solver throws away."""
+    A = gen.laplace2d(64, bs=4, seed=0)
+    S = orc.isai_setup(A)
+    b = gen.rhs(A.n, 0)
+    Ab = (A.rowptr, A.colind, A.val)
+    L = (S["TrowL"], S["TcolL"], S["McsrL"])
+    U = (S["TrowU"], S["TcolU"], S["McsrU"])
+    x64, it64, _, _, st64 = orc.gmres(Ab, L, U, b, precond=1, maxit=3000)
+    assert st64 == 0 and it64 == 1111
+    x, it, inner, rr, hist, st = orc.gmres_nested(Ab, L, U, b, inner=20, maxit=300)
+    assert st == 0 and rr <= 1e-10 and inner == 20 * it and inner < it64 / 2
+    r = b - orc.bcsr_spmv(A.nb, A.bs, A.rowptr, A.colind, A.val, x)
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.01e-10
+    assert np.max(np.abs(x - x64)) / np.max(np.abs(x64)) < 1e-8
+    cores = orc.num_threads()
+    orc.set_threads(1)
+    x1, it1, inner1, _, _, _ = orc.gmres_nested(Ab, L, U, b, inner=20, maxit=300)
+    orc.set_threads(cores)
+    assert it1 == it and inner1 == inner and np.array_equal(x1, x)
 
 
 def test_dinv_singular_retry(orc):
