@@ -3,22 +3,29 @@ convection-diffusion system (BSR 4x4, 2,097,152 block rows, 14,581,760
 blocks, FP64 matrix), synthetic seeded data.
 
 A step is one solve to 1e-10 relative residual from x0 = 0 with the
-mixed-precision path (FP32-stored ISAI inside FP64 flexible GMRES(30) with
-FP64 residuals, orthogonalisation and restarts); the preconditioner setup
+mixed-precision path: FP64 flexible GMRES(30) (FP64 residuals,
+orthogonalisation and true residual at every restart) whose preconditioned
+vectors are --inner steps of FP32 GMRES with the FP32-stored ISAI and the
+FP32-stored A (the nested, GMRES-IR form).  The preconditioner setup
 (BILU(0) + ISAI on the GPU) runs once before the timed region and is
-reported separately, as are the plain FP64 ISAI path, the FP32-operator
-variant (`fp32_inner`) and GMRES with the exact BILU(0) applied by
-level-scheduled triangular solves (`exact_ilu`).  `value` is the mean solve
-time (s) with the matrix resident in HBM (1.9 GB of values, larger than L2).
+reported separately, as are the plain FP64 ISAI path (the denominator of
+`speedup_mixed_vs_fp64`), the FP32 apply inside flat FGMRES (`fp32_apply`),
+the FP32-operator flat variant (`fp32_inner`), other inner lengths
+(`nested_inner_scan`) and GMRES with the exact BILU(0) applied by
+level-order triangular solves (`exact_ilu`).  `value` is the mean solve time
+(s) with the matrix resident in HBM (1.9 GB of values, larger than L2).
 `e2e` is the same metric through the C ABI call with host buffers
-(bilu_solve_host: H2D of A and b, setup, solve, D2H of x).  `roofline`
-rates the FP32 apply as the solver launches it (two k_bsr_spmv, FP32 basis
-vector in) against the measured copy bandwidth; `traffic` is the DRAM bytes
-of the same launches from the committed ncu capture.  `cpu_baseline` is the
-oracle on the host cores, plus the serial (one core) BILU(0) and triangular
-solves.  Secondary lines: --workload sptrsv | powerlaw | batch.
+(bilu_solve_host: H2D of A and b, setup, solve, D2H of x), the first call
+of the process.  `roofline` rates the FP32 apply as the inner solver
+launches it (two k_bsr_spmv, FP32 vectors in and out) against the measured
+copy bandwidth; `traffic` is the DRAM bytes of the same launches from the
+committed ncu capture.  `errors` states each mixed-precision result against
+the FP64 oracle.  `cpu_baseline` is the oracle's full nested solve on the
+host cores (measured, one solve), plus serial (one core) times.
+`--impl reference` times the oracle's solve of the same system in every
+step.  Secondary lines: --workload sptrsv | powerlaw | batch.
 
-    python bench.py [--steps K] [--warmup W] [--side 128] [--impl reference]
+    python bench.py [--steps K] [--warmup W] [--side 128] [--inner 20] [--impl reference]
     torchrun --nproc-per-node N bench.py --gpus N   (N independent replicas)
 """
 from __future__ import annotations
@@ -40,10 +47,6 @@ sys.path.insert(0, ROOT)
 
 METRIC = "time to 1e-10 rel. residual, mixed vs FP64 BILU-ISAI; precond-apply HBM GB/s"
 FALLBACK_HBM_GBS = 6800.0
-# FP64 and mixed iteration counts of the 128^3 system measured on GB300 with
-# this code (the FP64 count equals the oracle's at every size the oracle can
-# finish); used to scale the CPU baseline's per-iteration cost.
-C2_ITERS_REF = {"fp64": 328, "mixed": 328}
 
 
 def parse():
@@ -57,7 +60,8 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--maxit", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-iters", type=int, default=3)
+    ap.add_argument("--inner", type=int, default=20,
+                    help="inner FP32 GMRES steps per outer step of the nested mode")
     ap.add_argument("--workload", default="convdiff",
                     choices=["convdiff", "batch", "powerlaw", "sptrsv"],
                     help="convdiff: the headline line; batch / powerlaw / sptrsv: secondary lines")
@@ -141,23 +145,14 @@ def apply_bytes(nb, bs, nnzL, nnzU, s_val, s_tmp):
     return (nnzL + nnzU) * (bs * bs * s_val + 4) + 2 * (nb + 1) * 4 + n * (8 + 2 * s_tmp + 8)
 
 
-def apply_bytes_staged(nb, bs, nnzL, nnzU):
-    """Algorithmic bytes of the FP32 apply as the solver runs it (input is
-    the FP32 copy of the basis vector written by the normalisation): FP32
-    values + column indices, row pointers, read x32, write and read y32,
-    write z (FP64)."""
-    n = nb * bs
-    return (nnzL + nnzU) * (bs * bs * 4 + 4) + 2 * (nb + 1) * 4 + n * (4 + 2 * 4 + 8)
-
-
 def measured_traffic(side):
-    """DRAM bytes per FP32 apply from the committed ncu summary of the same
-    workload (profiles/roofline_traffic.json), or None."""
+    """DRAM bytes per inner FP32 apply from the committed ncu summary of the
+    same launches (profiles/roofline_traffic.json), or None."""
     p = os.path.join(ROOT, "profiles", "roofline_traffic.json")
     if not os.path.exists(p):
         return None, None
     d = json.load(open(p))
-    if d.get("side") != side:
+    if d.get("side") != side or d.get("form") != "inner":
         return None, None
     return float(d["dram_bytes_per_apply"]), d.get("source")
 
@@ -165,6 +160,20 @@ def measured_traffic(side):
 def spmv_bytes(nb, bs, nnzb):
     n = nb * bs
     return nnzb * (bs * bs * 8 + 4) + (nb + 1) * 4 + 2 * n * 8
+
+
+def spmv_bytes_f32(nb, bs, nnzb):
+    """FP32 values, FP32 vectors (the inner solver's operator product)."""
+    n = nb * bs
+    return nnzb * (bs * bs * 4 + 4) + (nb + 1) * 4 + 2 * n * 4
+
+
+def apply_bytes_inner(nb, bs, nnzL, nnzU):
+    """Algorithmic bytes of the FP32 apply as the inner solver runs it:
+    FP32 values + column indices of both factors, both row pointers, read
+    u (FP32), write and read the intermediate (FP32), write q (FP32)."""
+    n = nb * bs
+    return (nnzL + nnzU) * (bs * bs * 4 + 4) + 2 * (nb + 1) * 4 + n * 4 * 4
 
 
 def dist_init(args):
@@ -197,33 +206,62 @@ def max_over_ranks(v, world):
     return float(t.item())
 
 
-# ---------------------------------------------------------------- CPU baseline
-def cpu_baseline(side, iters_full, gmres_iters=3, seed=0):
-    """The oracle (plain-C restatement of the reference path, OpenMP over the
-    host cores) on the full system: the whole setup (BILU(0), patterns,
-    pairs, Dinv, ISAI-L/U, reorder) plus `gmres_iters` FGMRES iterations with
-    the FP32-stored ISAI; time to solution = setup + per-iteration cost x
-    the solver's iteration count for this system."""
+# ---------------------------------------------------------------- workload
+def convdiff_system(side):
     from isai_kernel_gb300 import gen
+
+    A = gen.convdiff3d(side, bs=4, seed=0)
+    return A, gen.rhs(A.n, 0)
+
+
+def workload_config(args, A):
+    """The config dict both arms print (identical by construction)."""
+    return {"workload": f"convdiff3d {args.side}^3 bs4 (nb={A.nb}, nnzb={A.nnzb}), "
+                        f"FGMRES({args.restart}) to {args.tol:g} from x0 = 0, nested mixed "
+                        f"precision: FP64 outer, FP32 inner GMRES({args.inner}) with FP32-stored "
+                        f"ISAI and A; setup outside the timed step",
+            "nb": A.nb, "nnzb": A.nnzb, "restart": args.restart, "inner": args.inner,
+            "tol": args.tol, "parallelism": "single GPU" if args.gpus <= 1 else
+            f"replicas x{args.gpus}",
+            "l2": "inputs larger than L2 (1.87 GB of FP64 values)"}
+
+
+# ---------------------------------------------------------------- CPU baseline
+def oracle_parts(A):
     from oracle import oracle
 
-    A = gen.convdiff3d(side, bs=4, seed=seed)
-    b = gen.rhs(A.n, seed)
     t0 = time.perf_counter()
     S = oracle.isai_setup(A)
     t_setup = time.perf_counter() - t0
     Ab = (A.rowptr, A.colind, A.val)
     L = (S["TrowL"], S["TcolL"], S["McsrL"])
     U = (S["TrowU"], S["TcolU"], S["McsrU"])
+    return S, Ab, L, U, t_setup
+
+
+def cpu_solve(A, b, parts, args, maxit=None):
+    """One oracle solve of the headline algorithm (nested mode) from x0 = 0,
+    timed on the host: (seconds, x, outer iterations, inner steps, relres)."""
+    from oracle import oracle
+
+    _, Ab, L, U, _ = parts
     t0 = time.perf_counter()
-    _, it, _, _, _ = oracle.gmres(Ab, L, U, b, precond=2, restart=30, maxit=gmres_iters)
-    t_it = (time.perf_counter() - t0) / max(it, 1)
-    est = t_setup + t_it * iters_full
+    x, it, inner, rr, _, st = oracle.gmres_nested(Ab, L, U, b, inner=args.inner,
+                                                  restart=args.restart, tol=args.tol,
+                                                  maxit=maxit or args.maxit)
+    return time.perf_counter() - t0, x, it, inner, rr, st
+
+
+def cpu_baseline(A, b, parts, args):
+    """The oracle (plain-C restatement of the path, OpenMP over the host
+    cores): one full nested solve to 1e-10 of the same system, measured
+    (not extrapolated), the setup measured beside it, and the serial (one
+    core) BILU(0), ISAI setup, applies and triangular solves."""
+    from oracle import oracle
+
+    S, Ab, L, U, t_setup = parts
+    t, x, it, inner, rr, st = cpu_solve(A, b, parts, args)
     cores = oracle.num_threads()
-    # the serial CPU path on one core: BILU(0), the whole ISAI setup (BILU(0)
-    # again, patterns, pairs, Dinv, ISAI-L/U, reorder), one FP64 and one
-    # FP32-stored apply, the two triangular solves (the reference has no CPU
-    # ILU / ISAI / SpTRSV; its GPU kernels are the restated algorithms)
     oracle.set_threads(1)
     try:
         t0 = time.perf_counter()
@@ -235,6 +273,7 @@ def cpu_baseline(side, iters_full, gmres_iters=3, seed=0):
         t0 = time.perf_counter()
         oracle.sptrsv_upper(A.nb, A.bs, A.rowptr, A.colind, LU, y)
         t_u1 = time.perf_counter() - t0
+        del LU
         t0 = time.perf_counter()
         oracle.isai_setup(A)
         t_s1 = time.perf_counter() - t0
@@ -249,43 +288,70 @@ def cpu_baseline(side, iters_full, gmres_iters=3, seed=0):
         t_a32 = time.perf_counter() - t0
     finally:
         oracle.set_threads(cores)
-    return {"value": est, "unit": "s", "cores": cores, "kind": "port",
-            "sample": (f"oracle on the full {side}^3 system: setup {t_setup:.2f} s measured, "
-                       f"{it} FGMRES(30) iterations measured at {t_it:.3f} s each, scaled to "
-                       f"{iters_full} iterations"),
-            "setup_s": t_setup, "per_iter_s": t_it,
+    return {"value": t, "unit": "s", "cores": cores, "kind": "port",
+            "sample": (f"the oracle's nested solve to {args.tol:g} of the full {args.side}^3 "
+                       f"system, measured once ({it} outer / {inner} inner steps, relres "
+                       f"{rr:.3g}); its setup measured separately ({t_setup:.2f} s)"),
+            "setup_s": t_setup, "iters": it, "inner_steps": inner, "relres": rr, "status": st,
             "serial_1_core": {"bilu0_s": t_f1, "isai_setup_s": t_s1, "apply_fp64_s": t_a64,
-                              "apply_fp32_s": t_a32, "sptrsv_L_s": t_l1, "sptrsv_U_s": t_u1}}
+                              "apply_fp32_s": t_a32, "sptrsv_L_s": t_l1, "sptrsv_U_s": t_u1},
+            "_x": x}
 
 
 def run_reference(args):
+    """The reference arm: the reference has no GPU solver and no Krylov
+    method, so its CPU implementation of the path is the oracle (the plain-C
+    restatement), run on the host cores with every thread, on the same
+    system and algorithm as the GPU arm.  Setup once (reported, outside the
+    steps, as on the GPU); every timed step is a full solve to the
+    tolerance; warm-up steps run one outer step each (untimed)."""
     rank, world = dist_init(args)
     if rank != 0:
         return
-    iters = C2_ITERS_REF["mixed"] or 700
-    vals = []
-    for i in range(args.warmup + args.steps):
-        r = cpu_baseline(args.side, iters, gmres_iters=args.cpu_iters)
-        if i >= args.warmup:
-            vals.append(r)
-    v = statistics.mean(r["value"] for r in vals)
+    from oracle import oracle
+
+    A, b = convdiff_system(args.side)
+    parts = oracle_parts(A)
+    for _ in range(args.warmup):
+        cpu_solve(A, b, parts, args, maxit=1)
+    times, its = [], []
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        t, x, it, inner, rr, st = cpu_solve(A, b, parts, args)
+        times.append(t)
+        its.append((it, inner, rr, st))
+    wall = time.perf_counter() - t_wall
+    v = statistics.mean(times)
+    it, inner, rr, st = its[-1]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3,
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded 128^3 convection-diffusion, BSR 4x4)",
-            "config": {"workload": f"convdiff3d {args.side}^3 bs4, FGMRES(30) tol 1e-10, mixed",
-                       "n": args.side ** 3 * 4},
-            "cpu_baseline": {"value": v, "unit": "s", "cores": vals[0]["cores"], "kind": "port",
-                             "sample": vals[0]["sample"]},
-            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64+f32",
+            "data": "synthetic (seeded 128^3 7-point convection-diffusion, 4 DOF, BSR 4x4)",
+            "config": workload_config(args, A),
+            "iters": {"outer": it, "inner": inner}, "relres": rr, "status": st,
+            "setup_s": parts[4], "step_s": times,
+            "cpu_baseline": {"value": v, "unit": "s", "cores": oracle.num_threads(),
+                             "kind": "port",
+                             "sample": (f"every timed step is the oracle's full nested solve to "
+                                        f"{args.tol:g} of the {args.side}^3 system on "
+                                        f"{oracle.num_threads()} threads; warm-up steps run "
+                                        f"one outer step each; setup {parts[4]:.2f} s once")},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
     print(json.dumps(line))
 
 
 # ---------------------------------------------------------------- GPU arm
+def relerr(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+
+
 def run_ours(args):
     import torch
 
-    from isai_kernel_gb300 import _lib, api, gen
+    from isai_kernel_gb300 import _lib, api
 
     rank, world = dist_init(args)
     local = int(os.environ.get("LOCAL_RANK", 0))
@@ -294,8 +360,7 @@ def run_ours(args):
     L = _lib.lib()
     stream = torch.cuda.current_stream()
 
-    A = gen.convdiff3d(args.side, bs=4, seed=0)
-    b_np = gen.rhs(A.n, 0)
+    A, b_np = convdiff_system(args.side)
     nb, bs, nnzb, n = A.nb, A.bs, A.nnzb, A.n
     row = torch.from_numpy(A.rowptr).to(dev)
     col = torch.from_numpy(A.colind).to(dev)
@@ -303,15 +368,18 @@ def run_ours(args):
     b = torch.from_numpy(b_np).to(dev)
     torch.cuda.synchronize()
 
-    P = api.Preconditioner(nb, bs, row, col, val, fp32=True, fp32_inner=True)
+    P = api.Preconditioner(nb, bs, row, col, val, fp32=True, fp32_inner=True, nested=True,
+                           inner=args.inner)
     setup_ms = P.setup_ms
     x = torch.empty_like(b)
+    NESTED = api.BILU_NESTED
 
-    def solve(prec):
-        return P.solve(b, x, prec=prec, restart=args.restart, tol=args.tol, maxit=args.maxit)
+    def solve(prec, out=None):
+        return P.solve(b, x if out is None else out, prec=prec, restart=args.restart,
+                       tol=args.tol, maxit=args.maxit)
 
     for _ in range(args.warmup):
-        _, res = solve(1)
+        _, res = solve(NESTED)
     barrier(world)
     torch.cuda.synchronize()
     clocks = Clocks(local)
@@ -321,44 +389,52 @@ def run_ours(args):
     for _ in range(args.steps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        _, res = solve(1)
+        _, res = solve(NESTED)
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
-        iters.append(res.iters)
+        iters.append((res.iters, res.inner_steps))
     torch.cuda.synchronize()
     barrier(world)
     wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     launches = L.bilu_kernel_launches() - l0
-    relres_mixed = res.relres
-    restarts_mixed = res.restarts
+    res_mixed = res
+    x_nested = x.cpu().numpy().copy()
     t_mixed = max_over_ranks(statistics.mean(times), world)
 
-    # plain FP64 path (reported beside the headline)
-    _, r64 = solve(0)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    _, r64 = solve(0)
-    e1.record(stream)
-    e1.synchronize()
-    t_fp64 = e0.elapsed_time(e1) / 1e3
+    def timed(prec, out=None):
+        solve(prec, out)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, r = solve(prec, out)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3, r
 
-    # FP32 ISAI plus FP32-stored A in the Arnoldi products (FP64
-    # orthogonalisation, true residuals and restarts), reported beside
-    _, r32i = solve(3)
-    e0.record(stream)
-    _, r32i = solve(3)
-    e1.record(stream)
-    e1.synchronize()
-    t_f32i = e0.elapsed_time(e1) / 1e3
+    # plain FP64 path: the denominator of the mixed-precision speed-up
+    x64 = torch.empty_like(b)
+    t_fp64, r64 = timed(api.BILU_FP64, x64)
+    # FP32-stored ISAI apply inside flat FP64 FGMRES(30) (FP64 Arnoldi products)
+    x32a = torch.empty_like(b)
+    t_f32, r32 = timed(api.BILU_FP32, x32a)
+    # FP32 ISAI plus FP32-stored A in the Arnoldi products of the flat solver
+    t_f32i, r32i = timed(api.BILU_FP32_INNER)
+    # the nested mode at other inner lengths (the headline uses --inner)
+    inner_scan = {}
+    for k in sorted({10, 16, 20, 24, 30} - {args.inner}):
+        P.set_inner(k)
+        t_k, r_k = timed(NESTED)
+        inner_scan[str(k)] = {"s": t_k, "outer": r_k.iters, "inner": r_k.inner_steps,
+                              "relres": r_k.relres}
+    P.set_inner(args.inner)
 
-    # exact BILU(0) preconditioner (two level-scheduled triangular solves
-    # per apply), FP64: reported beside the ISAI paths
+    # exact BILU(0) preconditioner (two level-order triangular solves per apply)
     Pi = api.Preconditioner(nb, bs, row, col, val, fp32=False, ilu=True)
     xi = torch.empty_like(b)
     _, ri = Pi.solve(b, xi, prec=api.BILU_ILU, restart=args.restart, tol=args.tol,
                      maxit=args.maxit)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     _, ri = Pi.solve(b, xi, prec=api.BILU_ILU, restart=args.restart, tol=args.tol,
                      maxit=args.maxit)
@@ -368,7 +444,6 @@ def run_ours(args):
     ilu_setup = Pi.setup_ms["total"]
     Pi.close()
     del Pi
-    # the same with the triangular solves in FP32 on an FP32 copy of the factor
     Pf = api.Preconditioner(nb, bs, row, col, val, fp32=False, ilu_fp32=True)
     _, rf = Pf.solve(b, xi, prec=api.BILU_ILU_FP32, restart=args.restart, tol=args.tol,
                      maxit=args.maxit)
@@ -382,8 +457,8 @@ def run_ours(args):
     Pf.close()
     del Pf, xi
 
-    # preconditioner apply kernels, timed alone with CUDA events on the
-    # launching stream (inputs: 1.1-1.9 GB of factors, larger than L2)
+    # kernels timed alone with CUDA events on the launching stream (inputs:
+    # 1.1-1.9 GB of factors, larger than L2)
     lu, Lf, Uf = P.factors()
     nnzL, nnzU = int(Lf[1].numel()), int(Uf[1].numel())
     L32, U32 = P.get(7).view(-1, bs, bs), P.get(8).view(-1, bs, bs)
@@ -403,86 +478,121 @@ def run_ours(args):
     t_apply64 = time_it(lambda: api.isai_apply(nb, bs, Lf, Uf, b, prec=0), reps)
     t_apply32 = time_it(lambda: api.isai_apply(nb, bs, (Lf[0], Lf[1], L32), (Uf[0], Uf[1], U32),
                                                b, prec=1), reps)
-    # the apply as the solver launches it: two k_bsr_spmv, FP32 input and
-    # intermediate, FP64 output
+    # the apply as the inner solver launches it: two k_bsr_spmv, FP32 in,
+    # FP32 intermediate, FP32 out
     b32 = b.float()
     y32 = torch.empty(n, dtype=torch.float32, device=dev)
-    z = torch.empty_like(b)
+    q32 = torch.empty(n, dtype=torch.float32, device=dev)
+    w32 = torch.empty(n, dtype=torch.float32, device=dev)
+    A32 = val.float()
 
-    def apply_staged():
+    def apply_inner():
         L.bilu_bcsr_spmv_f32(nb, bs, api._p(Lf[0]), api._p(Lf[1]), api._p(L32), api._p(b32), 1,
                              api._p(y32), 1, api._s())
         L.bilu_bcsr_spmv_f32(nb, bs, api._p(Uf[0]), api._p(Uf[1]), api._p(U32), api._p(y32), 1,
-                             api._p(z), 0, api._s())
-    t_apply32s = time_it(apply_staged, reps)
+                             api._p(q32), 1, api._s())
+    t_apply_in = time_it(apply_inner, reps)
+    t_spmvA32 = time_it(lambda: L.bilu_bcsr_spmv_f32(nb, bs, api._p(row), api._p(col),
+                                                     api._p(A32), api._p(q32), 1, api._p(w32),
+                                                     1, api._s()), reps)
     y = torch.empty_like(b)
     t_spmvA = time_it(lambda: api.bcsr_spmv(nb, bs, row, col, val, b, y), reps)
     B64 = apply_bytes(nb, bs, nnzL, nnzU, 8, 8)
     B32 = apply_bytes(nb, bs, nnzL, nnzU, 4, 4)
     BA = spmv_bytes(nb, bs, nnzb)
-    B32s = apply_bytes_staged(nb, bs, nnzL, nnzU)
+    Bin = apply_bytes_inner(nb, bs, nnzL, nnzU)
+    BA32 = spmv_bytes_f32(nb, bs, nnzb)
     peak, peak_kind = peaks()
-    gbs32 = B32 / t_apply32 / 1e9
-    gbs32s = B32s / t_apply32s / 1e9
+    gbs_in = Bin / t_apply_in / 1e9
     traffic, traffic_src = measured_traffic(args.side)
     rates = (ctypes.c_double * 3)()
     rc = probe_lib().probe_rates(rates)
     assert rc == 0, f"probe_rates returned {rc}"
     dfma_tf = rates[0]
-    # FP64 kernels: one DFMA per stored FP64 value, so their compute roofline
-    # is 2 * (#values) / DFMA rate
     flops64 = 2.0 * (nnzL + nnzU) * bs * bs
     flopsA = 2.0 * nnzb * bs * bs
 
-    # end to end through the C ABI with pinned host buffers
+    # end to end through the C ABI with pinned host buffers (the nested
+    # mode; the first call of the process grows the library's memory pool)
     hrow = torch.from_numpy(A.rowptr).pin_memory()
     hcol = torch.from_numpy(A.colind).pin_memory()
     hval = torch.from_numpy(A.val).pin_memory()
     hb = torch.from_numpy(b_np).pin_memory()
     hx = torch.empty(n, dtype=torch.float64).pin_memory()
     e2e = []
-    for _ in range(0 if args.profile else 2):
+    for _ in range(0 if args.profile else 3):
         it, rr = ctypes.c_int(0), ctypes.c_double(0)
         tm = (ctypes.c_double * 4)()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         st = L.bilu_solve_host(nb, nnzb, bs, ctypes.c_void_p(hrow.data_ptr()),
                                ctypes.c_void_p(hcol.data_ptr()), ctypes.c_void_p(hval.data_ptr()),
-                               ctypes.c_void_p(hb.data_ptr()), ctypes.c_void_p(hx.data_ptr()), 1,
-                               args.restart, args.tol, args.maxit, ctypes.byref(it),
+                               ctypes.c_void_p(hb.data_ptr()), ctypes.c_void_p(hx.data_ptr()),
+                               NESTED, args.restart, args.tol, args.maxit, ctypes.byref(it),
                                ctypes.byref(rr), tm, ctypes.c_void_p(stream.cuda_stream))
         e2e.append(time.perf_counter() - t0)
         assert st == 0, st
-    e2e_v = max_over_ranks(min(e2e), world) if e2e else None
     h2d = A.rowptr.nbytes + A.colind.nbytes + A.val.nbytes + b_np.nbytes
     d2h = n * 8
 
-    cpu = None
+    # errors against the FP64 oracle, the oracle's solve and the CPU baseline
+    cpu, errors = None, None
     if rank == 0 and not args.no_cpu_baseline:
-        try:
-            cpu = cpu_baseline(args.side, int(statistics.mean(iters)), gmres_iters=args.cpu_iters)
-            cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "setup_s",
-                                       "per_iter_s", "serial_1_core")}
-        except Exception as exc:  # report, never hide
-            cpu = {"value": None, "unit": "s", "cores": 0, "kind": "port",
-                   "sample": f"failed: {exc}"}
+        from oracle import oracle
+
+        parts = oracle_parts(A)
+        S = parts[0]
+        cpu = cpu_baseline(A, b_np, parts, args)
+        xo_nested = cpu.pop("_x")
+        x64h = x64.cpu().numpy()
+        ya = oracle.bcsr_spmv(nb, bs, parts[2][0], parts[2][1], parts[2][2], b_np)
+        za = oracle.bcsr_spmv(nb, bs, parts[3][0], parts[3][1], parts[3][2], ya)
+        z32 = api.isai_apply(nb, bs, (Lf[0], Lf[1], L32), (Uf[0], Uf[1], U32), b, prec=1)
+        # the reference's single-apply check (x_true = 0.7, b = A x_true)
+        xt = torch.full((n,), 0.7, dtype=torch.float64, device=dev)
+        bk = torch.empty_like(b)
+        api.bcsr_spmv(nb, bs, row, col, val, xt, bk)
+        kx64 = api.isai_apply(nb, bs, Lf, Uf, bk, prec=0)
+        kx32 = api.isai_apply(nb, bs, (Lf[0], Lf[1], L32), (Uf[0], Uf[1], U32), bk, prec=1)
+        ka64 = api.compute_rel_errors(nb, bs, row, col, val, bk, xt, kx64)
+        ka32 = api.compute_rel_errors(nb, bs, row, col, val, bk, xt, kx32)
+        errors = {
+            "ML_fp32_vs_oracle_fp64": relerr(L32.cpu().numpy().astype(np.float64), S["McsrL"]),
+            "MU_fp32_vs_oracle_fp64": relerr(U32.cpu().numpy().astype(np.float64), S["McsrU"]),
+            "apply_fp32_vs_oracle_fp64": relerr(z32.cpu().numpy(), za),
+            "apply_fp64_vs_oracle_fp64": relerr(api.isai_apply(nb, bs, Lf, Uf, b, prec=0)
+                                                .cpu().numpy(), za),
+            "x_nested_vs_fp64_solve": relerr(x_nested, x64h),
+            "x_fp32_apply_vs_fp64_solve": relerr(x32a.cpu().numpy(), x64h),
+            "x_nested_vs_oracle_nested": relerr(x_nested, xo_nested),
+            "single_apply_check_fp64": {"rel_error_x": ka64[0], "rel_residual": ka64[1]},
+            "single_apply_check_fp32": {"rel_error_x": ka32[0], "rel_residual": ka32[1]},
+            "what": "max |a - b| / max |b|; the FP64 GMRES x equals the oracle's FP64 GMRES x "
+                    "within 1e-8 and the FP64 iteration count equals the oracle's (tests)"}
+        del parts, S
     P.close()
     if rank != 0:
         return
+    it_o, it_i = iters[-1]
     line = {
         "metric": METRIC, "value": t_mixed, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_mixed * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
         "data": "synthetic (seeded 128^3 7-point convection-diffusion, 4 DOF, BSR 4x4)",
-        "config": {"workload": f"convdiff3d {args.side}^3 bs4 (nb={nb}, nnzb={nnzb}), "
-                               f"FGMRES({args.restart}) to {args.tol:g}, FP32-stored ISAI",
-                   "nb": nb, "nnzb": nnzb, "restart": args.restart, "tol": args.tol,
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (1.87 GB of FP64 values)"},
-        "iters": {"mixed": int(statistics.mean(iters)), "fp64": r64.iters},
-        "restart_cycles": {"mixed": restarts_mixed, "fp64": r64.restarts},
-        "relres": {"mixed": relres_mixed, "fp64": r64.relres},
+        "config": workload_config(args, A),
+        "iters": {"outer": it_o, "inner": it_i, "fp64": r64.iters, "fp32_apply": r32.iters},
+        "restart_cycles": {"mixed": res_mixed.restarts, "fp64": r64.restarts},
+        "relres": {"mixed": res_mixed.relres, "fp64": r64.relres},
         "fp64_solve_s": t_fp64, "speedup_mixed_vs_fp64": t_fp64 / t_mixed,
+        "fp32_apply": {"s": t_f32, "iters": r32.iters, "relres": r32.relres,
+                       "speedup_vs_fp64": t_fp64 / t_f32,
+                       "what": "FP32-stored ISAI apply inside flat FP64 FGMRES(30) "
+                               "(FP64 Arnoldi products and orthogonalisation)"},
+        "fp32_inner": {"s": t_f32i, "iters": r32i.iters, "relres": r32i.relres,
+                       "speedup_vs_fp64": t_fp64 / t_f32i,
+                       "what": "flat FGMRES(30) with FP32 ISAI and FP32-stored A in the Arnoldi "
+                               "products; FP64 orthogonalisation, true residual and restarts"},
+        "nested_inner_scan": inner_scan,
         "exact_ilu": {"s": t_ilu, "iters": ri.iters, "relres": ri.relres,
                       "setup_ms": ilu_setup, "speedup_vs_fp64_isai": t_fp64 / t_ilu,
                       "what": "FP64 FGMRES(30) with the exact BILU(0) applied by two "
@@ -491,20 +601,17 @@ def run_ours(args):
                            "setup_ms": iluf_setup, "speedup_vs_fp64_isai": t_fp64 / t_iluf,
                            "what": "FP64 FGMRES(30) with the exact BILU(0) applied in FP32 "
                                    "(FP32 copy of the factor, FP32 level-order solves)"},
-        "fp32_inner": {"s": t_f32i, "iters": r32i.iters, "relres": r32i.relres,
-                       "restart_cycles": r32i.restarts, "speedup_vs_fp64": t_fp64 / t_f32i,
-                       "what": "FP32 ISAI + FP32-stored A in the Arnoldi products; FP64 "
-                               "orthogonalisation, true residual and restarts"},
         "setup_ms": setup_ms,
-        "apply": {"fp32_s": t_apply32, "fp64_s": t_apply64, "fp32_GBs": gbs32,
-                  "fp32_solver_s": t_apply32s, "fp32_solver_GBs": gbs32s,
+        "apply": {"fp32_s": t_apply32, "fp64_s": t_apply64, "fp32_GBs": B32 / t_apply32 / 1e9,
+                  "inner_s": t_apply_in, "inner_GBs": gbs_in, "bytes_inner": Bin,
                   "fp64_GBs": B64 / t_apply64 / 1e9, "bytes_fp32": B32, "bytes_fp64": B64,
-                  "A_spmv_s": t_spmvA, "A_spmv_GBs": BA / t_spmvA / 1e9},
-        "roofline": {"bound": "hbm", "achieved": gbs32s, "peak": peak, "unit": "GB/s",
-                     "frac": gbs32s / peak, "traffic": traffic,
-                     "algorithmic_bytes": B32s, "duration_s": t_apply32s,
-                     "kernel": "FP32-stored ISAI apply as run in the solver (k_bsr_spmv x2: "
-                               "M_L on the FP32 basis vector, M_U to FP64)",
+                  "A_spmv_s": t_spmvA, "A_spmv_GBs": BA / t_spmvA / 1e9,
+                  "A32_spmv_s": t_spmvA32, "A32_spmv_GBs": BA32 / t_spmvA32 / 1e9},
+        "roofline": {"bound": "hbm", "achieved": gbs_in, "peak": peak, "unit": "GB/s",
+                     "frac": gbs_in / peak, "traffic": traffic,
+                     "algorithmic_bytes": Bin, "duration_s": t_apply_in,
+                     "kernel": "FP32-stored ISAI apply as the inner solver runs it "
+                               "(k_bsr_spmv x2: M_L then M_U, FP32 vectors in and out)",
                      "traffic_source": traffic_src,
                      "peak_source": f"{peak_kind} hbm_gbs"},
         "fp64_compute_roofline": {
@@ -513,8 +620,14 @@ def run_ours(args):
             "A_spmv_frac_of_dfma": flopsA / t_spmvA / 1e12 / dfma_tf,
             "apply_fp64_bound_s": max(flops64 / (dfma_tf * 1e12), B64 / (peak * 1e9)),
             "A_spmv_bound_s": max(flopsA / (dfma_tf * 1e12), BA / (peak * 1e9))},
+        "errors": errors,
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": max_over_ranks(e2e[0], world) if e2e else None, "unit": "s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "first_call": e2e[0] if e2e else None,
+                "repeat_calls": e2e[1:],
+                "what": "bilu_solve_host from pinned host buffers: H2D of A and b, setup, "
+                        "nested solve, D2H of x; value = the first call of the process"},
         "gpu_launches": int(launches),
         "clocks": clk, "wall_s": wall,
     }

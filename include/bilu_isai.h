@@ -444,7 +444,7 @@ int bilu_mtx_read(const char* path, int* h_nrows, int* h_ncols, long long* h_nnz
  * payload), then rowptr[nb+1], colind[nnzb] (int32) and the values
  * (nnzb*bs*bs doubles, row-major blocks), little-endian.  bilu_bsr_load
  * with NULL arrays reads the header only; with arrays it checks the sizes
- * against *h_nb/*h_nnzb/*h_bs, the checksum (BILU_ERR_IO on mismatch) and
+ * against *h_nb, *h_nnzb and *h_bs, the checksum (BILU_ERR_IO on mismatch) and
  * the structure (BILU_ERR_PATTERN). */
 int bilu_bsr_save(const char* path, int nb, int nnzb, int bs, const int* h_row, const int* h_col,
                   const double* h_val);

@@ -655,7 +655,6 @@ int inner_solve(bilu_ctx* c, double* z) {
     if (j + 1 < k) BILU_TRY(scale_rsqrt_f32(n, c->w32, ww + j, c->U32 + ld * (j + 1), st));
   }
   BILU_TRY(inner_lsq(k, H, ww, y, st));
-  c->inner_steps += k;
   return combine_f32(n, c->Q32, (long long)ld, k, y, z, st);
 }
 
@@ -799,8 +798,11 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
       BILU_TRY_CUDA(cudaEventRecord(c->ev, st));
       // the next basis vector's apply and SpMV do not depend on the host
       // Givens step: queue them before waiting (discarded if this step
-      // converges)
-      if (j + 1 < m && total + 1 < maxit) BILU_TRY(arnoldi_front(c, prec, j + 1));
+      // converges).  The nested mode's front is a whole inner solve, so it
+      // waits for the host's convergence test instead (one round trip per
+      // outer step, against an inner solve of milliseconds).
+      const bool speculate = prec != BILU_NESTED;
+      if (speculate && j + 1 < m && total + 1 < maxit) BILU_TRY(arnoldi_front(c, prec, j + 1));
       BILU_TRY_CUDA(cudaEventSynchronize(c->ev));
       for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hp[i];
       double hn = std::sqrt(hp[kPartStride]);
@@ -823,6 +825,7 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
       res = std::fabs(g[j + 1]) / bnorm;
       if (h_hist) h_hist[total] = res;
       if (res <= tol || hn == 0.0) break;
+      if (!speculate && j + 1 < m && total < maxit) BILU_TRY(arnoldi_front(c, prec, j + 1));
     }
     c->steps += jlast + 1;
     c->restarts += 1;
@@ -852,6 +855,7 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
     if (res <= tol) status = BILU_OK;
     if (beta == 0.0) break;
   }
+  if (prec == BILU_NESTED) c->inner_steps = (long long)total * c->inner_k;
   if (h_iters) *h_iters = total;
   if (h_relres) *h_relres = res;
   return status;
