@@ -51,8 +51,7 @@ def test_max_over_ranks_gloo(tmp_path):
 def test_reference_arm_under_torchrun():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py",
-           "--impl", "reference", "--gpus", "2", "--side", "10", "--steps", "1", "--warmup", "0",
-           "--cpu-iters", "1"]
+           "--impl", "reference", "--gpus", "2", "--side", "10", "--steps", "2", "--warmup", "1"]
     res = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600,
                          env={**os.environ, "OMP_NUM_THREADS": "2"})
     assert res.returncode == 0, res.stderr[-2000:]
@@ -61,3 +60,7 @@ def test_reference_arm_under_torchrun():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+    # every timed step is a full solve of the same workload the GPU arm runs
+    assert d["relres"] <= 1e-10 and d["status"] == 0 and len(d["step_s"]) == 2
+    assert d["iters"]["inner"] == d["iters"]["outer"] * d["config"]["inner"]
+    assert d["config"]["workload"].startswith("convdiff3d 10^3 bs4")
