@@ -25,7 +25,7 @@ host cores (measured, one solve), plus serial (one core) times.
 `--impl reference` times the oracle's solve of the same system in every
 step.  Secondary lines: --workload sptrsv | powerlaw | batch.
 
-    python bench.py [--steps K] [--warmup W] [--side 128] [--inner 20] [--impl reference]
+    python bench.py [--steps K] [--warmup W] [--side 128] [--inner 8] [--impl reference]
     torchrun --nproc-per-node N bench.py --gpus N   (N independent replicas)
 """
 from __future__ import annotations
@@ -60,11 +60,12 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--maxit", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--inner", type=int, default=20,
+    ap.add_argument("--inner", type=int, default=8,
                     help="inner FP32 GMRES steps per outer step of the nested mode")
     ap.add_argument("--workload", default="convdiff",
-                    choices=["convdiff", "batch", "powerlaw", "sptrsv"],
-                    help="convdiff: the headline line; batch / powerlaw / sptrsv: secondary lines")
+                    choices=["convdiff", "batch", "powerlaw", "sptrsv", "kernels"],
+                    help="convdiff: the headline line; batch / powerlaw / sptrsv: secondary "
+                         "lines; kernels: the inner solver's kernels alone, for ncu captures")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-lo", type=int, default=32)
     ap.add_argument("--batch-hi", type=int, default=512)
@@ -422,7 +423,7 @@ def run_ours(args):
     t_f32i, r32i = timed(api.BILU_FP32_INNER)
     # the nested mode at other inner lengths (the headline uses --inner)
     inner_scan = {}
-    for k in sorted({10, 16, 20, 24, 30} - {args.inner}):
+    for k in sorted({6, 12, 16, 24} - {args.inner}):
         P.set_inner(k)
         t_k, r_k = timed(NESTED)
         inner_scan[str(k)] = {"s": t_k, "outer": r_k.iters, "inner": r_k.inner_steps,
@@ -813,6 +814,36 @@ def run_sptrsv(args):
     print(json.dumps(out))
 
 
+def run_kernels(args):
+    """For ncu captures: the setup of the --side^3 system, then --steps
+    rounds of the inner solver's products as it launches them: M_L u and
+    M_U t (k_bsr_spmv, FP32 values and vectors) and A q (FP32-stored A),
+    each round in this order (three k_bsr_spmv launches per round)."""
+    import torch
+
+    from isai_kernel_gb300 import _lib, api
+
+    L = _lib.lib()
+    dev = torch.device("cuda", 0)
+    A, b_np = convdiff_system(args.side)
+    nb, bs, n = A.nb, A.bs, A.n
+    row, col, val = (torch.from_numpy(a).to(dev) for a in (A.rowptr, A.colind, A.val))
+    P = api.Preconditioner(nb, bs, row, col, val, fp32=True, nested=True)
+    _, Lf, Uf = P.factors()
+    L32, U32 = P.get(7), P.get(8)
+    A32 = val.float()
+    u = torch.from_numpy(b_np).to(dev).float()
+    t, q, w = (torch.empty(n, dtype=torch.float32, device=dev) for _ in range(3))
+    p_ = api._p
+    for _ in range(args.steps):
+        L.bilu_bcsr_spmv_f32(nb, bs, p_(Lf[0]), p_(Lf[1]), p_(L32), p_(u), 1, p_(t), 1, api._s())
+        L.bilu_bcsr_spmv_f32(nb, bs, p_(Uf[0]), p_(Uf[1]), p_(U32), p_(t), 1, p_(q), 1, api._s())
+        L.bilu_bcsr_spmv_f32(nb, bs, p_(row), p_(col), p_(A32), p_(q), 1, p_(w), 1, api._s())
+    torch.cuda.synchronize()
+    P.close()
+    print(json.dumps({"workload": f"kernels convdiff3d {args.side}^3", "rounds": args.steps}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -823,6 +854,8 @@ def main():
         run_powerlaw(args)
     elif args.workload == "sptrsv":
         run_sptrsv(args)
+    elif args.workload == "kernels":
+        run_kernels(args)
     else:
         run_ours(args)
 

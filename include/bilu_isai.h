@@ -373,7 +373,7 @@ int bilu_ctx_set_schedule(bilu_ctx* ctx, int schedule);
  * residual at every restart corrects the inner precision, as in GMRES with
  * iterative refinement), BILU_NESTED the nested GMRES-IR form: every
  * preconditioned vector z_j of the FP64 flexible outer GMRES is a fixed
- * number of steps (bilu_ctx_set_inner, default 20) of right-preconditioned
+ * number of steps (bilu_ctx_set_inner, default 8) of right-preconditioned
  * GMRES in FP32 on A z = v_j with the FP32-stored A and ISAI, FP32
  * Gram-Schmidt and the Hessenberg least squares on the device; the outer
  * residuals, orthogonalisation and true residual at every restart stay
@@ -388,7 +388,7 @@ int bilu_ctx_solve(bilu_ctx* ctx, int prec, const double* d_b, double* d_x, int 
  * cycles. */
 int bilu_ctx_stats(bilu_ctx* ctx, long long* h_out);
 /* Inner FP32 GMRES steps per outer step of the nested mode (1..32; default
- * 20), for the next solve; no counterpart in the reference. */
+ * 8), for the next solve; no counterpart in the reference. */
 int bilu_ctx_set_inner(bilu_ctx* ctx, int k);
 /* Inner steps the last BILU_NESTED solve took in total. */
 int bilu_ctx_inner_steps(bilu_ctx* ctx, long long* h_steps);

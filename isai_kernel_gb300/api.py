@@ -364,7 +364,7 @@ class Preconditioner:
 
     def __init__(self, nb: int, bs: int, row, col, val, fp32: bool = True, ilu: bool = False,
                  fp32_inner: bool = False, isai_level: int = 1, schedule: int = -1,
-                 stream=None, ilu_fp32: bool = False, nested: bool = False, inner: int = 20):
+                 stream=None, ilu_fp32: bool = False, nested: bool = False, inner: int = 8):
         self._h = ctypes.c_void_p()
         self.nb, self.bs = nb, bs
         self.stream = stream

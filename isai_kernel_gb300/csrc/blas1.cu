@@ -4,6 +4,7 @@
 // all basis vectors and does no redundant FP64 work; reductions go through
 // a fixed number of CTA partials summed in a fixed order (deterministic).
 #include "blas1.cuh"
+#include "gridsync.cuh"
 
 namespace bilu {
 
@@ -151,194 +152,6 @@ void launch_multiaxpy(long long n, const double* V, long long ldv, const double*
     default: return BILU_ERR_ARG;                                                    \
   }
 
-// One modified Gram-Schmidt step fused with the next one's dot product:
-// w -= h_prev * v_prev (h_prev read from device memory), then the partial of
-// v_next . w (or w . w).  The basis vectors stream through with evict-first
-// loads; w (one vector, 67 MB at 128^3) stays in the L2 (a sweep reads
-// only the two basis vectors from DRAM), which leaves the two DFMAs per
-// element as the bound.  Elements go in pairs through 16-byte accesses (the
-// basis stride is a multiple of 32 elements and every vector starts on a
-// 256-byte boundary) into two independent accumulators, so that a thread
-// has two FMA chains in flight.  The CTA that finishes last sums the CTA
-// partials in index order, so the result does not depend on which CTA
-// that is.
-__global__ void __launch_bounds__(kRedThreads, kSweepCTAs / 152) k_mgs_sweep(
-    long long n, const double* __restrict__ vp, const double* __restrict__ hp,
-    const double* __restrict__ vn, double* __restrict__ w, double* __restrict__ partial,
-    unsigned* counter, double* out) {
-  // launched as a programmatic dependent of the previous sweep: let the
-  // next sweep's CTAs be scheduled during this one's reduction tail, and
-  // wait here until the previous grid has finished and its writes (w, h,
-  // the counter reset) are visible
-  asm volatile("griddepcontrol.launch_dependents;");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  const double h = vp ? -__ldcg(hp) : 0.0;
-  double acc0 = 0.0, acc1 = 0.0;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double2* w2 = reinterpret_cast<double2*>(w);
-  const double2* vp2 = reinterpret_cast<const double2*>(vp);
-  const double2* vn2 = reinterpret_cast<const double2*>(vn);
-  for (long long e = tid; e < (n >> 1); e += stride) {
-    double2 we = __ldcg(w2 + e);  // L2: w was written by the previous sweep
-    if (vp) {
-      const double2 p = __ldcs(vp2 + e);
-      we.x = fma(h, p.x, we.x);
-      we.y = fma(h, p.y, we.y);
-      w2[e] = we;
-    }
-    const double2 o = vn ? __ldcs(vn2 + e) : we;
-    acc0 = fma(o.x, we.x, acc0);
-    acc1 = fma(o.y, we.y, acc1);
-  }
-  if ((n & 1) && tid == 0) {  // odd length: the last element
-    double we = __ldcg(w + n - 1);
-    if (vp) {
-      we = fma(h, __ldcs(vp + n - 1), we);
-      w[n - 1] = we;
-    }
-    const double o = vn ? __ldcs(vn + n - 1) : we;
-    acc0 = fma(o, we, acc0);
-  }
-  double acc = acc0 + acc1;
-  __shared__ double red[kRedThreads / 32];
-  __shared__ bool last;
-  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) red[warp] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-#pragma unroll
-    for (int i = 0; i < kRedThreads / 32; ++i) s += red[i];
-    partial[blockIdx.x] = s;
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  double s = 0.0;
-  for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) s += __ldcg(partial + c);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) red[warp] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-#pragma unroll
-    for (int i = 0; i < kRedThreads / 32; ++i) t += red[i];
-    *out = t;
-    *counter = 0u;
-  }
-}
-
-
-// FP32 form of k_mgs_sweep for the inner solver: four elements per 16-byte
-// access, FP32 products and sums per thread, FP64 from the warp sums on.
-// w (33.5 MB at 128^3) and vn stay in the L2 (vn is read with ld.global.cg,
-// so the next sweep finds it there as vp); vp streams with evict-first
-// loads, the last use of that basis vector in this step.
-__global__ void __launch_bounds__(kRedThreads, kSweepCTAs / 152) k_mgs_sweep_f32(
-    long long n, const float* __restrict__ vp, const double* __restrict__ hp,
-    const float* __restrict__ vn, float* __restrict__ w, double* __restrict__ partial,
-    unsigned* counter, double* out) {
-  asm volatile("griddepcontrol.launch_dependents;");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  const float h = vp ? -(float)__ldcg(hp) : 0.0f;
-  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  float4* w4 = reinterpret_cast<float4*>(w);
-  const float4* vp4 = reinterpret_cast<const float4*>(vp);
-  const float4* vn4 = reinterpret_cast<const float4*>(vn);
-  const long long n4 = n >> 2;
-  for (long long e = tid; e < n4; e += stride) {
-    float4 we = __ldcg(w4 + e);
-    if (vp) {
-      const float4 p = __ldcs(vp4 + e);
-      we.x = fmaf(h, p.x, we.x);
-      we.y = fmaf(h, p.y, we.y);
-      we.z = fmaf(h, p.z, we.z);
-      we.w = fmaf(h, p.w, we.w);
-      w4[e] = we;
-    }
-    const float4 o = vn ? __ldcg(vn4 + e) : we;
-    a0 = fmaf(o.x, we.x, a0);
-    a1 = fmaf(o.y, we.y, a1);
-    a2 = fmaf(o.z, we.z, a2);
-    a3 = fmaf(o.w, we.w, a3);
-  }
-  if (tid < (n & 3)) {  // the last n % 4 elements
-    const long long e = (n4 << 2) + tid;
-    float we = __ldcg(w + e);
-    if (vp) {
-      we = fmaf(h, __ldcs(vp + e), we);
-      w[e] = we;
-    }
-    const float o = vn ? __ldcg(vn + e) : we;
-    a0 = fmaf(o, we, a0);
-  }
-  float accf = (a0 + a1) + (a2 + a3);
-  __shared__ double red[kRedThreads / 32];
-  __shared__ bool last;
-  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) accf += __shfl_xor_sync(0xffffffffu, accf, o);
-  if (lane == 0) red[warp] = (double)accf;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-#pragma unroll
-    for (int i = 0; i < kRedThreads / 32; ++i) s += red[i];
-    partial[blockIdx.x] = s;
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  double s = 0.0;
-  for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) s += __ldcg(partial + c);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) red[warp] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-#pragma unroll
-    for (int i = 0; i < kRedThreads / 32; ++i) t += red[i];
-    *out = t;
-    *counter = 0u;
-  }
-}
-
-__global__ void k_scale_rsqrt_f32(long long n, const float* __restrict__ x,
-                                  const double* __restrict__ nrm2, float* __restrict__ y) {
-  __shared__ float a_s;
-  if (threadIdx.x == 0) {
-    const double v = *nrm2;
-    a_s = v > 0.0 ? (float)(1.0 / sqrt(v)) : 0.0f;
-  }
-  __syncthreads();
-  const float a = a_s;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long n4 = n >> 2;
-  const float4* x4 = reinterpret_cast<const float4*>(x);
-  float4* y4 = reinterpret_cast<float4*>(y);
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n4; e += stride) {
-    float4 v = x4[e];
-    v.x *= a;
-    v.y *= a;
-    v.z *= a;
-    v.w *= a;
-    y4[e] = v;
-  }
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (n & 3)) y[(n4 << 2) + t] = x[(n4 << 2) + t] * a;
-}
-
 // One thread: Givens QR of the inner Hessenberg matrix and the triangular
 // solve, as the host does for the outer one (the same rotation formulas).
 __global__ void k_inner_lsq(int k, const double* __restrict__ Hraw, const double* __restrict__ ww,
@@ -420,6 +233,167 @@ void launch_combine(long long n, const float* Q, long long ldq, const double* y,
   k_combine_f32<K><<<kRedCTAs, kRedThreads, 0, st>>>(n, Q, ldq, y, z);
 }
 
+
+// ---------------------------------------------------------------------------
+// Whole modified Gram-Schmidt step in one cooperative launch: sweeps
+// i = 0 .. j+1 over the same slice of w per CTA (w stays in the L2 between
+// sweeps), sweep i applying h_{i-1} v_{i-1} and taking v_i . w (the last
+// one w . w), then v_{j+1} = w / ||w|| (and its FP32 copy).  Between sweeps
+// a counting grid barrier replaces the kernel boundary: each CTA writes its
+// partial sum, meets the others at the barrier, and then every CTA adds all
+// partials in index order (warp 0, fixed lane strides and shuffle tree), so
+// every CTA holds the same h_i bit for bit and the result does not depend on
+// timing.  The partials alternate between two halves of the buffer: a CTA
+// writes sweep i+1's partial only after barrier i, and sweep i+2 (same half
+// as i) only after barrier i+1, which every CTA reaches after it has read
+// sweep i's partials.  A barrier that times out sets the error word and
+// every CTA returns.
+template <class T>
+struct MgsVec;
+template <>
+struct MgsVec<double> {
+  using V = double2;
+  static constexpr int W = 2;
+  __device__ static V ldcg(const V* p) { return __ldcg(p); }
+  __device__ static V ldcs(const V* p) { return __ldcs(p); }
+  __device__ static void axpy(double h, const V& p, V& w) {
+    w.x = fma(h, p.x, w.x);
+    w.y = fma(h, p.y, w.y);
+  }
+  __device__ static void dot(const V& o, const V& w, double (&a)[4]) {
+    a[0] = fma(o.x, w.x, a[0]);
+    a[1] = fma(o.y, w.y, a[1]);
+  }
+  __device__ static void scale(V& v, double a) {
+    v.x *= a;
+    v.y *= a;
+  }
+};
+template <>
+struct MgsVec<float> {
+  using V = float4;
+  static constexpr int W = 4;
+  __device__ static V ldcg(const V* p) { return __ldcg(p); }
+  __device__ static V ldcs(const V* p) { return __ldcs(p); }
+  __device__ static void axpy(float h, const V& p, V& w) {
+    w.x = fmaf(h, p.x, w.x);
+    w.y = fmaf(h, p.y, w.y);
+    w.z = fmaf(h, p.z, w.z);
+    w.w = fmaf(h, p.w, w.w);
+  }
+  __device__ static void dot(const V& o, const V& w, float (&a)[4]) {
+    a[0] = fmaf(o.x, w.x, a[0]);
+    a[1] = fmaf(o.y, w.y, a[1]);
+    a[2] = fmaf(o.z, w.z, a[2]);
+    a[3] = fmaf(o.w, w.w, a[3]);
+  }
+  __device__ static void scale(V& v, float a) {
+    v.x *= a;
+    v.y *= a;
+    v.z *= a;
+    v.w *= a;
+  }
+};
+
+constexpr int kStepThreads = 256;
+
+template <class T>
+__global__ void __launch_bounds__(kStepThreads, 4) k_mgs_step(
+    long long n, const T* __restrict__ V, long long ldv, int j, T* __restrict__ w,
+    double* __restrict__ hout, int hstride, double* __restrict__ wwout,
+    double* __restrict__ partial, GridSync gs, T* __restrict__ vnext,
+    float* __restrict__ vnext32) {
+  using M = MgsVec<T>;
+  using VT = typename M::V;
+  constexpr int W = M::W;
+  __shared__ double red[kStepThreads / 32];
+  __shared__ double h_s;
+  unsigned passed = 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int G = (int)gridDim.x;
+  const long long stride = (long long)G * blockDim.x;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nv = n / W;     // whole vectors
+  const long long tail = nv * W;  // first element of the scalar tail
+  VT* wv = reinterpret_cast<VT*>(w);
+  double h = 0.0;
+  for (int i = 0; i <= j + 1; ++i) {
+    const T* vp = i > 0 ? V + (long long)(i - 1) * ldv : nullptr;
+    const T* vn = i <= j ? V + (long long)i * ldv : nullptr;
+    const T hn = (T)(-h);
+    T a[4] = {T(0), T(0), T(0), T(0)};
+    const VT* vpv = reinterpret_cast<const VT*>(vp);
+    const VT* vnv = reinterpret_cast<const VT*>(vn);
+    for (long long e = tid; e < nv; e += stride) {
+      VT we = M::ldcg(wv + e);
+      if (vp) {
+        M::axpy(hn, M::ldcs(vpv + e), we);
+        wv[e] = we;
+      }
+      M::dot(vn ? M::ldcg(vnv + e) : we, we, a);
+    }
+    if (tid < n - tail) {  // the last n % W elements
+      const long long e = tail + tid;
+      T we = __ldcg(w + e);
+      if (vp) {
+        we = fma(hn, __ldcs(vp + e), we);
+        w[e] = we;
+      }
+      const T o = vn ? __ldcg(vn + e) : we;
+      a[0] = fma(o, we, a[0]);
+    }
+    // CTA partial in FP64 (FP32 sums stay per thread), fixed order
+    double acc = (double)((a[0] + a[1]) + (a[2] + a[3]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) red[warp] = acc;
+    __syncthreads();
+    double* part = partial + (long long)(i & 1) * G;
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+#pragma unroll
+      for (int q = 0; q < kStepThreads / 32; ++q) t += red[q];
+      part[blockIdx.x] = t;
+    }
+    if (!grid_sync_count(gs, passed)) return;
+    // every CTA adds the partials in the same order
+    if (warp == 0) {
+      double t = 0.0;
+      for (int c = lane; c < G; c += 32) t += __ldcg(part + c);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == 0) h_s = t;
+    }
+    __syncthreads();
+    h = h_s;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (i <= j) hout[(long long)i * hstride] = h;
+      else *wwout = h;
+    }
+  }
+  // v_{j+1} = w / ||w|| over this CTA's slice (zeros when ||w|| = 0)
+  if (vnext) {
+    const T s = h > 0.0 ? (T)(1.0 / sqrt(h)) : T(0);
+    VT* out = reinterpret_cast<VT*>(vnext);
+    for (long long e = tid; e < nv; e += stride) {
+      VT v = M::ldcg(wv + e);
+      M::scale(v, s);
+      out[e] = v;
+      if (vnext32) {
+        const T* vs = reinterpret_cast<const T*>(&v);
+#pragma unroll
+        for (int q = 0; q < W; ++q) vnext32[e * W + q] = (float)vs[q];
+      }
+    }
+    if (tid < n - tail) {
+      const long long e = tail + tid;
+      const T v = __ldcg(w + e) * s;
+      vnext[e] = v;
+      if (vnext32) vnext32[e] = (float)v;
+    }
+  }
+  grid_exit_count(gs);
+}
 }  // namespace
 
 int multidot(long long n, const double* V, long long ldv, int nv, const double* w, bool with_ww,
@@ -451,58 +425,44 @@ int scale_rsqrt(long long n, const double* x, const double* nrm2, double* y, cud
   return BILU_OK;
 }
 
-int mgs_sweep(long long n, const double* vp, const double* hp, const double* vn, double* w,
-              double* partial, unsigned* counter, double* out, cudaStream_t st) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(kSweepCTAs);
-  cfg.blockDim = dim3(kRedThreads);
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  BILU_TRY_CUDA(cudaLaunchKernelEx(&cfg, k_mgs_sweep, n, vp, hp, vn, w, partial, counter, out));
-  __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED);
-  return BILU_OK;
-}
-
-int mgs_sweep_f32(long long n, const float* vp, const double* hp, const float* vn, float* w,
-                  double* partial, unsigned* counter, double* out, cudaStream_t st) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(kSweepCTAs);
-  cfg.blockDim = dim3(kRedThreads);
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  BILU_TRY_CUDA(
-      cudaLaunchKernelEx(&cfg, k_mgs_sweep_f32, n, vp, hp, vn, w, partial, counter, out));
-  __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED);
-  return BILU_OK;
-}
-
-int scale_rsqrt_f32(long long n, const float* x, const double* nrm2, float* y, cudaStream_t st) {
-  k_scale_rsqrt_f32<<<kRedCTAs, kRedThreads, 0, st>>>(n, x, nrm2, y);
+template <class T>
+int mgs_step_t(long long n, const T* V, long long ldv, int j, T* w, double* hout, int hstride,
+               double* wwout, double* partial, unsigned* words, T* vnext, float* vnext32,
+               cudaStream_t st) {
+  static int grid = 0;
+  if (!grid) {
+    int per = 0, dev = 0, sms = 0;
+    BILU_TRY_CUDA(cudaGetDevice(&dev));
+    BILU_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    BILU_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mgs_step<T>,
+                                                                kStepThreads, 0));
+    grid = std::max(1, std::min(per, 4)) * sms;
+  }
+  if (grid > kStepMaxCTAs) return BILU_ERR_UNSUPPORTED;
+  GridSync gs;
+  gs.count = words;
+  gs.gen = words + 1;
+  gs.err = reinterpret_cast<int*>(words + 2);
+  gs.spin = kSpinLimit;
+  void* args[] = {&n, &V, &ldv, &j, &w, &hout, &hstride, &wwout, &partial, &gs, &vnext, &vnext32};
+  BILU_TRY_CUDA(cudaLaunchCooperativeKernel((const void*)k_mgs_step<T>, dim3(grid),
+                                            dim3(kStepThreads), args, 0, st));
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }
 
-int inner_lsq(int k, const double* H, const double* ww, double* y, cudaStream_t st) {
-  if (k < 1 || k > kMaxVec) return BILU_ERR_ARG;
-  k_inner_lsq<<<1, 32, 0, st>>>(k, H, ww, y);
-  BILU_LAUNCH_CHECK();
-  return BILU_OK;
+int mgs_step(long long n, const double* V, long long ldv, int j, double* w, double* hout,
+             int hstride, double* wwout, double* partial, unsigned* words, double* vnext,
+             float* vnext32, cudaStream_t st) {
+  return mgs_step_t<double>(n, V, ldv, j, w, hout, hstride, wwout, partial, words, vnext,
+                            vnext32, st);
 }
 
-int combine_f32(long long n, const float* Q, long long ldq, int k, const double* y, double* z,
-                cudaStream_t st) {
-  const int nv = k;
-  BILU_NV_CASES(launch_combine, n, Q, ldq, y, z, st);
-  BILU_LAUNCH_CHECK();
-  return BILU_OK;
+int mgs_step_f32(long long n, const float* V, long long ldv, int j, float* w, double* hout,
+                 int hstride, double* wwout, double* partial, unsigned* words, float* vnext,
+                 cudaStream_t st) {
+  return mgs_step_t<float>(n, V, ldv, j, w, hout, hstride, wwout, partial, words, vnext,
+                           nullptr, st);
 }
 
 int residual_norm(long long n, const double* b, const double* ax, double* r, double* partial,

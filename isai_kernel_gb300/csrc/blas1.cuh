@@ -9,7 +9,6 @@ constexpr int kRedCTAs = 152 * 4;  // partial-sum slots (fixed => deterministic)
 constexpr int kRedThreads = 256;
 constexpr int kMaxVec = 32;        // vectors per multi-dot / multi-axpy call
 constexpr int kPartStride = kMaxVec + 2;
-constexpr int kSweepCTAs = 152 * 6;  // CTAs of one MGS sweep (one partial each, one wave)
 
 // partial[cta * kPartStride + i] = sum_e V[i][e] * w[e] (i < nv), and at
 // index nv: sum_e w[e]^2 when with_ww.  Skipped (partials left as they
@@ -32,22 +31,7 @@ int scale_rsqrt(long long n, const double* x, const double* nrm2, double* y, cud
 int residual_norm(long long n, const double* b, const double* ax, double* r, double* partial,
                   cudaStream_t st);
 
-// One modified Gram-Schmidt sweep over w: if vp != null, w -= (*hp) * vp;
-// then *out = vn . w (or w . w when vn == null), the CTA partials summed in a
-// fixed order by the last CTA to finish (counter returns to 0 afterwards).
-int mgs_sweep(long long n, const double* vp, const double* hp, const double* vn, double* w,
-              double* partial, unsigned* counter, double* out, cudaStream_t st);
-
 // ---- FP32 inner solver of the nested (GMRES-IR) mode ----
-// The same fused sweep on FP32 vectors (vp, vn, w float; h read as double
-// and rounded to FP32): FP32 products and per-thread FP32 sums, the warp
-// sums widened to FP64 and the CTA partials added in a fixed order, so the
-// dot products are reproducible run to run.  vn is read with an L2-keeping
-// load (it is the next sweep's vp), vp with an evict-first load.
-int mgs_sweep_f32(long long n, const float* vp, const double* hp, const float* vn, float* w,
-                  double* partial, unsigned* counter, double* out, cudaStream_t st);
-// y = x * (1/sqrt(*nrm2)) in FP32 (zeros when *nrm2 == 0).
-int scale_rsqrt_f32(long long n, const float* x, const double* nrm2, float* y, cudaStream_t st);
 // Least squares of the inner Arnoldi steps on the device (one thread): H
 // holds (k+1) x k entries H[i*k + j] with the raw column entries h_ij
 // (i <= j) and, in ww[j], ||w_j||^2 (the subdiagonal squared); Givens
@@ -59,5 +43,25 @@ int inner_lsq(int k, const double* H, const double* ww, double* y, cudaStream_t 
 // FP64 (z is the outer flexible-GMRES direction).
 int combine_f32(long long n, const float* Q, long long ldq, int k, const double* y, double* z,
                 cudaStream_t st);
+
+// Whole modified Gram-Schmidt step of Arnoldi step j in one cooperative
+// launch: j+2 fused sweeps (sweep i applies w -= h_{i-1} v_{i-1} and takes
+// h_i = v_i . w; the last one w . w) with a counting grid barrier between
+// them, w held in the L2: h_i into hout[i * hstride]
+// (i <= j), ||w||^2 into *wwout, then vnext = w / ||w|| (and vnext32, its
+// FP32 copy, when given; zeros when ||w|| = 0).  partial holds
+// 2 * kStepMaxCTAs doubles; words are the barrier's count, exit count and
+// error word (zero before the first launch; every launch leaves them zero
+// unless a barrier timed out, which sets the error word to
+// BILU_ERR_TIMEOUT).
+constexpr int kStepMaxCTAs = 152 * 8;
+int mgs_step(long long n, const double* V, long long ldv, int j, double* w, double* hout,
+             int hstride, double* wwout, double* partial, unsigned* words, double* vnext,
+             float* vnext32, cudaStream_t st);
+// The FP32 form for the nested mode's inner solver (FP32 products and
+// per-thread sums, FP64 from the warp sums on).
+int mgs_step_f32(long long n, const float* V, long long ldv, int j, float* w, double* hout,
+                 int hstride, double* wwout, double* partial, unsigned* words, float* vnext,
+                 cudaStream_t st);
 
 }  // namespace bilu

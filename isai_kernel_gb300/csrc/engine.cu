@@ -173,12 +173,13 @@ struct bilu_ctx {
   double* hpin = nullptr;  // pinned host mirror of dscal
   cudaEvent_t ev = nullptr;
   unsigned* counter = nullptr;  // arrival counter of the MGS sweep reductions
+  unsigned* step_words = nullptr;  // barrier count, exit count, error word of mgs_step
   long long steps = 0, restarts = 0;  // Arnoldi steps and cycles of the last solve
   // nested (GMRES-IR) mode: FP32 inner GMRES of inner_k steps per outer
   // step; its basis U32 ((k+1) vectors, U32[0] = the outer basis vector in
   // FP32), the preconditioned vectors Q32 (k), the working vector w32 and
   // the small FP64 arrays (raw Hessenberg (k+1) x k, ||w||^2 per step, y)
-  int inner_k = 20, inner_alloc = 0;
+  int inner_k = 8, inner_alloc = 0;
   long long inner_steps = 0;  // inner steps of the last solve
   float *U32 = nullptr, *Q32 = nullptr, *w32 = nullptr;
   double* inner_small = nullptr;
@@ -200,7 +201,8 @@ struct bilu_ctx {
   }
   void free_solver() {
     for (void* p : {(void*)V, (void*)Z, (void*)w, (void*)r, (void*)tmp, (void*)v32, (void*)z32,
-                    (void*)partial, (void*)dscal, (void*)dcoef, (void*)counter, (void*)U32,
+                    (void*)partial, (void*)dscal, (void*)dcoef, (void*)counter,
+                    (void*)step_words, (void*)U32,
                     (void*)Q32, (void*)w32, (void*)inner_small})
       if (p) cudaFreeAsync(p, st);
     U32 = Q32 = w32 = nullptr;
@@ -209,6 +211,7 @@ struct bilu_ctx {
     v32 = nullptr;
     z32 = nullptr;
     counter = nullptr;
+    step_words = nullptr;
     if (hpin) cudaFreeHost(hpin);
     if (ev) cudaEventDestroy(ev);
     ev = nullptr;
@@ -558,6 +561,8 @@ int ensure_solver(bilu_ctx* c, int m) {
   BILU_TRY_CUDA(cudaMallocHost(&c->hpin, sizeof(double) * 6 * kPartStride));
   BILU_TRY_CUDA(get(&c->counter, sizeof(unsigned)));
   BILU_TRY_CUDA(cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->st));
+  BILU_TRY_CUDA(get(&c->step_words, sizeof(unsigned) * 4));
+  BILU_TRY_CUDA(cudaMemsetAsync(c->step_words, 0, sizeof(unsigned) * 4, c->st));
   c->m_alloc = m;
   return BILU_OK;
 }
@@ -623,8 +628,8 @@ int ensure_inner(bilu_ctx* c) {
 // basis starting from u_0 = v in FP32 (U32[0], written by the kernel that
 // normalised v; v has unit norm, so beta = 1: flexible GMRES accepts any
 // scaling of z).  Every step: q_i = M_U (M_L u_i) into Q32[i], w = A q_i,
-// i + 2 fused FP32 Gram-Schmidt sweeps writing h_0i..h_ii and ||w||^2,
-// u_{i+1} = w / ||w||.  Then the Hessenberg least-squares problem on the
+// then one cooperative launch of the i + 2 fused FP32 Gram-Schmidt sweeps
+// writing h_0i..h_ii and ||w||^2, and u_{i+1} = w / ||w||.  Then the Hessenberg least-squares problem on the
 // device and z = Q y widened to FP64.  Nothing waits on the host: the
 // whole inner solve is queued on the stream.
 int inner_solve(bilu_ctx* c, double* z) {
@@ -645,14 +650,9 @@ int inner_solve(bilu_ctx* c, double* z) {
                       c->spmv_layout[2]));
     BILU_TRY(spmv_any(c->nb, c->bs, BILU_FP32, c->Arow, c->Acol, c->Aval32, qj, 1, c->w32, 1, st,
                       c->spmv_layout[0]));
-    const float* U = c->U32;
-    BILU_TRY(mgs_sweep_f32(n, nullptr, nullptr, U, c->w32, c->partial, c->counter, H + j, st));
-    for (int i = 1; i <= j; ++i)
-      BILU_TRY(mgs_sweep_f32(n, U + ld * (i - 1), H + (size_t)(i - 1) * k + j, U + ld * i,
-                             c->w32, c->partial, c->counter, H + (size_t)i * k + j, st));
-    BILU_TRY(mgs_sweep_f32(n, U + ld * j, H + (size_t)j * k + j, nullptr, c->w32, c->partial,
-                           c->counter, ww + j, st));
-    if (j + 1 < k) BILU_TRY(scale_rsqrt_f32(n, c->w32, ww + j, c->U32 + ld * (j + 1), st));
+    // the j+2 FP32 sweeps and u_{j+1} = w / ||w|| in one cooperative launch
+    BILU_TRY(mgs_step_f32(n, c->U32, (long long)ld, j, c->w32, H + j, k, ww + j, c->partial,
+                          c->step_words, j + 1 < k ? c->U32 + ld * (j + 1) : nullptr, st));
   }
   BILU_TRY(inner_lsq(k, H, ww, y, st));
   return combine_f32(n, c->Q32, (long long)ld, k, y, z, st);
@@ -727,8 +727,9 @@ int arnoldi_front(bilu_ctx* c, int prec, int j) {
 
 // Orthogonalises w against V_0..V_j by modified Gram-Schmidt: j+2 fused
 // sweeps (w -= h_{i-1} v_{i-1} together with h_i = v_i . w; the last one
-// gives ||w||^2), each reduced in a fixed order on the device, then
-// V_{j+1} = w / ||w|| and the Hessenberg column is queued to hpin.
+// gives ||w||^2) and V_{j+1} = w / ||w|| in one cooperative launch, each
+// sum reduced in a fixed order on the device; the Hessenberg column and
+// the launch's error word are queued to hpin.
 // s[0..j] = h, s[kPartStride] = ||w||^2.
 int arnoldi_back(bilu_ctx* c, int j, int prec) {
   cudaStream_t st = c->st;
@@ -736,14 +737,12 @@ int arnoldi_back(bilu_ctx* c, int j, int prec) {
   size_t ld = (size_t)c->ldv;
   double* s = c->dscal;
   const double* V = c->V;
-  BILU_TRY(mgs_sweep(n, nullptr, nullptr, V, c->w, c->partial, c->counter, s, st));
-  for (int i = 1; i <= j; ++i)
-    BILU_TRY(mgs_sweep(n, V + ld * (i - 1), s + i - 1, V + ld * i, c->w, c->partial,
-                       c->counter, s + i, st));
-  BILU_TRY(mgs_sweep(n, V + ld * j, s + j, nullptr, c->w, c->partial, c->counter,
-                     s + kPartStride, st));
-  BILU_TRY(scale_rsqrt(n, c->w, s + kPartStride, c->V + ld * (j + 1), st, v32_of(c, prec)));
+  BILU_TRY(mgs_step(n, V, (long long)ld, j, c->w, s, 1, s + kPartStride, c->partial,
+                    c->step_words, c->V + ld * (j + 1), v32_of(c, prec), st));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->hpin, s, sizeof(double) * (kPartStride + 1),
+                                cudaMemcpyDeviceToHost, st));
+  // the barrier error word of this step's (and the inner solver's) launches
+  BILU_TRY_CUDA(cudaMemcpyAsync(c->hpin + kPartStride + 1, c->step_words + 2, sizeof(unsigned),
                                 cudaMemcpyDeviceToHost, st));
   return BILU_OK;
 }
@@ -765,6 +764,7 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
   cudaStream_t st = c->st;
   const bool ilu_mode = prec == BILU_ILU || prec == BILU_ILU_FP32;
   if (ilu_mode) BILU_TRY_CUDA(cudaMemsetAsync(c->ilu_words, 0, sizeof(unsigned) * 4, st));
+  BILU_TRY_CUDA(cudaMemsetAsync(c->step_words, 0, sizeof(unsigned) * 4, st));
   const int m = restart;
   const long long n = c->n;
   double* s = c->dscal;
@@ -804,6 +804,14 @@ extern "C" int bilu_ctx_solve(bilu_ctx* c, int prec, const double* d_b, double* 
       const bool speculate = prec != BILU_NESTED;
       if (speculate && j + 1 < m && total + 1 < maxit) BILU_TRY(arnoldi_front(c, prec, j + 1));
       BILU_TRY_CUDA(cudaEventSynchronize(c->ev));
+      unsigned step_err = 0;
+      std::memcpy(&step_err, hp + kPartStride + 1, sizeof(unsigned));
+      if (step_err != 0) {  // a grid barrier of the orthogonalisation timed out
+        cudaStreamSynchronize(st);
+        cudaMemsetAsync(c->step_words, 0, sizeof(unsigned) * 4, st);
+        cudaStreamSynchronize(st);
+        return (int)step_err;
+      }
       for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hp[i];
       double hn = std::sqrt(hp[kPartStride]);
       H[(size_t)(j + 1) * m + j] = hn;

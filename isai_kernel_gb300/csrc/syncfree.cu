@@ -24,6 +24,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "gridsync.cuh"
 #include "scan.cuh"
 
 namespace bilu {
@@ -47,22 +48,6 @@ struct SyncState {
   // updates in row I (null: not counted, every dependency searches)
   const int* nmatch = nullptr;
 };
-
-// Exponential back-off between polls (32 ns doubling to 256 ns): waiters that
-// spin at full rate flood the L2 with flag reads and slow the rows they wait
-// for.
-__device__ __forceinline__ void backoff(unsigned& ns) {
-  __nanosleep(ns);
-  ns = ns < 256u ? ns * 2u : 256u;
-}
-
-// Acquire side of the flag handshake.  Flags are polled with relaxed loads
-// (an acquire load per poll would invalidate L1 on every iteration of every
-// spinning warp); once the release store is observed, one acquire fence
-// orders the reads of the producer's data after it.
-__device__ __forceinline__ void fence_acquire() {
-  asm volatile("fence.acq_rel.gpu;" ::: "memory");
-}
 
 // Warp-wide wait until flags[K] != 0.  Returns false if the launch aborted.
 __device__ __forceinline__ bool warp_wait(const int* flag, int* err, long long spin) {
@@ -429,79 +414,6 @@ __global__ void k_level_scatter(int nb, const int* __restrict__ level, int* curs
 // processes the rows of a level with one warp each and then meets at a
 // grid-wide barrier; no per-row flags are polled.
 
-struct GridSync {
-  unsigned* count;  // arrivals since the launch started
-  unsigned* gen;    // CTAs that have left the kernel (grid_exit_count)
-  int* err;         // 0 or a bilu_status; set on a barrier timeout
-  long long spin;   // polls before a waiting CTA gives up
-  int per_sm = 1;   // CTAs of the launch resident on one SM
-};
-
-__device__ __forceinline__ unsigned ld_relaxed_u(const unsigned* p) {
-  unsigned v;
-  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ unsigned atom_add_acq_rel_u(unsigned* p, unsigned v) {
-  unsigned old;
-  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v)
-               : "memory");
-  return old;
-}
-
-// Counting grid barrier.  After __syncthreads, thread 0 of each CTA arrives
-// with an acquire-release atomic (release: the CTA's writes, ordered before
-// it by the CTA barrier, become visible with it); the arrival count grows
-// through the launch (barrier b is complete when it reaches
-// (b + 1) x gridDim.x) and every CTA polls the count itself with relaxed
-// loads and back-off, then takes one acquire fence, so the release reaches
-// the waiting CTAs with the last arrival's atomic.  (On GB300 an
-// acquire-release arrival costs ~0.9 us less than a fence + relaxed atomic
-// at 304 CTAs, and polling the count ~0.7 us less than a generation word
-// that the last arriver writes after its atomic returns.)  `passed` counts the
-// barriers this CTA has passed (thread 0's copy is the one used).  The
-// comparison is modulo 2^32.  g.gen counts CTAs that have left the kernel
-// (grid_exit_count); both words are 0 between launches.
-__device__ __forceinline__ bool grid_sync_count(const GridSync& g, unsigned& passed) {
-  __shared__ int ok_s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    const unsigned target = (passed + 1u) * gridDim.x;
-    unsigned v = atom_add_acq_rel_u(g.count, 1u) + 1u;
-    long long n = 0;
-    unsigned ns = 32;
-    while ((int)(v - target) < 0) {
-      if (ld_relaxed(g.err) != 0) { ok = 0; break; }
-      if (++n > g.spin) {
-        atomicCAS(g.err, 0, (int)BILU_ERR_TIMEOUT);
-        ok = 0;
-        break;
-      }
-      backoff(ns);
-      v = ld_relaxed_u(g.count);
-    }
-    fence_acquire();
-    passed += 1u;
-    ok_s = ok;
-  }
-  __syncthreads();
-  return ok_s != 0;
-}
-
-// End of a launch that used grid_sync_count: a CTA arrives here only after
-// passing every barrier, so when the last one arrives no CTA polls the
-// count any more and both words can go back to 0 for the next launch.  (A
-// launch that aborted skips this; its error word is set and the caller
-// clears the words before the next solve.)
-__device__ __forceinline__ void grid_exit_count(const GridSync& g) {
-  if (threadIdx.x == 0 && atomicAdd(g.gen, 1u) == gridDim.x - 1u) {
-    atomicExch(g.count, 0u);
-    atomicExch(g.gen, 0u);
-  }
-}
-
 // Dependencies of row I: lower -> columns in [row[I], diag[I]); upper ->
 // columns in (diag[I], row[I+1]).  cnt[K] += 1 per dependent of K.
 __global__ void k_dep_count(int nb, const int* __restrict__ row, const int* __restrict__ col,
@@ -528,16 +440,18 @@ __global__ void k_dep_fill(int nb, const int* __restrict__ row, const int* __res
   }
 }
 
-// Appends the rows of the warp's ready lanes to order[] with one atomic on
-// the tail per warp (ballot + prefix count).  Called by all 32 lanes.
-__device__ __forceinline__ void warp_append(bool ready, int J, int* order, int* tail) {
+// Appends the rows of the warp's ready lanes to order[base0 + ...] with one
+// atomic on the level's append counter per warp (ballot + prefix count).
+// Called by all 32 lanes.
+__device__ __forceinline__ void warp_append(bool ready, int J, int* order, int base0,
+                                            int* count) {
   const unsigned m = __ballot_sync(FULL, ready);
   if (!m) return;
   const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
   int base = 0;
-  if (lane == leader) base = atomicAdd(tail, __popc(m));
+  if (lane == leader) base = atomicAdd(count, __popc(m));
   base = __shfl_sync(FULL, base, leader);
-  if (ready) order[base + __popc(m & ((1u << lane) - 1u))] = J;
+  if (ready) order[base0 + base + __popc(m & ((1u << lane) - 1u))] = J;
 }
 
 // Breadth-first level sweep (Kahn's algorithm, one level per barrier):
@@ -545,13 +459,23 @@ __device__ __forceinline__ void warp_append(bool ready, int J, int* order, int* 
 // (lvl_ptr[nlev] = nb), *nlev the number of levels.  Warps take 32
 // consecutive frontier rows, walk their successor lists in step (one slot
 // per lane and round), decrement in-degrees and append the rows that reach
-// zero with one atomic per warp; after the counting barrier every CTA reads
-// where the next frontier ends from the append counter.  The rows inside a
-// level come in append order (k_sort_levels orders them afterwards); the
-// level sizes do not depend on it.
+// zero with one atomic per warp.  The rows inside a level come in append
+// order (k_sort_levels orders them afterwards); the level sizes do not
+// depend on it.
+//
+// Every CTA must see the same frontier: after the barrier that closes
+// level l, each CTA reads how many rows level l appended, while the CTAs
+// that left the barrier first are already appending level l + 1's rows.
+// So the levels count their appends in three rotating counters (cnt[l % 3];
+// the rows of the initial frontier in cnt[2]): the one a CTA reads after
+// barrier l is not written again until level l + 3, and CTA 0 clears the
+// counter of level l + 1 while it works on level l, after every CTA has
+// read it at level l - 2 (barrier l - 1 orders the reads before the clear,
+// barrier l the clear before the appends).  Rows go to absolute positions
+// e + count, e being the end of the current frontier, which every CTA knows.
 __global__ void __launch_bounds__(256) k_bfs_levels(int nb, const int* __restrict__ sptr,
                                                     const int* __restrict__ sidx, int* indeg,
-                                                    int* order, int* lvl_ptr, int* tail,
+                                                    int* order, int* lvl_ptr, int* cnt,
                                                     int* nlev, GridSync gs) {
   __shared__ int end_s;
   unsigned passed = 0;
@@ -561,10 +485,10 @@ __global__ void __launch_bounds__(256) k_bfs_levels(int nb, const int* __restric
   const long long nthr = (long long)gridDim.x * blockDim.x;
   for (long long I0 = wbase; I0 < nb; I0 += nthr) {
     const long long I = I0 + lane;
-    warp_append(I < nb && indeg[I] == 0, (int)I, order, tail);
+    warp_append(I < nb && indeg[I] == 0, (int)I, order, 0, cnt + 2);
   }
   if (!grid_sync_count(gs, passed)) return;
-  if (threadIdx.x == 0) end_s = ld_relaxed(tail);
+  if (threadIdx.x == 0) end_s = ld_relaxed(cnt + 2);
   __syncthreads();
   int s = 0, e = end_s;
   if (tid == 0) {
@@ -577,6 +501,8 @@ __global__ void __launch_bounds__(256) k_bfs_levels(int nb, const int* __restric
       grid_exit_count(gs);
       return;
     }
+    if (tid == 0) atomicExch(cnt + (l + 1) % 3, 0);
+    int* count = cnt + l % 3;
     for (long long q0 = s + wbase; q0 < e; q0 += nthr) {
       const long long q = q0 + lane;
       const int I = q < e ? __ldcg(order + q) : -1;
@@ -590,11 +516,11 @@ __global__ void __launch_bounds__(256) k_bfs_levels(int nb, const int* __restric
           ready = atomicSub(indeg + J, 1) == 1;
           ++p;
         }
-        warp_append(ready, J, order, tail);
+        warp_append(ready, J, order, e, count);
       }
     }
     if (!grid_sync_count(gs, passed)) return;
-    if (threadIdx.x == 0) end_s = ld_relaxed(tail);
+    if (threadIdx.x == 0) end_s = e + ld_relaxed(count);
     __syncthreads();
     s = e;
     e = end_s;
@@ -1851,13 +1777,15 @@ int build_levels(int nb, const int* row, const int* col, const int* diag, int lo
   int* cursor = ws.take<int>((size_t)nb + 1);
   int* indeg = ws.take<int>((size_t)nb + 1);
   int* sidx = ws.take<int>((size_t)std::max(ndeps_max, 1ll));
-  int* tail = ws.take<int>(2);
+  // tail[1]: the largest dependency count (k_dep_count); tail[4..6]: the
+  // breadth-first sweep's append counters
+  int* tail = ws.take<int>(8);
   if (!sptr || !cursor || !indeg || !sidx || !tail) return BILU_ERR_WORKSPACE;
   GridSync gs;
   BILU_TRY(grid_sync_init(gs, ws, st));
   BILU_TRY_CUDA(cudaMemsetAsync(sptr, 0, sizeof(int) * ((size_t)nb + 1), st));
   BILU_TRY_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * ((size_t)nb + 1), st));
-  BILU_TRY_CUDA(cudaMemsetAsync(tail, 0, sizeof(int) * 2, st));
+  BILU_TRY_CUDA(cudaMemsetAsync(tail, 0, sizeof(int) * 8, st));
   BILU_TRY_CUDA(cudaMemsetAsync(nlev_d, 0, sizeof(int) * 4, st));
   BILU_TRY_CUDA(cudaMemsetAsync(lvl_ptr, 0, sizeof(int) * ((size_t)nb + 2), st));
   if (nb == 0) {
@@ -1878,7 +1806,8 @@ int build_levels(int nb, const int* row, const int* col, const int* diag, int lo
   int grid = std::min<long long>(std::min(coop_grid((const void*)k_bfs_levels, 256),
                                           2 * sm_count()),
                                  ceil_div(nb, 256));
-  void* args[] = {&nb, &sptr, &sidx, &indeg, &order, &lvl_ptr, &tail, &nlev_d, &gs};
+  int* cnt = tail + 4;
+  void* args[] = {&nb, &sptr, &sidx, &indeg, &order, &lvl_ptr, &cnt, &nlev_d, &gs};
   BILU_TRY(launch_coop((const void*)k_bfs_levels, grid, 256, args, st));
   int herr = grid_sync_finish(gs, st);
   if (herr != 0) return herr;
@@ -2021,7 +1950,7 @@ size_t syncfree_ws(int nb) {
 // Level analysis scratch (successor lists of up to ndeps dependencies).
 size_t levels_ws(int nb, long long ndeps) {
   return carve_size(sizeof(int) * ((size_t)nb + 1)) * 3 +
-         carve_size(sizeof(int) * (size_t)std::max(ndeps, 1ll)) + carve_size(sizeof(int) * 2) +
+         carve_size(sizeof(int) * (size_t)std::max(ndeps, 1ll)) + carve_size(sizeof(int) * 8) +
          carve_size(sizeof(unsigned) * 4) + scan_ws_bytes(nb + 1);
 }
 

@@ -718,16 +718,45 @@ static void isai_apply(const isai_apply_t* P, int precond, const double* v,
   }
 }
 
-/* FP32 dot product: float products and float sums inside each chunk, the
- * chunk sums added in double in chunk order (thread-count independent). */
-static double dot_chunked_f32(size_t n, const float* a, const float* b) {
+/* One modified Gram-Schmidt sweep over w, chunk by chunk: w -= hp * vp
+ * (when vp is given), then the chunked dot product vn . w (w . w when vn is
+ * NULL).  Inside a chunk every element of w is updated before it enters the
+ * dot product, so the result equals the separate update pass followed by
+ * dot_chunked, bit for bit, with one pass over the vectors instead of two. */
+static double sweep_chunked(size_t n, const double* vp, double hp, const double* vn,
+                            double* w) {
   size_t nch = (n + CHUNK - 1) / CHUNK;
   double* part = (double*)malloc(sizeof(double) * (nch > 0 ? nch : 1));
 #pragma omp parallel for schedule(static)
   for (long c = 0; c < (long)nch; ++c) {
     size_t lo = (size_t)c * CHUNK, hi = lo + CHUNK < n ? lo + CHUNK : n;
+    if (vp)
+      for (size_t i = lo; i < hi; ++i) w[i] -= hp * vp[i];
+    const double* o = vn ? vn : w;
+    double s = 0.0;
+    for (size_t i = lo; i < hi; ++i) s += o[i] * w[i];
+    part[c] = s;
+  }
+  double s = 0.0;
+  for (size_t c = 0; c < nch; ++c) s += part[c];
+  free(part);
+  return s;
+}
+
+/* The same in FP32: float products and float sums inside each chunk, the
+ * chunk sums added in double in chunk order (thread-count independent). */
+static double sweep_chunked_f32(size_t n, const float* vp, float hp, const float* vn,
+                                float* w) {
+  size_t nch = (n + CHUNK - 1) / CHUNK;
+  double* part = (double*)malloc(sizeof(double) * (nch > 0 ? nch : 1));
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < (long)nch; ++c) {
+    size_t lo = (size_t)c * CHUNK, hi = lo + CHUNK < n ? lo + CHUNK : n;
+    if (vp)
+      for (size_t i = lo; i < hi; ++i) w[i] -= hp * vp[i];
+    const float* o = vn ? vn : w;
     float s = 0.0f;
-    for (size_t i = lo; i < hi; ++i) s += a[i] * b[i];
+    for (size_t i = lo; i < hi; ++i) s += o[i] * w[i];
     part[c] = (double)s;
   }
   double s = 0.0;
@@ -738,8 +767,8 @@ static double dot_chunked_f32(size_t n, const float* a, const float* b) {
 
 /* Inner solve of the nested (GMRES-IR) mode: k steps of right-preconditioned
  * GMRES in FP32 on A s = v, from s = 0, with the FP32-stored A and the
- * FP32-stored ISAI (M = M_U M_L), modified Gram-Schmidt in FP32 (dot
- * products as dot_chunked_f32), the Hessenberg least-squares problem in
+ * FP32-stored ISAI (M = M_U M_L), modified Gram-Schmidt in FP32 (fused
+ * sweeps, sweep_chunked_f32), the Hessenberg least-squares problem in
  * double.  v has unit norm (the outer basis vector), so the start vector is
  * v rounded to FP32 with beta = 1: FGMRES accepts any scaling of its
  * preconditioned vectors.  The preconditioned vectors q_i = M u_i are kept,
@@ -769,15 +798,14 @@ static int inner_gmres_f32(const inner_t* I, const double* v, double* z) {
     orc_bcsr_spmv_f32(I->nb, I->bs, I->Lrow, I->Lcol, I->L32, uj, I->t);
     orc_bcsr_spmv_f32(I->nb, I->bs, I->Urow, I->Ucol, I->U32, I->t, qj);
     orc_bcsr_spmv_f32(I->nb, I->bs, I->Arow, I->Acol, I->A32, qj, I->w);
+    /* fused sweeps: sweep i applies h_{i-1} u_{i-1} and takes u_i . w */
     for (int i = 0; i <= j; ++i) {
-      const float* ui = I->Ub + n * (size_t)i;
-      double h = dot_chunked_f32(n, ui, I->w);
-      I->H[i * k + j] = h;
-      float hf = (float)h;
-#pragma omp parallel for schedule(static)
-      for (long e = 0; e < (long)n; ++e) I->w[e] -= hf * ui[e];
+      const float* up = i > 0 ? I->Ub + n * (size_t)(i - 1) : NULL;
+      const float hp = i > 0 ? (float)I->H[(i - 1) * k + j] : 0.0f;
+      I->H[i * k + j] = sweep_chunked_f32(n, up, hp, I->Ub + n * (size_t)i, I->w);
     }
-    double hn = sqrt(dot_chunked_f32(n, I->w, I->w));
+    double hn = sqrt(sweep_chunked_f32(n, I->Ub + n * (size_t)j, (float)I->H[j * k + j], NULL,
+                                       I->w));
     I->H[(j + 1) * k + j] = hn;
     if (hn != 0.0) {
       float inv = (float)(1.0 / hn);
@@ -925,14 +953,11 @@ int orc_gmres_ex(int nb, int bs, const int* Arow, const int* Acol,
         orc_bcsr_spmv(nb, bs, Arow, Acol, Aval, zj, w);
       }
       /* modified Gram-Schmidt */
-      for (int i = 0; i <= j; ++i) {
-        const double* vi = V + n * (size_t)i;
-        double h = dot_chunked(n, vi, w);
-        H[i * m + j] = h;
-#pragma omp parallel for schedule(static)
-        for (long e = 0; e < (long)n; ++e) w[e] -= h * vi[e];
-      }
-      double hn = sqrt(dot_chunked(n, w, w));
+      /* fused sweeps: sweep i applies h_{i-1} v_{i-1} and takes v_i . w */
+      for (int i = 0; i <= j; ++i)
+        H[i * m + j] = sweep_chunked(n, i > 0 ? V + n * (size_t)(i - 1) : NULL,
+                                     i > 0 ? H[(i - 1) * m + j] : 0.0, V + n * (size_t)i, w);
+      double hn = sqrt(sweep_chunked(n, V + n * (size_t)j, H[j * m + j], NULL, w));
       H[(j + 1) * m + j] = hn;
       double* vn = V + n * (size_t)(j + 1);
       if (hn != 0.0) {

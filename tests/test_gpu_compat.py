@@ -53,7 +53,7 @@ def write_mtx(path, A):
         f.write(f"{A.n} {A.n} {len(val)}\n")
         for i in range(A.n):
             for p in range(row[i], row[i + 1]):
-                f.write(f"{i + 1} {col[p] + 1} {val[p]!r}\n")
+                f.write(f"{i + 1} {col[p] + 1} {float(val[p])!r}\n")
     return row, col, val
 
 
