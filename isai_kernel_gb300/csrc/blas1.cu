@@ -465,6 +465,21 @@ int mgs_step_f32(long long n, const float* V, long long ldv, int j, float* w, do
                            nullptr, st);
 }
 
+int inner_lsq(int k, const double* H, const double* ww, double* y, cudaStream_t st) {
+  if (k < 1 || k > kMaxVec) return BILU_ERR_ARG;
+  k_inner_lsq<<<1, 32, 0, st>>>(k, H, ww, y);
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
+}
+
+int combine_f32(long long n, const float* Q, long long ldq, int k, const double* y, double* z,
+                cudaStream_t st) {
+  const int nv = k;
+  BILU_NV_CASES(launch_combine, n, Q, ldq, y, z, st);
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
+}
+
 int residual_norm(long long n, const double* b, const double* ax, double* r, double* partial,
                   cudaStream_t st) {
   k_residual<<<kRedCTAs, kRedThreads, 0, st>>>(n, b, ax, r, partial);

@@ -29,6 +29,31 @@ def test_library_exports_every_declared_symbol():
         assert getattr(L, name) is not None
 
 
+def test_library_leaves_no_internal_symbol_undefined():
+    """Every function of the library's own namespace is defined inside it
+    (an undefined one only fails at load time on the GPU host)."""
+    out = subprocess.run(["nm", "-D", "--undefined-only", _lib.LIBPATH], capture_output=True,
+                         text=True, check=True).stdout
+    missing = [ln.split()[-1] for ln in out.splitlines() if "_ZN4bilu" in ln]
+    assert not missing, missing
+
+
+def test_nested_mode_argument_checks():
+    L = _lib.lib()
+    assert L.bilu_ctx_set_inner(None, 8) == -1
+    assert L.bilu_ctx_inner_steps(None, None) == -1
+    h = ctypes.c_void_p()
+    assert L.bilu_ctx_create(ctypes.byref(h), None) == 0
+    assert L.bilu_ctx_set_inner(h, 0) == -1 and L.bilu_ctx_set_inner(h, 33) == -1
+    assert L.bilu_ctx_set_inner(h, 8) == 0
+    steps = ctypes.c_longlong(-1)
+    assert L.bilu_ctx_inner_steps(h, ctypes.byref(steps)) == 0 and steps.value == 0
+    # a solve before any setup is refused without touching a GPU
+    assert L.bilu_ctx_solve(h, _lib.BILU_NESTED, ctypes.c_void_p(8), ctypes.c_void_p(16), 30,
+                            ctypes.c_double(1e-10), 10, None, None, None) == -1
+    assert L.bilu_ctx_destroy(h) == 0
+
+
 def test_host_queries():
     L = _lib.lib()
     assert L.bilu_version() >= 10000
