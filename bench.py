@@ -74,8 +74,8 @@ def parse():
     ap.add_argument("--batch-mem-gb", type=float, default=160.0)
     ap.add_argument("--pl-nb", type=int, default=500000)
     ap.add_argument("--profile", action="store_true",
-                    help="short run for ncu launch lists: setup, one warm-up and one timed "
-                         "solve capped at --maxit, the apply loop; no e2e, no CPU baseline")
+                    help="short run for ncu launch lists: the setup, then --warmup and --steps "
+                         "nested solves, nothing else")
     a = ap.parse_args()
     if a.profile:
         a.no_cpu_baseline = True
@@ -403,6 +403,14 @@ def run_ours(args):
     res_mixed = res
     x_nested = x.cpu().numpy().copy()
     t_mixed = max_over_ranks(statistics.mean(times), world)
+    if args.profile:
+        # launch lists: the setup, the warm-up and the timed nested solves only
+        P.close()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": t_mixed, "unit": "s", "profile": True,
+                              "iters": {"outer": res.iters, "inner": res.inner_steps},
+                              "gpu_launches": int(launches)}))
+        return
 
     def timed(prec, out=None):
         solve(prec, out)
@@ -841,7 +849,48 @@ def run_kernels(args):
         L.bilu_bcsr_spmv_f32(nb, bs, p_(row), p_(col), p_(A32), p_(q), 1, p_(w), 1, api._s())
     torch.cuda.synchronize()
     P.close()
-    print(json.dumps({"workload": f"kernels convdiff3d {args.side}^3", "rounds": args.steps}))
+    # one orthogonalisation step (j = 15: 17 fused sweeps) on basis vectors
+    # of the system's length, FP64 and FP32, CUDA events after a warm-up
+    out = {"workload": f"kernels convdiff3d {args.side}^3", "rounds": args.steps}
+    ldv = (n + 31) // 32 * 32
+    wsb = L.bilu_debug_mgs_step_ws_bytes()
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    j = 15
+    rates = (ctypes.c_double * 3)()
+    probe_lib().probe_rates(rates)
+    for fp32, dt in ((0, torch.float64), (1, torch.float32)):
+        g = torch.Generator(device=dev).manual_seed(1)
+        V = torch.randn((j + 1) * ldv, dtype=dt, device=dev, generator=g)
+        w0 = torch.randn(ldv, dtype=dt, device=dev, generator=g)
+        w = torch.empty_like(w0)
+        h = torch.empty(j + 2, dtype=torch.float64, device=dev)
+        vn = torch.empty_like(w0)
+        times = []
+        for rep in range(args.steps + 1):
+            w.copy_(w0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            rc = L.bilu_debug_mgs_step(n, fp32, p_(V), ldv, j, p_(w), p_(h), p_(vn), p_(ws), wsb,
+                                       api._s())
+            e1.record()
+            e1.synchronize()
+            assert rc == 0, rc
+            if rep:
+                times.append(e0.elapsed_time(e1) * 1e3)
+        us = statistics.mean(times)
+        sweeps = j + 2
+        key = "mgs_step_fp32" if fp32 else "mgs_step_fp64"
+        out[key] = {"us_per_step": us, "sweeps": sweeps, "us_per_sweep": us / sweeps}
+        if not fp32:
+            # two DFMAs per element and sweep (update and dot product)
+            floor = 2 * n * 2 / (rates[0] * 1e12) * 1e6
+            out[key]["dfma_floor_us_per_sweep"] = floor
+            out[key]["frac_of_dfma_floor"] = floor / (us / sweeps)
+        else:
+            # one basis vector from DRAM per sweep (w and v_i stay in the L2)
+            peak, _ = peaks()
+            out[key]["hbm_floor_us_per_sweep"] = n * 4 / (peak * 1e9) * 1e6
+    print(json.dumps(out))
 
 
 def main():

@@ -537,6 +537,17 @@ int bilu_debug_sptrsv_withhold_flow(int nb, int nnzb, int bs, const int* d_row, 
  * kernels give the product to within rounding for any pattern; this
  * exercises the one the check would not pick for a given pattern. */
 int bilu_debug_spmv_layout_set(int mb, int bs, const int* d_row, int layout);
+/* One modified Gram-Schmidt step of the Krylov solvers' orthogonalisation
+ * kernel (one cooperative launch): w is orthogonalised against the j+1
+ * basis vectors V[0..j] (stride ldv elements, FP64, or FP32 when fp32 != 0)
+ * by fused sweeps; d_h[0..j] receives h_i = v_i . w, d_h[j+1] = ||w||^2,
+ * and d_vnext (optional) w / ||w||.  Vectors start on 16-byte boundaries;
+ * workspace bilu_debug_mgs_step_ws_bytes().  Synchronises the stream;
+ * returns BILU_ERR_TIMEOUT if a grid barrier gave up. */
+size_t bilu_debug_mgs_step_ws_bytes(void);
+int bilu_debug_mgs_step(long long n, int fp32, const void* d_V, long long ldv, int j, void* d_w,
+                        double* d_h, void* d_vnext, void* d_ws, size_t ws_bytes,
+                        bilu_stream_t stream);
 
 #ifdef __cplusplus
 }

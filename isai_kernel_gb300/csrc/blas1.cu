@@ -256,6 +256,9 @@ struct MgsVec<double> {
   static constexpr int W = 2;
   __device__ static V ldcg(const V* p) { return __ldcg(p); }
   __device__ static V ldcs(const V* p) { return __ldcs(p); }
+  // v_i streams through with evict-first loads: w (67 MB at 128^3) and a
+  // kept v_i would not both fit in the L2
+  __device__ static V ldnext(const V* p) { return __ldcs(p); }
   __device__ static void axpy(double h, const V& p, V& w) {
     w.x = fma(h, p.x, w.x);
     w.y = fma(h, p.y, w.y);
@@ -275,6 +278,9 @@ struct MgsVec<float> {
   static constexpr int W = 4;
   __device__ static V ldcg(const V* p) { return __ldcg(p); }
   __device__ static V ldcs(const V* p) { return __ldcs(p); }
+  // v_i stays in the L2 for the next sweep, which reads it as v_{i-1}
+  // (w and v_i take 67 MB at 128^3)
+  __device__ static V ldnext(const V* p) { return __ldcg(p); }
   __device__ static void axpy(float h, const V& p, V& w) {
     w.x = fmaf(h, p.x, w.x);
     w.y = fmaf(h, p.y, w.y);
@@ -324,13 +330,15 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_mgs_step(
     T a[4] = {T(0), T(0), T(0), T(0)};
     const VT* vpv = reinterpret_cast<const VT*>(vp);
     const VT* vnv = reinterpret_cast<const VT*>(vn);
+    // two elements' loads in flight per thread
+#pragma unroll 2
     for (long long e = tid; e < nv; e += stride) {
       VT we = M::ldcg(wv + e);
       if (vp) {
         M::axpy(hn, M::ldcs(vpv + e), we);
         wv[e] = we;
       }
-      M::dot(vn ? M::ldcg(vnv + e) : we, we, a);
+      M::dot(vn ? M::ldnext(vnv + e) : we, we, a);
     }
     if (tid < n - tail) {  // the last n % W elements
       const long long e = tail + tid;
@@ -488,3 +496,36 @@ int residual_norm(long long n, const double* b, const double* ax, double* r, dou
 }
 
 }  // namespace bilu
+
+using namespace bilu;
+
+// Test and measurement hook: one modified Gram-Schmidt step (mgs_step or
+// its FP32 form) on caller vectors.
+extern "C" size_t bilu_debug_mgs_step_ws_bytes(void) {
+  return sizeof(double) * 2 * kStepMaxCTAs + 256 + sizeof(unsigned) * 4;
+}
+
+extern "C" int bilu_debug_mgs_step(long long n, int fp32, const void* d_V, long long ldv, int j,
+                                   void* d_w, double* d_h, void* d_vnext, void* d_ws,
+                                   size_t ws_bytes, bilu_stream_t stream) {
+  if (n < 1 || j < 0 || j >= kMaxVec || ldv < n || !d_V || !d_w || !d_h || !d_ws ||
+      ws_bytes < bilu_debug_mgs_step_ws_bytes())
+    return BILU_ERR_ARG;
+  // 16-byte vector accesses: every basis vector starts on a 16-byte boundary
+  if ((ldv * (fp32 ? 4 : 8)) % 16 != 0 || ((uintptr_t)d_V | (uintptr_t)d_w) % 16 != 0 ||
+      (d_vnext && (uintptr_t)d_vnext % 16 != 0))
+    return BILU_ERR_ARG;
+  cudaStream_t st = S(stream);
+  double* partial = (double*)d_ws;
+  unsigned* words = (unsigned*)((char*)d_ws + sizeof(double) * 2 * kStepMaxCTAs + 256);
+  BILU_TRY_CUDA(cudaMemsetAsync(words, 0, sizeof(unsigned) * 4, st));
+  int rc = fp32 ? mgs_step_f32(n, (const float*)d_V, ldv, j, (float*)d_w, d_h, 1, d_h + j + 1,
+                               partial, words, (float*)d_vnext, st)
+                : mgs_step(n, (const double*)d_V, ldv, j, (double*)d_w, d_h, 1, d_h + j + 1,
+                           partial, words, (double*)d_vnext, nullptr, st);
+  if (rc != BILU_OK) return rc;
+  int err = 0;
+  BILU_TRY_CUDA(cudaMemcpyAsync(&err, words + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BILU_TRY_CUDA(cudaStreamSynchronize(st));
+  return err;
+}

@@ -886,3 +886,51 @@ def test_gmres_nested_matches_oracle(cuda, orc, name, inner):
     if r is not None:
         assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.01e-10
     p.close()
+
+
+@pytest.mark.parametrize("fp32", [0, 1])
+def test_mgs_step_kernel(cuda, fp32):
+    """The one-launch Gram-Schmidt step (bilu_debug_mgs_step) against the
+    same modified Gram-Schmidt in numpy (FP64) on an orthonormal basis: h
+    within 1e-12 relative for FP64 vectors (2e-5 for FP32), v_{j+1} of unit
+    norm and orthogonal to the basis, n not a multiple of the vector width
+    (the scalar tail), two launches in a row identical bit for bit."""
+    import torch
+
+    from isai_kernel_gb300 import _lib, api
+
+    L = _lib.lib()
+    n, j = 100003, 6
+    ldv = (n + 31) // 32 * 32
+    rng = np.random.default_rng(3)
+    Vh = np.linalg.qr(rng.standard_normal((n, j + 1)))[0].T  # orthonormal rows
+    wh = rng.standard_normal(n)
+    dt = torch.float32 if fp32 else torch.float64
+    Vp = np.zeros((j + 1, ldv))
+    Vp[:, :n] = Vh
+    V = torch.from_numpy(Vp.ravel()).to(cuda).to(dt)
+    ws = torch.empty(L.bilu_debug_mgs_step_ws_bytes(), dtype=torch.uint8, device=cuda)
+    outs = []
+    for _ in range(2):
+        w = torch.zeros(ldv, dtype=dt, device=cuda)
+        w[:n] = torch.from_numpy(wh).to(dt)
+        h = torch.empty(j + 2, dtype=torch.float64, device=cuda)
+        vn = torch.zeros_like(w)
+        st = L.bilu_debug_mgs_step(n, fp32, api._p(V), ldv, j, api._p(w), api._p(h), api._p(vn),
+                                   api._p(ws), ws.numel(), api._s())
+        assert st == 0
+        outs.append((N(h), N(vn)))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    hg, vg = outs[0]
+    Vr = N(V).astype(np.float64).reshape(j + 1, ldv)[:, :n]
+    wr = N(torch.from_numpy(wh).to(dt)).astype(np.float64)
+    href = np.zeros(j + 2)
+    for i in range(j + 1):
+        href[i] = Vr[i] @ wr
+        wr = wr - href[i] * Vr[i]
+    href[j + 1] = wr @ wr
+    tol = 2e-5 if fp32 else 1e-12
+    np.testing.assert_allclose(hg, href, rtol=tol, atol=tol * np.abs(href).max())
+    v = vg[:n].astype(np.float64)
+    assert abs(np.linalg.norm(v) - 1.0) < (1e-5 if fp32 else 1e-12)
+    assert np.abs(Vr @ v).max() < (1e-4 if fp32 else 1e-10)
