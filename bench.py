@@ -72,6 +72,9 @@ def parse():
     ap.add_argument("--batch-rhs", type=int, default=32)
     ap.add_argument("--batch-seed", type=int, default=0)
     ap.add_argument("--batch-mem-gb", type=float, default=160.0)
+    ap.add_argument("--batch-schedule", default="persistent", choices=["persistent", "graph"],
+                    help="one cooperative launch per Arnoldi step, or a graph of per-phase "
+                         "launches")
     ap.add_argument("--pl-nb", type=int, default=500000)
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu launch lists: the setup, then --warmup and --steps "
@@ -646,8 +649,12 @@ def run_ours(args):
 def run_batch(args):
     """Secondary line: 256 seeded 2D 5-point 4-DOF systems, grid sides
     U{32..512} (seed s for system s), 32 uniform right-hand sides each, FP32
-    ISAI apply inside FP64 FGMRES(30), all systems in one block-diagonal setup
-    and per-step single launches; --maxit caps the Arnoldi steps per wave."""
+    ISAI apply inside FP64 FGMRES(30), all systems in one block-diagonal
+    setup, every Arnoldi step one cooperative launch over all (system, tile)
+    work of the wave; --maxit caps the Arnoldi steps per wave.  Systems of
+    this generator from a side of about 128 on are indefinite and restarted
+    GMRES stagnates on them, so the line reports the converged fraction by
+    grid side alongside the throughput."""
     import torch
 
     from isai_kernel_gb300 import api, gen
@@ -661,11 +668,21 @@ def run_batch(args):
     bt = api.Batch(mats)
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t0
+    bt.set_schedule(args.batch_schedule == "persistent")
     Bd = torch.from_numpy(B).cuda()
     X, iters, relres, stats = bt.solve(Bd, restart=args.restart, tol=args.tol, maxit=args.maxit,
                                        mem_budget=int(args.batch_mem_gb * (1 << 30)))
     cfg, tune_ms = bt.tuning()
     conv = float(np.mean(relres <= args.tol))
+    by_side = []
+    for lo, hi in ((32, 64), (65, 96), (97, 128), (129, 256), (257, 512)):
+        sel = (sides >= lo) & (sides <= hi)
+        if sel.any():
+            ok = relres[sel] <= args.tol
+            by_side.append({"sides": f"{lo}..{hi}", "systems": int(sel.sum()),
+                            "converged_fraction": float(ok.mean()),
+                            "median_iters_converged": float(np.median(iters[sel][ok]))
+                            if ok.any() else None})
     line = {"workload": f"batch {args.batch_count} x laplace2d U{{{args.batch_lo}..{args.batch_hi}}}"
                         f" bs4, {k} rhs, FGMRES({args.restart}) FP32 ISAI, maxit {args.maxit}",
             "systems": args.batch_count, "rhs": k, "block_rows": bt.nb,
@@ -673,6 +690,11 @@ def run_batch(args):
             "graph_launches": int(stats[1]), "pair_steps": int(stats[2]),
             "pair_steps_per_s": stats[2] / (stats[3] / 1e3),
             "converged_fraction": conv, "median_iters": float(np.median(iters)),
+            "by_side": by_side,
+            "schedule": ("one cooperative launch per Arnoldi step"
+                         if args.batch_schedule == "persistent" else
+                         "a replayed graph of per-phase launches per Arnoldi step"),
+            "ms_per_step": stats[3] / max(1, int(stats[1])),
             "autotune": {"rows_per_warp_A": cfg[0], "rows_per_warp_apply": cfg[1],
                          "tile_rows": cfg[2], "candidates_ms_A": tune_ms[:3],
                          "candidates_ms_apply": tune_ms[3:6]}}

@@ -483,6 +483,13 @@ int bilu_batch_solve(bilu_batch* batch, int k, const double* d_B, double* d_X, i
  * h_ms[6] = timed candidates (1, 2, 4 rows per warp) for the operator and
  * the apply. */
 int bilu_batch_tuning(bilu_batch* batch, int* h_cfg, double* h_ms);
+/* How bilu_batch_solve runs an Arnoldi step: 1 (default) as one
+ * cooperative launch over every (system, tile) of the wave -- the FP32
+ * apply, the operator SpMM, the Gram-Schmidt sweeps with their per-system
+ * sums, the normalisation and the Givens step, with bounded grid barriers
+ * between them; 0 as a replayed CUDA graph of one launch per phase.  Both
+ * give the same bits. */
+int bilu_batch_set_schedule(bilu_batch* batch, int persistent);
 
 /* ------------------------------------------------------------------ */
 /* Allocation-free solve                                               */

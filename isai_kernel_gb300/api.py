@@ -544,6 +544,11 @@ class Batch:
         self.setup_ms = list(times)
         self._np = np
 
+    def set_schedule(self, persistent: bool):
+        """One cooperative launch per Arnoldi step (True, the default) or a
+        graph of per-phase launches (False); the results are identical."""
+        call("bilu_batch_set_schedule", self._h, int(persistent))
+
     def close(self):
         if self._h:
             lib().bilu_batch_destroy(self._h)

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "gridsync.cuh"
 
 struct bilu_ctx;
 extern "C" int bilu_ctx_create(bilu_ctx** ctx, bilu_stream_t stream);
@@ -269,17 +270,15 @@ __global__ void k_cycle_init(int P, int m, PairState ps, const double* __restric
 
 // Givens step j of every running pair: hcol[q][pair] (q <= j) from the
 // sweeps, hn2[pair] = ||w||^2.
-__global__ void k_givens(int P, int m, int j, double tol, PairState ps,
-                         const double* __restrict__ hcol, const double* __restrict__ hn2) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= P) return;
+__device__ __forceinline__ void givens_pair(int i, int m, int j, double tol, PairState ps,
+                                            const double* hcol, const double* hn2, int P) {
   if (ps.status[i] != 0) return;
   double* H = ps.H + (long long)i * (m + 1) * m;
   double* cs = ps.cs + (long long)i * m;
   double* sn = ps.sn + (long long)i * m;
   double* g = ps.g + (long long)i * (m + 1);
-  for (int q = 0; q <= j; ++q) H[q * m + j] = hcol[(long long)q * P + i];
-  double hn = sqrt(hn2[i]);
+  for (int q = 0; q <= j; ++q) H[q * m + j] = __ldcg(hcol + (long long)q * P + i);
+  double hn = sqrt(__ldcg(hn2 + i));
   H[(j + 1) * m + j] = hn;
   for (int q = 0; q < j; ++q) {
     double a = H[q * m + j], b = H[(q + 1) * m + j];
@@ -299,6 +298,13 @@ __global__ void k_givens(int P, int m, int j, double tol, PairState ps,
   double res = fabs(g[j + 1]) / ps.bnorm[i];
   if (res <= tol || hn == 0.0 || j == m - 1) ps.status[i] = 1;
   else atomicAdd(ps.active, 1);
+}
+
+__global__ void k_givens(int P, int m, int j, double tol, PairState ps,
+                         const double* __restrict__ hcol, const double* __restrict__ hn2) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  givens_pair(i, m, j, tol, ps, hcol, hn2, P);
 }
 
 // Back substitution per pair (y = 0 for done pairs)
@@ -358,6 +364,214 @@ __global__ void k_bnorm(int P, PairState ps, const double* __restrict__ bb) {
   ps.iters[i] = 0;
 }
 
+
+// ---------------------------------------------------------------- one launch per step
+// The whole Arnoldi step of every pair of a wave in one cooperative launch
+// (k_batch_step): the FP32 apply (M_L, then M_U into Z_j), the operator
+// SpMM, the j+2 modified Gram-Schmidt sweeps with their per-system sums,
+// the normalisation of V_{j+1} and the Givens step of every pair, with a
+// counting grid barrier between dependent phases instead of a kernel
+// boundary.  Each phase walks its own work list: virtual warps of block
+// rows for the SpMMs (the rows-per-warp tile chosen by the autotuner),
+// tiles of scalar rows for the sweeps and the normalisation (two tiles at
+// a time, one per half of the 16-warp CTA, each reduced over its 8 warps
+// exactly as k_sweep does), systems for the segmented sums (16 warps each,
+// as k_segsum), pairs for Givens.  The arithmetic of every element and
+// every sum is that of the per-phase kernels, so both schedules give the
+// same bits; data written earlier in the launch is read through the L2.
+constexpr int kStepT = 32 * kSegWarps;  // threads of a k_batch_step CTA (16 warps)
+static_assert(kStepT == 2 * kBT, "a step CTA holds two sweep tiles of kBT threads");
+
+struct BatchStepArgs {
+  int r0, r1, k, j, m, P, nt, Sw;
+  double tol;
+  const int *Lrow, *Lcol, *Urow, *Ucol, *Arow, *Acol;
+  const float *L32, *U32;
+  const double* Aval;
+  float *v32, *t32;
+  double *V, *Zj, *w, *hcol, *hn2, *part;
+  long long vec;
+  const int *trow, *tsys, *stile;
+  PairState ps;
+  GridSync gs;
+};
+
+// k_spmm's rows for virtual warp vw, X read through the L2 (an earlier
+// phase of the same launch wrote it)
+template <int BS, class VT, class XT, class YT, int RPW>
+__device__ __forceinline__ void spmm_vwarp(long long vw, int lane, int r0, int r1, int k,
+                                           const int* __restrict__ row,
+                                           const int* __restrict__ col,
+                                           const VT* __restrict__ val, const XT* X, YT* Y) {
+  using AccT = VT;
+  constexpr int LPR = 32 / RPW;
+  constexpr int KL = RPW;
+  int sub = lane / LPR, l = lane - sub * LPR;
+  long long br = r0 + vw * RPW + sub;
+  if (br >= r1) return;
+  AccT acc[BS][KL];
+#pragma unroll
+  for (int r = 0; r < BS; ++r)
+#pragma unroll
+    for (int q = 0; q < KL; ++q) acc[r][q] = 0;
+  int s = __ldg(row + br), e = __ldg(row + br + 1);
+  for (int p = s; p < e; ++p) {
+    long long bc = (long long)__ldg(col + p) - r0;
+    const VT* blk = val + (long long)p * BS * BS;
+#pragma unroll
+    for (int kk = 0; kk < BS; ++kk) {
+      AccT xv[KL];
+#pragma unroll
+      for (int q = 0; q < KL; ++q) {
+        int c = l + q * LPR;
+        xv[q] = c < k ? (AccT)__ldcg(X + (bc * BS + kk) * k + c) : (AccT)0;
+      }
+#pragma unroll
+      for (int r = 0; r < BS; ++r) {
+        AccT a = __ldg(blk + r * BS + kk);
+#pragma unroll
+        for (int q = 0; q < KL; ++q) acc[r][q] = fma(a, xv[q], acc[r][q]);
+      }
+    }
+  }
+  long long yb = (br - r0) * BS;
+#pragma unroll
+  for (int q = 0; q < KL; ++q) {
+    int c = l + q * LPR;
+    if (c < k)
+#pragma unroll
+      for (int r = 0; r < BS; ++r) Y[(yb + r) * k + c] = (YT)acc[r][q];
+  }
+}
+
+template <int BS, class VT, class XT, class YT, int RPW>
+__device__ __forceinline__ void spmm_phase(int r0, int r1, int k, const int* row, const int* col,
+                                           const VT* val, const XT* X, YT* Y) {
+  const long long nvw = ((long long)(r1 - r0) + RPW - 1) / RPW;
+  const long long total = (long long)gridDim.x * (kStepT / 32);
+  const int lane = threadIdx.x & 31;
+  for (long long vw = (long long)blockIdx.x * (kStepT / 32) + (threadIdx.x >> 5); vw < nvw;
+       vw += total)
+    spmm_vwarp<BS, VT, XT, YT, RPW>(vw, lane, r0, r1, k, row, col, val, X, Y);
+}
+
+template <int BS, int RPWM, int RPWA>
+__global__ void __launch_bounds__(kStepT, BS <= 5 ? 2 : 1) k_batch_step(BatchStepArgs a) {
+  __shared__ double red[kStepT / 32][32];
+  unsigned passed = 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int half = warp >> 3, hw = warp & 7;  // sweep-tile half of the CTA, warp inside it
+  const int k = a.k, P = a.P, G = (int)gridDim.x;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *a.ps.active = 0;
+  // FP32 apply: t32 = M_L v32, Z_j = M_U t32 (FP64), then w = A Z_j
+  spmm_phase<BS, float, float, float, RPWM>(a.r0, a.r1, k, a.Lrow, a.Lcol, a.L32, a.v32, a.t32);
+  if (!grid_sync_count(a.gs, passed)) return;
+  spmm_phase<BS, float, float, double, RPWM>(a.r0, a.r1, k, a.Urow, a.Ucol, a.U32, a.t32, a.Zj);
+  if (!grid_sync_count(a.gs, passed)) return;
+  spmm_phase<BS, double, double, double, RPWA>(a.r0, a.r1, k, a.Arow, a.Acol, a.Aval, a.Zj,
+                                               a.w);
+  if (!grid_sync_count(a.gs, passed)) return;
+  for (int i = 0; i <= a.j + 1; ++i) {
+    const double* vp = i > 0 ? a.V + a.vec * (i - 1) : nullptr;
+    const double* hp = i > 0 ? a.hcol + (long long)(i - 1) * P : nullptr;
+    const double* vn = i <= a.j ? a.V + a.vec * i : nullptr;
+    double* out = i <= a.j ? a.hcol + (long long)i * P : a.hn2;
+    // sweep: tile partials (k_sweep's arithmetic per tile)
+    for (int t0 = 2 * blockIdx.x; t0 < a.nt; t0 += 2 * G) {
+      const int t = t0 + half;
+      double acc = 0.0;
+      if (t < a.nt && lane < k) {
+        const int sy = a.tsys[t];
+        const double h = vp ? -__ldcg(hp + (long long)sy * k + lane) : 0.0;
+        // the thread's rows in k_sweep's order, four rows' loads issued
+        // before their arithmetic
+        const long long re = a.trow[t + 1];
+        for (long long rr0 = a.trow[t] + hw; rr0 < re; rr0 += 4 * (kBT / 32)) {
+          double we[4], pv[4], ov[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const long long rr = rr0 + u * (kBT / 32);
+            const long long q = rr * k + lane;
+            const bool ok = rr < re;
+            we[u] = ok ? __ldcg(a.w + q) : 0.0;
+            pv[u] = (ok && vp) ? __ldcs(vp + q) : 0.0;
+            ov[u] = (ok && vn) ? __ldcs(vn + q) : 0.0;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const long long rr = rr0 + u * (kBT / 32);
+            if (rr >= re) break;
+            const long long q = rr * k + lane;
+            if (vp) {
+              we[u] = fma(h, pv[u], we[u]);
+              a.w[q] = we[u];
+            }
+            const double o = vn ? ov[u] : we[u];
+            acc = fma(o, we[u], acc);
+          }
+        }
+      }
+      red[warp][lane] = acc;
+      __syncthreads();
+      if (hw == 0 && t < a.nt) {
+        double v = 0.0;
+#pragma unroll
+        for (int q = 0; q < kBT / 32; ++q) v += red[half * 8 + q][lane];
+        if (lane < k) a.part[(long long)t * k + lane] = v;
+      }
+      __syncthreads();
+    }
+    if (!grid_sync_count(a.gs, passed)) return;
+    // per-system sums of the tile partials (k_segsum's order)
+    for (int sy = blockIdx.x; sy < a.Sw; sy += G) {
+      double v = 0.0;
+      if (lane < k) {
+        const int t1 = a.stile[sy + 1];
+        int t = a.stile[sy] + warp;
+        for (; t + 3 * kSegWarps < t1; t += 4 * kSegWarps) {
+          const double p0 = __ldcg(a.part + (long long)t * k + lane);
+          const double p1 = __ldcg(a.part + (long long)(t + kSegWarps) * k + lane);
+          const double p2 = __ldcg(a.part + (long long)(t + 2 * kSegWarps) * k + lane);
+          const double p3 = __ldcg(a.part + (long long)(t + 3 * kSegWarps) * k + lane);
+          v += p0;
+          v += p1;
+          v += p2;
+          v += p3;
+        }
+        for (; t < t1; t += kSegWarps) v += __ldcg(a.part + (long long)t * k + lane);
+      }
+      red[warp][lane] = v;
+      __syncthreads();
+      if (warp == 0 && lane < k) {
+        double r = 0.0;
+#pragma unroll
+        for (int q = 0; q < kSegWarps; ++q) r += red[q][lane];
+        out[(long long)sy * k + lane] = r;
+      }
+      __syncthreads();
+    }
+    if (!grid_sync_count(a.gs, passed)) return;
+  }
+  // V_{j+1} = w / ||w|| (k_scale_pairs) and the Givens step (k_givens)
+  double* vnext = a.V + a.vec * (a.j + 1);
+  for (int t0 = 2 * blockIdx.x; t0 < a.nt; t0 += 2 * G) {
+    const int t = t0 + half;
+    if (t >= a.nt || lane >= k) continue;
+    const int sy = a.tsys[t];
+    const double n2 = __ldcg(a.hn2 + (long long)sy * k + lane);
+    const double s = n2 > 0.0 ? 1.0 / sqrt(n2) : 0.0;
+    for (long long rr = a.trow[t] + hw; rr < a.trow[t + 1]; rr += kBT / 32) {
+      long long q = rr * k + lane;
+      double v = __ldcg(a.w + q) * s;
+      vnext[q] = v;
+      a.v32[q] = __double2float_rn(v);
+    }
+  }
+  for (int pi = blockIdx.x * kStepT + threadIdx.x; pi < P; pi += G * kStepT)
+    givens_pair(pi, a.m, a.j, a.tol, a.ps, a.hcol, a.hn2, P);
+  grid_exit_count(a.gs);
+}
+
 }  // namespace
 }  // namespace bilu
 
@@ -379,6 +593,9 @@ struct bilu_batch {
   // dot product, so the tile size is part of the arithmetic)
   int rpw_A = 1, rpw_M = 1, tile_rows = 128;
   bool tuned = false;
+  // 1: every Arnoldi step is one cooperative launch (k_batch_step); 0: a
+  // graph of per-phase kernels.  Both give the same bits.
+  int persistent = 1;
   double tune_ms[2][3] = {};
 };
 
@@ -434,7 +651,56 @@ int autotune(bilu_batch* B, int r0, int r1, int k, double* X, double* Y, float* 
   return BILU_OK;
 }
 
+template <int BS, int RM, int RA>
+int launch_batch_step_t(const BatchStepArgs& a, cudaStream_t st) {
+  static int grid = 0;
+  const void* fn = (const void*)k_batch_step<BS, RM, RA>;
+  if (!grid) {
+    int dev = 0, sms = 0, per = 0;
+    BILU_TRY_CUDA(cudaGetDevice(&dev));
+    BILU_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    BILU_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kStepT, 0));
+    if (per < 1) return BILU_ERR_UNSUPPORTED;
+    grid = per * sms;
+  }
+  BatchStepArgs arg = a;
+  void* args[] = {&arg};
+  BILU_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kStepT), args, 0, st));
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
+}
+
+template <int BS, int RM>
+int launch_batch_step_a(int ra, const BatchStepArgs& a, cudaStream_t st) {
+  switch (ra) {
+    case 1: return launch_batch_step_t<BS, RM, 1>(a, st);
+    case 2: return launch_batch_step_t<BS, RM, 2>(a, st);
+    case 4: return launch_batch_step_t<BS, RM, 4>(a, st);
+    default: return BILU_ERR_ARG;
+  }
+}
+
+template <int BS>
+int launch_batch_step_bs(int rm, int ra, const BatchStepArgs& a, cudaStream_t st) {
+  switch (rm) {
+    case 1: return launch_batch_step_a<BS, 1>(ra, a, st);
+    case 2: return launch_batch_step_a<BS, 2>(ra, a, st);
+    case 4: return launch_batch_step_a<BS, 4>(ra, a, st);
+    default: return BILU_ERR_ARG;
+  }
+}
+
+int launch_batch_step(int bs, int rm, int ra, const BatchStepArgs& a, cudaStream_t st) {
+  return BILU_DISPATCH_BS(bs, launch_batch_step_bs, rm, ra, a, st);
+}
+
 }  // namespace
+
+extern "C" int bilu_batch_set_schedule(bilu_batch* B, int persistent) {
+  if (!B || persistent < 0 || persistent > 1) return BILU_ERR_ARG;
+  B->persistent = persistent;
+  return BILU_OK;
+}
 
 extern "C" int bilu_batch_create(bilu_batch** b, bilu_stream_t stream) {
   if (!b) return BILU_ERR_ARG;
@@ -626,6 +892,9 @@ extern "C" int bilu_batch_solve(bilu_batch* Bt, int k, const double* d_B, double
   BILU_TRY(W.get(&W.tsys, (size_t)ntile_max));
   BILU_TRY(W.get(&W.stile, (size_t)ws_max + 1));
   BILU_TRY(W.get(&W.counters, 4));
+  unsigned* step_words = nullptr;  // count, exit count, error word of k_batch_step
+  BILU_TRY(W.get(&step_words, 4));
+  BILU_TRY_CUDA(cudaMemsetAsync(step_words, 0, sizeof(unsigned) * 4, st));
   BILU_TRY(W.get(&W.ps.H, (size_t)P * (m + 1) * m));
   BILU_TRY(W.get(&W.ps.cs, (size_t)P * m));
   BILU_TRY(W.get(&W.ps.sn, (size_t)P * m));
@@ -677,6 +946,33 @@ extern "C" int bilu_batch_solve(bilu_batch* Bt, int k, const double* d_B, double
       BILU_LAUNCH_CHECK();
       int jmax = -1;
       for (int j = 0; j < m && total < maxit; ++j) {
+        if (Bt->persistent) {
+          // the whole step in one cooperative launch, then the active count
+          // and the launch's barrier error word to the host
+          BatchStepArgs a{};
+          a.r0 = r0; a.r1 = r1; a.k = k; a.j = j; a.m = m; a.P = Pw; a.nt = nt; a.Sw = Sw;
+          a.tol = tol;
+          a.Lrow = Bt->Lrow; a.Lcol = Bt->Lcol; a.Urow = Bt->Urow; a.Ucol = Bt->Ucol;
+          a.Arow = Bt->Arow; a.Acol = Bt->Acol; a.L32 = Bt->L32; a.U32 = Bt->U32;
+          a.Aval = Bt->Aval; a.v32 = W.v32; a.t32 = W.t32; a.V = W.V; a.Zj = W.Z + vec * j;
+          a.w = W.w; a.hcol = W.hcol; a.hn2 = W.hn2; a.part = W.part; a.vec = (long long)vec;
+          a.trow = W.trow; a.tsys = W.tsys; a.stile = W.stile; a.ps = W.ps;
+          a.gs.count = step_words;
+          a.gs.gen = step_words + 1;
+          a.gs.err = reinterpret_cast<int*>(step_words + 2);
+          a.gs.spin = kSpinLimit;
+          BILU_TRY(launch_batch_step(bs, Bt->rpw_M, Bt->rpw_A, a, st));
+          ++graph_launches;
+          BILU_TRY_CUDA(cudaMemcpyAsync(W.hpin, W.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
+          BILU_TRY_CUDA(cudaMemcpyAsync(W.hpin + 2, step_words + 2, sizeof(int),
+                                        cudaMemcpyDeviceToHost, st));
+          BILU_TRY_CUDA(cudaStreamSynchronize(st));
+          if (W.hpin[2] != 0) return W.hpin[2];  // a grid barrier of the step timed out
+          ++total;
+          jmax = j;
+          if (W.hpin[0] == 0) break;
+          continue;
+        }
         if (!graphs[j]) {
           cudaGraph_t g;
           BILU_TRY_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));

@@ -364,15 +364,24 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_mgs_step(
       part[blockIdx.x] = t;
     }
     if (!grid_sync_count(gs, passed)) return;
-    // every CTA adds the partials in the same order
-    if (warp == 0) {
+    // every CTA adds the partials in the same order: thread t takes
+    // partials t, t + 256, ... (a few independent L2 loads, not one warp's
+    // chain of G / 32 of them), then the warp trees and the warps in order
+    {
       double t = 0.0;
-      for (int c = lane; c < G; c += 32) t += __ldcg(part + c);
+      for (int c = threadIdx.x; c < G; c += kStepThreads) t += __ldcg(part + c);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-      if (lane == 0) h_s = t;
+      if (lane == 0) red[warp] = t;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double u = 0.0;
+#pragma unroll
+        for (int q = 0; q < kStepThreads / 32; ++q) u += red[q];
+        h_s = u;
+      }
+      __syncthreads();
     }
-    __syncthreads();
     h = h_s;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       if (i <= j) hout[(long long)i * hstride] = h;

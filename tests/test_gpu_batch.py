@@ -3,7 +3,8 @@ several right-hand sides each, in one block-diagonal setup.  Every
 (system, rhs) pair must converge to 1e-10 true relative residual, take the
 iteration count of the single-RHS mixed-precision solve of the same system
 within +-2 (FP32 ISAI apply, different FP32 summation order), give the same
-answer whether the batch runs in one wave or in several (bit-identical),
+answer whether the batch runs in one wave or in several and whether a step
+is one cooperative launch or a graph of per-phase launches (bit-identical),
 and the SpMM of the apply must match the column-wise SpMV."""
 import numpy as np
 import pytest
@@ -51,6 +52,11 @@ def test_batch_matches_single_rhs(cuda, orc):
                                            mem_budget=1 << 20)
     assert stats2[0] > 1
     assert np.array_equal(iters2, iters) and np.array_equal(X2.cpu().numpy(), Xn)
+    # the graph of per-phase launches gives the bits of the one-launch step
+    bt.set_schedule(False)
+    X3, iters3, relres3, stats3 = bt.solve(torch.from_numpy(B_np).cuda(), maxit=3000)
+    assert np.array_equal(iters3, iters) and np.array_equal(X3.cpu().numpy(), Xn)
+    assert np.array_equal(relres3, relres)
     bt.close()
 
 
