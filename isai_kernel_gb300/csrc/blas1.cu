@@ -312,8 +312,11 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_mgs_step(
   using M = MgsVec<T>;
   using VT = typename M::V;
   constexpr int W = M::W;
-  __shared__ double red[kStepThreads / 32];
-  __shared__ double h_s;
+  // sums run in the kernel's own precision: on GB300 every FP64 add (and
+  // every FP32 <-> FP64 conversion) takes the FP64 pipe, which the FP64
+  // kernel needs for its DFMAs and the FP32 kernel should not touch
+  __shared__ T red_s[kStepThreads];
+  __shared__ T h_s;
   unsigned passed = 0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int G = (int)gridDim.x;
@@ -322,11 +325,11 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_mgs_step(
   const long long nv = n / W;     // whole vectors
   const long long tail = nv * W;  // first element of the scalar tail
   VT* wv = reinterpret_cast<VT*>(w);
-  double h = 0.0;
+  T h = T(0);
   for (int i = 0; i <= j + 1; ++i) {
     const T* vp = i > 0 ? V + (long long)(i - 1) * ldv : nullptr;
     const T* vn = i <= j ? V + (long long)i * ldv : nullptr;
-    const T hn = (T)(-h);
+    const T hn = -h;
     T a[4] = {T(0), T(0), T(0), T(0)};
     const VT* vpv = reinterpret_cast<const VT*>(vp);
     const VT* vnv = reinterpret_cast<const VT*>(vn);
@@ -350,47 +353,68 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_mgs_step(
       const T o = vn ? __ldcg(vn + e) : we;
       a[0] = fma(o, we, a[0]);
     }
-    // CTA partial in FP64 (FP32 sums stay per thread), fixed order
-    double acc = (double)((a[0] + a[1]) + (a[2] + a[3]));
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) red[warp] = acc;
+    // CTA partial, fixed order: the threads' sums through shared memory,
+    // warp 0 adds eight per lane and then the lanes by a shuffle tree
+    red_s[threadIdx.x] = (a[0] + a[1]) + (a[2] + a[3]);
     __syncthreads();
-    double* part = partial + (long long)(i & 1) * G;
-    if (threadIdx.x == 0) {
-      double t = 0.0;
+    T* part = reinterpret_cast<T*>(partial) + (long long)(i & 1) * kStepMaxCTAs;
+    if (warp == 0) {
+      T t = T(0);
 #pragma unroll
-      for (int q = 0; q < kStepThreads / 32; ++q) t += red[q];
-      part[blockIdx.x] = t;
+      for (int q = 0; q < kStepThreads / 32; ++q) t += red_s[lane + 32 * q];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == 0) part[blockIdx.x] = t;  // lane 0 of warp 0 arrives at the barrier
     }
     if (!grid_sync_count(gs, passed)) return;
-    // every CTA adds the partials in the same order: thread t takes
-    // partials t, t + 256, ... (a few independent L2 loads, not one warp's
-    // chain of G / 32 of them), then the warp trees and the warps in order
-    {
-      double t = 0.0;
+    // every CTA adds all partials in the same order
+    if constexpr (sizeof(T) == 8) {
+      // FP64: warp 0 alone (the adds take the FP64 pipe), lane l taking
+      // partials l, l + 32, ... in ascending order, eight loads in flight,
+      // then the shuffle tree
+      if (warp == 0) {
+        T t = T(0);
+        for (int c0 = 0; c0 < G; c0 += 8 * 32) {
+          T v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int c = c0 + lane + 32 * u;
+            v[u] = c < G ? __ldcg(part + c) : T(0);
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) t += v[u];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) h_s = t;
+      }
+    } else {
+      // FP32: every thread loads its few partials at once (one L2 round
+      // trip), the warps' trees, then warp 0 adds the eight warp sums
+      T t = T(0);
       for (int c = threadIdx.x; c < G; c += kStepThreads) t += __ldcg(part + c);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-      if (lane == 0) red[warp] = t;
+      __syncthreads();  // red_s is free again (warp 0 read it before the barrier)
+      if (lane == 0) red_s[warp] = t;
       __syncthreads();
       if (threadIdx.x == 0) {
-        double u = 0.0;
+        T u = T(0);
 #pragma unroll
-        for (int q = 0; q < kStepThreads / 32; ++q) u += red[q];
+        for (int q = 0; q < kStepThreads / 32; ++q) u += red_s[q];
         h_s = u;
       }
-      __syncthreads();
     }
+    __syncthreads();
     h = h_s;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-      if (i <= j) hout[(long long)i * hstride] = h;
-      else *wwout = h;
+      if (i <= j) hout[(long long)i * hstride] = (double)h;
+      else *wwout = (double)h;
     }
   }
   // v_{j+1} = w / ||w|| over this CTA's slice (zeros when ||w|| = 0)
   if (vnext) {
-    const T s = h > 0.0 ? (T)(1.0 / sqrt(h)) : T(0);
+    const T s = h > T(0) ? T(1) / sqrt(h) : T(0);
     VT* out = reinterpret_cast<VT*>(vnext);
     for (long long e = tid; e < nv; e += stride) {
       VT v = M::ldcg(wv + e);

@@ -49,8 +49,9 @@ int combine_f32(long long n, const float* Q, long long ldq, int k, const double*
 // h_i = v_i . w; the last one w . w) with a counting grid barrier between
 // them, w held in the L2: h_i into hout[i * hstride]
 // (i <= j), ||w||^2 into *wwout, then vnext = w / ||w|| (and vnext32, its
-// FP32 copy, when given; zeros when ||w|| = 0).  partial holds
-// 2 * kStepMaxCTAs doubles; words are the barrier's count, exit count and
+// FP32 copy, when given; zeros when ||w|| = 0).  Sums are in the vectors'
+// precision and in a fixed order (warp 0 of every CTA adds all CTA
+// partials alike).  partial holds 2 * kStepMaxCTAs doubles; words are the barrier's count, exit count and
 // error word (zero before the first launch; every launch leaves them zero
 // unless a barrier timed out, which sets the error word to
 // BILU_ERR_TIMEOUT).
@@ -58,8 +59,9 @@ constexpr int kStepMaxCTAs = 152 * 8;
 int mgs_step(long long n, const double* V, long long ldv, int j, double* w, double* hout,
              int hstride, double* wwout, double* partial, unsigned* words, double* vnext,
              float* vnext32, cudaStream_t st);
-// The FP32 form for the nested mode's inner solver (FP32 products and
-// per-thread sums, FP64 from the warp sums on).
+// The FP32 form for the nested mode's inner solver: FP32 products and FP32
+// sums throughout (the CTA partials and their sum too; the FP64 pipe is
+// left alone), h and ||w||^2 written as FP64.
 int mgs_step_f32(long long n, const float* V, long long ldv, int j, float* w, double* hout,
                  int hstride, double* wwout, double* partial, unsigned* words, float* vnext,
                  cudaStream_t st);
