@@ -71,7 +71,7 @@ def parse():
     ap.add_argument("--batch-hi", type=int, default=512)
     ap.add_argument("--batch-rhs", type=int, default=32)
     ap.add_argument("--batch-seed", type=int, default=0)
-    ap.add_argument("--batch-mem-gb", type=float, default=160.0)
+    ap.add_argument("--batch-mem-gb", type=float, default=96.0)
     ap.add_argument("--batch-schedule", default="persistent", choices=["persistent", "graph"],
                     help="one cooperative launch per Arnoldi step, or a graph of per-phase "
                          "launches")
