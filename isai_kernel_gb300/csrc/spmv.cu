@@ -168,19 +168,13 @@ __global__ void __launch_bounds__(256, sizeof(VT) == 4 ? 4 : 2) k_bsr_spmv(int m
   constexpr int U = sizeof(VT) == 4 ? 4 : 2;
   int lane = threadIdx.x & 31;
   int g = lane / BS, r = lane - g * BS;
-  bool mine_long = false;
+  long long base = (((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G + g) * RPG;
+  const bool active = g < G && base < mb;
+  if (!LONG && !active) return;
+  int s[RPG], e[RPG];
+  bool skip[RPG], mine_long = false;
   extern __shared__ int long_slots[];  // LONG: [8*G*RPG] slots, then the partials
   const int cg = (threadIdx.x >> 5) * G + g;
-  const int wib = threadIdx.x >> 5;  // warp in the CTA
-  // Without long rows the grid is one resident wave and each warp walks
-  // its virtual blocks vb = blockIdx.x, + gridDim.x, ... (no block launch
-  // and drain per 128 rows); the LONG instance covers the rows with its
-  // grid, one virtual block per CTA.
-  for (long long vb = blockIdx.x;; vb += gridDim.x) {
-  long long base = ((vb * (blockDim.x >> 5) + wib) * G + g) * RPG;
-  const bool active = g < G && base < mb;
-  int s[RPG], e[RPG];
-  bool skip[RPG];
 #pragma unroll
   for (int q = 0; q < RPG; ++q) {
     bool ok = active && base + q < mb;
@@ -243,9 +237,6 @@ __global__ void __launch_bounds__(256, sizeof(VT) == 4 ? 4 : 2) k_bsr_spmv(int m
       y[(base + q) * BS + r] = (YT)acc[q];
       if (y32) y32[(base + q) * BS + r] = (float)acc[q];  // optional FP32 copy
     }
-    if constexpr (LONG) break;
-    if ((((vb + gridDim.x) * (blockDim.x >> 5) + wib) * G) * RPG >= mb) break;
-  }
   if constexpr (LONG) {
     constexpr int NSLOT = 8 * G * RPG;
     // one CTA barrier, which also says whether the CTA holds a long row
@@ -273,19 +264,6 @@ int launch_spmv(int mb, const int* row, const int* col, const VT* val, const XT*
   long long groups = (mb + RPG - 1) / RPG;
   long long warps = (groups + G - 1) / G;
   unsigned grid = ceil_div(warps, 8);
-  if (!(layout & kLayoutLong)) {
-    // one resident wave; each warp walks several virtual blocks
-    static int resident = 0;
-    if (!resident) {
-      int dev = 0, sms = 0, per = 0;
-      BILU_TRY_CUDA(cudaGetDevice(&dev));
-      BILU_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-      BILU_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &per, k_bsr_spmv<BS, VT, XT, YT, AccT, RPG, false>, 256, 0));
-      resident = std::max(1, per) * sms;
-    }
-    grid = (unsigned)std::min<long long>(grid, resident);
-  }
   if (layout & kLayoutLong) {
     constexpr int NSLOT = 8 * G * RPG;
     const size_t smem = sizeof(int) * ((NSLOT + 1) & ~1) + sizeof(AccT) * 8 * G * BS;
