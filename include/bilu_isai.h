@@ -209,9 +209,11 @@ int bilu_isai_compute(int nb, int bs, const double* d_Aval, const int* d_Mptr, c
 int bilu_bcsr_spmv(int mb, int bs, const int* d_row, const int* d_col, const double* d_val,
                    const double* d_x, double* d_y, bilu_stream_t stream);
 /* The SpMV layout word of a pattern, as cached by the entry points above:
- * 1 when rows of more than 64 blocks are present (the kernel in which the
- * CTA shares such rows), else 0.  Synchronises the stream on the first
- * query of a pattern. */
+ * bit 0 (1) when rows of more than 64 blocks are present (the kernel in
+ * which the CTA shares such rows); bit 1 (2) when rows hold more than 5
+ * blocks on average (FP32-stored values: one block row per lane group
+ * instead of two).  Synchronises the stream on the first query of a
+ * pattern. */
 int bilu_spmv_layout(int mb, int bs, const int* d_row, bilu_stream_t stream, int* h_layout);
 /* FP32-stored values, FP32 accumulation; x and y each FP64 or FP32
  * (x_fp32 / y_fp32 flags). */
@@ -539,10 +541,10 @@ int bilu_debug_sptrsv_withhold_flow(int nb, int nnzb, int bs, const int* d_row, 
                                     const double* d_val, int lower, const double* d_b,
                                     double* d_x, int withhold_row, long long spin_limit,
                                     void* d_ws, size_t ws_bytes, bilu_stream_t stream);
-/* Sets the SpMV layout word (0 or 1, see bilu_spmv_layout) the entry points
- * use for the pattern (d_row, mb, bs), replacing the one they found.  Both
- * kernels give the product to within rounding for any pattern; this
- * exercises the one the check would not pick for a given pattern. */
+/* Sets the SpMV layout word (0 to 3, see bilu_spmv_layout) the entry
+ * points use for the pattern (d_row, mb, bs), replacing the one they found.
+ * Every layout gives the product to within rounding for any pattern; this
+ * exercises the kernels the check would not pick for a given pattern. */
 int bilu_debug_spmv_layout_set(int mb, int bs, const int* d_row, int layout);
 /* One modified Gram-Schmidt step of the Krylov solvers' orthogonalisation
  * kernel (one cooperative launch): w is orthogonalised against the j+1

@@ -236,8 +236,7 @@ void launch_combine(long long n, const float* Q, long long ldq, const double* y,
 
 // ---------------------------------------------------------------------------
 // Whole modified Gram-Schmidt step in one cooperative launch: sweeps
-// i = 0 .. j+1 over the same slice of w per CTA (w stays in the L2 between
-// sweeps), sweep i applying h_{i-1} v_{i-1} and taking v_i . w (the last
+// i = 0 .. j+1 over the same slice of w per CTA, sweep i applying h_{i-1} v_{i-1} and taking v_i . w (the last
 // one w . w), then v_{j+1} = w / ||w|| (and its FP32 copy).  Between sweeps
 // a counting grid barrier replaces the kernel boundary: each CTA writes its
 // partial sum, meets the others at the barrier, and then every CTA adds all
@@ -247,7 +246,12 @@ void launch_combine(long long n, const float* Q, long long ldq, const double* y,
 // writes sweep i+1's partial only after barrier i, and sweep i+2 (same half
 // as i) only after barrier i+1, which every CTA reaches after it has read
 // sweep i's partials.  A barrier that times out sets the error word and
-// every CTA returns.
+// every CTA returns.  Memory traffic at 128^3 (ncu, one step of 17 sweeps):
+// FP32 reads each basis vector once from DRAM (w and the previous basis
+// vector are L2 hits); FP64 moves ~2.8 vectors a sweep (3.17 GB a step):
+// w (67 MB) does not stay in the L2 beside the streamed basis vectors, with
+// or without evict-last hints on w, so an FP64 sweep is bound by HBM and
+// the DFMA pipe about equally.
 template <class T>
 struct MgsVec;
 template <>
@@ -301,10 +305,14 @@ struct MgsVec<float> {
   }
 };
 
-constexpr int kStepThreads = 256;
+// 512 threads, two CTAs per SM: half the partials and barrier arrivals of
+// 256-thread CTAs at the same occupancy (measured 3-6% faster a sweep at
+// 128^3, FP64 and FP32)
+constexpr int kStepThreads = 512;
+constexpr int kStepPerSM = 2;
 
 template <class T>
-__global__ void __launch_bounds__(kStepThreads, 4) k_mgs_step(
+__global__ void __launch_bounds__(kStepThreads, kStepPerSM) k_mgs_step(
     long long n, const T* __restrict__ V, long long ldv, int j, T* __restrict__ w,
     double* __restrict__ hout, int hstride, double* __restrict__ wwout,
     double* __restrict__ partial, GridSync gs, T* __restrict__ vnext,
@@ -477,7 +485,7 @@ int mgs_step_t(long long n, const T* V, long long ldv, int j, T* w, double* hout
     BILU_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     BILU_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mgs_step<T>,
                                                                 kStepThreads, 0));
-    grid = std::max(1, std::min(per, 4)) * sms;
+    grid = std::max(1, std::min(per, kStepPerSM)) * sms;
   }
   if (grid > kStepMaxCTAs) return BILU_ERR_UNSUPPORTED;
   GridSync gs;

@@ -47,7 +47,7 @@ int combine_f32(long long n, const float* Q, long long ldq, int k, const double*
 // Whole modified Gram-Schmidt step of Arnoldi step j in one cooperative
 // launch: j+2 fused sweeps (sweep i applies w -= h_{i-1} v_{i-1} and takes
 // h_i = v_i . w; the last one w . w) with a counting grid barrier between
-// them, w held in the L2: h_i into hout[i * hstride]
+// them: h_i into hout[i * hstride]
 // (i <= j), ||w||^2 into *wwout, then vnext = w / ||w|| (and vnext32, its
 // FP32 copy, when given; zeros when ||w|| = 0).  Sums are in the vectors'
 // precision and in a fixed order (warp 0 of every CTA adds all CTA

@@ -140,9 +140,9 @@ struct bilu_ctx {
   double *Aval = nullptr, *LU = nullptr;
   double* rdiag = nullptr;  // 1 / pivots of the factor's U_II (nb x bs), written by BILU(0)
   float *LU32 = nullptr, *rdiag32 = nullptr;  // FP32 copies for the mixed exact-ILU apply
-  // A, M_L, M_U: SpMV layout words from the setup (1 if the pattern has
-  // rows of more than 64 blocks: their SpMVs then take the kernel in which
-  // the CTA shares such rows)
+  // A, M_L, M_U: SpMV layout words from the setup (bit 0: the pattern has
+  // rows of more than 64 blocks, which the CTA then shares; bit 1: more
+  // than 5 blocks a row on average)
   int spmv_layout[3] = {0, 0, 0};
   int *Lrow = nullptr, *Lcol = nullptr, *Urow = nullptr, *Ucol = nullptr;
   double *Lval = nullptr, *Uval = nullptr;

@@ -148,24 +148,27 @@ __device__ __noinline__ void spmv_long_rows(const int* long_rows, const int* __r
 
 // y = M x: lane group of BS lanes per block row, lane r owns scalar row r.
 // A group handles RPG consecutive block rows and issues the loads of the
-// first U blocks of all of them before any arithmetic, so a warp keeps
-// RPG*U independent block loads per lane in flight (the rows of the ISAI
-// factors hold about 4 blocks, so one batch usually covers them).  FP64
-// values: U = 2, RPG = 1 (the DFMA pipe, not memory, is the limit); FP32
-// values: U = 4, RPG = 2 (memory latency is the limit).  LONG (matrices
-// with rows of more than kLongSpmvRow blocks): such a row is skipped by its
-// group and summed after the short rows by the whole CTA (dynamic shared
-// memory: the CTA's long-row slots and the group partials); the other
-// instance has no CTA barrier at all.
-template <int BS, class VT, class XT, class YT, class AccT, int RPG, bool LONG>
-__global__ void __launch_bounds__(256, sizeof(VT) == 4 ? 4 : 2) k_bsr_spmv(int mb, const int* __restrict__ row,
+// next U blocks of all of them before any arithmetic, so a warp keeps
+// RPG*U independent block loads per lane in flight; each row's sum runs in
+// block order whatever U and RPG are (the same bits).  Chosen by
+// launch_spmv from measurements on the 128^3 7-point pattern (7 blocks a
+// row) and its triangle (4 a row): FP64 values U = 1, RPG = 2 (two
+// independent DFMA chains per lane; one chain is latency-bound: 0.48 ->
+// 0.40 ms on the 7-point FP64 operator, the same on the triangle); FP32
+// values U = 4 with RPG = 2 for rows of ~4 blocks, RPG = 1 for wider rows
+// (0.199 -> 0.176 ms on the FP32 operator).  LONG (matrices with rows of
+// more than kLongSpmvRow blocks): such a row is skipped by its group and
+// summed after the short rows by the whole CTA (dynamic shared memory: the
+// CTA's long-row slots and the group partials); the other instance has no
+// CTA barrier at all.
+template <int BS, class VT, class XT, class YT, class AccT, int RPG, int U, int MINB, bool LONG>
+__global__ void __launch_bounds__(256, MINB) k_bsr_spmv(int mb, const int* __restrict__ row,
                                                      const int* __restrict__ col,
                                                      const VT* __restrict__ val,
                                                      const XT* __restrict__ x,
                                                      YT* __restrict__ y,
                                                      float* __restrict__ y32) {
   constexpr int G = 32 / BS;  // lane groups per warp
-  constexpr int U = sizeof(VT) == 4 ? 4 : 2;
   int lane = threadIdx.x & 31;
   int g = lane / BS, r = lane - g * BS;
   long long base = (((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G + g) * RPG;
@@ -248,33 +251,65 @@ __global__ void __launch_bounds__(256, sizeof(VT) == 4 ? 4 : 2) k_bsr_spmv(int m
 }
 
 // Layout word of a matrix for the SpMV: bit 0 = rows of more than
-// kLongSpmvRow blocks present (the LONG instance).  (Taking several blocks
-// of a row side by side, or rows in length order, was measured slower on
-// the power-law patterns: the product is latency-bound there, not bound by
-// the lanes an uneven warp leaves idle.)
+// kLongSpmvRow blocks present (the LONG instance); bit 1 = more than
+// kWideSpmvRow blocks a row on average (FP32 values: one row per lane
+// group).  (Taking several blocks of a row side by side, or rows in length
+// order, was measured slower on the power-law patterns: the product is
+// latency-bound there, not bound by the lanes an uneven warp leaves idle.)
 constexpr int kLayoutLong = 1;
+constexpr int kLayoutWide = 2;
+constexpr int kWideSpmvRow = 5;
 
-template <int BS, class VT, class XT, class YT>
-int launch_spmv(int mb, const int* row, const int* col, const VT* val, const XT* x, YT* y,
-                cudaStream_t st, int layout, float* y32 = nullptr) {
+template <int BS, class VT, class XT, class YT, int RPG, int U, int MINB, bool LONG>
+int launch_spmv_cfg(int mb, const int* row, const int* col, const VT* val, const XT* x, YT* y,
+                    cudaStream_t st, float* y32) {
   using AccT = VT;
-  if (mb == 0) return BILU_OK;
   constexpr int G = 32 / BS;
-  constexpr int RPG = sizeof(VT) == 4 ? 2 : 1;
   long long groups = (mb + RPG - 1) / RPG;
   long long warps = (groups + G - 1) / G;
   unsigned grid = ceil_div(warps, 8);
-  if (layout & kLayoutLong) {
+  if constexpr (LONG) {
     constexpr int NSLOT = 8 * G * RPG;
     const size_t smem = sizeof(int) * ((NSLOT + 1) & ~1) + sizeof(AccT) * 8 * G * BS;
-    k_bsr_spmv<BS, VT, XT, YT, AccT, RPG, true><<<grid, 256, smem, st>>>(mb, row, col, val, x,
-                                                                         y, y32);
+    k_bsr_spmv<BS, VT, XT, YT, AccT, RPG, U, MINB, true><<<grid, 256, smem, st>>>(
+        mb, row, col, val, x, y, y32);
   } else {
-    k_bsr_spmv<BS, VT, XT, YT, AccT, RPG, false><<<grid, 256, 0, st>>>(mb, row, col, val, x, y,
-                                                                       y32);
+    k_bsr_spmv<BS, VT, XT, YT, AccT, RPG, U, MINB, false><<<grid, 256, 0, st>>>(
+        mb, row, col, val, x, y, y32);
   }
   BILU_LAUNCH_CHECK();
   return BILU_OK;
+}
+
+// Patterns with long rows (power-law: rows of ~12 blocks on average, hubs
+// of up to 2000) are latency-bound per lane group and keep two blocks a
+// batch (FP64) or two rows a group (FP32); the configurations measured
+// faster on the stencil patterns (above) apply to patterns without long
+// rows, FP64 at block sizes 4 and 5.
+template <int BS, class VT, class XT, class YT>
+int launch_spmv(int mb, const int* row, const int* col, const VT* val, const XT* x, YT* y,
+                cudaStream_t st, int layout, float* y32 = nullptr) {
+  if (mb == 0) return BILU_OK;
+  const bool lng = (layout & kLayoutLong) != 0;
+  if constexpr (sizeof(VT) == 8) {
+    if (lng)
+      return launch_spmv_cfg<BS, VT, XT, YT, 1, 2, 2, true>(mb, row, col, val, x, y, st, y32);
+    if constexpr (BS <= 5)
+      return launch_spmv_cfg<BS, VT, XT, YT, 2, 1, 4, false>(mb, row, col, val, x, y, st, y32);
+    else
+      return launch_spmv_cfg<BS, VT, XT, YT, 1, 2, 2, false>(mb, row, col, val, x, y, st, y32);
+  } else if constexpr (BS == 8 && sizeof(XT) == 8) {
+    // two rows of 8x8 blocks with FP64 x segments spill at 64 registers
+    if (lng)
+      return launch_spmv_cfg<BS, VT, XT, YT, 1, 4, 4, true>(mb, row, col, val, x, y, st, y32);
+    return launch_spmv_cfg<BS, VT, XT, YT, 1, 4, 4, false>(mb, row, col, val, x, y, st, y32);
+  } else {
+    if (lng)
+      return launch_spmv_cfg<BS, VT, XT, YT, 2, 4, 4, true>(mb, row, col, val, x, y, st, y32);
+    if (layout & kLayoutWide)
+      return launch_spmv_cfg<BS, VT, XT, YT, 1, 4, 4, false>(mb, row, col, val, x, y, st, y32);
+    return launch_spmv_cfg<BS, VT, XT, YT, 2, 4, 4, false>(mb, row, col, val, x, y, st, y32);
+  }
 }
 
 // Multi-RHS: Y[n,k] = M X[n,k], row-major with ld = k.  One warp per block
@@ -394,22 +429,25 @@ int spmm_f32(int mb, int k, const int* row, const int* col, const float* val, co
 }  // namespace
 
 // SpMV layout word of a block pattern (see kLayoutLong): one reduction
-// over the row pointers into d_words (one device int) and a synchronising
-// read.  The engine calls it once per matrix at setup.
+// over the row pointers into d_words (one device int), then a synchronising
+// read of it and of the block count row[mb].  The engine calls it once per
+// matrix at setup.
 int spmv_layout_of(int mb, int bs, const int* row, void* d_words, cudaStream_t st,
                    int* h_layout) {
   (void)bs;
   *h_layout = 0;
   if (mb <= 0) return BILU_OK;
-  int h = 0;
+  int h[2] = {0, 0};  // longest row, blocks
   int* d = static_cast<int*>(d_words);
   BILU_TRY_CUDA(cudaMemsetAsync(d, 0, sizeof(int), st));
   k_row_len_max<<<(unsigned)std::min<long long>(ceil_div(mb, 256), 152 * 8), 256, 0, st>>>(
       mb, row, d);
   BILU_LAUNCH_CHECK();
-  BILU_TRY_CUDA(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BILU_TRY_CUDA(cudaMemcpyAsync(&h[0], d, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BILU_TRY_CUDA(cudaMemcpyAsync(&h[1], row + mb, sizeof(int), cudaMemcpyDeviceToHost, st));
   BILU_TRY_CUDA(cudaStreamSynchronize(st));
-  *h_layout = h > kLongSpmvRow ? kLayoutLong : 0;
+  *h_layout = (h[0] > kLongSpmvRow ? kLayoutLong : 0) |
+              ((long long)h[1] > (long long)kWideSpmvRow * mb ? kLayoutWide : 0);
   return BILU_OK;
 }
 
@@ -528,7 +566,8 @@ extern "C" int bilu_spmv_layout(int mb, int bs, const int* d_row, bilu_stream_t 
 }
 
 extern "C" int bilu_debug_spmv_layout_set(int mb, int bs, const int* d_row, int layout) {
-  if (mb < 0 || (mb > 0 && !d_row) || layout < 0 || layout > kLayoutLong) return BILU_ERR_ARG;
+  if (mb < 0 || (mb > 0 && !d_row) || layout < 0 || layout > (kLayoutLong | kLayoutWide))
+    return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> lock(g_layout_mu);
   if (LayoutEntry* e = layout_find(mb, bs, d_row)) {

@@ -498,10 +498,11 @@ def test_spmv_long_rows(cuda, orc, bs):
 
 @pytest.mark.parametrize("bs", [4, 5, 8])
 def test_spmv_every_layout(cuda, orc, bs):
-    """Both SpMV kernels (with and without the CTA's long-row pass) on a
-    pattern with rows of up to ~150 blocks, and the layout the check finds
-    for it and for a stencil: within 1e-12 of the oracle whichever kernel
-    runs."""
+    """Every SpMV layout (with and without the CTA's long-row pass, one or
+    two block rows per lane group) on a pattern with rows of up to ~150
+    blocks, and the layout the check finds for it and for a stencil: FP64
+    within 1e-12 of the oracle and FP32-stored values within 1e-5 of the
+    oracle on the rounded values, whichever kernel runs."""
     import ctypes
 
     import torch
@@ -512,20 +513,30 @@ def test_spmv_every_layout(cuda, orc, bs):
     x = gen.rhs(A.n, 13)
     row, col, val, xd = T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda), T(x, cuda)
     ref = orc.bcsr_spmv(A.nb, bs, A.rowptr, A.colind, A.val, x)
+    v32 = A.val.astype(np.float32)
+    ref32 = orc.bcsr_spmv(A.nb, bs, A.rowptr, A.colind, v32.astype(np.float64),
+                          x.astype(np.float32).astype(np.float64))
+    val32, x32 = T(v32, cuda), T(x.astype(np.float32), cuda)
     lay = ctypes.c_int(-1)
     api.call("bilu_spmv_layout", A.nb, bs, api._p(row), api._s(), ctypes.byref(lay))
-    assert lay.value == 1
+    assert lay.value == 3  # rows of ~150 blocks, 12 on average
     y = torch.empty(A.n, dtype=torch.float64, device="cuda")
-    for layout in (0, 1):
+    y32 = torch.empty(A.n, dtype=torch.float32, device="cuda")
+    for layout in (0, 1, 2, 3):
         api.call("bilu_debug_spmv_layout_set", A.nb, bs, api._p(row), layout)
         y.fill_(float("nan"))
         api.call("bilu_bcsr_spmv", A.nb, bs, api._p(row), api._p(col), api._p(val), api._p(xd),
                  api._p(y), api._s())
         assert relerr(N(y), ref) < 1e-12, layout
+        y32.fill_(float("nan"))
+        api.call("bilu_bcsr_spmv_f32", A.nb, bs, api._p(row), api._p(col), api._p(val32),
+                 api._p(x32), 1, api._p(y32), 1, api._s())
+        assert relerr(N(y32).astype(np.float64), ref32) < 1e-5, layout
+    # a 7-point stencil (~6 blocks a row) and a 5-point one (~5): no long rows
     S = gen.convdiff3d(6, bs=4, seed=0) if bs == 4 else gen.laplace2d(7, bs=bs, seed=2)
     srow = T(S.rowptr, cuda)
     api.call("bilu_spmv_layout", S.nb, bs, api._p(srow), api._s(), ctypes.byref(lay))
-    assert lay.value == 0
+    assert lay.value == (2 if S.nnzb > 5 * S.nb else 0)
 
 
 def test_long_rows_take_the_warp_path(cuda, orc):

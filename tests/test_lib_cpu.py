@@ -81,7 +81,7 @@ def test_argument_errors_without_gpu():
     assert L.bilu_spmv_layout(10, 4, ctypes.c_void_p(8), None, None) == -1
     assert L.bilu_spmv_layout(10, 6, ctypes.c_void_p(8), None, ctypes.byref(lay)) == -8
     assert lay.value == 7  # untouched on error
-    assert L.bilu_debug_spmv_layout_set(10, 4, ctypes.c_void_p(8), 2) == -1  # only 0 or 1
+    assert L.bilu_debug_spmv_layout_set(10, 4, ctypes.c_void_p(8), 4) == -1  # only 0 .. 3
     assert L.bilu_debug_spmv_layout_set(10, 4, None, 1) == -1
     assert L.bilu_debug_spmv_layout_set(10, 6, ctypes.c_void_p(8), 1) == -8
 
