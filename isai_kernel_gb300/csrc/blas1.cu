@@ -310,6 +310,39 @@ struct MgsVec<float> {
 // 128^3, FP64 and FP32)
 constexpr int kStepThreads = 512;
 constexpr int kStepPerSM = 2;
+// FP64 sweeps stage their loads through shared memory with cp.async,
+// kStepStages element iterations ahead of the arithmetic (each thread reads
+// back only its own slots): an FP64 sweep stalls on memory latency with the
+// FP64 pipe ~70% busy, and the registers of a deeper unroll are not there at
+// two CTAs of 512 threads per SM (41.2 -> 38.0 us a sweep at 128^3; the FP32
+// sweep, bound by synchronisation and L2 traffic, is slower this way).
+constexpr int kStepStages = 3;
+constexpr size_t kStepStageBytes = (size_t)kStepStages * 3 * kStepThreads * 16;
+
+__device__ __forceinline__ unsigned long long l2_policy_evict_last() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ unsigned long long l2_policy_evict_first() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+// 16 bytes global -> shared, asynchronous, through the L2 only
+__device__ __forceinline__ void cp_async16(void* smem, const void* g, unsigned long long pol) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(sa), "l"(g),
+               "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 template <class T>
 __global__ void __launch_bounds__(kStepThreads, kStepPerSM) k_mgs_step(
@@ -333,6 +366,13 @@ __global__ void __launch_bounds__(kStepThreads, kStepPerSM) k_mgs_step(
   const long long nv = n / W;     // whole vectors
   const long long tail = nv * W;  // first element of the scalar tail
   VT* wv = reinterpret_cast<VT*>(w);
+  // FP64 staging: w kept in the L2 as long as it fits, the basis vectors
+  // streamed through
+  unsigned long long pol_w = 0, pol_v = 0;
+  if constexpr (sizeof(T) == 8) {
+    pol_w = l2_policy_evict_last();
+    pol_v = l2_policy_evict_first();
+  }
   T h = T(0);
   for (int i = 0; i <= j + 1; ++i) {
     const T* vp = i > 0 ? V + (long long)(i - 1) * ldv : nullptr;
@@ -341,15 +381,49 @@ __global__ void __launch_bounds__(kStepThreads, kStepPerSM) k_mgs_step(
     T a[4] = {T(0), T(0), T(0), T(0)};
     const VT* vpv = reinterpret_cast<const VT*>(vp);
     const VT* vnv = reinterpret_cast<const VT*>(vn);
-    // two elements' loads in flight per thread
-#pragma unroll 2
-    for (long long e = tid; e < nv; e += stride) {
-      VT we = M::ldcg(wv + e);
-      if (vp) {
-        M::axpy(hn, M::ldcs(vpv + e), we);
-        wv[e] = we;
+    if constexpr (sizeof(T) == 8) {
+      // iteration k of this thread: element tid + k * stride; slot k % S of
+      // the thread's w, v_{i-1} and v_i stages, loaded S - 1 iterations ahead
+      constexpr int S = kStepStages;
+      extern __shared__ __align__(16) unsigned char step_stage[];
+      VT* stage = reinterpret_cast<VT*>(step_stage);  // [S][3][kStepThreads]
+      const long long K = tid < nv ? (nv - tid + stride - 1) / stride : 0;
+      auto issue = [&](long long k) {
+        const long long e = tid + k * stride;
+        VT* sl = stage + (int)(k % S) * 3 * kStepThreads + threadIdx.x;
+        cp_async16(sl, wv + e, pol_w);
+        if (vpv) cp_async16(sl + kStepThreads, vpv + e, pol_v);
+        if (vnv) cp_async16(sl + 2 * kStepThreads, vnv + e, pol_v);
+      };
+#pragma unroll
+      for (int k = 0; k < S - 1; ++k) {
+        if (k < K) issue(k);
+        cp_async_commit();
       }
-      M::dot(vn ? M::ldnext(vnv + e) : we, we, a);
+      for (long long k = 0; k < K; ++k) {
+        if (k + S - 1 < K) issue(k + S - 1);
+        cp_async_commit();
+        cp_async_wait<S - 1>();  // iteration k's group has landed
+        const VT* sl = stage + (int)(k % S) * 3 * kStepThreads + threadIdx.x;
+        VT we = sl[0];
+        if (vpv) {
+          M::axpy(hn, sl[kStepThreads], we);
+          wv[tid + k * stride] = we;
+        }
+        M::dot(vnv ? sl[2 * kStepThreads] : we, we, a);
+      }
+      cp_async_wait<0>();
+    } else {
+      // two elements' loads in flight per thread
+#pragma unroll 2
+      for (long long e = tid; e < nv; e += stride) {
+        VT we = M::ldcg(wv + e);
+        if (vp) {
+          M::axpy(hn, M::ldcs(vpv + e), we);
+          wv[e] = we;
+        }
+        M::dot(vn ? M::ldnext(vnv + e) : we, we, a);
+      }
     }
     if (tid < n - tail) {  // the last n % W elements
       const long long e = tail + tid;
@@ -479,12 +553,16 @@ int mgs_step_t(long long n, const T* V, long long ldv, int j, T* w, double* hout
                double* wwout, double* partial, unsigned* words, T* vnext, float* vnext32,
                cudaStream_t st) {
   static int grid = 0;
+  const size_t smem = sizeof(T) == 8 ? kStepStageBytes : 0;
   if (!grid) {
     int per = 0, dev = 0, sms = 0;
     BILU_TRY_CUDA(cudaGetDevice(&dev));
     BILU_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (smem)
+      BILU_TRY_CUDA(cudaFuncSetAttribute(k_mgs_step<T>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     BILU_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mgs_step<T>,
-                                                                kStepThreads, 0));
+                                                                kStepThreads, smem));
     grid = std::max(1, std::min(per, kStepPerSM)) * sms;
   }
   if (grid > kStepMaxCTAs) return BILU_ERR_UNSUPPORTED;
@@ -495,7 +573,7 @@ int mgs_step_t(long long n, const T* V, long long ldv, int j, T* w, double* hout
   gs.spin = kSpinLimit;
   void* args[] = {&n, &V, &ldv, &j, &w, &hout, &hstride, &wwout, &partial, &gs, &vnext, &vnext32};
   BILU_TRY_CUDA(cudaLaunchCooperativeKernel((const void*)k_mgs_step<T>, dim3(grid),
-                                            dim3(kStepThreads), args, 0, st));
+                                            dim3(kStepThreads), args, smem, st));
   BILU_LAUNCH_CHECK();
   return BILU_OK;
 }
