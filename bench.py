@@ -33,6 +33,7 @@ from __future__ import annotations
 import argparse
 import ctypes
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -76,6 +77,9 @@ def parse():
                     help="one cooperative launch per Arnoldi step, or a graph of per-phase "
                          "launches")
     ap.add_argument("--pl-nb", type=int, default=500000)
+    ap.add_argument("--mgs-only", action="store_true",
+                    help="--workload kernels: only the Gram-Schmidt step timings (no system "
+                         "setup on the device: small enough for multi-pass ncu captures at 128^3)")
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu launch lists: the setup, then --warmup and --steps "
                          "nested solves, nothing else")
@@ -848,29 +852,38 @@ def run_kernels(args):
     """For ncu captures: the setup of the --side^3 system, then --steps
     rounds of the inner solver's products as it launches them: M_L u and
     M_U t (k_bsr_spmv, FP32 values and vectors) and A q (FP32-stored A),
-    each round in this order (three k_bsr_spmv launches per round)."""
+    each round in this order (three k_bsr_spmv launches per round); then
+    the Gram-Schmidt step timings.  --mgs-only: the step timings alone, on
+    vectors of the system's length."""
     import torch
 
     from isai_kernel_gb300 import _lib, api
 
     L = _lib.lib()
     dev = torch.device("cuda", 0)
-    A, b_np = convdiff_system(args.side)
-    nb, bs, n = A.nb, A.bs, A.n
-    row, col, val = (torch.from_numpy(a).to(dev) for a in (A.rowptr, A.colind, A.val))
-    P = api.Preconditioner(nb, bs, row, col, val, fp32=True, nested=True)
-    _, Lf, Uf = P.factors()
-    L32, U32 = P.get(7), P.get(8)
-    A32 = val.float()
-    u = torch.from_numpy(b_np).to(dev).float()
-    t, q, w = (torch.empty(n, dtype=torch.float32, device=dev) for _ in range(3))
     p_ = api._p
-    for _ in range(args.steps):
-        L.bilu_bcsr_spmv_f32(nb, bs, p_(Lf[0]), p_(Lf[1]), p_(L32), p_(u), 1, p_(t), 1, api._s())
-        L.bilu_bcsr_spmv_f32(nb, bs, p_(Uf[0]), p_(Uf[1]), p_(U32), p_(t), 1, p_(q), 1, api._s())
-        L.bilu_bcsr_spmv_f32(nb, bs, p_(row), p_(col), p_(A32), p_(q), 1, p_(w), 1, api._s())
-    torch.cuda.synchronize()
-    P.close()
+    if args.mgs_only:
+        n = 4 * args.side ** 3  # 4 DOF per grid point
+    else:
+        A, b_np = convdiff_system(args.side)
+        nb, bs, n = A.nb, A.bs, A.n
+        row, col, val = (torch.from_numpy(a).to(dev) for a in (A.rowptr, A.colind, A.val))
+        P = api.Preconditioner(nb, bs, row, col, val, fp32=True, nested=True)
+        _, Lf, Uf = P.factors()
+        L32, U32 = P.get(7), P.get(8)
+        A32 = val.float()
+        u = torch.from_numpy(b_np).to(dev).float()
+        t, q, w = (torch.empty(n, dtype=torch.float32, device=dev) for _ in range(3))
+        for _ in range(args.steps):
+            L.bilu_bcsr_spmv_f32(nb, bs, p_(Lf[0]), p_(Lf[1]), p_(L32), p_(u), 1, p_(t), 1,
+                                 api._s())
+            L.bilu_bcsr_spmv_f32(nb, bs, p_(Uf[0]), p_(Uf[1]), p_(U32), p_(t), 1, p_(q), 1,
+                                 api._s())
+            L.bilu_bcsr_spmv_f32(nb, bs, p_(row), p_(col), p_(A32), p_(q), 1, p_(w), 1,
+                                 api._s())
+        torch.cuda.synchronize()
+        P.close()
+        del P, A32, row, col, val, t, q, w, u
     # one orthogonalisation step (j = 15: 17 fused sweeps) on basis vectors
     # of the system's length, FP64 and FP32, CUDA events after a warm-up
     out = {"workload": f"kernels convdiff3d {args.side}^3", "rounds": args.steps}
@@ -882,7 +895,9 @@ def run_kernels(args):
     probe_lib().probe_rates(rates)
     for fp32, dt in ((0, torch.float64), (1, torch.float32)):
         g = torch.Generator(device=dev).manual_seed(1)
-        V = torch.randn((j + 1) * ldv, dtype=dt, device=dev, generator=g)
+        # basis vectors of about unit norm (the sweeps then neither grow nor
+        # overflow w)
+        V = torch.randn((j + 1) * ldv, dtype=dt, device=dev, generator=g) / math.sqrt(n)
         w0 = torch.randn(ldv, dtype=dt, device=dev, generator=g)
         w = torch.empty_like(w0)
         h = torch.empty(j + 2, dtype=torch.float64, device=dev)
