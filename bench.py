@@ -80,6 +80,8 @@ def parse():
     ap.add_argument("--mgs-only", action="store_true",
                     help="--workload kernels: only the Gram-Schmidt step timings (no system "
                          "setup on the device: small enough for multi-pass ncu captures at 128^3)")
+    ap.add_argument("--profile-prec", default="nested", choices=["nested", "fp64"],
+                    help="--profile: the solve mode of the warm-up and timed solves")
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu launch lists: the setup, then --warmup and --steps "
                          "nested solves, nothing else")
@@ -386,8 +388,11 @@ def run_ours(args):
         return P.solve(b, x if out is None else out, prec=prec, restart=args.restart,
                        tol=args.tol, maxit=args.maxit)
 
+    # the timed mode: the nested solve (a --profile run may take the plain
+    # FP64 solve instead, for its launch list)
+    MAIN = api.BILU_FP64 if (args.profile and args.profile_prec == "fp64") else NESTED
     for _ in range(args.warmup):
-        _, res = solve(NESTED)
+        _, res = solve(MAIN)
     barrier(world)
     torch.cuda.synchronize()
     clocks = Clocks(local)
@@ -397,7 +402,7 @@ def run_ours(args):
     for _ in range(args.steps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        _, res = solve(NESTED)
+        _, res = solve(MAIN)
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
@@ -411,10 +416,11 @@ def run_ours(args):
     x_nested = x.cpu().numpy().copy()
     t_mixed = max_over_ranks(statistics.mean(times), world)
     if args.profile:
-        # launch lists: the setup, the warm-up and the timed nested solves only
+        # launch lists: the setup, the warm-up and the timed solves only
         P.close()
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": t_mixed, "unit": "s", "profile": True,
+                              "mode": args.profile_prec,
                               "iters": {"outer": res.iters, "inner": res.inner_steps},
                               "gpu_launches": int(launches)}))
         return
@@ -864,9 +870,10 @@ def run_kernels(args):
     """For ncu captures: the setup of the --side^3 system, then --steps
     rounds of the inner solver's products as it launches them: M_L u and
     M_U t (k_bsr_spmv, FP32 values and vectors) and A q (FP32-stored A),
-    each round in this order (three k_bsr_spmv launches per round); then
-    the Gram-Schmidt step timings.  --mgs-only: the step timings alone, on
-    vectors of the system's length."""
+    each round in this order (three k_bsr_spmv launches per round), then
+    --steps FP64 operator products (k_bsr_spmv, FP64 values and vectors),
+    then the Gram-Schmidt step timings.  --mgs-only: the step timings alone,
+    on vectors of the system's length."""
     import torch
 
     from isai_kernel_gb300 import _lib, api
@@ -893,9 +900,13 @@ def run_kernels(args):
                                  api._s())
             L.bilu_bcsr_spmv_f32(nb, bs, p_(row), p_(col), p_(A32), p_(q), 1, p_(w), 1,
                                  api._s())
+        # then --steps FP64 operator products (the outer solver's A z)
+        z64, y64 = u.double(), torch.empty(n, dtype=torch.float64, device=dev)
+        for _ in range(args.steps):
+            L.bilu_bcsr_spmv(nb, bs, p_(row), p_(col), p_(val), p_(z64), p_(y64), api._s())
         torch.cuda.synchronize()
         P.close()
-        del P, A32, row, col, val, t, q, w, u
+        del P, A32, row, col, val, t, q, w, u, z64, y64
     # one orthogonalisation step (j = 15: 17 fused sweeps) on basis vectors
     # of the system's length, FP64 and FP32, CUDA events after a warm-up
     out = {"workload": f"kernels convdiff3d {args.side}^3", "rounds": args.steps}
