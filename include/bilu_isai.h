@@ -409,9 +409,12 @@ int bilu_ctx_select(bilu_ctx* ctx, const double* d_b, int restart, int cycles, d
 
 /* Host-buffer convenience (the end-to-end call): copies A and b from host
  * memory, runs the setup `prec` needs (any bilu_precision) and the solve,
- * copies x back.  Device buffers of this call and of every handle come from
- * a memory pool private to the library that keeps freed memory reserved, so
- * repeated calls do not map their buffers again. */
+ * copies x back.  The values and b copy on a second stream while the
+ * setup's structure phase (level analysis, ISAI patterns, pair lists) runs
+ * on `stream`; with pinned host buffers the two overlap.  Device buffers of
+ * this call and of every handle come from a memory pool private to the
+ * library that keeps freed memory reserved, so repeated calls do not map
+ * their buffers again. */
 int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const int* h_col,
                     const double* h_val, const double* h_b, double* h_x, int prec, int restart,
                     double tol, int maxit, int* h_iters, double* h_relres, double* h_times,

@@ -123,6 +123,7 @@ constexpr long long kSpinLimit = 1ll << 22;
 struct LevelOut {
   int *order = nullptr, *lvl = nullptr, *nlev = nullptr;
   int h_nlev = 0, h_sched = 0, h_maxdeg = 0;  // levels, solve schedule, largest dependency count
+  int h_fsched = 0;                           // recommended factorisation schedule
 };
 
 }  // namespace bilu

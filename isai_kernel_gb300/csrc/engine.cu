@@ -63,6 +63,11 @@ int sptrsv_levels_async(int nb, int bs, const int* row, const int* col, const in
 int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, const int* diag,
                double* val, int* h_zp, Carver& ws, cudaStream_t st, int schedule,
                double* rdiag, LevelOut* keep);
+int bilu0_analyze(int nb, long long nnzb, const int* row, const int* col, const int* diag,
+                  LevelOut& keep, Carver& ws, cudaStream_t st);
+int bilu0_factor(int nb, long long nnzb, int bs, const int* row, const int* col,
+                 const int* diag, double* val, int* h_zp, Carver& ws, cudaStream_t st,
+                 int schedule, double* rdiag, const LevelOut& keep);
 int dinv_impl(int nb, int bs, const int* row, const int* col, const double* val, int lower,
               double* Dinv, int* d_fail, cudaStream_t st);
 size_t pairs_ws(long long mnnz);
@@ -251,7 +256,7 @@ extern "C" int bilu_ctx_destroy(bilu_ctx* ctx) {
 namespace {
 
 struct Timer {
-  cudaEvent_t e[5];
+  cudaEvent_t e[6];
   cudaStream_t st;
   explicit Timer(cudaStream_t s) : st(s) {
     for (auto& x : e) cudaEventCreate(&x);
@@ -268,85 +273,111 @@ struct Timer {
   }
 };
 
-// One triangle of the ISAI: pattern (BCSC), BCSR pattern + map, pairs,
-// Dinv, column solves, BCSC->BCSR reorder.  Outputs BCSR rowptr/col/val.
-int build_isai_side(bilu_ctx* c, int lower, Carver& ws, int** orow, int** ocol, double** oval,
-                    int* onnz, double* t_pattern, double* t_isai, float** oval32) {
+// The structure of one ISAI side: M's BCSC pattern (Mptr, Mind), its BCSR
+// view (Trow, Tcol) with the BCSC -> BCSR map, and the pair lists.
+struct IsaiSym {
+  int *Mptr = nullptr, *Mind = nullptr, *Trow = nullptr, *Tcol = nullptr, *map = nullptr;
+  int *pp = nullptr, *pl = nullptr, *ps = nullptr;
+  int mnnz = 0;
+};
+
+// Structure only (A's pattern, or pattern(A^k) for ISAI(k)): may run before
+// the values are on the device.
+int build_isai_sym(bilu_ctx* c, int lower, Carver& ws, IsaiSym& y, double* t_pattern) {
   cudaStream_t st = c->st;
-  int nb = c->nb, bs = c->bs, bs2 = bs * bs;
+  int nb = c->nb;
   // the M patterns come from pattern(A^k) for ISAI(k); the pair lists, Dinv
   // and the column solves still read the factor on A's pattern
   const int* pr = c->Prow ? c->Prow : c->Arow;
   const int* pc = c->Pcol ? c->Pcol : c->Acol;
   Timer tm(st);
   tm.mark(0);
-  int *Mptr, *Trow;
-  BILU_TRY(c->alloc(&Mptr, nb + 1));
-  BILU_TRY(c->alloc(&Trow, nb + 1));
+  BILU_TRY(c->alloc(&y.Mptr, nb + 1));
+  BILU_TRY(c->alloc(&y.Trow, nb + 1));
   int mnnz = 0, tnnz = 0;
   {
     Carver w2 = ws;
-    BILU_TRY(isai_pattern_colptr_impl(nb, pr, pc, lower, Mptr, &mnnz, w2, st));
+    BILU_TRY(isai_pattern_colptr_impl(nb, pr, pc, lower, y.Mptr, &mnnz, w2, st));
   }
   {
     Carver w2 = ws;
-    BILU_TRY(tri_pattern_rowptr_impl(nb, pr, pc, lower, Trow, &tnnz, w2, st));
+    BILU_TRY(tri_pattern_rowptr_impl(nb, pr, pc, lower, y.Trow, &tnnz, w2, st));
   }
   // the reference's guard (main.cu:537-546): both views must hold the same
   // blocks, i.e. every diagonal block is stored
   if (mnnz != tnnz) return BILU_ERR_PATTERN;
-  int *Mind, *Tcol, *map;
-  BILU_TRY(c->alloc(&Mind, mnnz));
-  BILU_TRY(c->alloc(&Tcol, tnnz));
-  BILU_TRY(c->alloc(&map, mnnz));
+  BILU_TRY(c->alloc(&y.Mind, mnnz));
+  BILU_TRY(c->alloc(&y.Tcol, tnnz));
+  BILU_TRY(c->alloc(&y.map, mnnz));
   {
     Carver w2 = ws;
     if (!w2.take<int>(2)) return BILU_ERR_WORKSPACE;
-    BILU_TRY(isai_pattern_fill_impl(nb, pr, pc, lower, Mptr, Mind, mnnz, w2, st));
+    BILU_TRY(isai_pattern_fill_impl(nb, pr, pc, lower, y.Mptr, y.Mind, mnnz, w2, st));
   }
-  BILU_TRY(tri_pattern_fill_impl(nb, pr, pc, lower, Trow, Tcol, st));
+  BILU_TRY(tri_pattern_fill_impl(nb, pr, pc, lower, y.Trow, y.Tcol, st));
   {
     Carver w2 = ws;
-    BILU_TRY(map_impl(nb, Mptr, Mind, Trow, Tcol, map, nullptr, w2, st));
+    BILU_TRY(map_impl(nb, y.Mptr, y.Mind, y.Trow, y.Tcol, y.map, nullptr, w2, st));
   }
-  tm.mark(1);
-  int *pp, *pl, *ps;
-  BILU_TRY(c->alloc(&pp, (size_t)mnnz + 1));
+  BILU_TRY(c->alloc(&y.pp, (size_t)mnnz + 1));
   int total = 0;
   {
     Carver w2 = ws;
-    BILU_TRY(pairs_ptr_impl(nb, c->Arow, c->Acol, Mptr, Mind, lower, pp, mnnz, &total, nullptr,
-                            w2, st));
+    BILU_TRY(pairs_ptr_impl(nb, c->Arow, c->Acol, y.Mptr, y.Mind, lower, y.pp, mnnz, &total,
+                            nullptr, w2, st));
   }
-  BILU_TRY(c->alloc(&pl, total));
-  BILU_TRY(c->alloc(&ps, total));
-  BILU_TRY(pairs_fill_impl(nb, c->Arow, c->Acol, Mptr, Mind, lower, pp, mnnz, pl, ps, st));
+  BILU_TRY(c->alloc(&y.pl, total));
+  BILU_TRY(c->alloc(&y.ps, total));
+  BILU_TRY(pairs_fill_impl(nb, c->Arow, c->Acol, y.Mptr, y.Mind, lower, y.pp, mnnz, y.pl, y.ps,
+                           st));
+  y.mnnz = mnnz;
+  tm.mark(1);
+  *t_pattern += tm.ms(0, 1);
+  return BILU_OK;
+}
+
+// The values of one ISAI side on the factor: Dinv, the column solves into
+// BCSC and the reorder into BCSR (with the FP32 copy when asked for).
+int build_isai_num(bilu_ctx* c, int lower, const IsaiSym& y, int** orow, int** ocol,
+                   double** oval, int* onnz, double* t_isai, float** oval32) {
+  cudaStream_t st = c->st;
+  int nb = c->nb, bs = c->bs, bs2 = bs * bs;
+  Timer tm(st);
+  tm.mark(0);
   double *Dinv, *Mcsc, *Mcsr;
   BILU_TRY(c->alloc(&Dinv, (size_t)nb * bs2));
-  BILU_TRY(c->alloc(&Mcsc, (size_t)mnnz * bs2));
-  BILU_TRY(c->alloc(&Mcsr, (size_t)mnnz * bs2));
+  BILU_TRY(c->alloc(&Mcsc, (size_t)y.mnnz * bs2));
+  BILU_TRY(c->alloc(&Mcsr, (size_t)y.mnnz * bs2));
   BILU_TRY(dinv_impl(nb, bs, c->Arow, c->Acol, c->LU, lower, Dinv, nullptr, st));
-  BILU_TRY(isai_impl(nb, bs, c->LU, Mptr, Mind, lower, pp, pl, ps, Dinv, Mcsc, st));
+  BILU_TRY(isai_impl(nb, bs, c->LU, y.Mptr, y.Mind, lower, y.pp, y.pl, y.ps, Dinv, Mcsc, st));
   // the FP32 copy of the mixed apply is written by the same pass
   float* M32 = nullptr;
-  if (oval32) BILU_TRY(c->alloc(&M32, (size_t)mnnz * bs2));
-  BILU_TRY(reorder_impl(mnnz, bs, map, Mcsc, Mcsr, st, M32));
+  if (oval32) BILU_TRY(c->alloc(&M32, (size_t)y.mnnz * bs2));
+  BILU_TRY(reorder_impl(y.mnnz, bs, y.map, Mcsc, Mcsr, st, M32));
   if (oval32) *oval32 = M32;
-  tm.mark(2);
-  *t_pattern += tm.ms(0, 1);
-  *t_isai += tm.ms(1, 2);
-  *orow = Trow;
-  *ocol = Tcol;
+  tm.mark(1);
+  *t_isai += tm.ms(0, 1);
+  *orow = y.Trow;
+  *ocol = y.Tcol;
   *oval = Mcsr;
-  *onnz = mnnz;
+  *onnz = y.mnnz;
   return BILU_OK;
 }
 
 }  // namespace
 
-extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* d_row,
-                              const int* d_col, const double* d_val, int prec_mask,
-                              double* h_times) {
+namespace {
+
+// Setup in two phases.  Structure first (row pointers and column indices
+// only): diagonal positions, BILU(0)'s level analysis, pattern(A^k), the
+// ISAI patterns and pair lists of both sides, the SpMV layouts and the upper
+// level analysis of the exact-ILU modes.  Then, after values_ready (an event
+// the caller records when d_val is on the device; null: already there), the
+// values: BILU(0), Dinv, the ISAI column solves, the reorders and the FP32
+// copies.  The structure phase thus overlaps a host-to-device copy of the
+// values that the caller issues on another stream.
+int ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* d_row, const int* d_col,
+              const double* d_val, int prec_mask, double* h_times, cudaEvent_t values_ready) {
   if (!c || nb < 1 || nnzb < nb || !d_row || !d_col || !d_val) return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   cudaStream_t st = c->st;
@@ -362,14 +393,9 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   tm.mark(0);
   BILU_TRY(c->alloc(&c->Arow, nb + 1));
   BILU_TRY(c->alloc(&c->Acol, nnzb));
-  BILU_TRY(c->alloc(&c->Aval, nnzb * bs2));
-  BILU_TRY(c->alloc(&c->LU, nnzb * bs2));
   BILU_TRY(c->alloc(&c->diag, nb + 1));
-  BILU_TRY(c->alloc(&c->rdiag, (size_t)nb * bs + 1));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->Arow, d_row, sizeof(int) * (nb + 1), cudaMemcpyDeviceToDevice, st));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->Acol, d_col, sizeof(int) * nnzb, cudaMemcpyDeviceToDevice, st));
-  BILU_TRY_CUDA(cudaMemcpyAsync(c->Aval, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
-  BILU_TRY_CUDA(cudaMemcpyAsync(c->LU, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
   // scratch shared by every step
   size_t wsb = std::max({isai_pattern_ws(nb, nnzb), bilu0_ws(nb, nnzb), pairs_ws(nnzb + nb),
                          levels_ws(nb, nnzb), pattern_product_ws(nb),
@@ -381,26 +407,21 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
     Carver w2 = ws;
     BILU_TRY(diag_positions(nb, c->Arow, c->Acol, c->diag, nullptr, w2, st));
   }
-  tm.mark(1);
-  // the exact-ILU apply's lower solves reuse BILU(0)'s analysis of the
-  // lower DAG
+  // BILU(0)'s analysis of the lower DAG, kept: the exact-ILU apply's lower
+  // solves reuse it
   const int ilu_bits = (1 << BILU_ILU) | (1 << BILU_ILU_FP32);
   const bool ilu = (prec_mask & ilu_bits) != 0;
+  BILU_TRY(c->alloc(&c->ordL, (size_t)nb + 1));
+  BILU_TRY(c->alloc(&c->lvlL, (size_t)nb + 2));
+  BILU_TRY(c->alloc(&c->nlevL, 4));
   LevelOut keepL;
-  if (ilu) {
-    BILU_TRY(c->alloc(&c->ordL, (size_t)nb + 1));
-    BILU_TRY(c->alloc(&c->lvlL, (size_t)nb + 2));
-    BILU_TRY(c->alloc(&c->nlevL, 4));
-    keepL.order = c->ordL;
-    keepL.lvl = c->lvlL;
-    keepL.nlev = c->nlevL;
-  }
+  keepL.order = c->ordL;
+  keepL.lvl = c->lvlL;
+  keepL.nlev = c->nlevL;
+  tm.mark(1);
   {
     Carver w2 = ws;
-    int zp = -1;
-    int rc = bilu0_impl(nb, nnzb, bs, c->Arow, c->Acol, c->diag, c->LU, &zp, w2, st,
-                        c->schedule, c->rdiag, ilu ? &keepL : nullptr);
-    if (rc != BILU_OK) return rc;
+    BILU_TRY(bilu0_analyze(nb, nnzb, c->Arow, c->Acol, c->diag, keepL, w2, st));
   }
   tm.mark(2);
   double t_pat = 0, t_isai = 0;
@@ -437,13 +458,10 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
       ws = Carver(wsq, need);
     }
   }
+  IsaiSym symL, symU;
   if (isai) {
-    const bool want32 =
-        (prec_mask & ((1 << BILU_FP32) | (1 << BILU_FP32_INNER) | (1 << BILU_NESTED))) != 0;
-    BILU_TRY(build_isai_side(c, 1, ws, &c->Lrow, &c->Lcol, &c->Lval, &c->nnzL, &t_pat, &t_isai,
-                             want32 ? &c->Lval32 : nullptr));
-    BILU_TRY(build_isai_side(c, 0, ws, &c->Urow, &c->Ucol, &c->Uval, &c->nnzU, &t_pat, &t_isai,
-                             want32 ? &c->Uval32 : nullptr));
+    BILU_TRY(build_isai_sym(c, 1, ws, symL, &t_pat));
+    BILU_TRY(build_isai_sym(c, 0, ws, symU, &t_pat));
   }
   {
     Carver w2 = ws;
@@ -452,13 +470,9 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
     BILU_TRY(spmv_layout_of(nb, bs, c->Arow, words, st, &c->spmv_layout[0]));
     c->spmv_layout[1] = c->spmv_layout[2] = 0;
     if (isai) {
-      BILU_TRY(spmv_layout_of(nb, bs, c->Lrow, words, st, &c->spmv_layout[1]));
-      BILU_TRY(spmv_layout_of(nb, bs, c->Urow, words, st, &c->spmv_layout[2]));
+      BILU_TRY(spmv_layout_of(nb, bs, symL.Trow, words, st, &c->spmv_layout[1]));
+      BILU_TRY(spmv_layout_of(nb, bs, symU.Trow, words, st, &c->spmv_layout[2]));
     }
-  }
-  if (prec_mask & ((1 << BILU_FP32_INNER) | (1 << BILU_NESTED))) {
-    BILU_TRY(c->alloc(&c->Aval32, (size_t)nnzb * bs2));
-    BILU_TRY(bilu_convert_f64_to_f32((size_t)nnzb * bs2, c->Aval, c->Aval32, st));
   }
   if (ilu) {
     // level analyses of both triangles of the packed factor for the exact
@@ -477,6 +491,36 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
     }
     for (int t = 0; t < 2; ++t)
       if (c->schedule == 0 || c->schedule == 1) c->ilu_sched[t] = c->schedule;
+  }
+  // the values
+  if (values_ready) BILU_TRY_CUDA(cudaStreamWaitEvent(st, values_ready, 0));
+  tm.mark(3);
+  BILU_TRY(c->alloc(&c->Aval, nnzb * bs2));
+  BILU_TRY(c->alloc(&c->LU, nnzb * bs2));
+  BILU_TRY(c->alloc(&c->rdiag, (size_t)nb * bs + 1));
+  BILU_TRY_CUDA(cudaMemcpyAsync(c->Aval, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
+  BILU_TRY_CUDA(cudaMemcpyAsync(c->LU, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
+  {
+    Carver w2 = ws;
+    int zp = -1;
+    int rc = bilu0_factor(nb, nnzb, bs, c->Arow, c->Acol, c->diag, c->LU, &zp, w2, st,
+                          c->schedule, c->rdiag, keepL);
+    if (rc != BILU_OK) return rc;
+  }
+  tm.mark(4);
+  if (isai) {
+    const bool want32 =
+        (prec_mask & ((1 << BILU_FP32) | (1 << BILU_FP32_INNER) | (1 << BILU_NESTED))) != 0;
+    BILU_TRY(build_isai_num(c, 1, symL, &c->Lrow, &c->Lcol, &c->Lval, &c->nnzL, &t_isai,
+                            want32 ? &c->Lval32 : nullptr));
+    BILU_TRY(build_isai_num(c, 0, symU, &c->Urow, &c->Ucol, &c->Uval, &c->nnzU, &t_isai,
+                            want32 ? &c->Uval32 : nullptr));
+  }
+  if (prec_mask & ((1 << BILU_FP32_INNER) | (1 << BILU_NESTED))) {
+    BILU_TRY(c->alloc(&c->Aval32, (size_t)nnzb * bs2));
+    BILU_TRY(bilu_convert_f64_to_f32((size_t)nnzb * bs2, c->Aval, c->Aval32, st));
+  }
+  if (ilu) {
     BILU_TRY(c->alloc(&c->ilu_flags, (size_t)nb + 2));
     BILU_TRY(c->alloc(&c->ilu_words, 4));
     BILU_TRY_CUDA(cudaMemsetAsync(c->ilu_words, 0, sizeof(unsigned) * 4, st));
@@ -490,8 +534,9 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
     }
   }
 
-  tm.mark(3);
-  double t_factor = tm.ms(1, 2), t_total = tm.ms(0, 3);
+  tm.mark(5);
+  // factor: BILU(0)'s analysis and factorisation
+  double t_factor = tm.ms(1, 2) + tm.ms(3, 4), t_total = tm.ms(0, 5);
   BILU_TRY_CUDA(cudaStreamSynchronize(st));
   if (h_times) {
     h_times[0] = t_factor;
@@ -501,6 +546,14 @@ extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* 
   }
   c->ready = true;
   return BILU_OK;
+}
+
+}  // namespace
+
+extern "C" int bilu_ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* d_row,
+                              const int* d_col, const double* d_val, int prec_mask,
+                              double* h_times) {
+  return ctx_setup(c, nb, nnzb, bs, d_row, d_col, d_val, prec_mask, h_times, nullptr);
 }
 
 extern "C" int bilu_ctx_set_schedule(bilu_ctx* c, int schedule) {
@@ -973,15 +1026,24 @@ extern "C" int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const
   cu(dev_alloc((void**)&val, sizeof(double) * nnzb * bs2, dev, st));
   cu(dev_alloc((void**)&b, sizeof(double) * n, dev, st));
   cu(dev_alloc((void**)&x, sizeof(double) * n, dev, st));
+  // the pattern on the caller's stream, the values (most of the bytes) and
+  // b on a second stream: the setup's structure phase runs while they copy
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev = nullptr;
+  cu(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+  cu(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   if (rc == BILU_OK) {
+    cu(cudaEventRecord(ev, st));  // the buffers were allocated on st
+    cu(cudaStreamWaitEvent(side, ev, 0));
     cu(cudaMemcpyAsync(row, h_row, sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, st));
     cu(cudaMemcpyAsync(col, h_col, sizeof(int) * nnzb, cudaMemcpyHostToDevice, st));
-    cu(cudaMemcpyAsync(val, h_val, sizeof(double) * nnzb * bs2, cudaMemcpyHostToDevice, st));
-    cu(cudaMemcpyAsync(b, h_b, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    cu(cudaMemcpyAsync(val, h_val, sizeof(double) * nnzb * bs2, cudaMemcpyHostToDevice, side));
+    cu(cudaMemcpyAsync(b, h_b, sizeof(double) * n, cudaMemcpyHostToDevice, side));
+    cu(cudaEventRecord(ev, side));
   }
   if (rc == BILU_OK) rc = bilu_ctx_create(&c, stream);
   if (rc == BILU_OK)
-    rc = bilu_ctx_setup(c, nb, nnzb, bs, row, col, val, prec > 0 ? (1 << prec) : 0, h_times);
+    rc = ctx_setup(c, nb, nnzb, bs, row, col, val, prec > 0 ? (1 << prec) : 0, h_times, ev);
   int src = BILU_OK;
   if (rc == BILU_OK) {
     src = bilu_ctx_solve(c, prec, b, x, restart, tol, maxit, h_iters, h_relres, nullptr);
@@ -992,8 +1054,13 @@ extern "C" int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const
     cu(cudaStreamSynchronize(st));
   }
   bilu_ctx_destroy(c);
+  // the side stream's copies are finished before the buffers go back (on a
+  // failed setup the solve never waited for them)
+  if (ev) cudaStreamWaitEvent(st, ev, 0);
   for (void* p : {(void*)row, (void*)col, (void*)val, (void*)b, (void*)x})
     if (p) cudaFreeAsync(p, st);
   cudaStreamSynchronize(st);
+  if (ev) cudaEventDestroy(ev);
+  if (side) cudaStreamDestroy(side);
   return rc != BILU_OK ? rc : src;
 }

@@ -2004,26 +2004,27 @@ int sync_init_words(SyncState& ss, Carver& ws, cudaStream_t st) {
 // barrier per dependency level of the lower DAG) or sync-free.  rdiag
 // (nb x bs) receives the reciprocal pivots; null: carved from ws.  keep
 // (optional): where the level analysis of the lower DAG is built and kept.
-int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, const int* diag,
-               double* val, int* h_zp, Carver& ws, cudaStream_t st, int schedule,
-               double* rdiag, LevelOut* keep) {
-  const bool kept = keep && keep->order && keep->lvl && keep->nlev;
-  int* order = kept ? keep->order : ws.take<int>((size_t)nb + 1);
-  int* lvl = kept ? keep->lvl : ws.take<int>((size_t)nb + 2);
-  int* nlev_d = kept ? keep->nlev : ws.take<int>(4);
+// Level analysis of BILU(0)'s lower DAG into keep (order, lvl, nlev on the
+// device; level count, schedules and largest dependency count on the host).
+// Structure only: it may run before the values are on the device.
+int bilu0_analyze(int nb, long long nnzb, const int* row, const int* col, const int* diag,
+                  LevelOut& keep, Carver& ws, cudaStream_t st) {
+  if (!keep.order || !keep.lvl || !keep.nlev) return BILU_ERR_WORKSPACE;
+  return build_levels(nb, row, col, diag, 1, std::max(nnzb - nb, 0ll), keep.order, keep.lvl,
+                      keep.nlev, &keep.h_nlev, ws, st, &keep.h_sched, &keep.h_maxdeg,
+                      &keep.h_fsched);
+}
+
+// BILU(0) on an analysis from bilu0_analyze.
+int bilu0_factor(int nb, long long nnzb, int bs, const int* row, const int* col,
+                 const int* diag, double* val, int* h_zp, Carver& ws, cudaStream_t st,
+                 int schedule, double* rdiag, const LevelOut& keep) {
+  int* order = keep.order;
+  int* lvl = keep.lvl;
+  int* nlev_d = keep.nlev;
   if (!rdiag) rdiag = ws.take<double>((size_t)nb * bs + 1);
   if (!order || !lvl || !nlev_d || !rdiag) return BILU_ERR_WORKSPACE;
-  int nlev = 0, sched = 0, ssched = 0, maxdeg = 0;
-  {
-    Carver w2 = ws;
-    BILU_TRY(build_levels(nb, row, col, diag, 1, std::max(nnzb - nb, 0ll), order, lvl, nlev_d,
-                          &nlev, w2, st, &ssched, &maxdeg, &sched));
-  }
-  if (kept) {
-    keep->h_nlev = nlev;
-    keep->h_sched = ssched;
-    keep->h_maxdeg = maxdeg;
-  }
+  int sched = keep.h_fsched;
   if (schedule == 0 || schedule == 1) sched = schedule;  // caller's choice
   if (sched == 1) {
     // narrow levels or long rows: sync-free, tickets in level order
@@ -2055,6 +2056,27 @@ int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, c
   int herr = grid_sync_finish(gs, st);
   if (herr != 0) return herr;
   return sync_finish(ss, h_zp, st);
+}
+
+// Analysis and factorisation; the analysis goes to keep when its arrays are
+// given, else to the workspace.
+int bilu0_impl(int nb, long long nnzb, int bs, const int* row, const int* col, const int* diag,
+               double* val, int* h_zp, Carver& ws, cudaStream_t st, int schedule,
+               double* rdiag, LevelOut* keep) {
+  const bool kept = keep && keep->order && keep->lvl && keep->nlev;
+  LevelOut local;
+  LevelOut& k = kept ? *keep : local;
+  if (!kept) {
+    k.order = ws.take<int>((size_t)nb + 1);
+    k.lvl = ws.take<int>((size_t)nb + 2);
+    k.nlev = ws.take<int>(4);
+    if (!k.order || !k.lvl || !k.nlev) return BILU_ERR_WORKSPACE;
+  }
+  {
+    Carver w2 = ws;
+    BILU_TRY(bilu0_analyze(nb, nnzb, row, col, diag, k, w2, st));
+  }
+  return bilu0_factor(nb, nnzb, bs, row, col, diag, val, h_zp, ws, st, schedule, rdiag, k);
 }
 
 // Sync-free solve (dynamic tickets over the level order, per-row flags).

@@ -853,14 +853,41 @@ def test_pattern_product_too_dense_is_reported(cuda):
 
 
 def test_solve_host_end_to_end(cuda, orc):
+    """bilu_solve_host from pageable and from pinned host buffers (pinned: the
+    values copy on a second stream while the setup's structure phase runs,
+    and the value phase waits for it).  Every mode reaches 1e-10; the FP64
+    and FP32 modes give the bits of the solve on device buffers, and the
+    FP64 mode the oracle's iteration count."""
+    import torch
+
     from isai_kernel_gb300 import api
 
     A = gen.laplace2d(20, bs=4, seed=1)
     b = gen.rhs(A.n, 5)
-    x, res, times = api.solve_host(A.nb, A.bs, A.rowptr, A.colind, A.val, b, prec=1)
-    assert res.converged
-    r = b - A.to_dense() @ x
-    assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.01e-10
+    S = orc.isai_setup(A)
+    _, ito, _, _, sto = orc.gmres((A.rowptr, A.colind, A.val), (S["TrowL"], S["TcolL"], S["McsrL"]),
+                                  (S["TrowU"], S["TcolU"], S["McsrU"]), b, precond=1, maxit=3000)
+    assert sto == 0
+    keep = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            for a in (A.rowptr, A.colind, A.val.reshape(-1), b)]
+    pinned = [t.numpy() for t in keep]
+    P = api.Preconditioner(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda),
+                           fp32=True)
+    for prec in (api.BILU_FP64, api.BILU_FP32, api.BILU_NESTED):
+        xs = []
+        for bufs in ((A.rowptr, A.colind, A.val, b), pinned):
+            x, res, times = api.solve_host(A.nb, A.bs, *bufs, prec=prec)
+            assert res.converged, prec
+            r = b - A.to_dense() @ x
+            assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.01e-10
+            xs.append(x)
+        assert np.array_equal(xs[0], xs[1]), prec
+        if prec != api.BILU_NESTED:
+            xd, resd = P.solve(T(b, cuda), prec=prec, maxit=10000)
+            assert resd.iters == res.iters and np.array_equal(N(xd), xs[0]), prec
+        if prec == api.BILU_FP64:
+            assert res.iters == ito
+    P.close()
 
 
 @pytest.mark.parametrize("name,inner", [("c1_s16", 10), ("c2_s6", 20), ("c3_nb200", 20),
