@@ -232,6 +232,18 @@ struct bilu_ctx {
     setup_bufs.push_back(*p);
     return BILU_OK;
   }
+  // a setup buffer no longer needed goes back to the pool now (stream
+  // ordered), so the solver's buffers reuse its memory
+  void release(void* p) {
+    if (!p) return;
+    for (size_t i = 0; i < setup_bufs.size(); ++i)
+      if (setup_bufs[i] == p) {
+        setup_bufs[i] = setup_bufs.back();
+        setup_bufs.pop_back();
+        cudaFreeAsync(p, st);
+        return;
+      }
+  }
 };
 
 extern "C" int bilu_ctx_create(bilu_ctx** ctx, bilu_stream_t stream) {
@@ -355,6 +367,8 @@ int build_isai_num(bilu_ctx* c, int lower, const IsaiSym& y, int** orow, int** o
   if (oval32) BILU_TRY(c->alloc(&M32, (size_t)y.mnnz * bs2));
   BILU_TRY(reorder_impl(y.mnnz, bs, y.map, Mcsc, Mcsr, st, M32));
   if (oval32) *oval32 = M32;
+  c->release(Mcsc);
+  c->release(Dinv);
   tm.mark(1);
   *t_isai += tm.ms(0, 1);
   *orow = y.Trow;
@@ -401,6 +415,7 @@ int ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* d_row, const int
                          levels_ws(nb, nnzb), pattern_product_ws(nb),
                          scan_ws_bytes(nnzb + nb + 1)}) + (1 << 16);
   void* wsp = nullptr;
+  void* wsq = nullptr;  // a larger scratch for the pattern(A^k) steps
   BILU_TRY(c->alloc((char**)&wsp, wsb));
   Carver ws(wsp, wsb);
   {
@@ -453,7 +468,6 @@ int ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* d_row, const int
     size_t need = std::max({isai_pattern_ws(nb, np), pairs_ws(np + nb),
                             scan_ws_bytes(np + nb + 1)}) + (1 << 16);
     if (need > wsb) {
-      void* wsq = nullptr;
       BILU_TRY(c->alloc((char**)&wsq, need));
       ws = Carver(wsq, need);
     }
@@ -534,6 +548,14 @@ int ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* d_row, const int
     }
   }
 
+  // the structure of the ISAI columns, the pair lists and the scratch are
+  // not read after the setup
+  for (IsaiSym* y : {&symL, &symU})
+    for (void* p : {(void*)y->Mptr, (void*)y->Mind, (void*)y->map, (void*)y->pp, (void*)y->pl,
+                    (void*)y->ps})
+      c->release(p);
+  c->release(wsp);
+  c->release(wsq);
   tm.mark(5);
   // factor: BILU(0)'s analysis and factorisation
   double t_factor = tm.ms(1, 2) + tm.ms(3, 4), t_total = tm.ms(0, 5);
