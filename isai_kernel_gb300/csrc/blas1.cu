@@ -152,44 +152,54 @@ void launch_multiaxpy(long long n, const double* V, long long ldv, const double*
     default: return BILU_ERR_ARG;                                                    \
   }
 
-// One thread: Givens QR of the inner Hessenberg matrix and the triangular
-// solve, as the host does for the outer one (the same rotation formulas).
+// Givens QR of the inner Hessenberg matrix and the triangular solve, with
+// the host's rotation formulas for the outer one, on one warp: lane j owns
+// column j; rotation q is formed from column q once rotations 0..q-1 have
+// reached it and is then applied to the columns right of it by their lanes
+// at once, so every element sees the same operations in the same order as
+// a column-by-column loop (the same bits); the back substitution runs in
+// lane 0.
 __global__ void k_inner_lsq(int k, const double* __restrict__ Hraw, const double* __restrict__ ww,
                             double* __restrict__ y) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double H[kMaxVec + 1][kMaxVec];
-  double cs[kMaxVec], sn[kMaxVec], g[kMaxVec + 1];
-  int steps = k;
-  for (int j = 0; j < k; ++j) {
+  __shared__ double H[kMaxVec + 1][kMaxVec];
+  __shared__ double g[kMaxVec + 1];
+  const int j = threadIdx.x;
+  if (blockIdx.x != 0 || j >= 32) return;
+  // the steps end at the first zero subdiagonal entry
+  const bool zero = j < k && ww[j] == 0.0;
+  const unsigned zmask = __ballot_sync(0xffffffffu, zero);
+  const int steps = zmask ? __ffs(zmask) : k;
+  if (j < steps) {
     for (int i = 0; i <= j; ++i) H[i][j] = Hraw[i * k + j];
-    const double hn = sqrt(ww[j]);
-    H[j + 1][j] = hn;
-    if (hn == 0.0) {
-      steps = j + 1;
-      break;
-    }
+    H[j + 1][j] = sqrt(ww[j]);
   }
-  g[0] = 1.0;
-  for (int j = 0; j < steps; ++j) {
-    for (int i = 0; i < j; ++i) {
-      const double a = H[i][j], b = H[i + 1][j];
-      H[i][j] = cs[i] * a + sn[i] * b;
-      H[i + 1][j] = -sn[i] * a + cs[i] * b;
-    }
-    const double a = H[j][j], b = H[j + 1][j];
+  if (j == 0) g[0] = 1.0;
+  __syncwarp();
+  for (int q = 0; q < steps; ++q) {
+    const double a = H[q][q], b = H[q + 1][q];
     const double den = sqrt(a * a + b * b);
-    cs[j] = den != 0.0 ? a / den : 1.0;
-    sn[j] = den != 0.0 ? b / den : 0.0;
-    H[j][j] = cs[j] * a + sn[j] * b;
-    g[j + 1] = -sn[j] * g[j];
-    g[j] = cs[j] * g[j];
+    const double cs = den != 0.0 ? a / den : 1.0;
+    const double sn = den != 0.0 ? b / den : 0.0;
+    __syncwarp();
+    if (j == q) {
+      H[q][q] = cs * a + sn * b;
+      g[q + 1] = -sn * g[q];
+      g[q] = cs * g[q];
+    } else if (j > q && j < steps) {
+      const double c0 = H[q][j], c1 = H[q + 1][j];
+      H[q][j] = cs * c0 + sn * c1;
+      H[q + 1][j] = -sn * c0 + cs * c1;
+    }
+    __syncwarp();
   }
-  for (int i = steps - 1; i >= 0; --i) {
-    double v = g[i];
-    for (int l = i + 1; l < steps; ++l) v -= H[i][l] * y[l];
-    y[i] = H[i][i] != 0.0 ? v / H[i][i] : 0.0;
+  if (j == 0) {
+    for (int i = steps - 1; i >= 0; --i) {
+      double v = g[i];
+      for (int l = i + 1; l < steps; ++l) v -= H[i][l] * y[l];
+      y[i] = H[i][i] != 0.0 ? v / H[i][i] : 0.0;
+    }
+    for (int i = steps; i < k; ++i) y[i] = 0.0;
   }
-  for (int i = steps; i < k; ++i) y[i] = 0.0;
 }
 
 template <int K>
