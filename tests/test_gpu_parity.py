@@ -872,8 +872,8 @@ def test_solve_host_end_to_end(cuda, orc):
             for a in (A.rowptr, A.colind, A.val.reshape(-1), b)]
     pinned = [t.numpy() for t in keep]
     P = api.Preconditioner(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda),
-                           fp32=True)
-    for prec in (api.BILU_FP64, api.BILU_FP32, api.BILU_NESTED):
+                           fp32=True, ilu=True, ilu_fp32=True)
+    for prec in (api.BILU_FP64, api.BILU_FP32, api.BILU_ILU, api.BILU_ILU_FP32, api.BILU_NESTED):
         xs = []
         for bufs in ((A.rowptr, A.colind, A.val, b), pinned):
             x, res, times = api.solve_host(A.nb, A.bs, *bufs, prec=prec)
