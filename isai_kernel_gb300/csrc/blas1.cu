@@ -246,8 +246,9 @@ void launch_combine(long long n, const float* Q, long long ldq, const double* y,
 
 // ---------------------------------------------------------------------------
 // Whole modified Gram-Schmidt step in one cooperative launch: sweeps
-// i = 0 .. j+1 over the same slice of w per CTA, sweep i applying h_{i-1} v_{i-1} and taking v_i . w (the last
-// one w . w), then v_{j+1} = w / ||w|| (and its FP32 copy).  Between sweeps
+// i = 0 .. j+1 over the same slice of w per CTA, sweep i applying
+// h_{i-1} v_{i-1} and taking v_i . w (the last one w . w), then
+// v_{j+1} = w / ||w|| (and its FP32 copy).  Between sweeps
 // a counting grid barrier replaces the kernel boundary: each CTA writes its
 // partial sum, meets the others at the barrier, and then every CTA adds all
 // partials in index order (warp 0, fixed lane strides and shuffle tree), so
