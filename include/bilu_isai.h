@@ -514,8 +514,9 @@ int bilu_batch_set_schedule(bilu_batch* batch, int persistent);
  *   - d_b and d_x may not be the same buffer (BILU_ERR_ARG); a block row
  *     without a stored diagonal block returns BILU_ERR_PATTERN.
  *   - The first call on a device looks up the array's device address with
- *     cudaGetSymbolAddress (no allocation) and caches it; make that first call
- *     before any stream capture on that device.
+ *     cudaGetSymbolAddress (no allocation) and caches it.
+ *   - The call synchronises its stream, so it cannot be recorded into a
+ *     CUDA graph.
  *   - All calls share the one array and every call re-initialises the parts
  *     that must start at zero.  Calls whose executions overlap on the GPU
  *     (different streams, or different host threads) race on it: serialise
