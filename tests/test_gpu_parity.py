@@ -891,7 +891,7 @@ def test_solve_host_end_to_end(cuda, orc):
 
 
 @pytest.mark.parametrize("name,inner", [("c1_s16", 10), ("c2_s6", 20), ("c3_nb200", 20),
-                                        ("bs5_s7", 8)])
+                                        ("bs5_s7", 8), ("c1_s16", 1), ("c2_s6", 32)])
 def test_gmres_nested_matches_oracle(cuda, orc, name, inner):
     """BILU_NESTED (GMRES-IR): FP64 flexible outer GMRES(30) whose every
     preconditioned vector is `inner` steps of FP32 ISAI-preconditioned GMRES
