@@ -424,6 +424,15 @@ __global__ void __launch_bounds__(kStepThreads, kStepPerSM) k_mgs_step(
         M::dot(vnv ? sl[2 * kStepThreads] : we, we, a);
       }
       cp_async_wait<0>();
+      // the next sweep's first stages read v_i (as v_{i-1}) and v_{i+1}: start
+      // those lines towards the L2 before the grid barrier (1-2% a sweep)
+      for (long long k = 0; k < S - 1 && k < K; ++k) {
+        const long long e = tid + k * stride;
+        if (vnv) asm volatile("prefetch.global.L2 [%0];" ::"l"(vnv + e));
+        if (i + 1 <= j)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(
+              reinterpret_cast<const VT*>(V + (long long)(i + 1) * ldv) + e));
+      }
     } else {
       // two elements' loads in flight per thread
 #pragma unroll 2
