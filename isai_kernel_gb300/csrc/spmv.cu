@@ -155,12 +155,12 @@ __device__ __noinline__ void spmv_long_rows(const int* long_rows, const int* __r
 // row) and its triangle (4 a row): FP64 values U = 1, RPG = 2 (two
 // independent DFMA chains per lane; one chain is latency-bound: 0.48 ->
 // 0.40 ms on the 7-point FP64 operator, the same on the triangle); FP32
-// values U = 4 with RPG = 2 for rows of ~4 blocks, RPG = 1 for wider rows
-// (0.199 -> 0.176 ms on the FP32 operator).  LONG (matrices with rows of
-// more than kLongSpmvRow blocks): such a row is skipped by its group and
-// summed after the short rows by the whole CTA (dynamic shared memory: the
-// CTA's long-row slots and the group partials); the other instance has no
-// CTA barrier at all.
+// values U = 4 with RPG = 1 for wider rows (0.199 -> 0.176 ms on the FP32
+// operator), RPG = 1 at 8 CTAs per SM for bs 4 rows of ~4 blocks, else
+// RPG = 2.  LONG (matrices with rows of more than kLongSpmvRow blocks):
+// such a row is skipped by its group and summed after the short rows by
+// the whole CTA (dynamic shared memory: the CTA's long-row slots and the
+// group partials); the other instance has no CTA barrier at all.
 template <int BS, class VT, class XT, class YT, class AccT, int RPG, int U, int MINB, bool LONG>
 __global__ void __launch_bounds__(256, MINB) k_bsr_spmv(int mb, const int* __restrict__ row,
                                                      const int* __restrict__ col,
@@ -308,6 +308,11 @@ int launch_spmv(int mb, const int* row, const int* col, const VT* val, const XT*
       return launch_spmv_cfg<BS, VT, XT, YT, 2, 4, 4, true>(mb, row, col, val, x, y, st, y32);
     if (layout & kLayoutWide)
       return launch_spmv_cfg<BS, VT, XT, YT, 1, 4, 4, false>(mb, row, col, val, x, y, st, y32);
+    // bs 4 rows of ~4 blocks (the ISAI triangles of a 7-point pattern): one
+    // row per group at 32 registers, 8 CTAs per SM (0.2214 -> 0.2185 ms
+    // for the 128^3 inner apply)
+    if constexpr (BS == 4)
+      return launch_spmv_cfg<BS, VT, XT, YT, 1, 4, 8, false>(mb, row, col, val, x, y, st, y32);
     return launch_spmv_cfg<BS, VT, XT, YT, 2, 4, 4, false>(mb, row, col, val, x, y, st, y32);
   }
 }
