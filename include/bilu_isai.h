@@ -352,8 +352,10 @@ int bilu_ctx_destroy(bilu_ctx* ctx);
  * and of A when it has 1 << BILU_NESTED.  A prec_mask of exact-ILU bits
  * alone builds BILU(0) and the level analyses only (no ISAI; solves in the
  * other modes then return BILU_ERR_ARG).
- * h_times (optional, 4 doubles, milliseconds): factor, patterns, isai,
- * total. */
+ * h_times (optional, 4 doubles, milliseconds): factor (BILU(0)'s level
+ * analysis and factorisation, with the copies of A), patterns (ISAI
+ * patterns and pair lists), isai (Dinv, column solves, reorders), total.
+ * The structure steps run first, then the value steps. */
 int bilu_ctx_setup(bilu_ctx* ctx, int nb, int nnzb, int bs, const int* d_row, const int* d_col,
                    const double* d_val, int prec_mask, double* h_times);
 
