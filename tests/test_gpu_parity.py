@@ -852,17 +852,18 @@ def test_pattern_product_too_dense_is_reported(cuda):
     assert e.value.status == -8
 
 
-def test_solve_host_end_to_end(cuda, orc):
+@pytest.mark.parametrize("name", ["l20", "c3_nb200", "bs5_s7"])
+def test_solve_host_end_to_end(cuda, orc, name):
     """bilu_solve_host from pageable and from pinned host buffers (pinned: the
     values copy on a second stream while the setup's structure phase runs,
-    and the value phase waits for it).  Every mode reaches 1e-10; the FP64
-    and FP32 modes give the bits of the solve on device buffers, and the
-    FP64 mode the oracle's iteration count."""
+    and the value phase waits for it), block sizes 4, 8 and 5.  Every mode
+    reaches 1e-10; the modes the device path also builds give its bits,
+    and the FP64 mode the oracle's iteration count."""
     import torch
 
     from isai_kernel_gb300 import api
 
-    A = gen.laplace2d(20, bs=4, seed=1)
+    A = gen.laplace2d(20, bs=4, seed=1) if name == "l20" else mats()[name]
     b = gen.rhs(A.n, 5)
     S = orc.isai_setup(A)
     _, ito, _, _, sto = orc.gmres((A.rowptr, A.colind, A.val), (S["TrowL"], S["TcolL"], S["McsrL"]),
@@ -871,9 +872,11 @@ def test_solve_host_end_to_end(cuda, orc):
     keep = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
             for a in (A.rowptr, A.colind, A.val.reshape(-1), b)]
     pinned = [t.numpy() for t in keep]
+    stencil = name != "c3_nb200"  # the FP32 exact-ILU apply takes rows of <= 32 dependencies
     P = api.Preconditioner(A.nb, A.bs, T(A.rowptr, cuda), T(A.colind, cuda), T(A.val, cuda),
-                           fp32=True, ilu=True, ilu_fp32=True)
-    for prec in (api.BILU_FP64, api.BILU_FP32, api.BILU_ILU, api.BILU_ILU_FP32, api.BILU_NESTED):
+                           fp32=True, ilu=True, ilu_fp32=stencil)
+    modes = (api.BILU_FP64, api.BILU_FP32, api.BILU_ILU, api.BILU_NESTED)
+    for prec in modes + ((api.BILU_ILU_FP32,) if stencil else ()):
         xs = []
         for bufs in ((A.rowptr, A.colind, A.val, b), pinned):
             x, res, times = api.solve_host(A.nb, A.bs, *bufs, prec=prec)
