@@ -23,7 +23,12 @@ committed ncu capture.  `errors` states each mixed-precision result against
 the FP64 oracle.  `cpu_baseline` is the oracle's full nested solve on the
 host cores (measured, one solve), plus serial (one core) times.
 `--impl reference` times the oracle's solve of the same system in every
-step.  Secondary lines: --workload sptrsv | powerlaw | batch.
+step.  Secondary lines: --workload sptrsv | powerlaw | batch (give the batch
+a step cap, e.g. --maxit 60: its larger systems do not converge).  For ncu:
+--workload kernels (the inner solver's products, the FP64 operator product
+and the Gram-Schmidt step kernels; --mgs-only for the step kernels alone)
+and --profile (setup and solves only; --profile-prec fp64 for the plain
+path).
 
     python bench.py [--steps K] [--warmup W] [--side 128] [--inner 8] [--impl reference]
     torchrun --nproc-per-node N bench.py --gpus N   (N independent replicas)
