@@ -64,3 +64,22 @@ def test_reference_arm_under_torchrun():
     assert d["relres"] <= 1e-10 and d["status"] == 0 and len(d["step_s"]) == 2
     assert d["iters"]["inner"] == d["iters"]["outer"] * d["config"]["inner"]
     assert d["config"]["workload"].startswith("convdiff3d 10^3 bs4")
+
+
+def test_bench_options_parse(monkeypatch):
+    """The measurement modes the docstring and the profiles name parse, with
+    the defaults the headline line uses."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    monkeypatch.setattr(sys, "argv", ["bench.py"])
+    a = bench.parse()
+    assert (a.gpus, a.steps, a.warmup, a.side, a.inner, a.impl) == (1, 5, 3, 128, 8, "ours")
+    assert a.workload == "convdiff" and not a.profile and not a.mgs_only
+    assert a.profile_prec == "nested"
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--workload", "kernels", "--side", "96",
+                                      "--mgs-only", "--profile", "--profile-prec", "fp64",
+                                      "--maxit", "60", "--impl", "reference"])
+    a = bench.parse()
+    assert (a.workload, a.side, a.mgs_only, a.profile, a.profile_prec, a.maxit, a.impl) == (
+        "kernels", 96, True, True, "fp64", 60, "reference")
