@@ -704,9 +704,10 @@ int ensure_inner(bilu_ctx* c) {
 // normalised v; v has unit norm, so beta = 1: flexible GMRES accepts any
 // scaling of z).  Every step: q_i = M_U (M_L u_i) into Q32[i], w = A q_i,
 // then one cooperative launch of the i + 2 fused FP32 Gram-Schmidt sweeps
-// writing h_0i..h_ii and ||w||^2, and u_{i+1} = w / ||w||.  Then the Hessenberg least-squares problem on the
-// device and z = Q y widened to FP64.  Nothing waits on the host: the
-// whole inner solve is queued on the stream.
+// writing h_0i..h_ii and ||w||^2, and u_{i+1} = w / ||w||.  Then the
+// Hessenberg least-squares problem on the device and z = Q y widened to
+// FP64.  Nothing waits on the host: the whole inner solve is queued on the
+// stream.
 int inner_solve(bilu_ctx* c, double* z) {
   cudaStream_t st = c->st;
   const long long n = c->n;
