@@ -727,8 +727,8 @@ def run_powerlaw(args):
     A = gen.powerlaw(args.pl_nb, bs=8, seed=0)
     b = torch.from_numpy(gen.rhs(A.n, 0)).cuda()
     row, col, val = (torch.from_numpy(a).cuda() for a in (A.rowptr, A.colind, A.val))
-    # the first setup grows the library's memory pool (the driver maps
-    # ~20 GB, at a cost that differs from box to box); the second one, after
+    # the first setup grows the library's memory pool (the CUDA driver maps
+    # ~20 GB, at a cost that differs from machine to machine); the second one, after
     # the first handle returned its buffers to the pool, times the kernels
     P = api.Preconditioner(A.nb, 8, row, col, val)
     cold = P.setup_ms

@@ -127,9 +127,11 @@ cudaMemPool_t lib_pool(int dev) {
   return pools[dev];
 }
 
+// Every buffer from here is freed with cudaFreeAsync, so the fallback when
+// no private pool could be made is the device's default stream-ordered pool.
 cudaError_t dev_alloc(void** p, size_t bytes, int dev, cudaStream_t st) {
   cudaMemPool_t pool = lib_pool(dev);
-  if (!pool) return cudaMalloc(p, bytes);
+  if (!pool) return cudaMallocAsync(p, bytes, st);
   return cudaMallocFromPoolAsync(p, bytes, pool, st);
 }
 
