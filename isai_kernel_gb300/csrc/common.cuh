@@ -124,6 +124,10 @@ struct LevelOut {
   int *order = nullptr, *lvl = nullptr, *nlev = nullptr;
   int h_nlev = 0, h_sched = 0, h_maxdeg = 0;  // levels, solve schedule, largest dependency count
   int h_fsched = 0;                           // recommended factorisation schedule
+  // optional match lists of BILU(0)'s updates (bilu0_match_count / _fill):
+  // positions mptr[p] .. mptr[p+1] of mpair for block position p
+  const int* mptr = nullptr;
+  const int2* mpair = nullptr;
 };
 
 }  // namespace bilu

@@ -3,6 +3,7 @@
 // (patterns, bsrilu02, Dinv, pairs, ISAI-L/U, reorder, one apply), extended
 // with the Krylov solver the reference does not have.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -68,6 +69,10 @@ int bilu0_analyze(int nb, long long nnzb, const int* row, const int* col, const 
 int bilu0_factor(int nb, long long nnzb, int bs, const int* row, const int* col,
                  const int* diag, double* val, int* h_zp, Carver& ws, cudaStream_t st,
                  int schedule, double* rdiag, const LevelOut& keep);
+int bilu0_match_count(int nb, long long nnzb, const int* row, const int* col, const int* diag,
+                      int* mptr, long long cap, long long* h_total, Carver& ws, cudaStream_t st);
+int bilu0_match_fill(int nb, long long nnzb, const int* row, const int* col, const int* diag,
+                     const int* mptr, int2* mpair, cudaStream_t st);
 int dinv_impl(int nb, int bs, const int* row, const int* col, const double* val, int lower,
               double* Dinv, int* d_fail, cudaStream_t st);
 size_t pairs_ws(long long mnnz);
@@ -392,8 +397,12 @@ namespace {
 // values: BILU(0), Dinv, the ISAI column solves, the reorders and the FP32
 // copies.  The structure phase thus overlaps a host-to-device copy of the
 // values that the caller issues on another stream.
+// adopt_val: d_val is a buffer of the library's pool that the handle takes
+// over as its copy of A (the host-buffer entry point's upload), instead of
+// copying it.
 int ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* d_row, const int* d_col,
-              const double* d_val, int prec_mask, double* h_times, cudaEvent_t values_ready) {
+              const double* d_val, int prec_mask, double* h_times, cudaEvent_t values_ready,
+              bool adopt_val = false) {
   if (!c || nb < 1 || nnzb < nb || !d_row || !d_col || !d_val) return BILU_ERR_ARG;
   if (!bs_supported(bs)) return BILU_ERR_UNSUPPORTED;
   cudaStream_t st = c->st;
@@ -439,6 +448,30 @@ int ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* d_row, const int
   {
     Carver w2 = ws;
     BILU_TRY(bilu0_analyze(nb, nnzb, c->Arow, c->Acol, c->diag, keepL, w2, st));
+  }
+  // the level-order factorisation's match lists (which A_IJ each L_IK
+  // updates, with U_KJ), built here from the pattern instead of searched
+  // for inside every row's dependency chain; at most 4 pairs a block
+  int* mptr = nullptr;
+  int2* mpair = nullptr;
+  const int fsched = (c->schedule == 0 || c->schedule == 1) ? c->schedule : keepL.h_fsched;
+  if (fsched == 0) {
+    BILU_TRY(c->alloc(&mptr, (size_t)nnzb + 1));
+    long long total = 0;
+    const long long cap = 4ll * nnzb;
+    {
+      Carver w2 = ws;
+      BILU_TRY(bilu0_match_count(nb, nnzb, c->Arow, c->Acol, c->diag, mptr, cap, &total, w2, st));
+    }
+    if (total <= cap && total <= (long long)INT_MAX) {
+      BILU_TRY(c->alloc(&mpair, (size_t)total));
+      BILU_TRY(bilu0_match_fill(nb, nnzb, c->Arow, c->Acol, c->diag, mptr, mpair, st));
+      keepL.mptr = mptr;
+      keepL.mpair = mpair;
+    } else {
+      c->release(mptr);
+      mptr = nullptr;
+    }
   }
   tm.mark(2);
   double t_pat = 0, t_isai = 0;
@@ -511,10 +544,16 @@ int ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* d_row, const int
   // the values
   if (values_ready) BILU_TRY_CUDA(cudaStreamWaitEvent(st, values_ready, 0));
   tm.mark(3);
-  BILU_TRY(c->alloc(&c->Aval, nnzb * bs2));
+  if (adopt_val) {
+    c->Aval = const_cast<double*>(d_val);
+    c->setup_bufs.push_back(c->Aval);
+  } else {
+    BILU_TRY(c->alloc(&c->Aval, nnzb * bs2));
+    BILU_TRY_CUDA(cudaMemcpyAsync(c->Aval, d_val, sizeof(double) * nnzb * bs2,
+                                  cudaMemcpyDeviceToDevice, st));
+  }
   BILU_TRY(c->alloc(&c->LU, nnzb * bs2));
   BILU_TRY(c->alloc(&c->rdiag, (size_t)nb * bs + 1));
-  BILU_TRY_CUDA(cudaMemcpyAsync(c->Aval, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
   BILU_TRY_CUDA(cudaMemcpyAsync(c->LU, d_val, sizeof(double) * nnzb * bs2, cudaMemcpyDeviceToDevice, st));
   {
     Carver w2 = ws;
@@ -523,6 +562,10 @@ int ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* d_row, const int
                           c->schedule, c->rdiag, keepL);
     if (rc != BILU_OK) return rc;
   }
+  c->release(mptr);
+  c->release(mpair);
+  keepL.mptr = nullptr;
+  keepL.mpair = nullptr;
   tm.mark(4);
   if (isai) {
     const bool want32 =
@@ -1067,8 +1110,13 @@ extern "C" int bilu_solve_host(int nb, int nnzb, int bs, const int* h_row, const
     cu(cudaEventRecord(ev, side));
   }
   if (rc == BILU_OK) rc = bilu_ctx_create(&c, stream);
-  if (rc == BILU_OK)
-    rc = ctx_setup(c, nb, nnzb, bs, row, col, val, prec > 0 ? (1 << prec) : 0, h_times, ev);
+  if (rc == BILU_OK) {
+    // the handle keeps the uploaded values as its copy of A (one device
+    // copy and 8 bytes per value less) and frees them with its other buffers
+    rc = ctx_setup(c, nb, nnzb, bs, row, col, val, prec > 0 ? (1 << prec) : 0, h_times, ev,
+                   true);
+    if (c->Aval == val) val = nullptr;
+  }
   int src = BILU_OK;
   if (rc == BILU_OK) {
     src = bilu_ctx_solve(c, prec, b, x, restart, tol, maxit, h_iters, h_relres, nullptr);

@@ -1050,13 +1050,15 @@ struct BRowPre {
   int I;               // < 0: no row
   int rs, re, dI;      // row pointers and diagonal position
   int K, dK, ke;       // first dependency: column, its diagonal position, its row end
+  int m0, m1;          // its match list [m0, m1) when the lists were built
 };
 
 __device__ __forceinline__ void brow_prefetch(int I, const int* __restrict__ row,
                                               const int* __restrict__ col,
-                                              const int* __restrict__ diag, BRowPre& p) {
+                                              const int* __restrict__ diag,
+                                              const int* __restrict__ mptr, BRowPre& p) {
   p.I = I;
-  p.rs = p.re = p.dI = p.K = p.dK = p.ke = 0;
+  p.rs = p.re = p.dI = p.K = p.dK = p.ke = p.m0 = p.m1 = 0;
   if (I < 0) return;
   p.rs = __ldg(row + I);
   p.re = __ldg(row + I + 1);
@@ -1065,25 +1067,40 @@ __device__ __forceinline__ void brow_prefetch(int I, const int* __restrict__ row
     p.K = __ldg(col + p.rs);
     p.dK = __ldg(diag + p.K);
     p.ke = __ldg(row + p.K + 1);
+    if (mptr) {
+      p.m0 = __ldg(mptr + p.rs);
+      p.m1 = __ldg(mptr + p.rs + 1);
+    }
   }
 }
 
+// mptr / mpair (optional): the match lists of k_bilu0_match_fill, which
+// take the searches of phase 2 out of the row's dependency chain; the
+// updates and their arithmetic are the same either way.
 template <int BS>
 __device__ __forceinline__ void bilu0_grow(const BRowPre& pr, const int* __restrict__ row,
                                            const int* __restrict__ col,
                                            const int* __restrict__ diag, double* val,
-                                           const SyncState& ss, unsigned gmask, int r, int gb) {
+                                           const SyncState& ss, unsigned gmask, int r, int gb,
+                                           const int* __restrict__ mptr,
+                                           const int2* __restrict__ mpair) {
   constexpr int BS2 = BS * BS;
   const int I = pr.I, rs = pr.rs, re = pr.re, dI = pr.dI;
   // structure of the next dependency, loaded one step ahead
   int Kn = pr.K, dKn = pr.dK, ken = pr.ke;
+  int ms = pr.m0, men = pr.m1;
   for (int pk = rs; pk < dI; ++pk) {
     const int K = Kn, dK = dKn, ke = ken;
+    const int me = men;
     if (pk + 1 < dI) {
       Kn = __ldg(col + pk + 1);
       dKn = __ldg(diag + Kn);
       ken = __ldg(row + Kn + 1);
+      if (mptr) men = __ldg(mptr + pk + 2);
     }
+    // the first match's positions load beside phase 1's operands
+    int2 mfirst = make_int2(0, 0);
+    if (mptr && ms < me) mfirst = __ldg(mpair + ms);
     double* L = val + (long long)pk * BS2;
     const double* Ukk = val + (long long)dK * BS2;
     const double* rK = ss.rdiag + (long long)K * BS;  // 1 / pivots of U_KK
@@ -1099,8 +1116,25 @@ __device__ __forceinline__ void bilu0_grow(const BRowPre& pr, const int* __restr
     }
 #pragma unroll
     for (int c = 0; c < BS; ++c) L[r * BS + c] = a[c];
-    // phase 2: A_IJ -= L_IK U_KJ for J > K in rows I and K; the shorter
-    // column list supplies the candidates, BS at a time
+    // phase 2: A_IJ -= L_IK U_KJ for J > K in rows I and K
+    if (mptr) {
+      for (int q = ms; q < me; ++q) {
+        const int2 m = q == ms ? mfirst : __ldg(mpair + q);
+        double* Aij = val + (long long)m.x * BS2 + r * BS;
+        const double* Ukj = val + (long long)m.y * BS2;
+#pragma unroll
+        for (int c = 0; c < BS; ++c) {
+          double v = Aij[c];
+#pragma unroll
+          for (int k = 0; k < BS; ++k) v -= a[k] * __ldcg(Ukj + k * BS + c);
+          Aij[c] = v;
+        }
+      }
+      ms = me;
+      continue;
+    }
+    // without match lists the shorter column list supplies the candidates,
+    // BS at a time, searched for in the other
     const bool from_i = (re - pk - 1) <= (ke - dK - 1);
     const int cs = from_i ? pk + 1 : dK + 1, ce = from_i ? re : ke;
     const int ss_ = from_i ? dK + 1 : pk + 1, se = from_i ? ke : re;
@@ -1452,7 +1486,8 @@ template <int BS>
 __global__ void __launch_bounds__(kLvlThreads, 2) k_bilu0_levels(
     const int* __restrict__ row, const int* __restrict__ col, const int* __restrict__ diag,
     double* val, const int* __restrict__ order, const int* __restrict__ lvl_ptr,
-    const int* __restrict__ nlev_p, SyncState ss, GridSync gs) {
+    const int* __restrict__ nlev_p, SyncState ss, GridSync gs, const int* __restrict__ mptr,
+    const int2* __restrict__ mpair) {
   constexpr int G = 32 / BS;
   unsigned passed = 0;
   const int lane = threadIdx.x & 31, g = lane / BS, r = lane - g * BS, gb = g * BS;
@@ -1468,21 +1503,21 @@ __global__ void __launch_bounds__(kLvlThreads, 2) k_bilu0_levels(
   {
     const long long t = __ldg(lvl_ptr) + mygrp;
     brow_prefetch(g < G && nlev > 0 && t < __ldg(lvl_ptr + 1) ? __ldg(order + t) : -1, row, col,
-                  diag, pre);
+                  diag, mptr, pre);
   }
   for (int l = 0; l < nlev; ++l) {
     const int s = __ldg(lvl_ptr + l), e = __ldg(lvl_ptr + l + 1);
-    if (pre.I >= 0) bilu0_grow<BS>(pre, row, col, diag, val, ss, gmask, r, gb);
+    if (pre.I >= 0) bilu0_grow<BS>(pre, row, col, diag, val, ss, gmask, r, gb, mptr, mpair);
     if (g < G)
       for (long long t = s + mygrp + ngrp; t < e; t += ngrp) {
         BRowPre q;
-        brow_prefetch(__ldg(order + t), row, col, diag, q);
-        bilu0_grow<BS>(q, row, col, diag, val, ss, gmask, r, gb);
+        brow_prefetch(__ldg(order + t), row, col, diag, mptr, q);
+        bilu0_grow<BS>(q, row, col, diag, val, ss, gmask, r, gb, mptr, mpair);
       }
     if (l + 1 < nlev) {
       const long long t = e + mygrp;
       brow_prefetch(g < G && t < __ldg(lvl_ptr + l + 2) ? __ldg(order + t) : -1, row, col, diag,
-                    pre);
+                    mptr, pre);
       if (!grid_sync_count(gs, passed)) return;
     }
   }
@@ -1606,6 +1641,7 @@ constexpr int kMatchSerial = 32;
 
 struct MatchLists {
   int cs, ce, s, e;  // candidates [cs, ce) searched for in positions [s, e)
+  bool from_i;       // the candidates are row I's positions (else row K's)
 };
 
 __device__ __forceinline__ MatchLists match_lists(long long pk, int nb,
@@ -1618,7 +1654,7 @@ __device__ __forceinline__ MatchLists match_lists(long long pk, int nb,
     if (__ldg(row + mid) <= pk) lo = mid; else hi = mid - 1;
   }
   I = lo;
-  MatchLists m{0, 0, 0, 0};
+  MatchLists m{0, 0, 0, 0, true};
   if (pk >= __ldg(diag + I)) return m;  // diagonal or upper position
   const int re = __ldg(row + I + 1);
   const int K = __ldg(col + pk), dK = __ldg(diag + K), ke = __ldg(row + K + 1);
@@ -1627,6 +1663,7 @@ __device__ __forceinline__ MatchLists match_lists(long long pk, int nb,
   m.ce = from_i ? re : ke;
   m.s = from_i ? dK + 1 : (int)pk + 1;
   m.e = from_i ? ke : re;
+  m.from_i = from_i;
   return m;
 }
 
@@ -1669,6 +1706,42 @@ __global__ void __launch_bounds__(256) k_bilu0_nmatch_long(int nb, long long nnz
       n += __popc(__ballot_sync(FULL, hit));
     }
     if (lane == 0) nmatch[pk] = n;
+  }
+}
+
+// Total of the match counts in 64 bits (the caller decides from it whether
+// the lists fit before their int32 scan).
+__global__ void __launch_bounds__(256) k_match_total(long long n, const int* __restrict__ cnt,
+                                                     unsigned long long* __restrict__ total) {
+  unsigned long long s = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    s += (unsigned)max(__ldg(cnt + i), 0);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(total, s);
+}
+
+// The match lists themselves for the level-order factorisation: a thread
+// per lower position writes, in its candidates' order, the pairs (position
+// of A_IJ in row I, position of U_KJ in row K) that the factorisation would
+// otherwise find by searching inside its dependency chain.
+__global__ void __launch_bounds__(256) k_bilu0_match_fill(int nb, long long nnzb,
+                                                          const int* __restrict__ row,
+                                                          const int* __restrict__ col,
+                                                          const int* __restrict__ diag,
+                                                          const int* __restrict__ mptr,
+                                                          int2* __restrict__ mpair) {
+  const long long pk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pk >= nnzb) return;
+  int out = __ldg(mptr + pk);
+  const int end = __ldg(mptr + pk + 1);
+  if (out >= end) return;
+  int I;
+  const MatchLists m = match_lists(pk, nb, row, col, diag, I);
+  for (int c = m.cs; c < m.ce && out < end; ++c) {
+    const int o = find_in_row(col, m.s, m.e, __ldg(col + c));
+    if (o >= 0) mpair[out++] = m.from_i ? make_int2(c, o) : make_int2(o, c);
   }
 }
 
@@ -1930,12 +2003,12 @@ int launch_bilu0_syncfree(int nb, const int* row, const int* col, const int* dia
 template <int BS>
 int launch_bilu0_levels(int nb, const int* row, const int* col, const int* diag, double* val,
                         const int* order, const int* lvl_ptr, const int* nlev_d, SyncState ss,
-                        GridSync gs, cudaStream_t st) {
+                        GridSync gs, const int* mptr, const int2* mpair, cudaStream_t st) {
   const void* fn = (const void*)k_bilu0_levels<BS>;
   int grid = std::min<long long>(coop_grid(fn, kLvlThreads),
                                  ceil_div(nb, (kLvlThreads / 32) * (32 / BS)));
   gs.per_sm = std::max(1, std::min(occupancy_per_sm(fn, kLvlThreads), (int)ceil_div(grid, sm_count())));
-  void* args[] = {&row, &col, &diag, &val, &order, &lvl_ptr, &nlev_d, &ss, &gs};
+  void* args[] = {&row, &col, &diag, &val, &order, &lvl_ptr, &nlev_d, &ss, &gs, &mptr, &mpair};
   return launch_coop(fn, grid, kLvlThreads, args, st);
 }
 
@@ -2015,7 +2088,46 @@ int bilu0_analyze(int nb, long long nnzb, const int* row, const int* col, const 
                       &keep.h_fsched);
 }
 
-// BILU(0) on an analysis from bilu0_analyze.
+// BILU(0)'s match lists from the pattern alone (a structure step, before
+// the values): mptr (nnzb + 1 ints) receives the per-position counts and
+// *h_total their sum; when the sum is at most cap, mptr is turned into
+// their exclusive scan for bilu0_match_fill, else it is left as counts and
+// the lists are not to be built.  Synchronises the stream once.
+int bilu0_match_count(int nb, long long nnzb, const int* row, const int* col, const int* diag,
+                      int* mptr, long long cap, long long* h_total, Carver& ws,
+                      cudaStream_t st) {
+  *h_total = 0;
+  if (nb < 1 || nnzb < 1) return BILU_OK;
+  unsigned long long* tot = ws.take<unsigned long long>(1);
+  if (!tot) return BILU_ERR_WORKSPACE;
+  const unsigned grid = ceil_div(nnzb, 256);
+  k_bilu0_nmatch<<<grid, 256, 0, st>>>(nb, nnzb, row, col, diag, mptr);
+  BILU_LAUNCH_CHECK();
+  k_bilu0_nmatch_long<<<grid, 256, 0, st>>>(nb, nnzb, row, col, diag, mptr);
+  BILU_LAUNCH_CHECK();
+  BILU_TRY_CUDA(cudaMemsetAsync(tot, 0, sizeof(unsigned long long), st));
+  k_match_total<<<std::min(grid, 1024u), 256, 0, st>>>(nnzb, mptr, tot);
+  BILU_LAUNCH_CHECK();
+  unsigned long long h = 0;
+  BILU_TRY_CUDA(cudaMemcpyAsync(&h, tot, sizeof(h), cudaMemcpyDeviceToHost, st));
+  BILU_TRY_CUDA(cudaStreamSynchronize(st));
+  *h_total = (long long)std::min<unsigned long long>(h, (unsigned long long)LLONG_MAX);
+  if (*h_total > cap || *h_total > (long long)INT_MAX) return BILU_OK;
+  return scan_exclusive(mptr, mptr, nnzb, nullptr, ws, st);
+}
+
+// The lists themselves, into mpair (mptr[nnzb] pairs) after bilu0_match_count.
+int bilu0_match_fill(int nb, long long nnzb, const int* row, const int* col, const int* diag,
+                     const int* mptr, int2* mpair, cudaStream_t st) {
+  if (nb < 1 || nnzb < 1) return BILU_OK;
+  k_bilu0_match_fill<<<ceil_div(nnzb, 256), 256, 0, st>>>(nb, nnzb, row, col, diag, mptr,
+                                                          mpair);
+  BILU_LAUNCH_CHECK();
+  return BILU_OK;
+}
+
+// BILU(0) on an analysis from bilu0_analyze (with the match lists when
+// keep has them and the level-order kernel runs).
 int bilu0_factor(int nb, long long nnzb, int bs, const int* row, const int* col,
                  const int* diag, double* val, int* h_zp, Carver& ws, cudaStream_t st,
                  int schedule, double* rdiag, const LevelOut& keep) {
@@ -2052,7 +2164,7 @@ int bilu0_factor(int nb, long long nnzb, int bs, const int* row, const int* col,
   BILU_TRY(grid_sync_init(gs, ws, st));
   if (nb > 0)
     BILU_TRY(BILU_DISPATCH_BS(bs, launch_bilu0_levels, nb, row, col, diag, val, order, lvl,
-                              nlev_d, ss, gs, st));
+                              nlev_d, ss, gs, keep.mptr, keep.mpair, st));
   int herr = grid_sync_finish(gs, st);
   if (herr != 0) return herr;
   return sync_finish(ss, h_zp, st);

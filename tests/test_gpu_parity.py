@@ -714,6 +714,41 @@ def test_single_block_and_empty_offdiag(cuda, orc):
 
 
 # ------------------------------------------------------------------ engine + GMRES
+@pytest.mark.parametrize("name", ["c1_s16", "c2_s6", "c3_nb200", "bs5_s7", "long_rows", "dense"])
+@pytest.mark.parametrize("schedule", [-1, 0])
+def test_engine_factor_match_lists(cuda, orc, name, schedule):
+    """A handle's setup builds BILU(0)'s match lists from the pattern before
+    the level-order factorisation; its factor is the same bit for bit as
+    the entry point that searches for the matches inside the factorisation
+    (bsrilu02_inplace, level schedule), on short-row, long-row and dense
+    patterns, and within 1e-12 of the oracle."""
+    from isai_kernel_gb300 import api
+
+    if name == "long_rows":
+        A = gen.powerlaw(400, bs=8, seed=5, kmax=150)
+    elif name == "dense":
+        nb, bs = 40, 4
+        rng = np.random.default_rng(17)
+        val = rng.uniform(-1.0, 1.0, (nb * nb, bs, bs))
+        for i in range(nb):
+            val[i * nb + i] += np.eye(bs) * (4.0 * nb)
+        A = gen.BSRMatrix(nb, bs, (np.arange(nb + 1) * nb).astype(np.int32),
+                          np.tile(np.arange(nb, dtype=np.int32), nb), val)
+    else:
+        A = mats()[name]
+    LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
+    row, col = T(A.rowptr, cuda), T(A.colind, cuda)
+    lu0 = T(A.val, cuda).clone()
+    assert api.bsrilu02_inplace(A.nb, A.nnzb, A.bs, row, col, lu0, schedule=0) == -1
+    p = api.Preconditioner(A.nb, A.bs, row, col, T(A.val, cuda), fp32=False, ilu=True,
+                           schedule=schedule)
+    lu = N(p.get(0)).reshape(LU.shape)
+    p.close()
+    assert relerr(lu, LU) < 1e-12
+    if schedule == 0:
+        assert np.array_equal(lu.ravel(), N(lu0).ravel())
+
+
 @pytest.mark.parametrize("name", ["c1_s16", "c2_s6", "c3_nb200"])
 def test_engine_setup_matches_oracle(cuda, orc, name):
     from isai_kernel_gb300 import api
