@@ -353,7 +353,7 @@ int bilu_ctx_destroy(bilu_ctx* ctx);
  * alone builds BILU(0) and the level analyses only (no ISAI; solves in the
  * other modes then return BILU_ERR_ARG).
  * h_times (optional, 4 doubles, milliseconds): factor (BILU(0)'s level
- * analysis and factorisation, with the copies of A), patterns (ISAI
+ * analysis, its match lists and the factorisation, with the copies of A), patterns (ISAI
  * patterns and pair lists), isai (Dinv, column solves, reorders), total.
  * The structure steps run first, then the value steps. */
 int bilu_ctx_setup(bilu_ctx* ctx, int nb, int nnzb, int bs, const int* d_row, const int* d_col,
@@ -412,8 +412,10 @@ int bilu_ctx_select(bilu_ctx* ctx, const double* d_b, int restart, int cycles, d
 /* Host-buffer convenience (the end-to-end call): copies A and b from host
  * memory, runs the setup `prec` needs (any bilu_precision) and the solve,
  * copies x back.  The values and b copy on a second stream while the
- * setup's structure phase (level analysis, ISAI patterns, pair lists) runs
- * on `stream`; with pinned host buffers the two overlap.  Device buffers of
+ * setup's structure phase (level analysis, BILU(0)'s match lists, ISAI
+ * patterns, pair lists) runs on `stream`; with pinned host buffers the two
+ * overlap.  The uploaded values become the handle's copy of A (no second
+ * device copy).  Device buffers of
  * this call and of every handle come from a memory pool private to the
  * library that keeps freed memory reserved, so repeated calls do not map
  * their buffers again. */
