@@ -928,6 +928,42 @@ def test_solve_host_end_to_end(cuda, orc, name):
     P.close()
 
 
+def test_solve_host_errors(cuda, orc):
+    """bilu_solve_host's failure paths free what the call allocated: a
+    missing diagonal block and an unsorted row fail in the setup's structure
+    phase (BILU_ERR_PATTERN, before the uploaded values are handed to the
+    handle), a solve that stops at maxit returns BILU_ERR_NOT_CONVERGED with
+    its last iterate (after the hand-over); calls before and after give the
+    same x bit for bit."""
+    from isai_kernel_gb300 import api
+
+    A = gen.laplace2d(8, bs=4, seed=0)
+    b = gen.rhs(A.n, 2)
+    x0, res0, _ = api.solve_host(A.nb, A.bs, A.rowptr, A.colind, A.val, b, prec=api.BILU_NESTED)
+    assert res0.converged and res0.relres <= 1e-10
+    # row 3 without its diagonal block
+    p = int(A.rowptr[3] + np.nonzero(A.colind[A.rowptr[3]:A.rowptr[4]] == 3)[0][0])
+    row = A.rowptr.copy()
+    row[4:] -= 1
+    col = np.delete(A.colind, p)
+    val = np.delete(A.val, p, axis=0)
+    with pytest.raises(api.BiluError) as e:
+        api.solve_host(A.nb, A.bs, row, col, val, b, prec=api.BILU_NESTED)
+    assert e.value.status == -2
+    # row 5 with two columns swapped
+    col = A.colind.copy()
+    s5 = int(A.rowptr[5])
+    col[s5], col[s5 + 1] = col[s5 + 1], col[s5]
+    with pytest.raises(api.BiluError) as e:
+        api.solve_host(A.nb, A.bs, A.rowptr, col, A.val, b, prec=api.BILU_FP64)
+    assert e.value.status == -2
+    x2, res2, _ = api.solve_host(A.nb, A.bs, A.rowptr, A.colind, A.val, b, prec=api.BILU_FP64,
+                                 maxit=2)
+    assert not res2.converged and res2.iters == 2 and np.all(np.isfinite(x2))
+    x3, res3, _ = api.solve_host(A.nb, A.bs, A.rowptr, A.colind, A.val, b, prec=api.BILU_NESTED)
+    assert res3.iters == res0.iters and np.array_equal(x3, x0)
+
+
 @pytest.mark.parametrize("name,inner", [("c1_s16", 10), ("c2_s6", 20), ("c3_nb200", 20),
                                         ("bs5_s7", 8), ("c1_s16", 1), ("c2_s6", 32)])
 def test_gmres_nested_matches_oracle(cuda, orc, name, inner):
