@@ -47,6 +47,9 @@ struct SyncState {
   // per lower position pk of the factor: how many blocks dependency K
   // updates in row I (null: not counted, every dependency searches)
   const int* nmatch = nullptr;
+  // match lists of the updates (bilu0_match_count / _fill; null: search)
+  const int* mptr = nullptr;
+  const int2* mpair = nullptr;
 };
 
 // Warp-wide wait until flags[K] != 0.  Returns false if the launch aborted.
@@ -1391,7 +1394,29 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
     // the matched blocks.  Every block is updated once per K, so the
     // update order of each element is the same either way.  A dependency
     // counted as updating no block skips the searches.
-    if (nm != 0) {
+    if (ss.mpair) {
+      // the matches from the structure phase, TPW at a time
+      const int ms = __ldg(ss.mptr + pk), me = __ldg(ss.mptr + pk + 1);
+      for (int q0 = ms; q0 < me; q0 += TPW) {
+        const int q = q0 + team;
+        if (team_on && q < me) {
+          const int2 mq = __ldg(ss.mpair + q);
+          double* Aij = val + (long long)mq.x * BS2;
+          const double* Ukj = val + (long long)mq.y * BS2;
+#pragma unroll
+          for (int u = 0; u < EPL; ++u) {
+            int e = tl * EPL + u;
+            if (e < BS2) {
+              int r = e / BS, c = e - r * BS;
+              double v = Aij[e];
+#pragma unroll
+              for (int k = 0; k < BS; ++k) v -= L[r * BS + k] * __ldcg(Ukj + k * BS + c);
+              Aij[e] = v;
+            }
+          }
+        }
+      }
+    } else if (nm != 0) {
       const bool from_i = (re - pk - 1) <= (ke - dK - 1);
       const int cs = from_i ? pk + 1 : dK + 1, ce = from_i ? re : ke;
       const int ss_ = from_i ? dK + 1 : pk + 1, se = from_i ? ke : re;
@@ -1739,9 +1764,47 @@ __global__ void __launch_bounds__(256) k_bilu0_match_fill(int nb, long long nnzb
   if (out >= end) return;
   int I;
   const MatchLists m = match_lists(pk, nb, row, col, diag, I);
+  if (m.ce - m.cs > kMatchSerial) return;  // k_bilu0_match_fill_long
   for (int c = m.cs; c < m.ce && out < end; ++c) {
     const int o = find_in_row(col, m.s, m.e, __ldg(col + c));
     if (o >= 0) mpair[out++] = m.from_i ? make_int2(c, o) : make_int2(o, c);
+  }
+}
+
+// The positions with more than kMatchSerial candidates (two hub rows): a
+// warp per 32 positions takes them one at a time, 32 candidates per pass,
+// and writes the matches of a pass in candidate order.
+__global__ void __launch_bounds__(256) k_bilu0_match_fill_long(int nb, long long nnzb,
+                                                               const int* __restrict__ row,
+                                                               const int* __restrict__ col,
+                                                               const int* __restrict__ diag,
+                                                               const int* __restrict__ mptr,
+                                                               int2* __restrict__ mpair) {
+  const long long p0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll;
+  const int lane = threadIdx.x & 31;
+  if (p0 >= nnzb) return;  // the whole warp
+  bool mine = false;
+  if (p0 + lane < nnzb && __ldg(mptr + p0 + lane + 1) > __ldg(mptr + p0 + lane)) {
+    int I;
+    const MatchLists m = match_lists(p0 + lane, nb, row, col, diag, I);
+    mine = m.ce - m.cs > kMatchSerial;
+  }
+  unsigned todo = __ballot_sync(FULL, mine);
+  while (todo) {
+    const long long pk = p0 + __ffs(todo) - 1;
+    todo &= todo - 1;
+    int I;
+    const MatchLists m = match_lists(pk, nb, row, col, diag, I);
+    int out = __ldg(mptr + pk);
+    const int end = __ldg(mptr + pk + 1);
+    for (int c0 = m.cs; c0 < m.ce; c0 += 32) {
+      const int c = c0 + lane;
+      const int o = c < m.ce ? find_in_row(col, m.s, m.e, __ldg(col + c)) : -1;
+      const unsigned hit = __ballot_sync(FULL, o >= 0);
+      const int at = out + __popc(hit & ((1u << lane) - 1u));
+      if (o >= 0 && at < end) mpair[at] = m.from_i ? make_int2(c, o) : make_int2(o, c);
+      out += __popc(hit);
+    }
   }
 }
 
@@ -2123,6 +2186,9 @@ int bilu0_match_fill(int nb, long long nnzb, const int* row, const int* col, con
   k_bilu0_match_fill<<<ceil_div(nnzb, 256), 256, 0, st>>>(nb, nnzb, row, col, diag, mptr,
                                                           mpair);
   BILU_LAUNCH_CHECK();
+  k_bilu0_match_fill_long<<<ceil_div(nnzb, 256), 256, 0, st>>>(nb, nnzb, row, col, diag, mptr,
+                                                               mpair);
+  BILU_LAUNCH_CHECK();
   return BILU_OK;
 }
 
@@ -2147,6 +2213,8 @@ int bilu0_factor(int nb, long long nnzb, int bs, const int* row, const int* col,
     ss.order = order;
     ss.rdiag = rdiag;
     ss.nmatch = nmatch;
+    ss.mptr = keep.mptr;
+    ss.mpair = keep.mpair;
     if (nb > 0) {
       const unsigned grid = ceil_div(std::max(nnzb, 1ll), 256);
       k_bilu0_nmatch<<<grid, 256, 0, st>>>(nb, nnzb, row, col, diag, nmatch);

@@ -715,13 +715,15 @@ def test_single_block_and_empty_offdiag(cuda, orc):
 
 # ------------------------------------------------------------------ engine + GMRES
 @pytest.mark.parametrize("name", ["c1_s16", "c2_s6", "c3_nb200", "bs5_s7", "long_rows", "dense"])
-@pytest.mark.parametrize("schedule", [-1, 0])
+@pytest.mark.parametrize("schedule", [-1, 0, 1])
 def test_engine_factor_match_lists(cuda, orc, name, schedule):
     """A handle's setup builds BILU(0)'s match lists from the pattern before
-    the level-order factorisation; its factor is the same bit for bit as
-    the entry point that searches for the matches inside the factorisation
-    (bsrilu02_inplace, level schedule), on short-row, long-row and dense
-    patterns, and within 1e-12 of the oracle."""
+    the factorisation (a thread per dependency, a warp for the ones with
+    more than 32 candidates); its factor is the same bit for bit as the
+    entry point that searches for the matches inside the factorisation
+    (bsrilu02_inplace, same schedule: recommended, level order, sync-free),
+    on short-row, long-row and dense patterns, and within 1e-12 of the
+    oracle."""
     from isai_kernel_gb300 import api
 
     if name == "long_rows":
@@ -739,14 +741,13 @@ def test_engine_factor_match_lists(cuda, orc, name, schedule):
     LU, _ = orc.bsrilu0(A.nb, A.bs, A.rowptr, A.colind, A.val)
     row, col = T(A.rowptr, cuda), T(A.colind, cuda)
     lu0 = T(A.val, cuda).clone()
-    assert api.bsrilu02_inplace(A.nb, A.nnzb, A.bs, row, col, lu0, schedule=0) == -1
+    assert api.bsrilu02_inplace(A.nb, A.nnzb, A.bs, row, col, lu0, schedule=schedule) == -1
     p = api.Preconditioner(A.nb, A.bs, row, col, T(A.val, cuda), fp32=False, ilu=True,
                            schedule=schedule)
     lu = N(p.get(0)).reshape(LU.shape)
     p.close()
     assert relerr(lu, LU) < 1e-12
-    if schedule == 0:
-        assert np.array_equal(lu.ravel(), N(lu0).ravel())
+    assert np.array_equal(lu.ravel(), N(lu0).ravel())
 
 
 @pytest.mark.parametrize("name", ["c1_s16", "c2_s6", "c3_nb200"])
