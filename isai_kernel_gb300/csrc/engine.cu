@@ -449,12 +449,15 @@ int ctx_setup(bilu_ctx* c, int nb, int nnzb, int bs, const int* d_row, const int
     Carver w2 = ws;
     BILU_TRY(bilu0_analyze(nb, nnzb, c->Arow, c->Acol, c->diag, keepL, w2, st));
   }
-  // the factorisation's match lists (which A_IJ each L_IK updates, with
-  // U_KJ), built here from the pattern instead of searched for inside every
-  // row's dependency chain; at most 4 pairs a block
+  // the level-order factorisation's match lists (which A_IJ each L_IK
+  // updates, with U_KJ), built here from the pattern instead of searched
+  // for inside every row's dependency chain; at most 4 pairs a block.  The
+  // sync-free factorisation (long rows) keeps its searches: on the
+  // power-law system the lists cost as much to build as they saved.
   int* mptr = nullptr;
   int2* mpair = nullptr;
-  {
+  const int fsched = (c->schedule == 0 || c->schedule == 1) ? c->schedule : keepL.h_fsched;
+  if (fsched == 0) {
     BILU_TRY(c->alloc(&mptr, (size_t)nnzb + 1));
     long long total = 0;
     const long long cap = 4ll * nnzb;

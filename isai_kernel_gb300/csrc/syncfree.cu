@@ -47,9 +47,6 @@ struct SyncState {
   // per lower position pk of the factor: how many blocks dependency K
   // updates in row I (null: not counted, every dependency searches)
   const int* nmatch = nullptr;
-  // match lists of the updates (bilu0_match_count / _fill; null: search)
-  const int* mptr = nullptr;
-  const int2* mpair = nullptr;
 };
 
 // Warp-wide wait until flags[K] != 0.  Returns false if the launch aborted.
@@ -1394,29 +1391,7 @@ __device__ __forceinline__ bool bilu0_wrow(int I, const int* __restrict__ row,
     // the matched blocks.  Every block is updated once per K, so the
     // update order of each element is the same either way.  A dependency
     // counted as updating no block skips the searches.
-    if (ss.mpair) {
-      // the matches from the structure phase, TPW at a time
-      const int ms = __ldg(ss.mptr + pk), me = __ldg(ss.mptr + pk + 1);
-      for (int q0 = ms; q0 < me; q0 += TPW) {
-        const int q = q0 + team;
-        if (team_on && q < me) {
-          const int2 mq = __ldg(ss.mpair + q);
-          double* Aij = val + (long long)mq.x * BS2;
-          const double* Ukj = val + (long long)mq.y * BS2;
-#pragma unroll
-          for (int u = 0; u < EPL; ++u) {
-            int e = tl * EPL + u;
-            if (e < BS2) {
-              int r = e / BS, c = e - r * BS;
-              double v = Aij[e];
-#pragma unroll
-              for (int k = 0; k < BS; ++k) v -= L[r * BS + k] * __ldcg(Ukj + k * BS + c);
-              Aij[e] = v;
-            }
-          }
-        }
-      }
-    } else if (nm != 0) {
+    if (nm != 0) {
       const bool from_i = (re - pk - 1) <= (ke - dK - 1);
       const int cs = from_i ? pk + 1 : dK + 1, ce = from_i ? re : ke;
       const int ss_ = from_i ? dK + 1 : pk + 1, se = from_i ? ke : re;
@@ -2213,8 +2188,6 @@ int bilu0_factor(int nb, long long nnzb, int bs, const int* row, const int* col,
     ss.order = order;
     ss.rdiag = rdiag;
     ss.nmatch = nmatch;
-    ss.mptr = keep.mptr;
-    ss.mpair = keep.mpair;
     if (nb > 0) {
       const unsigned grid = ceil_div(std::max(nnzb, 1ll), 256);
       k_bilu0_nmatch<<<grid, 256, 0, st>>>(nb, nnzb, row, col, diag, nmatch);

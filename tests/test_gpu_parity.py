@@ -718,12 +718,12 @@ def test_single_block_and_empty_offdiag(cuda, orc):
 @pytest.mark.parametrize("schedule", [-1, 0, 1])
 def test_engine_factor_match_lists(cuda, orc, name, schedule):
     """A handle's setup builds BILU(0)'s match lists from the pattern before
-    the factorisation (a thread per dependency, a warp for the ones with
-    more than 32 candidates); its factor is the same bit for bit as the
-    entry point that searches for the matches inside the factorisation
-    (bsrilu02_inplace, same schedule: recommended, level order, sync-free),
-    on short-row, long-row and dense patterns, and within 1e-12 of the
-    oracle."""
+    a level-order factorisation (a thread per dependency, a warp for the
+    ones with more than 32 candidates); its factor is the same bit for bit
+    as the entry point that searches for the matches inside the
+    factorisation (bsrilu02_inplace, same schedule: recommended, level
+    order, sync-free), on short-row, long-row and dense patterns, and within
+    1e-12 of the oracle."""
     from isai_kernel_gb300 import api
 
     if name == "long_rows":
