@@ -260,9 +260,10 @@ void launch_combine(long long n, const float* Q, long long ldq, const double* y,
 // every CTA returns.  Memory traffic at 128^3 (ncu, one step of 17 sweeps):
 // FP32 reads each basis vector once from DRAM (w and the previous basis
 // vector are L2 hits); FP64 moves ~2.8 vectors a sweep (3.17 GB a step):
-// w (67 MB) does not stay in the L2 beside the streamed basis vectors, with
-// or without evict-last hints on w, so an FP64 sweep is bound by HBM and
-// the DFMA pipe about equally.
+// w (67 MB) does not stay fully in the L2 beside the streamed basis
+// vectors, even with evict-last hints on w; held there by an L2 persisting
+// window it costs 3% less a sweep, which is then bound by the DFMA pipe's
+// issue and the per-sweep synchronisation rather than by HBM.
 template <class T>
 struct MgsVec;
 template <>
